@@ -1,0 +1,303 @@
+/* scirs_sparse.h -- C ABI of the GB300 sparse iterative-solve library.
+ *
+ * Drop-in device backend for the iterative-solve path of scirs2-sparse
+ * (cool-japan/scirs, workspace 0.1.0-alpha.6): CSR construction and
+ * transpose, CSR SpMV, the LinearOperator slot (operators and
+ * preconditioners), and the cg / bicgstab / gmres solvers.  Every entry point
+ * names the reference item it replaces (paths relative to the reference
+ * workspace).  A Rust shim implementing the crate's traits on top of these
+ * calls is shown in INTEGRATION.md.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Indices cross the boundary as uint64_t
+ *    (Rust usize); the device keeps int32 indices and rejects larger values
+ *    with SX_ERR_INDEX_CAST_OVERFLOW (index_dtype.rs:109-170 semantics).
+ *  - Values are float (SX_F32) or double (SX_F64); `const void*` value
+ *    pointers point at the dtype of the handle they go with.
+ *  - `mem` arguments say where vector buffers live: SX_MEM_HOST (pageable or
+ *    pinned host memory, copied in/out inside the call) or SX_MEM_DEVICE
+ *    (device pointers on the context's device, used in place).
+ *  - Calls are synchronous on the context's stream, like the reference's
+ *    blocking calls.  Handles are not thread-safe: one context per thread.
+ *  - Errors: a non-zero sx_status; sx_last_error() returns the structured
+ *    payload and the SparseError Display string for the calling thread.
+ *  - Solver non-convergence and breakdown are NOT errors: they return SX_OK
+ *    with converged = 0 and a message code, as IterationResult does.
+ */
+#ifndef SCIRS_SPARSE_H
+#define SCIRS_SPARSE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+/* 1..14 follow SparseError's variants in declaration order
+ * (scirs2-sparse/src/error.rs:9-74). */
+typedef enum {
+  SX_OK = 0,
+  SX_ERR_COMPUTATION = 1,             /* ComputationError(String)            */
+  SX_ERR_DIMENSION_MISMATCH = 2,      /* DimensionMismatch{expected, found}  */
+  SX_ERR_INDEX_OUT_OF_BOUNDS = 3,     /* IndexOutOfBounds{index, shape}      */
+  SX_ERR_INVALID_AXIS = 4,            /* InvalidAxis                          */
+  SX_ERR_INVALID_SLICE_RANGE = 5,     /* InvalidSliceRange                    */
+  SX_ERR_INCONSISTENT_DATA = 6,       /* InconsistentData{reason}            */
+  SX_ERR_NOT_IMPLEMENTED = 7,         /* NotImplemented(String)              */
+  SX_ERR_SINGULAR_MATRIX = 8,         /* SingularMatrix(String)              */
+  SX_ERR_VALUE = 9,                   /* ValueError(String)                  */
+  SX_ERR_CONVERSION = 10,             /* ConversionError(String)             */
+  SX_ERR_OPERATION_NOT_SUPPORTED = 11,/* OperationNotSupported(String)       */
+  SX_ERR_SHAPE_MISMATCH = 12,         /* ShapeMismatch{expected, found}      */
+  SX_ERR_ITERATIVE_SOLVER_FAILURE = 13,/* IterativeSolverFailure(String)     */
+  SX_ERR_INDEX_CAST_OVERFLOW = 14,    /* IndexCastOverflow{value, target}    */
+  /* device-side conditions with no SparseError counterpart */
+  SX_ERR_CUDA = 100,                  /* a CUDA runtime call failed           */
+  SX_ERR_DEVICE_TIMEOUT = 101,        /* a bounded device-side wait ran out   */
+  SX_ERR_INVALID_ARGUMENT = 102,      /* null handle, bad enum, dtype clash   */
+  SX_ERR_OUT_OF_MEMORY = 103          /* device allocation failed             */
+} sx_status;
+
+typedef struct {
+  int code;          /* sx_status */
+  uint64_t v0, v1;   /* DimensionMismatch: expected, found; IndexOutOfBounds: index (r, c);
+                        IndexCastOverflow: value */
+  uint64_t v2, v3;   /* IndexOutOfBounds / ShapeMismatch: shape (r, c) */
+  char message[512]; /* the SparseError Display text, e.g.
+                        "Value error: Row index out of bounds" */
+} sx_error_info;
+
+/* Last error of the calling thread (copies into *out). */
+void sx_last_error(sx_error_info* out);
+const char* sx_status_string(int status);
+
+typedef enum { SX_F32 = 0, SX_F64 = 1 } sx_dtype;
+typedef enum { SX_MEM_HOST = 0, SX_MEM_DEVICE = 1 } sx_mem;
+
+/* ----------------------------------------------------------------- context */
+typedef struct sx_ctx_s* sx_ctx;
+
+/* A context owns a non-blocking CUDA stream, reusable scratch space and the
+ * SpMV autotune cache.  (No reference counterpart: the reference runs on the
+ * caller's thread.) */
+int sx_ctx_create(int device, sx_ctx* out);
+/* Same, but work is enqueued on a caller-owned stream (cudaStream_t). */
+int sx_ctx_create_on_stream(int device, void* stream, sx_ctx* out);
+int sx_ctx_destroy(sx_ctx ctx);
+void* sx_ctx_stream(sx_ctx ctx);
+int sx_ctx_synchronize(sx_ctx ctx);
+/* Number of kernels this library launched on the context (graph-launched
+ * kernels included), for launch accounting. */
+uint64_t sx_ctx_kernel_launches(sx_ctx ctx);
+
+/* --------------------------------------------------------------- operators */
+/* One handle type for matrices, operators and preconditioners: the
+ * reference's preconditioner slot is itself Box<dyn LinearOperator<F>>
+ * (linalg/interface.rs:13-52, linalg/iterative.rs:17-23). */
+typedef struct sx_op_s* sx_op;
+
+typedef enum {
+  SX_OP_CSR = 0,             /* MatrixLinearOperator<F, CsrMatrix<F>>  interface.rs:232-296 */
+  SX_OP_IDENTITY = 1,        /* IdentityOperator                       interface.rs:55-93   */
+  SX_OP_SCALED_IDENTITY = 2, /* ScaledIdentityOperator                 interface.rs:95-130  */
+  SX_OP_DIAGONAL = 3,        /* DiagonalOperator                       interface.rs:132-175 */
+  SX_OP_JACOBI = 4,          /* JacobiPreconditioner                   preconditioners.rs:14-92 */
+  SX_OP_IC0 = 5,             /* IC0Preconditioner                      ic.rs:15-230 */
+  SX_OP_FSAI = 6,            /* M^-1 = G G^T (learned factorised SAI; no reference counterpart) */
+  SX_OP_HOST = 7             /* user operator called back on the host  (dyn LinearOperator) */
+} sx_op_kind;
+
+/* Which reference constructor's validation and error semantics to follow. */
+typedef enum {
+  SX_API_CSR_MATRIX = 0, /* CsrMatrix::new / from_raw_csr   csr.rs:92-227         */
+  SX_API_CSR_ARRAY = 1   /* CsrArray::from_triplets / new   csr_array.rs:77-219   */
+} sx_csr_api;
+
+/* Triplets -> CSR on the device: validation, stable sort by (row, col) with
+ * duplicates kept, row pointers by count + prefix sum.  Bit-exact with
+ * CsrMatrix::new (csr.rs:92-160) or CsrArray::from_triplets(.., sorted)
+ * (csr_array.rs:152-219).  rows/cols/data are host arrays of length nnz. */
+int sx_csr_from_triplets(sx_ctx ctx, sx_dtype dtype, sx_csr_api api, const uint64_t* rows,
+                         const uint64_t* cols, const void* data, uint64_t nnz, uint64_t nrows,
+                         uint64_t ncols, int sorted, sx_op* out);
+
+/* Raw CSR arrays (host): validation of CsrMatrix::from_raw_csr
+ * (csr.rs:174-227) or CsrArray::new (csr_array.rs:77-136); arrays are kept
+ * as given.  indptr has indptr_len entries, indices/data have nnz. */
+int sx_csr_from_raw(sx_ctx ctx, sx_dtype dtype, sx_csr_api api, const uint64_t* indptr,
+                    uint64_t indptr_len, const uint64_t* indices, const void* data, uint64_t nnz,
+                    uint64_t nrows, uint64_t ncols, sx_op* out);
+
+/* Device-native upload: int64 row pointers, int32 columns, values of
+ * `dtype`, in host or device memory.  Validated like from_raw_csr.  (No
+ * reference counterpart: saves the usize->int32 narrowing pass.) */
+int sx_csr_from_raw_i32(sx_ctx ctx, sx_dtype dtype, const int64_t* indptr, const int32_t* indices,
+                        const void* data, uint64_t nrows, uint64_t ncols, uint64_t nnz,
+                        sx_mem mem, sx_op* out);
+
+/* Counting-sort transpose, bit-exact with CsrMatrix::transpose
+ * (csr.rs:289-326) and CsrArray::transpose (csr_array.rs:595-625). */
+int sx_csr_transpose(sx_ctx ctx, sx_op a, sx_op* out);
+
+/* Value-type conversion of a CSR matrix (e.g. the FP32 copy used by the
+ * mixed-precision solver).  No reference counterpart. */
+int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out);
+
+/* CSR accessors: shape/nnz (csr.rs:244-264), arrays back to the host as
+ * usize (the public indptr/indices/data fields, csr.rs:20-25), get(i, j)
+ * with first-match semantics (csr.rs:33-48), has_sorted_indices
+ * (csr_array.rs:221-233). */
+int sx_csr_info(sx_op a, uint64_t* nrows, uint64_t* ncols, uint64_t* nnz, int* has_sorted_indices);
+int sx_csr_download(sx_ctx ctx, sx_op a, uint64_t* indptr, uint64_t* indices, void* data);
+int sx_csr_get(sx_ctx ctx, sx_op a, uint64_t i, uint64_t j, void* out_value);
+
+int sx_op_identity(sx_ctx ctx, sx_dtype dtype, uint64_t n, sx_op* out);
+int sx_op_scaled_identity(sx_ctx ctx, sx_dtype dtype, uint64_t n, double scale, sx_op* out);
+int sx_op_diagonal(sx_ctx ctx, sx_dtype dtype, const void* diag, uint64_t n, sx_op* out);
+
+/* Host-callback operator for a user-defined LinearOperator: the library
+ * stages x to the host, calls fn(user, x, y, n), and copies y back.  The
+ * solver loop itself stays on the device. */
+typedef int (*sx_host_matvec_fn)(void* user, const void* x, void* y, uint64_t n);
+int sx_op_host(sx_ctx ctx, sx_dtype dtype, uint64_t nrows, uint64_t ncols, sx_host_matvec_fn fn,
+               void* user, sx_op* out);
+
+int sx_op_kind_of(sx_op op, int* kind);
+int sx_op_shape(sx_op op, uint64_t* nrows, uint64_t* ncols);
+int sx_op_dtype(sx_op op, int* dtype);
+int sx_op_destroy(sx_op op);
+
+/* y = A x (LinearOperator::matvec, interface.rs:18; CSR: interface.rs:257-279,
+ * CsrArray::dot_vector csr_array.rs:569-593, CsrMatrix::dot csr.rs:479-497).
+ * x has x_len entries (DimensionMismatch otherwise), y has nrows. */
+int sx_op_matvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, sx_mem mem);
+/* y = A^T x (LinearOperator::rmatvec; CSR: interface.rs:281-285, through a
+ * cached device transpose instead of a transpose per call). */
+int sx_op_rmatvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, sx_mem mem);
+
+/* SpMV flags for sx_spmv_ex */
+#define SX_SPMV_EXACT 1u /* per-row sequential sum of rounded products (reference order) */
+/* Device-pointer SpMV with an explicit summation mode (the default of
+ * sx_op_matvec is the exact mode). */
+int sx_spmv_ex(sx_ctx ctx, sx_op a, const void* x_dev, void* y_dev, unsigned flags);
+
+/* --------------------------------------------------------- preconditioners */
+/* JacobiPreconditioner::new (preconditioners.rs:21-44): 1/get(i,i) with the
+ * FIRST duplicate's value; ValueError "Zero diagonal element at position i"
+ * when |d| < epsilon. */
+int sx_precond_jacobi(sx_ctx ctx, sx_op a, sx_op* out);
+/* JacobiPreconditioner::from_diagonal (preconditioners.rs:47-62). */
+int sx_precond_jacobi_from_diagonal(sx_ctx ctx, sx_dtype dtype, const void* diag, uint64_t n,
+                                    sx_op* out);
+
+typedef enum {
+  SX_IC0_REFERENCE = 0, /* the reference factorisation, ic.rs:22-135, bit-exact */
+  SX_IC0_TEXTBOOK = 1   /* standard IC(0): L_ij = (a_ij - sum) / L_jj, d_i = sqrt(a_ii - sum L_ik^2) */
+} sx_ic0_variant;
+/* IC0Preconditioner::new (ic.rs:22-135) and its apply (ic.rs:143-220). */
+int sx_precond_ic0(sx_ctx ctx, sx_op a, int variant, sx_op* out);
+
+/* Factorised approximate inverse M^-1 = G G^T from a lower-triangular CSR G
+ * (no reference counterpart; apply = two SpMVs through a cached G^T). */
+int sx_precond_fsai(sx_ctx ctx, sx_op g, sx_op* out);
+
+/* ----------------------------------------------------------------- solvers */
+typedef enum {
+  SX_MSG_CONVERGED = 0,           /* "Converged" */
+  SX_MSG_MAX_ITER = 1,            /* "Maximum iterations reached" */
+  SX_MSG_NOT_POSITIVE_DEFINITE = 2,/* "Matrix not positive definite (p^T*A*p <= 0)" */
+  SX_MSG_CONVERGED_INITIAL = 3,   /* "Converged with initial guess" */
+  SX_MSG_BREAKDOWN_RHO = 4,       /* "BiCGSTAB breakdown: rho ≈ 0" */
+  SX_MSG_BREAKDOWN_RHAT_V = 5,    /* "BiCGSTAB breakdown: (r_hat, v) ≈ 0" */
+  SX_MSG_BREAKDOWN_ALPHA = 6,     /* "BiCGSTAB breakdown: alpha is not finite" */
+  SX_MSG_BREAKDOWN_TT = 7,        /* "BiCGSTAB breakdown: (t, t) ≈ 0" */
+  SX_MSG_BREAKDOWN_OMEGA = 8      /* "BiCGSTAB breakdown: omega is not finite or too small" */
+} sx_message;
+/* The exact message strings of the reference (UTF-8). */
+const char* sx_message_string(int message);
+
+/* IterationResult (iterative.rs:8-14); x is returned through x_out. */
+typedef struct {
+  uint64_t iterations;
+  double residual_norm;
+  int converged;
+  int message; /* sx_message */
+} sx_iter_result;
+
+/* CGOptions (iterative.rs:17-35); defaults: 1000, 1e-8, 1e-12, none, none. */
+typedef struct {
+  uint64_t max_iter;
+  double rtol;
+  double atol;
+  const void* x0;      /* NULL = zeros; lives in `mem` like b */
+  sx_op preconditioner;/* NULL = none */
+} sx_cg_options;
+/* BiCGSTABOptions (iterative.rs:348-368). */
+typedef struct {
+  uint64_t max_iter;
+  double rtol;
+  double atol;
+  const void* x0;
+  sx_op left_preconditioner;
+  sx_op right_preconditioner;
+} sx_bicgstab_options;
+/* GMRESOptions (iterative.rs:614-634); restart default 30. */
+typedef struct {
+  uint64_t max_iter;
+  uint64_t restart;
+  double rtol;
+  double atol;
+  const void* x0;
+  sx_op preconditioner;
+} sx_gmres_options;
+
+void sx_cg_options_default(sx_cg_options* o);
+void sx_bicgstab_options_default(sx_bicgstab_options* o);
+void sx_gmres_options_default(sx_gmres_options* o);
+
+/* cg (iterative.rs:40-162).  b has b_len entries; x_out has nrows(a). */
+int sx_cg(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_cg_options* opt,
+          void* x_out, sx_mem mem, sx_iter_result* res);
+/* bicgstab (iterative.rs:377-611). */
+int sx_bicgstab(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len,
+                const sx_bicgstab_options* opt, void* x_out, sx_mem mem, sx_iter_result* res);
+/* gmres (iterative.rs:641-816). */
+int sx_gmres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_gmres_options* opt,
+             void* x_out, sx_mem mem, sx_iter_result* res);
+
+/* ------------------------------------------- mixed precision (no reference
+ * counterpart; nearest dense analogue scirs2-linalg mixed_precision) */
+/* FP64 iterative refinement around an FP32 preconditioned CG:
+ *   x = x0 (FP64); repeat { r = b - A x in FP64; stop when
+ *   ||r||_2 <= tol ||b||_2; solve A d = r/||r|| with FP32 PCG to inner_rtol;
+ *   x += ||r|| d (FP64) }.
+ * a64 must be SX_F64; the FP32 copy is made inside (or pass a32). */
+typedef struct {
+  uint64_t max_outer;    /* default 30 */
+  uint64_t max_inner;    /* default 10000 */
+  double tol;            /* default 1e-10 */
+  double inner_rtol;     /* default 1e-4 */
+  const void* x0;        /* FP64, NULL = zeros */
+  sx_op preconditioner;  /* FP32 operator (JACOBI/IC0/FSAI) or NULL = Jacobi of a32 */
+  sx_op a32;             /* optional FP32 copy of a64 */
+} sx_ir_options;
+typedef struct {
+  uint64_t outer_iterations;
+  uint64_t inner_iterations;
+  double rel_residual;   /* final FP64 true relative residual ||b - A x|| / ||b|| */
+  int converged;
+} sx_ir_result;
+void sx_ir_options_default(sx_ir_options* o);
+int sx_cg_mixed(sx_ctx ctx, sx_op a64, const double* b, uint64_t b_len, const sx_ir_options* opt,
+                double* x_out, sx_mem mem, sx_ir_result* res);
+
+/* FP64 true relative residual ||b - A x||_2 / ||b||_2 of an FP64 CSR. */
+int sx_true_rel_residual(sx_ctx ctx, sx_op a64, const double* b, const double* x, sx_mem mem,
+                         double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SCIRS_SPARSE_H */

@@ -1,0 +1,256 @@
+"""ctypes loader of the CPU oracle (test infrastructure only).
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg, as the checker or the timed CPU baseline.  Builds the oracle with its
+Makefile on first use.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libsx_oracle.so")
+
+
+def build() -> str:
+    r = subprocess.run(["make", "-s", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB
+
+
+class Err(C.Structure):
+    _fields_ = [("code", C.c_int), ("v0", C.c_uint64), ("v1", C.c_uint64), ("v2", C.c_uint64),
+                ("v3", C.c_uint64), ("msg", C.c_char * 256)]
+
+
+class Res(C.Structure):
+    _fields_ = [("iterations", C.c_uint64), ("residual_norm", C.c_double), ("converged", C.c_int),
+                ("message", C.c_int)]
+
+
+class IROpt(C.Structure):
+    _fields_ = [("max_outer", C.c_uint64), ("max_inner", C.c_uint64), ("tol", C.c_double),
+                ("inner_rtol", C.c_double), ("jacobi", C.c_int)]
+
+
+class IRRes(C.Structure):
+    _fields_ = [("outer_iterations", C.c_uint64), ("inner_iterations", C.c_uint64),
+                ("rel_residual", C.c_double), ("converged", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp, u64, i64, dbl, ip = C.c_void_p, C.c_uint64, C.c_int64, C.c_double, C.c_int
+        E = C.POINTER(Err)
+        sig = {
+            "or_csr_matrix_new_f64": (ip, [vp, vp, vp, u64, u64, u64, vp, vp, vp, E]),
+            "or_csr_matrix_new_f32": (ip, [vp, vp, vp, u64, u64, u64, vp, vp, vp, E]),
+            "or_csr_matrix_from_raw_check": (ip, [vp, u64, vp, u64, u64, u64, u64, E]),
+            "or_csr_array_new_check": (ip, [vp, u64, vp, u64, u64, u64, u64, vp, E]),
+            "or_csr_array_from_triplets_f64": (ip, [vp, vp, vp, u64, u64, u64, ip, vp, vp, vp, vp, E]),
+            "or_csr_array_from_triplets_f32": (ip, [vp, vp, vp, u64, u64, u64, ip, vp, vp, vp, vp, E]),
+            "or_csr_transpose_f64": (None, [vp, vp, vp, u64, u64, vp, vp, vp]),
+            "or_csr_transpose_f32": (None, [vp, vp, vp, u64, u64, vp, vp, vp]),
+            "or_csr_get_f64": (dbl, [vp, vp, vp, u64, u64, u64, u64]),
+            "or_spmv_f64": (None, [vp, vp, vp, u64, vp, vp]),
+            "or_spmv_f32": (None, [vp, vp, vp, u64, vp, vp]),
+            "or_spmv_i32_f64": (None, [vp, vp, vp, i64, vp, vp]),
+            "or_spmv_i32_f32": (None, [vp, vp, vp, i64, vp, vp]),
+            "or_op_csr": (vp, [ip, vp, vp, vp, u64, u64]),
+            "or_op_csr_i32": (vp, [ip, vp, vp, vp, i64, i64]),
+            "or_op_identity": (vp, [ip, u64]),
+            "or_op_scaled_identity": (vp, [ip, u64, dbl]),
+            "or_op_diagonal": (vp, [ip, vp, u64]),
+            "or_op_jacobi": (vp, [vp, E]),
+            "or_op_jacobi_from_diagonal": (vp, [ip, vp, u64, E]),
+            "or_op_ic0": (vp, [vp, ip, E]),
+            "or_op_fsai": (vp, [vp]),
+            "or_op_destroy": (None, [vp]),
+            "or_op_matvec": (ip, [vp, vp, vp]),
+            "or_op_rows": (u64, [vp]),
+            "or_ic0_nnz": (u64, [vp]),
+            "or_ic0_factor": (None, [vp, vp, vp, vp]),
+            "or_cg": (ip, [vp, vp, u64, dbl, dbl, vp, vp, vp, C.POINTER(Res), E]),
+            "or_bicgstab": (ip, [vp, vp, u64, dbl, dbl, vp, vp, vp, vp, C.POINTER(Res), E]),
+            "or_gmres": (ip, [vp, vp, u64, u64, dbl, dbl, vp, vp, vp, C.POINTER(Res), E]),
+            "or_cg_mixed_ir": (ip, [vp, vp, vp, i64, vp, C.POINTER(IROpt), vp, C.POINTER(IRRes)]),
+            "or_true_rel_residual": (dbl, [vp, vp, vp, i64, vp, vp]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def p(a: np.ndarray):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+class Op:
+    """An oracle LinearOperator handle."""
+
+    def __init__(self, handle, n, f64=True):
+        self.h = handle
+        self.n = n
+        self.f64 = f64
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_op_destroy(self.h)
+            self.h = None
+
+    def matvec(self, x):
+        dt = np.float64 if self.f64 else np.float32
+        x = np.ascontiguousarray(x, dtype=dt)
+        y = np.empty(self.n, dtype=dt)
+        lib().or_op_matvec(self.h, p(x), p(y))
+        return y
+
+
+def op_csr(indptr, indices, data, shape):
+    f64 = np.asarray(data).dtype == np.float64
+    ip = np.ascontiguousarray(indptr, dtype=np.uint64)
+    ix = np.ascontiguousarray(indices, dtype=np.uint64)
+    d = np.ascontiguousarray(data)
+    h = lib().or_op_csr(1 if f64 else 0, p(ip), p(ix), p(d), shape[0], shape[1])
+    return Op(h, shape[0], f64)
+
+
+def op_csr_i32(indptr, indices, data, shape, f64=True):
+    ip = np.ascontiguousarray(indptr, dtype=np.int64)
+    ix = np.ascontiguousarray(indices, dtype=np.int32)
+    d = np.ascontiguousarray(data, dtype=np.float64)
+    h = lib().or_op_csr_i32(1, p(ip), p(ix), p(d), shape[0], shape[1])
+    op = Op(h, shape[0], True)
+    if not f64:
+        # an FP32 operator over the same arrays (values rounded to float)
+        d32 = d.astype(np.float32)
+        h32 = lib().or_op_csr(0, p(ip.astype(np.uint64)), p(ix.astype(np.uint64)), p(d32), shape[0], shape[1])
+        return Op(h32, shape[0], False)
+    return op
+
+
+def op_identity(n, f64=True):
+    return Op(lib().or_op_identity(1 if f64 else 0, n), n, f64)
+
+
+def op_diagonal(d, f64=True):
+    d = np.ascontiguousarray(d, dtype=np.float64 if f64 else np.float32)
+    return Op(lib().or_op_diagonal(1 if f64 else 0, p(d), d.size), d.size, f64)
+
+
+def op_jacobi(a: Op):
+    e = Err()
+    h = lib().or_op_jacobi(a.h, C.byref(e))
+    if not h:
+        raise ValueError(e.msg.decode())
+    return Op(h, a.n, a.f64)
+
+
+def op_ic0(a: Op, fast=True):
+    e = Err()
+    h = lib().or_op_ic0(a.h, 1 if fast else 0, C.byref(e))
+    if not h:
+        raise ValueError(e.msg.decode())
+    return Op(h, a.n, a.f64)
+
+
+def op_fsai(g: Op):
+    return Op(lib().or_op_fsai(g.h), g.n, g.f64)
+
+
+MESSAGES = [
+    "Converged",
+    "Maximum iterations reached",
+    "Matrix not positive definite (p^T*A*p <= 0)",
+    "Converged with initial guess",
+    "BiCGSTAB breakdown: rho ≈ 0",
+    "BiCGSTAB breakdown: (r_hat, v) ≈ 0",
+    "BiCGSTAB breakdown: alpha is not finite",
+    "BiCGSTAB breakdown: (t, t) ≈ 0",
+    "BiCGSTAB breakdown: omega is not finite or too small",
+]
+
+
+def _solve(kind, a: Op, b, max_iter, rtol, atol, x0, m=None, m2=None, restart=30):
+    dt = np.float64 if a.f64 else np.float32
+    b = np.ascontiguousarray(b, dtype=dt)
+    x = np.empty(a.n, dtype=dt)
+    x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=dt)
+    r, e = Res(), Err()
+    L = lib()
+    mh = m.h if m is not None else None
+    if kind == "cg":
+        rc = L.or_cg(a.h, p(b), max_iter, rtol, atol, p(x0a), mh, p(x), C.byref(r), C.byref(e))
+    elif kind == "bicgstab":
+        m2h = m2.h if m2 is not None else None
+        rc = L.or_bicgstab(a.h, p(b), max_iter, rtol, atol, p(x0a), mh, m2h, p(x), C.byref(r), C.byref(e))
+    else:
+        rc = L.or_gmres(a.h, p(b), max_iter, restart, rtol, atol, p(x0a), mh, p(x), C.byref(r), C.byref(e))
+    if rc:
+        raise ValueError(e.msg.decode())
+    return dict(x=x, iterations=int(r.iterations), residual_norm=float(r.residual_norm),
+                converged=bool(r.converged), message=MESSAGES[r.message])
+
+
+def cg(a, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None, preconditioner=None):
+    return _solve("cg", a, b, max_iter, rtol, atol, x0, preconditioner)
+
+
+def bicgstab(a, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None, left=None, right=None):
+    return _solve("bicgstab", a, b, max_iter, rtol, atol, x0, left, right)
+
+
+def gmres(a, b, max_iter=1000, restart=30, rtol=1e-8, atol=1e-12, x0=None, preconditioner=None):
+    return _solve("gmres", a, b, max_iter, rtol, atol, x0, preconditioner, restart=restart)
+
+
+def spmv_i32(indptr, indices, data, x):
+    indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+    indices = np.ascontiguousarray(indices, dtype=np.int32)
+    f64 = np.asarray(data).dtype == np.float64
+    data = np.ascontiguousarray(data)
+    x = np.ascontiguousarray(x, dtype=data.dtype)
+    y = np.empty(len(indptr) - 1, dtype=data.dtype)
+    if f64:
+        lib().or_spmv_i32_f64(p(indptr), p(indices), p(data), len(indptr) - 1, p(x), p(y))
+    else:
+        lib().or_spmv_i32_f32(p(indptr), p(indices), p(data), len(indptr) - 1, p(x), p(y))
+    return y
+
+
+def cg_mixed_ir(indptr, indices, data, b, tol=1e-10, inner_rtol=1e-4, max_outer=30,
+                max_inner=10000, jacobi=True):
+    indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+    indices = np.ascontiguousarray(indices, dtype=np.int32)
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = len(indptr) - 1
+    x = np.empty(n, dtype=np.float64)
+    o = IROpt(max_outer, max_inner, tol, inner_rtol, 1 if jacobi else 0)
+    r = IRRes()
+    lib().or_cg_mixed_ir(p(indptr), p(indices), p(data), n, p(b), C.byref(o), p(x), C.byref(r))
+    return dict(x=x, outer=int(r.outer_iterations), inner=int(r.inner_iterations),
+                rel_residual=float(r.rel_residual), converged=bool(r.converged))
+
+
+def true_rel_residual(indptr, indices, data, b, x):
+    indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+    indices = np.ascontiguousarray(indices, dtype=np.int32)
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    return lib().or_true_rel_residual(p(indptr), p(indices), p(data), len(indptr) - 1, p(b), p(x))

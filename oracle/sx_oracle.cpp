@@ -1,0 +1,1077 @@
+// CPU oracle for the scirs2-sparse iterative-solve path -- TEST INFRASTRUCTURE.
+//
+// A restatement, in C++17, of the reference functions listed beside each
+// routine (paths relative to the reference workspace).  Only tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg load this library,
+// and only as the checker or the timed CPU baseline: the product never does.
+//
+// Build: oracle/Makefile (g++ -O2 -ffp-contract=off).  The flag matters: Rust
+// evaluates `sum += a * b` as a rounded product followed by a rounded add.
+//
+// Parity pins: tests/test_oracle_golden.py replays the reference's own unit
+// and integration tests against this file (csr.rs, csr_array.rs, lib.rs,
+// iterative.rs, preconditioners.rs, ic.rs tests and tests/*.rs).  gmres has
+// no test in the reference crate: its parity is pinned only by this
+// restatement.
+
+#include "sx_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+namespace {
+
+enum ErrCode {
+  E_OK = 0,
+  E_COMPUTATION = 1,
+  E_DIMENSION_MISMATCH = 2,
+  E_INDEX_OUT_OF_BOUNDS = 3,
+  E_INVALID_AXIS = 4,
+  E_INVALID_SLICE = 5,
+  E_INCONSISTENT_DATA = 6,
+  E_NOT_IMPLEMENTED = 7,
+  E_SINGULAR = 8,
+  E_VALUE = 9,
+  E_CONVERSION = 10,
+  E_NOT_SUPPORTED = 11,
+  E_SHAPE_MISMATCH = 12,
+  E_SOLVER_FAILURE = 13,
+  E_INDEX_CAST_OVERFLOW = 14,
+};
+
+enum Msg {
+  M_CONVERGED = 0,
+  M_MAX_ITER = 1,
+  M_NOT_PD = 2,
+  M_CONVERGED_INITIAL = 3,
+  M_BD_RHO = 4,
+  M_BD_RHAT_V = 5,
+  M_BD_ALPHA = 6,
+  M_BD_TT = 7,
+  M_BD_OMEGA = 8,
+};
+
+int set_err(or_err* e, int code, const std::string& msg, uint64_t v0 = 0, uint64_t v1 = 0,
+            uint64_t v2 = 0, uint64_t v3 = 0) {
+  if (e) {
+    e->code = code;
+    e->v0 = v0; e->v1 = v1; e->v2 = v2; e->v3 = v3;
+    std::snprintf(e->msg, sizeof(e->msg), "%s", msg.c_str());
+  }
+  return code;
+}
+int ok(or_err* e) {
+  if (e) { e->code = 0; e->msg[0] = 0; }
+  return 0;
+}
+std::string dim_msg(uint64_t expected, uint64_t found) {
+  return "Dimension mismatch: expected " + std::to_string(expected) + ", found " +
+         std::to_string(found);
+}
+std::string value_msg(const std::string& s) { return "Value error: " + s; }
+std::string incons_msg(const std::string& s) { return "Inconsistent data: " + s; }
+
+// ------------------------------------------------------------------ CSR
+// CsrMatrix::new, scirs2-sparse/src/csr.rs:92-160.  The caller's single nnz
+// argument already implies equal lengths of data/rows/cols.
+template <class T>
+int csr_matrix_new(const T* data, const uint64_t* rows, const uint64_t* cols, uint64_t nnz,
+                   uint64_t nrows, uint64_t ncols, uint64_t* indptr, uint64_t* indices, T* out,
+                   or_err* err) {
+  for (uint64_t k = 0; k < nnz; ++k)
+    if (rows[k] >= nrows) return set_err(err, E_VALUE, value_msg("Row index out of bounds"));
+  for (uint64_t k = 0; k < nnz; ++k)
+    if (cols[k] >= ncols) return set_err(err, E_VALUE, value_msg("Column index out of bounds"));
+  // stable sort by (row, col): duplicates are kept in input order (csr.rs:129)
+  std::vector<uint64_t> perm(nnz);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [&](uint64_t a, uint64_t b) {
+    if (rows[a] != rows[b]) return rows[a] < rows[b];
+    return cols[a] < cols[b];
+  });
+  for (uint64_t i = 0; i <= nrows; ++i) indptr[i] = 0;
+  for (uint64_t k = 0; k < nnz; ++k) indptr[rows[k] + 1] += 1;
+  for (uint64_t i = 1; i <= nrows; ++i) indptr[i] += indptr[i - 1];
+  for (uint64_t k = 0; k < nnz; ++k) {
+    indices[k] = cols[perm[k]];
+    out[k] = data[perm[k]];
+  }
+  return ok(err);
+}
+
+// CsrMatrix::from_raw_csr validation, csr.rs:174-227 (the arrays are kept
+// as given).
+int csr_matrix_from_raw_check(const uint64_t* indptr, uint64_t indptr_len, const uint64_t* indices,
+                              uint64_t indices_len, uint64_t data_len, uint64_t nrows,
+                              uint64_t ncols, or_err* err) {
+  if (indptr_len != nrows + 1)
+    return set_err(err, E_DIMENSION_MISMATCH, dim_msg(nrows + 1, indptr_len), nrows + 1,
+                   indptr_len);
+  if (data_len != indices_len)
+    return set_err(err, E_DIMENSION_MISMATCH, dim_msg(data_len, indices_len), data_len,
+                   indices_len);
+  for (uint64_t i = 1; i < indptr_len; ++i)
+    if (indptr[i] < indptr[i - 1])
+      return set_err(err, E_VALUE,
+                     value_msg("Row pointer array must be monotonically increasing"));
+  if (indptr[nrows] != data_len)
+    return set_err(err, E_VALUE, value_msg("Last row pointer entry must match data length"));
+  for (uint64_t k = 0; k < indices_len; ++k)
+    if (indices[k] >= ncols) return set_err(err, E_VALUE, value_msg("Column index out of bounds"));
+  return ok(err);
+}
+
+// CsrArray::check_sorted_indices, csr_array.rs:221-233
+bool check_sorted_indices(const uint64_t* indices, uint64_t indices_len, const uint64_t* indptr,
+                          uint64_t indptr_len) {
+  for (uint64_t row = 0; row + 1 < indptr_len; ++row) {
+    uint64_t start = indptr[row], end = indptr[row + 1];
+    uint64_t stop = end > 0 ? end - 1 : 0;  // saturating_sub(1)
+    for (uint64_t i = start; i < stop; ++i)
+      if (i + 1 < indices_len && indices[i] > indices[i + 1]) return false;
+  }
+  return true;
+}
+
+// CsrArray::new validation, csr_array.rs:77-136
+int csr_array_new_check(const uint64_t* indptr, uint64_t indptr_len, const uint64_t* indices,
+                        uint64_t indices_len, uint64_t data_len, uint64_t nrows, uint64_t ncols,
+                        int* sorted, or_err* err) {
+  if (data_len != indices_len)
+    return set_err(err, E_INCONSISTENT_DATA,
+                   incons_msg("data and indices must have the same length"));
+  if (indptr_len != nrows + 1)
+    return set_err(err, E_INCONSISTENT_DATA,
+                   incons_msg("indptr length (" + std::to_string(indptr_len) +
+                              ") must be one more than the number of rows (" +
+                              std::to_string(nrows) + ")"));
+  if (indices_len > 0) {
+    uint64_t mx = 0;
+    for (uint64_t k = 0; k < indices_len; ++k) mx = std::max(mx, indices[k]);
+    if (mx >= ncols)
+      return set_err(err, E_INDEX_OUT_OF_BOUNDS,
+                     "Index (0, " + std::to_string(mx) + ") out of bounds for array with shape (" +
+                         std::to_string(nrows) + ", " + std::to_string(ncols) + ")",
+                     0, mx, nrows, ncols);
+  }
+  if (indptr_len > 0) {
+    uint64_t first = indptr[0], last = indptr[indptr_len - 1];
+    if (first != 0)
+      return set_err(err, E_INCONSISTENT_DATA, incons_msg("first element of indptr must be 0"));
+    if (last != data_len)
+      return set_err(err, E_INCONSISTENT_DATA,
+                     incons_msg("last element of indptr (" + std::to_string(last) +
+                                ") must equal data length (" + std::to_string(data_len) + ")"));
+  }
+  if (sorted) *sorted = check_sorted_indices(indices, indices_len, indptr, indptr_len) ? 1 : 0;
+  return ok(err);
+}
+
+// CsrArray::from_triplets, csr_array.rs:152-219
+template <class T>
+int csr_array_from_triplets(const uint64_t* rows, const uint64_t* cols, const T* data,
+                            uint64_t nnz, uint64_t nrows, uint64_t ncols, int sorted,
+                            uint64_t* indptr, uint64_t* indices, T* out, int* has_sorted,
+                            or_err* err) {
+  if (nnz == 0) {
+    for (uint64_t i = 0; i <= nrows; ++i) indptr[i] = 0;
+    return csr_array_new_check(indptr, nrows + 1, indices, 0, 0, nrows, ncols, has_sorted, err);
+  }
+  for (uint64_t k = 0; k < nnz; ++k)
+    if (rows[k] >= nrows || cols[k] >= ncols)
+      return set_err(err, E_INDEX_OUT_OF_BOUNDS,
+                     "Index (" + std::to_string(rows[k]) + ", " + std::to_string(cols[k]) +
+                         ") out of bounds for array with shape (" + std::to_string(nrows) + ", " +
+                         std::to_string(ncols) + ")",
+                     rows[k], cols[k], nrows, ncols);
+  std::vector<uint64_t> perm(nnz);
+  std::iota(perm.begin(), perm.end(), 0);
+  if (!sorted)
+    std::stable_sort(perm.begin(), perm.end(), [&](uint64_t a, uint64_t b) {
+      if (rows[a] != rows[b]) return rows[a] < rows[b];
+      return cols[a] < cols[b];
+    });
+  std::vector<uint64_t> counts(nrows, 0);
+  for (uint64_t k = 0; k < nnz; ++k) counts[rows[k]] += 1;
+  indptr[0] = 0;
+  uint64_t cum = 0;
+  for (uint64_t i = 0; i < nrows; ++i) { cum += counts[i]; indptr[i + 1] = cum; }
+  for (uint64_t k = 0; k < nnz; ++k) {
+    indices[k] = cols[perm[k]];
+    out[k] = data[perm[k]];
+  }
+  return csr_array_new_check(indptr, nrows + 1, indices, nnz, nnz, nrows, ncols, has_sorted, err);
+}
+
+// CsrMatrix::transpose (counting sort), csr.rs:289-326.  Column counts run
+// over the whole indices array, exactly as the reference does, and slots no
+// row range reaches keep (0, 0).  CsrArray::transpose (csr_array.rs:595-625)
+// produces the same arrays through a stable sort of swapped triplets.
+template <class T>
+void csr_transpose(const uint64_t* indptr, const uint64_t* indices, const T* data, uint64_t nrows,
+                   uint64_t ncols, uint64_t* indptr_t, uint64_t* indices_t, T* data_t) {
+  // The reference counts over indices.len(), which equals indptr[nrows] for
+  // every matrix its constructors accept (from_raw_csr checks last == len).
+  std::vector<uint64_t> counts(ncols, 0);
+  for (uint64_t k = 0; k < indptr[nrows]; ++k) counts[indices[k]] += 1;
+  indptr_t[0] = 0;
+  for (uint64_t c = 0; c < ncols; ++c) indptr_t[c + 1] = indptr_t[c] + counts[c];
+  uint64_t total = indptr_t[ncols];
+  for (uint64_t k = 0; k < total; ++k) { indices_t[k] = 0; data_t[k] = T(0); }
+  std::fill(counts.begin(), counts.end(), 0);
+  for (uint64_t r = 0; r < nrows; ++r)
+    for (uint64_t k = indptr[r]; k < indptr[r + 1]; ++k) {
+      uint64_t c = indices[k];
+      uint64_t dst = indptr_t[c] + counts[c];
+      indices_t[dst] = r;
+      data_t[dst] = data[k];
+      counts[c] += 1;
+    }
+}
+
+// CsrMatrix::get, csr.rs:33-48: first match in storage order
+template <class T>
+T csr_get(const uint64_t* indptr, const uint64_t* indices, const T* data, uint64_t nrows,
+          uint64_t ncols, uint64_t i, uint64_t j) {
+  if (i >= nrows || j >= ncols) return T(0);
+  for (uint64_t k = indptr[i]; k < indptr[i + 1]; ++k)
+    if (indices[k] == j) return data[k];
+  return T(0);
+}
+
+// CsrArray::dot_vector (csr_array.rs:569-593), CsrMatrix::dot (csr.rs:479-497)
+// and MatrixLinearOperator::matvec (interface.rs:257-279) are the same loop:
+// sum starts at zero, then sum = sum + a*x in storage order.  A row whose
+// end precedes its start (possible through CsrArray::new) is empty.
+template <class T, class IP, class IX>
+void spmv(const IP* indptr, const IX* indices, const T* data, uint64_t nrows, const T* x, T* y) {
+  for (uint64_t i = 0; i < nrows; ++i) {
+    T sum = T(0);
+    for (IP k = indptr[i]; k < indptr[i + 1]; ++k) sum = sum + data[k] * x[indices[k]];
+    y[i] = sum;
+  }
+}
+
+// iterative.rs:827-834: `.sum()` of f32/f64 folds from -0.0 in current Rust
+template <class F>
+F dot(const std::vector<F>& a, const std::vector<F>& b) {
+  F s = F(-0.0);
+  for (size_t i = 0; i < a.size(); ++i) s = s + a[i] * b[i];
+  return s;
+}
+template <class F>
+F norm2(const std::vector<F>& a) {
+  return std::sqrt(dot(a, a));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- operators
+struct or_op {
+  virtual ~or_op() {}
+  int f64 = 1;
+  uint64_t nrows = 0, ncols = 0;
+  virtual void mv64(const double* x, double* y) const = 0;
+  virtual void mv32(const float* x, float* y) const = 0;
+};
+
+namespace {
+
+template <class F>
+void op_matvec(const or_op* op, const F* x, F* y);
+template <>
+void op_matvec<double>(const or_op* op, const double* x, double* y) { op->mv64(x, y); }
+template <>
+void op_matvec<float>(const or_op* op, const float* x, float* y) { op->mv32(x, y); }
+
+template <class F>
+std::vector<F> op_apply(const or_op* op, const std::vector<F>& x) {
+  std::vector<F> y(op->nrows);
+  op_matvec<F>(op, x.data(), y.data());
+  return y;
+}
+
+// MatrixLinearOperator<F, CsrMatrix<F>> (interface.rs:232-296)
+struct CsrOp : or_op {
+  std::vector<uint64_t> indptr, indices;
+  std::vector<double> d64;
+  std::vector<float> d32;
+  void mv64(const double* x, double* y) const override {
+    spmv<double>(indptr.data(), indices.data(), d64.data(), nrows, x, y);
+  }
+  void mv32(const float* x, float* y) const override {
+    spmv<float>(indptr.data(), indices.data(), d32.data(), nrows, x, y);
+  }
+};
+
+// IdentityOperator (interface.rs:55-93)
+struct IdentityOp : or_op {
+  void mv64(const double* x, double* y) const override { std::memcpy(y, x, nrows * 8); }
+  void mv32(const float* x, float* y) const override { std::memcpy(y, x, nrows * 4); }
+};
+
+// ScaledIdentityOperator (interface.rs:95-130): x_i * scale
+struct ScaledIdentityOp : or_op {
+  double s64 = 1; float s32 = 1;
+  void mv64(const double* x, double* y) const override {
+    for (uint64_t i = 0; i < nrows; ++i) y[i] = x[i] * s64;
+  }
+  void mv32(const float* x, float* y) const override {
+    for (uint64_t i = 0; i < nrows; ++i) y[i] = x[i] * s32;
+  }
+};
+
+// DiagonalOperator (interface.rs:132-175) and the apply of
+// JacobiPreconditioner (preconditioners.rs:64-82): y_i = x_i * d_i
+struct DiagOp : or_op {
+  std::vector<double> d64;
+  std::vector<float> d32;
+  void mv64(const double* x, double* y) const override {
+    for (uint64_t i = 0; i < nrows; ++i) y[i] = x[i] * d64[i];
+  }
+  void mv32(const float* x, float* y) const override {
+    for (uint64_t i = 0; i < nrows; ++i) y[i] = x[i] * d32[i];
+  }
+};
+
+// IC0Preconditioner (ic.rs:15-230)
+template <class F>
+struct IC0Data {
+  std::vector<uint64_t> indptr, indices;
+  std::vector<F> data;
+  // transposed factor for the backward solve: for column i, the rows j > i
+  // whose FIRST entry with column i is taken (ic.rs:199-214 breaks at it)
+  std::vector<uint64_t> tptr, trow;
+  std::vector<F> tval;
+  std::vector<F> diag_first;  // first diagonal entry per row (ic.rs:185-191)
+};
+
+template <class F>
+int ic0_factor(const CsrOp* a, IC0Data<F>& L, or_err* err) {
+  const uint64_t n = a->nrows;
+  if (n != a->ncols)
+    return set_err(err, E_DIMENSION_MISMATCH, dim_msg(n, a->ncols), n, a->ncols);
+  const F* ad = nullptr;
+  if constexpr (sizeof(F) == 8) ad = a->d64.data(); else ad = a->d32.data();
+  // lower-triangular copy in storage order (ic.rs:32-49)
+  L.indptr.assign(1, 0);
+  for (uint64_t i = 0; i < n; ++i) {
+    for (uint64_t k = a->indptr[i]; k < a->indptr[i + 1]; ++k) {
+      uint64_t j = a->indices[k];
+      if (j <= i) { L.indices.push_back(j); L.data.push_back(ad[k]); }
+    }
+    L.indptr.push_back(L.indices.size());
+  }
+  auto& li = L.indices;
+  auto& ld = L.data;
+  auto& lp = L.indptr;
+  // factorisation loop (ic.rs:52-129)
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t rs = lp[i], re = lp[i + 1];
+    uint64_t di = UINT64_MAX;
+    for (uint64_t k = rs; k < re; ++k)
+      if (li[k] == i) { di = k; break; }
+    if (di == UINT64_MAX)
+      return set_err(err, E_VALUE,
+                     value_msg("Missing diagonal element at position " + std::to_string(i)));
+    F dv = ld[di];
+    for (uint64_t k = rs; k < di; ++k) {
+      uint64_t j = li[k];
+      F ljj = F(0);
+      for (uint64_t q = lp[j]; q < lp[j + 1]; ++q)
+        if (li[q] == j) { ljj = ld[q]; break; }
+      dv -= ld[k] * ld[k] / ljj;
+    }
+    if (dv <= F(0))
+      return set_err(err, E_VALUE,
+                     value_msg("Matrix is not positive definite or factorization broke down"));
+    ld[di] = std::sqrt(dv);
+    for (uint64_t k = di + 1; k < re; ++k) {
+      uint64_t j = li[k];
+      F sum = F(0);
+      for (uint64_t p = rs; p < di; ++p) {
+        uint64_t cp = li[p];
+        for (uint64_t q = lp[j]; q < lp[j + 1]; ++q)
+          if (li[q] == cp) { sum += ld[p] * ld[q]; break; }
+      }
+      ld[k] = (ld[k] - sum) / ld[di];
+    }
+  }
+  // CsrMatrix::from_raw_csr on the factor (ic.rs:132) cannot fail here:
+  // indptr is monotone by construction and every column is <= its row.
+  // Backward-solve helpers.
+  L.diag_first.assign(n, F(1));
+  for (uint64_t i = 0; i < n; ++i)
+    for (uint64_t k = lp[i]; k < lp[i + 1]; ++k)
+      if (li[k] == i) { L.diag_first[i] = ld[k]; break; }
+  std::vector<uint64_t> cnt(n + 1, 0);
+  std::vector<char> seen;
+  // first occurrence of (row j, column c) for c < j
+  std::vector<uint64_t> first_k;
+  for (uint64_t j = 0; j < n; ++j) {
+    for (uint64_t k = lp[j]; k < lp[j + 1]; ++k) {
+      uint64_t c = li[k];
+      if (c >= j) continue;
+      bool dup = false;
+      for (uint64_t q = lp[j]; q < k; ++q)
+        if (li[q] == c) { dup = true; break; }
+      if (!dup) { cnt[c + 1] += 1; first_k.push_back(k); }
+    }
+  }
+  for (uint64_t c = 0; c < n; ++c) cnt[c + 1] += cnt[c];
+  L.tptr = cnt;
+  L.trow.assign(cnt[n], 0);
+  L.tval.assign(cnt[n], F(0));
+  std::vector<uint64_t> fill(n, 0);
+  // first_k is in ascending row order, so each column list is ascending in j
+  uint64_t fk = 0;
+  for (uint64_t j = 0; j < n; ++j) {
+    for (uint64_t k = lp[j]; k < lp[j + 1]; ++k) {
+      if (fk < first_k.size() && first_k[fk] == k) {
+        uint64_t c = li[k];
+        uint64_t dst = L.tptr[c] + fill[c]++;
+        L.trow[dst] = j;
+        L.tval[dst] = ld[k];
+        ++fk;
+      }
+    }
+  }
+  return ok(err);
+}
+
+template <class F>
+void ic0_apply(const IC0Data<F>& L, uint64_t n, const F* x, F* y, bool fast) {
+  // forward solve L z = x (ic.rs:154-174): the LAST diagonal entry wins
+  std::vector<F> z(n, F(0));
+  for (uint64_t i = 0; i < n; ++i) {
+    F sum = x[i];
+    F dv = F(1);
+    for (uint64_t k = L.indptr[i]; k < L.indptr[i + 1]; ++k) {
+      uint64_t j = L.indices[k];
+      F v = L.data[k];
+      if (j < i) sum -= v * z[j];
+      else if (j == i) dv = v;
+    }
+    z[i] = sum / dv;
+  }
+  // backward solve L^T y = z (ic.rs:177-217): first diagonal entry; for each
+  // j > i in ascending order, the first entry of row j in column i
+  for (uint64_t ii = n; ii-- > 0;) {
+    F sum = z[ii];
+    if (fast) {
+      for (uint64_t t = L.tptr[ii]; t < L.tptr[ii + 1]; ++t) sum -= L.tval[t] * y[L.trow[t]];
+    } else {
+      for (uint64_t j = ii + 1; j < n; ++j)
+        for (uint64_t k = L.indptr[j]; k < L.indptr[j + 1]; ++k)
+          if (L.indices[k] == ii) { sum -= L.data[k] * y[j]; break; }
+    }
+    y[ii] = sum / L.diag_first[ii];
+  }
+}
+
+struct IC0Op : or_op {
+  IC0Data<double> l64;
+  IC0Data<float> l32;
+  bool fast = true;
+  void mv64(const double* x, double* y) const override { ic0_apply(l64, nrows, x, y, fast); }
+  void mv32(const float* x, float* y) const override { ic0_apply(l32, nrows, x, y, fast); }
+};
+
+// M^-1 = G G^T: y = G (G^T x), G^T kept explicitly through the counting-sort
+// transpose; both products are plain CSR SpMVs.
+struct FsaiOp : or_op {
+  std::vector<uint64_t> gp, gi, tp, ti;
+  std::vector<double> g64, t64;
+  std::vector<float> g32, t32;
+  void mv64(const double* x, double* y) const override {
+    std::vector<double> w(nrows);
+    spmv<double>(tp.data(), ti.data(), t64.data(), nrows, x, w.data());
+    spmv<double>(gp.data(), gi.data(), g64.data(), nrows, w.data(), y);
+  }
+  void mv32(const float* x, float* y) const override {
+    std::vector<float> w(nrows);
+    spmv<float>(tp.data(), ti.data(), t32.data(), nrows, x, w.data());
+    spmv<float>(gp.data(), gi.data(), g32.data(), nrows, w.data(), y);
+  }
+};
+
+// ------------------------------------------------------------------ solvers
+template <class F>
+struct SolveOut {
+  std::vector<F> x;
+  uint64_t iterations = 0;
+  F residual_norm = F(0);
+  bool converged = false;
+  int message = M_MAX_ITER;
+};
+
+template <class F>
+F eps10() { return std::numeric_limits<F>::epsilon() * F(10); }
+
+// cg, iterative.rs:40-162
+template <class F>
+SolveOut<F> cg(const or_op* a, const std::vector<F>& b, uint64_t max_iter, F rtol, F atol,
+               const F* x0, const or_op* m) {
+  const uint64_t n = a->nrows;
+  SolveOut<F> o;
+  std::vector<F> x(n, F(0));
+  if (x0) x.assign(x0, x0 + n);
+  std::vector<F> ax = op_apply(a, x);
+  std::vector<F> r(n);
+  for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - ax[i];
+  std::vector<F> z = m ? op_apply(m, r) : r;
+  std::vector<F> p = z;
+  F rz_old = dot(r, z);
+  F bnorm = norm2(b);
+  F tol = std::fmax(atol, rtol * bnorm);
+  uint64_t it = 0;
+  while (it < max_iter) {
+    std::vector<F> ap = op_apply(a, p);
+    F pap = dot(p, ap);
+    if (pap <= F(0)) {
+      o.x = x; o.iterations = it; o.residual_norm = norm2(r); o.converged = false;
+      o.message = M_NOT_PD;
+      return o;
+    }
+    F alpha = rz_old / pap;
+    for (uint64_t i = 0; i < n; ++i) x[i] += alpha * p[i];
+    for (uint64_t i = 0; i < n; ++i) r[i] -= alpha * ap[i];
+    F rnorm = norm2(r);
+    if (rnorm <= tol) {
+      o.x = x; o.iterations = it + 1; o.residual_norm = rnorm; o.converged = true;
+      o.message = M_CONVERGED;
+      return o;
+    }
+    z = m ? op_apply(m, r) : r;
+    F rz_new = dot(r, z);
+    F beta = rz_new / rz_old;
+    for (uint64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    rz_old = rz_new;
+    ++it;
+  }
+  o.x = x; o.iterations = it; o.residual_norm = norm2(r); o.converged = false;
+  o.message = M_MAX_ITER;
+  return o;
+}
+
+// bicgstab, iterative.rs:377-611 (left preconditioner M1 applied to p and
+// s; right preconditioner M2 applied to v, t and to x every iteration)
+template <class F>
+SolveOut<F> bicgstab(const or_op* a, const std::vector<F>& b, uint64_t max_iter, F rtol, F atol,
+                     const F* x0, const or_op* m1, const or_op* m2) {
+  const uint64_t n = a->nrows;
+  SolveOut<F> o;
+  std::vector<F> x(n, F(0));
+  if (x0) x.assign(x0, x0 + n);
+  std::vector<F> ax = op_apply(a, x);
+  std::vector<F> r(n);
+  for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - ax[i];
+  F rnorm = norm2(r);
+  F bnorm = norm2(b);
+  F tol = std::fmax(atol, rtol * bnorm);
+  auto finish = [&](uint64_t it, F res, bool conv, int msg) {
+    o.x = x; o.iterations = it; o.residual_norm = res; o.converged = conv; o.message = msg;
+    return o;
+  };
+  if (rnorm <= tol) return finish(0, rnorm, true, M_CONVERGED_INITIAL);
+  std::vector<F> r_hat = r;
+  std::vector<F> v(n, F(0)), p(n, F(0)), y(n, F(0)), s(n, F(0)), t;
+  F rho_old = F(1), alpha = F(0), omega = F(1);
+  uint64_t it = 0;
+  const F e10 = eps10<F>();
+  while (it < max_iter) {
+    F rho = dot(r_hat, r);
+    if (std::fabs(rho) < e10) return finish(it, rnorm, false, M_BD_RHO);
+    F beta = (rho / rho_old) * (alpha / omega);
+    for (uint64_t i = 0; i < n; ++i) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+    std::vector<F> p_t = m1 ? op_apply(m1, p) : p;
+    v = op_apply(a, p_t);
+    if (m2) v = op_apply(m2, v);
+    F den = dot(r_hat, v);
+    if (std::fabs(den) < e10) return finish(it, rnorm, false, M_BD_RHAT_V);
+    alpha = rho / den;
+    if (!std::isfinite(alpha)) return finish(it, rnorm, false, M_BD_ALPHA);
+    for (uint64_t i = 0; i < n; ++i) {
+      y[i] = x[i] + alpha * p_t[i];
+      s[i] = r[i] - alpha * v[i];
+    }
+    F snorm = norm2(s);
+    if (snorm <= tol) {
+      x = y;
+      if (m2) x = op_apply(m2, x);
+      return finish(it + 1, snorm, true, M_CONVERGED);
+    }
+    std::vector<F> s_t = m1 ? op_apply(m1, s) : s;
+    t = op_apply(a, s_t);
+    if (m2) t = op_apply(m2, t);
+    F ts = dot(t, s);
+    F tt = dot(t, t);
+    if (tt < e10) return finish(it, rnorm, false, M_BD_TT);
+    omega = ts / tt;
+    if (!std::isfinite(omega) || std::fabs(omega) < e10)
+      return finish(it, rnorm, false, M_BD_OMEGA);
+    for (uint64_t i = 0; i < n; ++i) {
+      x[i] = y[i] + omega * s_t[i];
+      r[i] = s[i] - omega * t[i];
+    }
+    if (m2) x = op_apply(m2, x);
+    rnorm = norm2(r);
+    if (rnorm <= tol) return finish(it + 1, rnorm, true, M_CONVERGED);
+    rho_old = rho;
+    ++it;
+  }
+  return finish(it, rnorm, false, M_MAX_ITER);
+}
+
+// gmres, iterative.rs:641-816: left-preconditioned restarted GMRES with
+// modified Gram-Schmidt and Givens rotations.  On a happy breakdown the
+// column being built is dropped (the loop breaks before the rotation and
+// before inner_iter is advanced).
+template <class F>
+SolveOut<F> gmres(const or_op* a, const std::vector<F>& b, uint64_t max_iter, uint64_t restart_opt,
+                  F rtol, F atol, const F* x0, const or_op* m) {
+  const uint64_t n = a->nrows;
+  const uint64_t restart = std::min(restart_opt, n);
+  SolveOut<F> o;
+  std::vector<F> x(n, F(0));
+  if (x0) x.assign(x0, x0 + n);
+  std::vector<F> ax = op_apply(a, x);
+  std::vector<F> r(n);
+  for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - ax[i];
+  if (m) r = op_apply(m, r);
+  F rnorm = norm2(r);
+  F bnorm = norm2(b);
+  F tol = std::fmax(atol, rtol * bnorm);
+  uint64_t outer = 0;
+  const F e10 = eps10<F>();
+  while (outer < max_iter && rnorm > tol) {
+    std::vector<std::vector<F>> v(restart + 1, std::vector<F>(n, F(0)));
+    std::vector<std::vector<F>> h(restart + 1, std::vector<F>(restart, F(0)));
+    std::vector<F> cs(restart, F(0)), sn(restart, F(0)), s(restart + 1, F(0));
+    for (uint64_t i = 0; i < n; ++i) v[0][i] = r[i] / rnorm;
+    s[0] = rnorm;
+    uint64_t j = 0;
+    while (j < restart && j + outer < max_iter) {
+      std::vector<F> w = op_apply(a, v[j]);
+      if (m) w = op_apply(m, w);
+      for (uint64_t i = 0; i <= j; ++i) {
+        h[i][j] = dot(v[i], w);
+        for (uint64_t k = 0; k < n; ++k) w[k] -= h[i][j] * v[i][k];
+      }
+      h[j + 1][j] = norm2(w);
+      if (h[j + 1][j] < e10) break;
+      for (uint64_t k = 0; k < n; ++k) v[j + 1][k] = w[k] / h[j + 1][j];
+      for (uint64_t i = 0; i < j; ++i) {
+        F temp = cs[i] * h[i][j] + sn[i] * h[i + 1][j];
+        h[i + 1][j] = -sn[i] * h[i][j] + cs[i] * h[i + 1][j];
+        h[i][j] = temp;
+      }
+      F rho = std::sqrt(h[j][j] * h[j][j] + h[j + 1][j] * h[j + 1][j]);
+      cs[j] = h[j][j] / rho;
+      sn[j] = h[j + 1][j] / rho;
+      h[j][j] = rho;
+      h[j + 1][j] = F(0);
+      F temp = cs[j] * s[j] + sn[j] * s[j + 1];
+      s[j + 1] = -sn[j] * s[j] + cs[j] * s[j + 1];
+      s[j] = temp;
+      ++j;
+      if (std::fabs(s[j]) <= tol) break;
+    }
+    std::vector<F> yv(j, F(0));
+    for (uint64_t ii = j; ii-- > 0;) {
+      yv[ii] = s[ii];
+      for (uint64_t q = ii + 1; q < j; ++q) yv[ii] = yv[ii] - h[ii][q] * yv[q];
+      yv[ii] /= h[ii][ii];
+    }
+    for (uint64_t ii = 0; ii < j; ++ii)
+      for (uint64_t k = 0; k < n; ++k) x[k] += yv[ii] * v[ii][k];
+    ax = op_apply(a, x);
+    for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - ax[i];
+    if (m) r = op_apply(m, r);
+    rnorm = norm2(r);
+    outer += j;
+    if (rnorm <= tol) break;
+  }
+  o.x = x;
+  o.iterations = outer;
+  o.residual_norm = rnorm;
+  o.converged = rnorm <= tol;
+  o.message = o.converged ? M_CONVERGED : M_MAX_ITER;
+  return o;
+}
+
+template <class F>
+void fill_result(const SolveOut<F>& s, void* x_out, or_result* res) {
+  std::memcpy(x_out, s.x.data(), s.x.size() * sizeof(F));
+  if (res) {
+    res->iterations = s.iterations;
+    res->residual_norm = (double)s.residual_norm;
+    res->converged = s.converged ? 1 : 0;
+    res->message = s.message;
+  }
+}
+
+template <class F>
+int check_square_and_len(const or_op* a, const char* solver, or_err* err) {
+  if (a->nrows != a->ncols)
+    return set_err(err, E_VALUE,
+                   value_msg(std::string("Matrix must be square for ") + solver + " solver"));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_csr_matrix_new_f64(const double* data, const uint64_t* rows, const uint64_t* cols,
+                          uint64_t nnz, uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
+                          uint64_t* indices_out, double* data_out, or_err* err) {
+  return csr_matrix_new<double>(data, rows, cols, nnz, nrows, ncols, indptr_out, indices_out,
+                                data_out, err);
+}
+int or_csr_matrix_new_f32(const float* data, const uint64_t* rows, const uint64_t* cols,
+                          uint64_t nnz, uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
+                          uint64_t* indices_out, float* data_out, or_err* err) {
+  return csr_matrix_new<float>(data, rows, cols, nnz, nrows, ncols, indptr_out, indices_out,
+                               data_out, err);
+}
+int or_csr_matrix_from_raw_check(const uint64_t* indptr, uint64_t indptr_len,
+                                 const uint64_t* indices, uint64_t indices_len, uint64_t data_len,
+                                 uint64_t nrows, uint64_t ncols, or_err* err) {
+  return csr_matrix_from_raw_check(indptr, indptr_len, indices, indices_len, data_len, nrows,
+                                   ncols, err);
+}
+int or_csr_array_new_check(const uint64_t* indptr, uint64_t indptr_len, const uint64_t* indices,
+                           uint64_t indices_len, uint64_t data_len, uint64_t nrows,
+                           uint64_t ncols, int* has_sorted_indices, or_err* err) {
+  return csr_array_new_check(indptr, indptr_len, indices, indices_len, data_len, nrows, ncols,
+                             has_sorted_indices, err);
+}
+int or_csr_array_from_triplets_f64(const uint64_t* rows, const uint64_t* cols,
+                                   const double* data, uint64_t nnz, uint64_t nrows,
+                                   uint64_t ncols, int sorted, uint64_t* indptr_out,
+                                   uint64_t* indices_out, double* data_out,
+                                   int* has_sorted_indices, or_err* err) {
+  return csr_array_from_triplets<double>(rows, cols, data, nnz, nrows, ncols, sorted, indptr_out,
+                                         indices_out, data_out, has_sorted_indices, err);
+}
+int or_csr_array_from_triplets_f32(const uint64_t* rows, const uint64_t* cols, const float* data,
+                                   uint64_t nnz, uint64_t nrows, uint64_t ncols, int sorted,
+                                   uint64_t* indptr_out, uint64_t* indices_out, float* data_out,
+                                   int* has_sorted_indices, or_err* err) {
+  return csr_array_from_triplets<float>(rows, cols, data, nnz, nrows, ncols, sorted, indptr_out,
+                                        indices_out, data_out, has_sorted_indices, err);
+}
+void or_csr_transpose_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                          uint64_t nrows, uint64_t ncols, uint64_t* indptr_t,
+                          uint64_t* indices_t, double* data_t) {
+  csr_transpose<double>(indptr, indices, data, nrows, ncols, indptr_t, indices_t, data_t);
+}
+void or_csr_transpose_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                          uint64_t nrows, uint64_t ncols, uint64_t* indptr_t,
+                          uint64_t* indices_t, float* data_t) {
+  csr_transpose<float>(indptr, indices, data, nrows, ncols, indptr_t, indices_t, data_t);
+}
+double or_csr_get_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                      uint64_t nrows, uint64_t ncols, uint64_t i, uint64_t j) {
+  return csr_get<double>(indptr, indices, data, nrows, ncols, i, j);
+}
+void or_spmv_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                 uint64_t nrows, const double* x, double* y) {
+  spmv<double>(indptr, indices, data, nrows, x, y);
+}
+void or_spmv_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                 uint64_t nrows, const float* x, float* y) {
+  spmv<float>(indptr, indices, data, nrows, x, y);
+}
+void or_spmv_i32_f64(const int64_t* indptr, const int32_t* indices, const double* data,
+                     int64_t nrows, const double* x, double* y) {
+  spmv<double>(indptr, indices, data, (uint64_t)nrows, x, y);
+}
+void or_spmv_i32_f32(const int64_t* indptr, const int32_t* indices, const float* data,
+                     int64_t nrows, const float* x, float* y) {
+  spmv<float>(indptr, indices, data, (uint64_t)nrows, x, y);
+}
+
+or_op* or_op_csr(int f64, const uint64_t* indptr, const uint64_t* indices, const void* data,
+                 uint64_t nrows, uint64_t ncols) {
+  auto* op = new CsrOp();
+  op->f64 = f64; op->nrows = nrows; op->ncols = ncols;
+  op->indptr.assign(indptr, indptr + nrows + 1);
+  uint64_t nnz = indptr[nrows];
+  op->indices.assign(indices, indices + nnz);
+  if (f64) {
+    const double* d = (const double*)data;
+    op->d64.assign(d, d + nnz);
+    op->d32.resize(nnz);
+    for (uint64_t k = 0; k < nnz; ++k) op->d32[k] = (float)d[k];
+  } else {
+    const float* d = (const float*)data;
+    op->d32.assign(d, d + nnz);
+    op->d64.resize(nnz);
+    for (uint64_t k = 0; k < nnz; ++k) op->d64[k] = (double)d[k];
+  }
+  return op;
+}
+or_op* or_op_csr_i32(int f64, const int64_t* indptr, const int32_t* indices, const void* data,
+                     int64_t nrows, int64_t ncols) {
+  std::vector<uint64_t> p(nrows + 1), ix(indptr[nrows]);
+  for (int64_t i = 0; i <= nrows; ++i) p[i] = (uint64_t)indptr[i];
+  for (int64_t k = 0; k < indptr[nrows]; ++k) ix[k] = (uint64_t)indices[k];
+  return or_op_csr(f64, p.data(), ix.data(), data, nrows, ncols);
+}
+or_op* or_op_identity(int f64, uint64_t n) {
+  auto* op = new IdentityOp();
+  op->f64 = f64; op->nrows = op->ncols = n;
+  return op;
+}
+or_op* or_op_scaled_identity(int f64, uint64_t n, double scale) {
+  auto* op = new ScaledIdentityOp();
+  op->f64 = f64; op->nrows = op->ncols = n;
+  op->s64 = scale; op->s32 = (float)scale;
+  return op;
+}
+or_op* or_op_diagonal(int f64, const void* diag, uint64_t n) {
+  auto* op = new DiagOp();
+  op->f64 = f64; op->nrows = op->ncols = n;
+  op->d64.resize(n); op->d32.resize(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    if (f64) { op->d64[i] = ((const double*)diag)[i]; op->d32[i] = (float)op->d64[i]; }
+    else { op->d32[i] = ((const float*)diag)[i]; op->d64[i] = op->d32[i]; }
+  }
+  return op;
+}
+
+// JacobiPreconditioner::new / from_diagonal, preconditioners.rs:21-62
+or_op* or_op_jacobi(const or_op* csr_base, or_err* err) {
+  const CsrOp* a = dynamic_cast<const CsrOp*>(csr_base);
+  if (!a) { set_err(err, E_NOT_SUPPORTED, "Operation not supported: not a CSR operator"); return nullptr; }
+  auto* op = new DiagOp();
+  op->f64 = a->f64; op->nrows = op->ncols = a->nrows;
+  op->d64.resize(a->nrows); op->d32.resize(a->nrows);
+  for (uint64_t i = 0; i < a->nrows; ++i) {
+    if (a->f64) {
+      double d = csr_get<double>(a->indptr.data(), a->indices.data(), a->d64.data(), a->nrows,
+                                 a->ncols, i, i);
+      if (std::fabs(d) < std::numeric_limits<double>::epsilon()) {
+        delete op;
+        set_err(err, E_VALUE, value_msg("Zero diagonal element at position " + std::to_string(i)));
+        return nullptr;
+      }
+      op->d64[i] = 1.0 / d;
+      op->d32[i] = (float)op->d64[i];
+    } else {
+      float d = csr_get<float>(a->indptr.data(), a->indices.data(), a->d32.data(), a->nrows,
+                               a->ncols, i, i);
+      if (std::fabs(d) < std::numeric_limits<float>::epsilon()) {
+        delete op;
+        set_err(err, E_VALUE, value_msg("Zero diagonal element at position " + std::to_string(i)));
+        return nullptr;
+      }
+      op->d32[i] = 1.0f / d;
+      op->d64[i] = op->d32[i];
+    }
+  }
+  ok(err);
+  return op;
+}
+or_op* or_op_jacobi_from_diagonal(int f64, const void* diag, uint64_t n, or_err* err) {
+  auto* op = new DiagOp();
+  op->f64 = f64; op->nrows = op->ncols = n;
+  op->d64.resize(n); op->d32.resize(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    if (f64) {
+      double d = ((const double*)diag)[i];
+      if (std::fabs(d) < std::numeric_limits<double>::epsilon()) {
+        delete op;
+        set_err(err, E_VALUE, value_msg("Zero diagonal element at position " + std::to_string(i)));
+        return nullptr;
+      }
+      op->d64[i] = 1.0 / d; op->d32[i] = (float)op->d64[i];
+    } else {
+      float d = ((const float*)diag)[i];
+      if (std::fabs(d) < std::numeric_limits<float>::epsilon()) {
+        delete op;
+        set_err(err, E_VALUE, value_msg("Zero diagonal element at position " + std::to_string(i)));
+        return nullptr;
+      }
+      op->d32[i] = 1.0f / d; op->d64[i] = op->d32[i];
+    }
+  }
+  ok(err);
+  return op;
+}
+
+or_op* or_op_ic0(const or_op* csr_base, int fast, or_err* err) {
+  const CsrOp* a = dynamic_cast<const CsrOp*>(csr_base);
+  if (!a) { set_err(err, E_NOT_SUPPORTED, "Operation not supported: not a CSR operator"); return nullptr; }
+  auto* op = new IC0Op();
+  op->f64 = a->f64; op->nrows = op->ncols = a->nrows; op->fast = fast != 0;
+  int rc = a->f64 ? ic0_factor<double>(a, op->l64, err) : ic0_factor<float>(a, op->l32, err);
+  if (rc) { delete op; return nullptr; }
+  return op;
+}
+
+uint64_t or_ic0_nnz(const or_op* base) {
+  const IC0Op* op = dynamic_cast<const IC0Op*>(base);
+  if (!op) return 0;
+  return op->f64 ? op->l64.indices.size() : op->l32.indices.size();
+}
+void or_ic0_factor(const or_op* base, uint64_t* indptr, uint64_t* indices, void* data) {
+  const IC0Op* op = dynamic_cast<const IC0Op*>(base);
+  if (!op) return;
+  if (op->f64) {
+    std::copy(op->l64.indptr.begin(), op->l64.indptr.end(), indptr);
+    std::copy(op->l64.indices.begin(), op->l64.indices.end(), indices);
+    std::memcpy(data, op->l64.data.data(), op->l64.data.size() * 8);
+  } else {
+    std::copy(op->l32.indptr.begin(), op->l32.indptr.end(), indptr);
+    std::copy(op->l32.indices.begin(), op->l32.indices.end(), indices);
+    std::memcpy(data, op->l32.data.data(), op->l32.data.size() * 4);
+  }
+}
+
+or_op* or_op_fsai(const or_op* g_base) {
+  const CsrOp* g = dynamic_cast<const CsrOp*>(g_base);
+  if (!g) return nullptr;
+  auto* op = new FsaiOp();
+  op->f64 = g->f64; op->nrows = op->ncols = g->nrows;
+  op->gp = g->indptr; op->gi = g->indices; op->g64 = g->d64; op->g32 = g->d32;
+  uint64_t nnz = g->indptr[g->nrows];
+  op->tp.resize(g->ncols + 1); op->ti.resize(nnz); op->t64.resize(nnz); op->t32.resize(nnz);
+  csr_transpose<double>(g->indptr.data(), g->indices.data(), g->d64.data(), g->nrows, g->ncols,
+                        op->tp.data(), op->ti.data(), op->t64.data());
+  std::vector<uint64_t> tp2(g->ncols + 1), ti2(nnz);
+  csr_transpose<float>(g->indptr.data(), g->indices.data(), g->d32.data(), g->nrows, g->ncols,
+                       tp2.data(), ti2.data(), op->t32.data());
+  return op;
+}
+
+void or_op_destroy(or_op* op) { delete op; }
+uint64_t or_op_rows(const or_op* op) { return op->nrows; }
+int or_op_matvec(const or_op* op, const void* x, void* y) {
+  if (op->f64) op->mv64((const double*)x, (double*)y);
+  else op->mv32((const float*)x, (float*)y);
+  return 0;
+}
+
+int or_cg(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+          const void* x0, const or_op* m, void* x_out, or_result* res, or_err* err) {
+  if (int rc = check_square_and_len<double>(a, "CG", err)) return rc;
+  const uint64_t n = a->nrows;
+  if (a->f64) {
+    std::vector<double> bv((const double*)b, (const double*)b + n);
+    auto s = cg<double>(a, bv, max_iter, rtol, atol, (const double*)x0, m);
+    fill_result(s, x_out, res);
+  } else {
+    std::vector<float> bv((const float*)b, (const float*)b + n);
+    auto s = cg<float>(a, bv, max_iter, (float)rtol, (float)atol, (const float*)x0, m);
+    fill_result(s, x_out, res);
+  }
+  return ok(err);
+}
+
+int or_bicgstab(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+                const void* x0, const or_op* m1, const or_op* m2, void* x_out, or_result* res,
+                or_err* err) {
+  if (int rc = check_square_and_len<double>(a, "BiCGSTAB", err)) return rc;
+  const uint64_t n = a->nrows;
+  if (a->f64) {
+    std::vector<double> bv((const double*)b, (const double*)b + n);
+    auto s = bicgstab<double>(a, bv, max_iter, rtol, atol, (const double*)x0, m1, m2);
+    fill_result(s, x_out, res);
+  } else {
+    std::vector<float> bv((const float*)b, (const float*)b + n);
+    auto s = bicgstab<float>(a, bv, max_iter, (float)rtol, (float)atol, (const float*)x0, m1, m2);
+    fill_result(s, x_out, res);
+  }
+  return ok(err);
+}
+
+int or_gmres(const or_op* a, const void* b, uint64_t max_iter, uint64_t restart, double rtol,
+             double atol, const void* x0, const or_op* m, void* x_out, or_result* res,
+             or_err* err) {
+  if (int rc = check_square_and_len<double>(a, "GMRES", err)) return rc;
+  const uint64_t n = a->nrows;
+  if (a->f64) {
+    std::vector<double> bv((const double*)b, (const double*)b + n);
+    auto s = gmres<double>(a, bv, max_iter, restart, rtol, atol, (const double*)x0, m);
+    fill_result(s, x_out, res);
+  } else {
+    std::vector<float> bv((const float*)b, (const float*)b + n);
+    auto s = gmres<float>(a, bv, max_iter, restart, (float)rtol, (float)atol, (const float*)x0, m);
+    fill_result(s, x_out, res);
+  }
+  return ok(err);
+}
+
+double or_true_rel_residual(const int64_t* indptr, const int32_t* indices, const double* data,
+                            int64_t n, const double* b, const double* x) {
+  std::vector<double> ax(n);
+  spmv<double>(indptr, indices, data, (uint64_t)n, x, ax.data());
+  double rr = 0, bb = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    double r = b[i] - ax[i];
+    rr = rr + r * r;
+    bb = bb + b[i] * b[i];
+  }
+  return std::sqrt(rr) / std::sqrt(bb);
+}
+
+// FP64 iterative refinement around an FP32 Jacobi-PCG (the algorithm of the
+// device's mixed-precision solver; no reference counterpart):
+//   x = 0; repeat: r = b - A x (FP64); stop if ||r|| <= tol ||b||;
+//   d = cg_f32(A32, r / ||r||); x += ||r|| * d.
+int or_cg_mixed_ir(const int64_t* indptr, const int32_t* indices, const double* data, int64_t n,
+                   const double* b, const or_ir_options* opt, double* x, or_ir_result* res) {
+  or_op* a32 = or_op_csr_i32(1, indptr, indices, data, n, n);
+  // the inner operator works on the FP32 copy of the values
+  a32->f64 = 0;
+  or_op* m = nullptr;
+  if (opt->jacobi) {
+    or_err e;
+    m = or_op_jacobi(a32, &e);
+    if (!m) { delete a32; return 1; }
+  }
+  std::vector<double> xv(n, 0.0), r(n), ax(n);
+  double bb = 0;
+  for (int64_t i = 0; i < n; ++i) bb = bb + b[i] * b[i];
+  const double bnorm = std::sqrt(bb);
+  uint64_t outer = 0, inner_total = 0;
+  double rel = 0;
+  bool conv = false;
+  while (true) {
+    spmv<double>(indptr, indices, data, (uint64_t)n, xv.data(), ax.data());
+    double rr = 0;
+    for (int64_t i = 0; i < n; ++i) { r[i] = b[i] - ax[i]; rr = rr + r[i] * r[i]; }
+    double rnorm = std::sqrt(rr);
+    rel = rnorm / bnorm;
+    if (rnorm <= opt->tol * bnorm) { conv = true; break; }
+    if (outer >= opt->max_outer) break;
+    std::vector<float> r32(n);
+    for (int64_t i = 0; i < n; ++i) r32[i] = (float)(r[i] / rnorm);
+    auto s = cg<float>(a32, r32, opt->max_inner, (float)opt->inner_rtol, 0.0f, nullptr, m);
+    inner_total += s.iterations;
+    for (int64_t i = 0; i < n; ++i) xv[i] = xv[i] + rnorm * (double)s.x[i];
+    ++outer;
+  }
+  std::memcpy(x, xv.data(), n * 8);
+  if (res) {
+    res->outer_iterations = outer;
+    res->inner_iterations = inner_total;
+    res->rel_residual = rel;
+    res->converged = conv ? 1 : 0;
+  }
+  delete m;
+  delete a32;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+/* CPU oracle for the scirs2-sparse iterative-solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a C++ restatement of the reference's
+ * Rust code (scirs2-sparse 0.1.0-alpha.6), used by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker.
+ * The product library never links, loads or calls it.
+ *
+ * Arithmetic rules that make it a faithful restatement:
+ *   - compiled with -O2 -ffp-contract=off (Rust never fuses mul+add);
+ *   - every sum is a strict left fold starting at zero, in storage order;
+ *   - sort_by_key is std::stable_sort on the same key;
+ *   - the same epsilon thresholds (F::epsilon() * 10), messages and
+ *     iteration counting as the Rust source.
+ * Indices are uint64_t (Rust usize).  All pointers are host pointers.
+ */
+#ifndef SX_ORACLE_H
+#define SX_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error record: code follows SparseError's declaration order
+ * (scirs2-sparse/src/error.rs:9-74), 0 = Ok. */
+typedef struct {
+  int code;
+  uint64_t v0, v1, v2, v3; /* payload: expected/found, index(r,c)/shape(r,c) */
+  char msg[256];
+} or_err;
+
+typedef struct {
+  uint64_t iterations;
+  double residual_norm;
+  int converged;
+  int message; /* same numbering as the device library's sx_message */
+} or_result;
+
+/* ---- construction (f32 / f64 variants) ---- */
+int or_csr_matrix_new_f64(const double* data, const uint64_t* rows, const uint64_t* cols,
+                          uint64_t nnz, uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
+                          uint64_t* indices_out, double* data_out, or_err* err);
+int or_csr_matrix_new_f32(const float* data, const uint64_t* rows, const uint64_t* cols,
+                          uint64_t nnz, uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
+                          uint64_t* indices_out, float* data_out, or_err* err);
+int or_csr_matrix_from_raw_check(const uint64_t* indptr, uint64_t indptr_len,
+                                 const uint64_t* indices, uint64_t indices_len, uint64_t data_len,
+                                 uint64_t nrows, uint64_t ncols, or_err* err);
+int or_csr_array_new_check(const uint64_t* indptr, uint64_t indptr_len, const uint64_t* indices,
+                           uint64_t indices_len, uint64_t data_len, uint64_t nrows,
+                           uint64_t ncols, int* has_sorted_indices, or_err* err);
+int or_csr_array_from_triplets_f64(const uint64_t* rows, const uint64_t* cols,
+                                   const double* data, uint64_t nnz, uint64_t nrows,
+                                   uint64_t ncols, int sorted, uint64_t* indptr_out,
+                                   uint64_t* indices_out, double* data_out,
+                                   int* has_sorted_indices, or_err* err);
+int or_csr_array_from_triplets_f32(const uint64_t* rows, const uint64_t* cols, const float* data,
+                                   uint64_t nnz, uint64_t nrows, uint64_t ncols, int sorted,
+                                   uint64_t* indptr_out, uint64_t* indices_out, float* data_out,
+                                   int* has_sorted_indices, or_err* err);
+void or_csr_transpose_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                          uint64_t nrows, uint64_t ncols, uint64_t* indptr_t,
+                          uint64_t* indices_t, double* data_t);
+void or_csr_transpose_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                          uint64_t nrows, uint64_t ncols, uint64_t* indptr_t,
+                          uint64_t* indices_t, float* data_t);
+double or_csr_get_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                      uint64_t nrows, uint64_t ncols, uint64_t i, uint64_t j);
+
+/* ---- SpMV ---- */
+void or_spmv_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                 uint64_t nrows, const double* x, double* y);
+void or_spmv_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                 uint64_t nrows, const float* x, float* y);
+/* Same as above with int64 row pointers and int32 columns (generator layout). */
+void or_spmv_i32_f64(const int64_t* indptr, const int32_t* indices, const double* data,
+                     int64_t nrows, const double* x, double* y);
+void or_spmv_i32_f32(const int64_t* indptr, const int32_t* indices, const float* data,
+                     int64_t nrows, const float* x, float* y);
+
+/* ---- operators (LinearOperator restatements) ---- */
+typedef struct or_op or_op;
+or_op* or_op_csr(int f64, const uint64_t* indptr, const uint64_t* indices, const void* data,
+                 uint64_t nrows, uint64_t ncols);
+or_op* or_op_csr_i32(int f64, const int64_t* indptr, const int32_t* indices, const void* data,
+                     int64_t nrows, int64_t ncols);
+or_op* or_op_identity(int f64, uint64_t n);
+or_op* or_op_scaled_identity(int f64, uint64_t n, double scale);
+or_op* or_op_diagonal(int f64, const void* diag, uint64_t n);
+/* JacobiPreconditioner::new from a CSR operator; NULL + err on a zero diagonal. */
+or_op* or_op_jacobi(const or_op* csr, or_err* err);
+or_op* or_op_jacobi_from_diagonal(int f64, const void* diag, uint64_t n, or_err* err);
+/* IC0Preconditioner::new; fast=1 applies the backward solve through a
+ * transposed factor in the same subtraction order (bit-identical). */
+or_op* or_op_ic0(const or_op* csr, int fast, or_err* err);
+/* Factorised approximate inverse M^-1 = G G^T from a lower-triangular CSR G. */
+or_op* or_op_fsai(const or_op* g_csr);
+void or_op_destroy(or_op* op);
+int or_op_matvec(const or_op* op, const void* x, void* y);
+uint64_t or_op_rows(const or_op* op);
+/* IC(0) factor export: nnz of L and its arrays. */
+uint64_t or_ic0_nnz(const or_op* ic0);
+void or_ic0_factor(const or_op* ic0, uint64_t* indptr, uint64_t* indices, void* data);
+
+/* ---- solvers (iterative.rs) ---- */
+int or_cg(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+          const void* x0, const or_op* m, void* x_out, or_result* res, or_err* err);
+int or_bicgstab(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+                const void* x0, const or_op* m1, const or_op* m2, void* x_out, or_result* res,
+                or_err* err);
+int or_gmres(const or_op* a, const void* b, uint64_t max_iter, uint64_t restart, double rtol,
+             double atol, const void* x0, const or_op* m, void* x_out, or_result* res,
+             or_err* err);
+
+/* ---- FP64 iterative refinement around an FP32 inner PCG (no reference
+ * counterpart; restates the device algorithm of the same name) ---- */
+typedef struct {
+  uint64_t max_outer;
+  uint64_t max_inner;
+  double tol;        /* outer stop: ||b - A x||_2 <= tol * ||b||_2, FP64 */
+  double inner_rtol; /* inner FP32 PCG relative tolerance */
+  int jacobi;        /* 1: Jacobi inner preconditioner, 0: none */
+} or_ir_options;
+typedef struct {
+  uint64_t outer_iterations;
+  uint64_t inner_iterations;
+  double rel_residual; /* final FP64 true relative residual */
+  int converged;
+} or_ir_result;
+int or_cg_mixed_ir(const int64_t* indptr, const int32_t* indices, const double* data, int64_t n,
+                   const double* b, const or_ir_options* opt, double* x, or_ir_result* res);
+
+/* FP64 true relative residual ||b - A x|| / ||b|| with sequential sums. */
+double or_true_rel_residual(const int64_t* indptr, const int32_t* indices, const double* data,
+                            int64_t n, const double* b, const double* x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

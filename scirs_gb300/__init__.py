@@ -1,0 +1,35 @@
+"""GB300-native backend for the scirs2-sparse iterative-solve path.
+
+CSR construction / transpose / SpMV, the LinearOperator slot (operators and
+preconditioners), and the cg / bicgstab / gmres solvers run as hand-written
+sm_103a CUDA kernels behind the C ABI in include/scirs_sparse.h; this
+package is the Python mirror of the reference API over that ABI.
+"""
+from .sparse import (  # noqa: F401
+    Context,
+    IRResult,
+    IterationResult,
+    Operator,
+    SparseError,
+    bicgstab,
+    cg,
+    cg_mixed,
+    csr_array,
+    csr_array_from_triplets,
+    csr_from_arrays,
+    csr_matrix,
+    csr_matrix_from_raw,
+    diagonal,
+    fsai,
+    generate,
+    gmres,
+    host_operator,
+    ic0,
+    identity,
+    jacobi,
+    jacobi_from_diagonal,
+    message_string,
+    rhs_normal,
+    scaled_identity,
+    true_rel_residual,
+)

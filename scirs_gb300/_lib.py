@@ -1,0 +1,181 @@
+"""ctypes binding of the C ABI declared in include/scirs_sparse.h.
+
+The shared library is built in-tree by scirs_gb300/build.py.  Importing this
+module never builds or falls back to anything: if the library is missing the
+import raises, so no code path can silently run without the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB_PATH
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        f"{LIB_PATH} is missing: build the CUDA library first "
+        "(python -c 'import __graft_entry__ as g; g.build()')"
+    )
+
+lib = C.CDLL(LIB_PATH)
+
+c_u64 = C.c_uint64
+c_i64 = C.c_int64
+c_vp = C.c_void_p
+c_int = C.c_int
+c_dbl = C.c_double
+ctx_t = c_vp
+op_t = c_vp
+
+SX_F32, SX_F64 = 0, 1
+SX_MEM_HOST, SX_MEM_DEVICE = 0, 1
+SX_API_CSR_MATRIX, SX_API_CSR_ARRAY = 0, 1
+SX_OP_CSR, SX_OP_IDENTITY, SX_OP_SCALED_IDENTITY, SX_OP_DIAGONAL = 0, 1, 2, 3
+SX_OP_JACOBI, SX_OP_IC0, SX_OP_FSAI, SX_OP_HOST = 4, 5, 6, 7
+SX_IC0_REFERENCE, SX_IC0_TEXTBOOK = 0, 1
+SX_SPMV_EXACT = 1
+
+
+class ErrorInfo(C.Structure):
+    _fields_ = [
+        ("code", c_int),
+        ("v0", c_u64),
+        ("v1", c_u64),
+        ("v2", c_u64),
+        ("v3", c_u64),
+        ("message", C.c_char * 512),
+    ]
+
+
+class IterResult(C.Structure):
+    _fields_ = [
+        ("iterations", c_u64),
+        ("residual_norm", c_dbl),
+        ("converged", c_int),
+        ("message", c_int),
+    ]
+
+
+class CGOptions(C.Structure):
+    _fields_ = [
+        ("max_iter", c_u64),
+        ("rtol", c_dbl),
+        ("atol", c_dbl),
+        ("x0", c_vp),
+        ("preconditioner", op_t),
+    ]
+
+
+class BiCGSTABOptions(C.Structure):
+    _fields_ = [
+        ("max_iter", c_u64),
+        ("rtol", c_dbl),
+        ("atol", c_dbl),
+        ("x0", c_vp),
+        ("left_preconditioner", op_t),
+        ("right_preconditioner", op_t),
+    ]
+
+
+class GMRESOptions(C.Structure):
+    _fields_ = [
+        ("max_iter", c_u64),
+        ("restart", c_u64),
+        ("rtol", c_dbl),
+        ("atol", c_dbl),
+        ("x0", c_vp),
+        ("preconditioner", op_t),
+    ]
+
+
+class IROptions(C.Structure):
+    _fields_ = [
+        ("max_outer", c_u64),
+        ("max_inner", c_u64),
+        ("tol", c_dbl),
+        ("inner_rtol", c_dbl),
+        ("x0", c_vp),
+        ("preconditioner", op_t),
+        ("a32", op_t),
+    ]
+
+
+class IRResult(C.Structure):
+    _fields_ = [
+        ("outer_iterations", c_u64),
+        ("inner_iterations", c_u64),
+        ("rel_residual", c_dbl),
+        ("converged", c_int),
+    ]
+
+
+class GenSpec(C.Structure):
+    _fields_ = [
+        ("kind", c_int),
+        ("nx", c_i64),
+        ("ny", c_i64),
+        ("nz", c_i64),
+        ("seed", c_u64),
+        ("param0", c_dbl),
+        ("param1", c_dbl),
+    ]
+
+
+HOST_MATVEC_FN = C.CFUNCTYPE(c_int, c_vp, c_vp, c_vp, c_u64)
+
+P = C.POINTER
+_SIGS = {
+    "sx_last_error": (None, [P(ErrorInfo)]),
+    "sx_status_string": (C.c_char_p, [c_int]),
+    "sx_message_string": (C.c_char_p, [c_int]),
+    "sx_ctx_create": (c_int, [c_int, P(ctx_t)]),
+    "sx_ctx_create_on_stream": (c_int, [c_int, c_vp, P(ctx_t)]),
+    "sx_ctx_destroy": (c_int, [ctx_t]),
+    "sx_ctx_stream": (c_vp, [ctx_t]),
+    "sx_ctx_synchronize": (c_int, [ctx_t]),
+    "sx_ctx_kernel_launches": (c_u64, [ctx_t]),
+    "sx_csr_from_triplets": (c_int, [ctx_t, c_int, c_int, c_vp, c_vp, c_vp, c_u64, c_u64, c_u64, c_int, P(op_t)]),
+    "sx_csr_from_raw": (c_int, [ctx_t, c_int, c_int, c_vp, c_u64, c_vp, c_vp, c_u64, c_u64, c_u64, P(op_t)]),
+    "sx_csr_from_raw_i32": (c_int, [ctx_t, c_int, c_vp, c_vp, c_vp, c_u64, c_u64, c_u64, c_int, P(op_t)]),
+    "sx_csr_transpose": (c_int, [ctx_t, op_t, P(op_t)]),
+    "sx_csr_astype": (c_int, [ctx_t, op_t, c_int, P(op_t)]),
+    "sx_csr_info": (c_int, [op_t, P(c_u64), P(c_u64), P(c_u64), P(c_int)]),
+    "sx_csr_download": (c_int, [ctx_t, op_t, c_vp, c_vp, c_vp]),
+    "sx_csr_get": (c_int, [ctx_t, op_t, c_u64, c_u64, c_vp]),
+    "sx_op_identity": (c_int, [ctx_t, c_int, c_u64, P(op_t)]),
+    "sx_op_scaled_identity": (c_int, [ctx_t, c_int, c_u64, c_dbl, P(op_t)]),
+    "sx_op_diagonal": (c_int, [ctx_t, c_int, c_vp, c_u64, P(op_t)]),
+    "sx_op_host": (c_int, [ctx_t, c_int, c_u64, c_u64, HOST_MATVEC_FN, c_vp, P(op_t)]),
+    "sx_op_kind_of": (c_int, [op_t, P(c_int)]),
+    "sx_op_shape": (c_int, [op_t, P(c_u64), P(c_u64)]),
+    "sx_op_dtype": (c_int, [op_t, P(c_int)]),
+    "sx_op_destroy": (c_int, [op_t]),
+    "sx_op_matvec": (c_int, [ctx_t, op_t, c_vp, c_u64, c_vp, c_int]),
+    "sx_op_rmatvec": (c_int, [ctx_t, op_t, c_vp, c_u64, c_vp, c_int]),
+    "sx_spmv_ex": (c_int, [ctx_t, op_t, c_vp, c_vp, C.c_uint]),
+    "sx_precond_jacobi": (c_int, [ctx_t, op_t, P(op_t)]),
+    "sx_precond_jacobi_from_diagonal": (c_int, [ctx_t, c_int, c_vp, c_u64, P(op_t)]),
+    "sx_precond_ic0": (c_int, [ctx_t, op_t, c_int, P(op_t)]),
+    "sx_precond_fsai": (c_int, [ctx_t, op_t, P(op_t)]),
+    "sx_cg_options_default": (None, [P(CGOptions)]),
+    "sx_bicgstab_options_default": (None, [P(BiCGSTABOptions)]),
+    "sx_gmres_options_default": (None, [P(GMRESOptions)]),
+    "sx_cg": (c_int, [ctx_t, op_t, c_vp, c_u64, P(CGOptions), c_vp, c_int, P(IterResult)]),
+    "sx_bicgstab": (c_int, [ctx_t, op_t, c_vp, c_u64, P(BiCGSTABOptions), c_vp, c_int, P(IterResult)]),
+    "sx_gmres": (c_int, [ctx_t, op_t, c_vp, c_u64, P(GMRESOptions), c_vp, c_int, P(IterResult)]),
+    "sx_ir_options_default": (None, [P(IROptions)]),
+    "sx_cg_mixed": (c_int, [ctx_t, op_t, c_vp, c_u64, P(IROptions), c_vp, c_int, P(IRResult)]),
+    "sx_true_rel_residual": (c_int, [ctx_t, op_t, c_vp, c_vp, c_int, P(c_dbl)]),
+    "sx_gen_matrix": (c_int, [P(GenSpec), P(c_i64), P(c_i64), c_vp, c_vp, c_vp]),
+    "sx_gen_rhs_normal": (None, [c_u64, c_i64, c_vp]),
+}
+
+MISSING = []
+for _name, (_res, _args) in _SIGS.items():
+    try:
+        _f = getattr(lib, _name)
+    except AttributeError:
+        MISSING.append(_name)
+        continue
+    _f.restype = _res
+    _f.argtypes = _args

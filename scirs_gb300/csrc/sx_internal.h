@@ -1,0 +1,144 @@
+// Internal declarations shared by the translation units of the GB300 sparse
+// library.  Nothing here is part of the C ABI (include/scirs_sparse.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "scirs_sparse.h"
+
+namespace sx {
+
+// ----------------------------------------------------------------- errors
+int set_error(int code, const std::string& msg, uint64_t v0 = 0, uint64_t v1 = 0, uint64_t v2 = 0,
+              uint64_t v3 = 0);
+int clear_error();
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define SX_CUDA(...)                                                             \
+  do {                                                                           \
+    cudaError_t sx_e_ = (__VA_ARGS__);                                           \
+    if (sx_e_ != cudaSuccess) return ::sx::cuda_fail(sx_e_, #__VA_ARGS__, __FILE__, __LINE__); \
+  } while (0)
+
+#define SX_CHECK(...)                   \
+  do {                                  \
+    int sx_rc_ = (__VA_ARGS__);         \
+    if (sx_rc_ != SX_OK) return sx_rc_; \
+  } while (0)
+
+// Message codes of IterationResult.message (sx_message in the ABI).
+enum : int {
+  MSG_CONVERGED = 0,
+  MSG_MAX_ITER = 1,
+  MSG_NOT_PD = 2,
+  MSG_CONVERGED_INITIAL = 3,
+  MSG_BD_RHO = 4,
+  MSG_BD_RHAT_V = 5,
+  MSG_BD_ALPHA = 6,
+  MSG_BD_TT = 7,
+  MSG_BD_OMEGA = 8,
+};
+
+// ------------------------------------------------------------ device CSR
+// int32 row pointers and columns (nnz < 2^31), values of the handle dtype.
+struct DevCsr {
+  int64_t nrows = 0, ncols = 0, nnz = 0;
+  int32_t* indptr = nullptr;   // nrows + 1
+  int32_t* indices = nullptr;  // nnz
+  void* vals = nullptr;        // nnz values
+  bool has_sorted_indices = true;
+  bool monotone = true;        // indptr non-decreasing
+  int32_t max_row_len = 0;
+  double mean_row_len = 0.0;
+};
+
+struct IC0Dev;   // defined in sx_ic0.cu
+struct HostOp {
+  sx_host_matvec_fn fn = nullptr;
+  void* user = nullptr;
+};
+
+}  // namespace sx
+
+struct sx_op_s {
+  int kind = SX_OP_CSR;
+  int dtype = SX_F64;
+  int device = 0;
+  int64_t nrows = 0, ncols = 0;
+  sx::DevCsr csr;                     // CSR, and G for FSAI
+  void* diag = nullptr;               // DIAGONAL: d; JACOBI: 1/d
+  double scale = 1.0;                 // SCALED_IDENTITY
+  sx_op_s* transpose = nullptr;       // cached transpose (rmatvec, FSAI's G^T)
+  sx::IC0Dev* ic0 = nullptr;
+  sx::HostOp host;
+  void* work = nullptr;               // per-operator temporary vector (FSAI: G^T x)
+  uint64_t serial = 0;                // unique id, keys the solver graph cache
+};
+
+struct sx_ctx_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int num_sms = 0;
+  uint64_t launches = 0;
+  // grow-only scratch; synchronises the stream before it is replaced
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  // pinned host staging for scalar readback
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+  // reduction partials (3 slots per block) and the last-block counter
+  void* red_partials = nullptr;
+  size_t red_bytes = 0;
+  unsigned int* red_counter = nullptr;
+  // solver workspaces and instantiated graphs (sx_krylov.cu)
+  void* solver_cache = nullptr;
+};
+
+namespace sx {
+
+int ctx_scratch(sx_ctx ctx, size_t bytes, void** out);
+int ctx_pinned(sx_ctx ctx, size_t bytes, void** out);
+inline size_t elt_size(int dtype) { return dtype == SX_F64 ? 8 : 4; }
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Allocation helpers that record the CUDA error.
+int dev_alloc(void** p, size_t bytes);
+void dev_free(void* p);
+
+// Upload host-side CSR arrays (already validated, int32) into a DevCsr and
+// compute row statistics.
+int csr_finalize_stats(sx_ctx ctx, DevCsr& c);
+
+// ------------------------------------------------------------ kernels API
+// Plain device SpMV entry used by the ABI (y = A x, device pointers).
+int spmv_device(sx_ctx ctx, sx_op a, const void* x, void* y, unsigned flags);
+
+// y = op(x) for operators whose apply is more than one kernel (IC0, FSAI,
+// host callbacks).  Enqueued on ctx->stream; no allocation, no sync except
+// for host callbacks.
+int apply_general(sx_ctx ctx, sx_op op, const void* x, void* y);
+
+// Cached transpose of a CSR operator (rmatvec, FSAI's G^T).
+int ensure_transpose(sx_ctx ctx, sx_op a);
+int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out);
+void destroy_op_internal(sx_op op);
+
+// Grid geometry for the vector kernels (fixed per device -> deterministic
+// reductions).
+int vec_grid(sx_ctx ctx, int64_t n);
+
+// Counter/partials area used by every fused reduction launch: it must be
+// zero-initialised once and is left zeroed by the finalizing block.
+struct ReduceArea {
+  double* partials = nullptr;   // 3 * max_blocks doubles (or floats)
+  unsigned int* counter = nullptr;
+  int max_blocks = 0;
+};
+int ctx_reduce_area(sx_ctx ctx, int64_t blocks, ReduceArea* out);
+
+}  // namespace sx

@@ -1,0 +1,191 @@
+// Device building blocks shared by the kernels of the sparse library:
+//  - deterministic grid reductions: per-block partials, the last block to
+//    finish sums them in a fixed order and runs a finalize step;
+//  - the CSR "stream" SpMV: a block owns a run of consecutive rows, streams
+//    their nonzeros through shared memory in coalesced tiles, and each thread
+//    sums its own row sequentially in storage order (the reference's order,
+//    so the result is bit-identical to `sum = sum + a*x` per row);
+//  - a grid-stride elementwise kernel with the same reduction tail.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sx {
+
+constexpr int kBlock = 256;        // threads per block of every kernel here
+constexpr int kWarps = kBlock / 32;
+
+template <typename T>
+struct Acc3 {
+  T a, b, c;
+};
+
+// Products and sums with rounding made explicit, so that the compiler never
+// contracts a*b+c into one FMA: the reference rounds both operations.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of three values; the result is valid in every thread.
+template <typename T>
+__device__ __forceinline__ Acc3<T> block_sum3(Acc3<T> v) {
+  __shared__ T sh[3][kWarps];
+  __shared__ T out[3];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v.a = warp_sum(v.a);
+  v.b = warp_sum(v.b);
+  v.c = warp_sum(v.c);
+  if (lane == 0) { sh[0][w] = v.a; sh[1][w] = v.b; sh[2][w] = v.c; }
+  __syncthreads();
+  if (w == 0) {
+    T a = lane < kWarps ? sh[0][lane] : T(0);
+    T b = lane < kWarps ? sh[1][lane] : T(0);
+    T c = lane < kWarps ? sh[2][lane] : T(0);
+    a = warp_sum(a); b = warp_sum(b); c = warp_sum(c);
+    if (lane == 0) { out[0] = a; out[1] = b; out[2] = c; }
+  }
+  __syncthreads();
+  Acc3<T> r{out[0], out[1], out[2]};
+  __syncthreads();
+  return r;
+}
+
+// Grid reduction tail.  Every block calls this once with its thread-local
+// partials.  Returns true in the block that finished last; there, `tot`
+// holds the grid totals (in every thread).  The counter is left at zero for
+// the next launch.  The totals do not depend on which block finishes last.
+template <typename T>
+__device__ __forceinline__ bool grid_reduce3(Acc3<T> v, T* partials, unsigned int* counter,
+                                             Acc3<T>& tot) {
+  __shared__ bool s_last;
+  Acc3<T> b = block_sum3(v);
+  if (threadIdx.x == 0) {
+    partials[3 * blockIdx.x + 0] = b.a;
+    partials[3 * blockIdx.x + 1] = b.b;
+    partials[3 * blockIdx.x + 2] = b.c;
+    __threadfence();
+    unsigned int t = atomicAdd(counter, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  Acc3<T> s{T(0), T(0), T(0)};
+  for (unsigned int j = threadIdx.x; j < gridDim.x; j += kBlock) {
+    s.a += __ldcg(partials + 3 * j + 0);
+    s.b += __ldcg(partials + 3 * j + 1);
+    s.c += __ldcg(partials + 3 * j + 2);
+  }
+  tot = block_sum3(s);
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+// --------------------------------------------------------------- SpMV
+// Epilogue interface (all __device__):
+//   bool skip() const                        -> whole launch is a no-op
+//   T out(int64_t row, T ax) const           -> value stored to y[row]
+//   void acc(int64_t row, T y, Acc3<T>& a)   -> per-row reduction terms
+//   static constexpr bool kReduce            -> run the grid reduction
+//   void finish(const Acc3<T>& tot)          -> thread 0 of the last block
+template <typename T, int ITEMS, class Epi>
+__global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
+    const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+    const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, int64_t nrows,
+    T* partials, unsigned int* counter, Epi epi) {
+  if (epi.skip()) return;
+  constexpr int TILE = kBlock * ITEMS;
+  __shared__ int32_t s_ptr[kBlock + 1];
+  __shared__ T s_prod[TILE];
+  const int tid = threadIdx.x;
+  const int64_t r0 = (int64_t)blockIdx.x * kBlock;
+  const int nr = (int)min((int64_t)kBlock, nrows - r0);
+  if (tid <= nr) s_ptr[tid] = indptr[r0 + tid];
+  if (tid == 0 && nr == kBlock) s_ptr[kBlock] = indptr[r0 + kBlock];
+  __syncthreads();
+  const int32_t s = s_ptr[0], e = s_ptr[nr];
+  int32_t my_s = 0, my_e = 0;
+  if (tid < nr) { my_s = s_ptr[tid]; my_e = s_ptr[tid + 1]; }
+  T acc = T(0);
+  for (int32_t base = s; base < e; base += TILE) {
+    const int32_t tend = min(e, base + TILE);
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+      const int32_t k = base + j * kBlock + tid;
+      if (k < tend) s_prod[k - base] = mul_rn(vals[k], __ldg(x + indices[k]));
+    }
+    __syncthreads();
+    if (tid < nr) {
+      const int32_t lo = max(my_s, base), hi = min(my_e, tend);
+      for (int32_t k = lo; k < hi; ++k) acc = add_rn(acc, s_prod[k - base]);
+    }
+    __syncthreads();
+  }
+  Acc3<T> a{T(0), T(0), T(0)};
+  if (tid < nr) {
+    const int64_t row = r0 + tid;
+    const T v = epi.out(row, acc);
+    y[row] = v;
+    epi.acc(row, v, a);
+  }
+  if constexpr (Epi::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && tid == 0) epi.finish(tot);
+  }
+}
+
+// Rows whose end precedes their start (accepted by CsrArray::new) are
+// empty; this one-thread-per-row kernel serves such irregular matrices.
+template <typename T, class Epi>
+__global__ void __launch_bounds__(kBlock) spmv_rowseq_kernel(
+    const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+    const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, int64_t nrows,
+    T* partials, unsigned int* counter, Epi epi) {
+  if (epi.skip()) return;
+  const int64_t row = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  Acc3<T> a{T(0), T(0), T(0)};
+  if (row < nrows) {
+    T acc = T(0);
+    for (int32_t k = indptr[row]; k < indptr[row + 1]; ++k)
+      acc = add_rn(acc, mul_rn(vals[k], __ldg(x + indices[k])));
+    const T v = epi.out(row, acc);
+    y[row] = v;
+    epi.acc(row, v, a);
+  }
+  if constexpr (Epi::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) epi.finish(tot);
+  }
+}
+
+// -------------------------------------------------------- elementwise
+// Body interface (all __device__):
+//   bool skip() const
+//   void elem(int64_t i, Acc3<T>& a)   (grid-stride over [0, n))
+//   static constexpr bool kReduce
+//   void finish(const Acc3<T>& tot)
+template <typename T, class Body>
+__global__ void __launch_bounds__(kBlock) vec_kernel(int64_t n, T* partials,
+                                                     unsigned int* counter, Body body) {
+  if (body.skip()) return;
+  Acc3<T> a{T(0), T(0), T(0)};
+  const int64_t stride = (int64_t)gridDim.x * kBlock;
+  for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) body.elem(i, a);
+  if constexpr (Body::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) body.finish(tot);
+  }
+}
+
+}  // namespace sx

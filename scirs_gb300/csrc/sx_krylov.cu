@@ -1,0 +1,1225 @@
+// Krylov solvers of scirs2-sparse on the device (linalg/iterative.rs):
+// cg (:40-162), bicgstab (:377-611), gmres (:641-816).
+//
+// Every scalar of the recurrences lives in a device-side state struct.  The
+// reductions of an iteration are fused into the kernel that produces their
+// operands (the SpMV epilogue for p.Ap, the vector update for r.r and r.z),
+// and the last block of each reduction performs the reference's scalar step
+// and its exits (breakdown, convergence, max_iter) in the reference's order.
+// Kernels of later steps return at once when the state says the solve has
+// ended, so an iteration can be replayed without host involvement: the loop
+// body is captured once into a CUDA graph whose conditional WHILE node is
+// re-armed by the last kernel of each iteration.  A graph launch runs at most
+// `budget` iterations, so the host regains control periodically.
+
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sx_launch.cuh"
+
+namespace sx {
+
+enum : int { ST_RUNNING = 0, ST_DONE = 1 };
+enum : int { PK_NONE = 0, PK_DIAG = 1, PK_SCALED = 2, PK_GENERAL = 3 };
+constexpr unsigned kBudget = 4096;
+
+// Elementwise preconditioners fused into the vector updates.
+template <typename T>
+struct PrecFused {
+  int kind = PK_NONE;
+  const T* d = nullptr;
+  T s = T(1);
+  __device__ __forceinline__ T apply(int64_t i, T r) const {
+    if (kind == PK_DIAG) return mul_rn(r, d[i]);
+    if (kind == PK_SCALED) return mul_rn(r, s);
+    return r;
+  }
+};
+
+static int prec_kind(sx_op m) {
+  if (!m) return PK_NONE;
+  switch (m->kind) {
+    case SX_OP_IDENTITY: return PK_NONE;
+    case SX_OP_DIAGONAL:
+    case SX_OP_JACOBI: return PK_DIAG;
+    case SX_OP_SCALED_IDENTITY: return PK_SCALED;
+    default: return PK_GENERAL;
+  }
+}
+
+template <typename T>
+static PrecFused<T> prec_fused(sx_op m) {
+  PrecFused<T> p;
+  p.kind = prec_kind(m);
+  if (p.kind == PK_DIAG) p.d = (const T*)m->diag;
+  if (p.kind == PK_SCALED) p.s = (T)m->scale;
+  return p;
+}
+
+__device__ __forceinline__ void set_cond(int use, cudaGraphConditionalHandle h, unsigned v) {
+  if (use) cudaGraphSetConditional(h, v);
+}
+
+template <typename T>
+__device__ __forceinline__ T eps_of() { return sizeof(T) == 8 ? (T)2.220446049250313e-16 : (T)1.1920928955078125e-07f; }
+
+// Epilogue y = b - A x (initial residuals: iterative.rs:78-79, :416-417, :677-678).
+template <typename T>
+struct EpiResid {
+  const T* b;
+  static constexpr bool kReduce = false;
+  __device__ bool skip() const { return false; }
+  __device__ T out(int64_t i, T ax) const { return sub_rn(b[i], ax); }
+  __device__ void acc(int64_t, T, Acc3<T>&) const {}
+  __device__ void finish(const Acc3<T>&) const {}
+};
+
+// Loop control shared by every solver state (first member of each state):
+// the host rewrites only the tail fields (use_cond .. cond) between graph
+// launches; everything else is owned by the device.
+struct LoopCtl {
+  unsigned long long iterations, max_iter;
+  int status, message, converged, use_cond;
+  unsigned int budget, pad;
+  cudaGraphConditionalHandle cond;
+};
+constexpr size_t kCtlTail = offsetof(LoopCtl, use_cond);
+
+// Epilogue that stores A x but is skipped once the solve has ended.
+template <typename T, class S>
+struct EpiSkip {
+  const S* st;
+  static constexpr bool kReduce = false;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ T out(int64_t, T ax) const { return ax; }
+  __device__ void acc(int64_t, T, Acc3<T>&) const {}
+  __device__ void finish(const Acc3<T>&) const {}
+};
+
+
+// ================================================================ infra
+struct GraphEntry {
+  uint64_t key[8];
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphConditionalHandle cond = 0;
+  int kernels_per_iter = 0;
+};
+
+struct SolverCache {
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  void* state = nullptr;  // device state block
+  std::vector<GraphEntry> graphs;
+};
+
+static SolverCache* cache_of(sx_ctx ctx) {
+  if (!ctx->solver_cache) ctx->solver_cache = new SolverCache();
+  return (SolverCache*)ctx->solver_cache;
+}
+
+static void drop_graphs(SolverCache* c) {
+  for (auto& g : c->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+  }
+  c->graphs.clear();
+}
+
+constexpr size_t kStateBytes = 4096;
+
+static int ws_get(sx_ctx ctx, size_t bytes, void** ws, void** state) {
+  SolverCache* c = cache_of(ctx);
+  if (bytes > c->ws_bytes) {
+    SX_CUDA(cudaStreamSynchronize(ctx->stream));
+    drop_graphs(c);  // graphs captured against the old workspace are stale
+    dev_free(c->ws);
+    c->ws = nullptr;
+    c->ws_bytes = 0;
+    SX_CHECK(dev_alloc(&c->ws, bytes));
+    c->ws_bytes = bytes;
+  }
+  if (!c->state) SX_CHECK(dev_alloc(&c->state, kStateBytes));
+  *ws = c->ws;
+  *state = c->state;
+  return SX_OK;
+}
+
+static GraphEntry* graph_find(sx_ctx ctx, const uint64_t key[8]) {
+  SolverCache* c = cache_of(ctx);
+  for (auto& g : c->graphs)
+    if (std::memcmp(g.key, key, sizeof(g.key)) == 0) return &g;
+  return nullptr;
+}
+
+// graph = WHILE(cond) { body }, body captured from `record` (one iteration).
+template <class Rec>
+static int graph_build(sx_ctx ctx, const uint64_t key[8], Rec record, GraphEntry** out) {
+  SolverCache* c = cache_of(ctx);
+  if (c->graphs.size() >= 16) drop_graphs(c);
+  GraphEntry e;
+  std::memcpy(e.key, key, sizeof(e.key));
+  SX_CUDA(cudaGraphCreate(&e.graph, 0));
+  SX_CUDA(cudaGraphConditionalHandleCreate(&e.cond, e.graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.conditional.handle = e.cond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  SX_CUDA(cudaGraphAddNode(&node, e.graph, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  SX_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal));
+  const uint64_t before = ctx->launches;
+  int rc = record();
+  cudaGraph_t captured = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &captured);
+  e.kernels_per_iter = (int)(ctx->launches - before);
+  ctx->launches = before;
+  if (rc != SX_OK || ce != cudaSuccess) {
+    cudaGraphDestroy(e.graph);
+    cudaGetLastError();
+    if (rc != SX_OK) return rc;
+    return cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+  }
+  cudaError_t ie = cudaGraphInstantiate(&e.exec, e.graph, 0);
+  if (ie != cudaSuccess) {
+    cudaGraphDestroy(e.graph);
+    return cuda_fail(ie, "cudaGraphInstantiate", __FILE__, __LINE__);
+  }
+  c->graphs.push_back(e);
+  *out = &c->graphs.back();
+  return SX_OK;
+}
+
+static bool op_graphable(sx_op op) { return !op || op->kind != SX_OP_HOST; }
+
+static int check_prec(sx_op a, sx_op m) {
+  if (!m) return SX_OK;
+  if (m->dtype != a->dtype)
+    return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: preconditioner dtype differs");
+  if (m->ncols != a->nrows)
+    return set_error(SX_ERR_DIMENSION_MISMATCH,
+                     "Dimension mismatch: expected " + std::to_string(m->ncols) + ", found " +
+                         std::to_string(a->nrows),
+                     (uint64_t)m->ncols, (uint64_t)a->nrows);
+  return SX_OK;
+}
+
+static int read_ctl(sx_ctx ctx, const void* d_state, void* h, size_t bytes) {
+  void* pin = nullptr;
+  SX_CHECK(ctx_pinned(ctx, 2 * kStateBytes, &pin));
+  SX_CUDA(cudaMemcpyAsync(pin, d_state, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(h, pin, bytes);
+  return SX_OK;
+}
+
+static int write_bytes(sx_ctx ctx, void* d_dst, const void* h, size_t bytes) {
+  void* pin = nullptr;
+  SX_CHECK(ctx_pinned(ctx, 2 * kStateBytes, &pin));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  char* w = (char*)pin + kStateBytes;
+  std::memcpy(w, h, bytes);
+  SX_CUDA(cudaMemcpyAsync(d_dst, w, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return SX_OK;
+}
+
+static int vec_in(sx_ctx ctx, void* dst, const void* src, size_t bytes, sx_mem mem) {
+  if (bytes == 0) return SX_OK;
+  SX_CUDA(cudaMemcpyAsync(dst, src, bytes,
+                          mem == SX_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                          ctx->stream));
+  return SX_OK;
+}
+static int vec_out(sx_ctx ctx, void* dst, const void* src, size_t bytes, sx_mem mem) {
+  if (bytes == 0) return SX_OK;
+  SX_CUDA(cudaMemcpyAsync(dst, src, bytes,
+                          mem == SX_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  return SX_OK;
+}
+
+// Runs iterations until the state reports the end.  With a graph, one launch
+// executes up to kBudget iterations of the captured body; otherwise the same
+// body is enqueued in chunks of 32 iterations.
+template <class Rec>
+static int run_loop(sx_ctx ctx, void* d_state, const uint64_t key[8], bool graphable,
+                    Rec record) {
+  LoopCtl h;
+  SX_CHECK(read_ctl(ctx, d_state, &h, sizeof(h)));
+  if (h.status != ST_RUNNING) return SX_OK;
+  GraphEntry* g = nullptr;
+  if (graphable) {
+    g = graph_find(ctx, key);
+    if (!g) {
+      int rc = graph_build(ctx, key, record, &g);
+      if (rc != SX_OK) g = nullptr;  // fall back to eager launches
+    }
+  }
+  for (int guard = 0;; ++guard) {
+    const unsigned long long it0 = h.iterations;
+    LoopCtl tail;
+    std::memset(&tail, 0, sizeof(tail));
+    tail.use_cond = g ? 1 : 0;
+    tail.budget = kBudget;
+    tail.cond = g ? g->cond : 0;
+    SX_CHECK(write_bytes(ctx, (char*)d_state + kCtlTail, (const char*)&tail + kCtlTail,
+                         sizeof(LoopCtl) - kCtlTail));
+    if (g) {
+      SX_CUDA(cudaGraphLaunch(g->exec, ctx->stream));
+    } else {
+      for (int k = 0; k < 32; ++k) SX_CHECK(record());
+    }
+    SX_CHECK(read_ctl(ctx, d_state, &h, sizeof(h)));
+    if (g) ctx->launches += (uint64_t)g->kernels_per_iter * (h.iterations - it0 + 1);
+    if (h.status != ST_RUNNING) break;
+    if (h.iterations == it0 && guard > 2)
+      return set_error(SX_ERR_ITERATIVE_SOLVER_FAILURE,
+                       "Iterative solver failure: device loop made no progress");
+  }
+  return SX_OK;
+}
+
+// ===================================================================== CG
+template <typename T>
+struct CgState {
+  LoopCtl c;
+  T rz_old, alpha, beta, rnorm, tol, pap, rtol, atol, result_norm;
+};
+
+// z = M r, p = z, rz = r.z, ||b||, ||r|| (iterative.rs:82-93)
+template <typename T>
+struct CgSetup {
+  CgState<T>* st;
+  const T *b, *r, *z;  // z only for a general preconditioner
+  T* p;
+  PrecFused<T> pf;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<T>& a) const {
+    T ri = r[i];
+    T zi = pf.kind == PK_GENERAL ? z[i] : pf.apply(i, ri);
+    p[i] = zi;
+    a.a += ri * zi;
+    a.b += b[i] * b[i];
+    a.c += ri * ri;
+  }
+  __device__ void finish(const Acc3<T>& t) const {
+    st->rz_old = t.a;
+    T bnorm = sqrt(t.b);
+    st->tol = fmax(st->atol, st->rtol * bnorm);
+    st->rnorm = sqrt(t.c);
+    st->result_norm = st->rnorm;
+    if (st->c.max_iter == 0) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_MAX_ITER;
+    }
+  }
+};
+
+// Ap with pAp fused (iterative.rs:98-111)
+template <typename T>
+struct EpiCgPap {
+  CgState<T>* st;
+  const T* p;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ T out(int64_t, T ax) const { return ax; }
+  __device__ void acc(int64_t i, T y, Acc3<T>& a) const { a.a += p[i] * y; }
+  __device__ void finish(const Acc3<T>& t) const {
+    T pap = t.a;
+    st->pap = pap;
+    if (pap <= T(0)) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_NOT_PD;
+      st->result_norm = st->rnorm;
+      return;
+    }
+    st->alpha = st->rz_old / pap;
+  }
+};
+
+// x += alpha p; r -= alpha Ap; ||r||; r.z for a fused M (iterative.rs:113-144)
+template <typename T>
+struct CgUpdate {
+  CgState<T>* st;
+  T *x, *r;
+  const T *p, *ap;
+  PrecFused<T> pf;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ void elem(int64_t i, Acc3<T>& a) const {
+    const T alpha = st->alpha;
+    x[i] = add_rn(x[i], mul_rn(alpha, p[i]));
+    T ri = sub_rn(r[i], mul_rn(alpha, ap[i]));
+    r[i] = ri;
+    a.a += ri * ri;
+    if (pf.kind != PK_GENERAL) a.b += ri * pf.apply(i, ri);
+  }
+  __device__ void finish(const Acc3<T>& t) const {
+    T rnorm = sqrt(t.a);
+    st->rnorm = rnorm;
+    if (rnorm <= st->tol) {
+      st->c.status = ST_DONE;
+      st->c.converged = 1;
+      st->c.message = MSG_CONVERGED;
+      st->c.iterations += 1;
+      st->result_norm = rnorm;
+      return;
+    }
+    if (pf.kind != PK_GENERAL) {
+      T rz_new = t.b;
+      st->beta = rz_new / st->rz_old;
+      st->rz_old = rz_new;
+    }
+  }
+};
+
+// r.z and beta for a general preconditioner (iterative.rs:143-144)
+template <typename T>
+struct CgRz {
+  CgState<T>* st;
+  const T *r, *z;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ void elem(int64_t i, Acc3<T>& a) const { a.a += r[i] * z[i]; }
+  __device__ void finish(const Acc3<T>& t) const {
+    st->beta = t.a / st->rz_old;
+    st->rz_old = t.a;
+  }
+};
+
+// p = z + beta p; iteration count; loop condition (iterative.rs:147-152)
+template <typename T>
+struct CgP {
+  CgState<T>* st;
+  T* p;
+  const T *r, *z;
+  PrecFused<T> pf;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const {
+    if (st->c.status != ST_RUNNING) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(st->c.use_cond, st->c.cond, 0u);
+      return true;
+    }
+    return false;
+  }
+  __device__ void elem(int64_t i, Acc3<T>&) const {
+    T zi = pf.kind == PK_GENERAL ? z[i] : pf.apply(i, r[i]);
+    p[i] = add_rn(zi, mul_rn(st->beta, p[i]));
+  }
+  __device__ void finish(const Acc3<T>&) const {
+    st->c.iterations += 1;
+    if (st->c.iterations >= st->c.max_iter) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_MAX_ITER;
+      st->result_norm = st->rnorm;
+    }
+    if (st->c.budget > 0) st->c.budget -= 1;
+    set_cond(st->c.use_cond, st->c.cond,
+             (st->c.status == ST_RUNNING && st->c.budget > 0) ? 1u : 0u);
+  }
+};
+
+template <typename T>
+static int cg_run(sx_ctx ctx, sx_op a, const void* b, const sx_cg_options* opt, void* x_out,
+                  sx_mem mem, sx_iter_result* res) {
+  const int64_t n = a->nrows;
+  sx_op m = opt->preconditioner;
+  SX_CHECK(check_prec(a, m));
+  const int pk = prec_kind(m);
+  const size_t w = sizeof(T);
+  const size_t vb = align_up((size_t)std::max<int64_t>(n, 1) * w, 256);
+  void *ws = nullptr, *dstate = nullptr;
+  SX_CHECK(ws_get(ctx, vb * 6, &ws, &dstate));
+  T* vb_ = (T*)ws;
+  T* B = (T*)((char*)ws + 0 * vb);
+  T* X = (T*)((char*)ws + 1 * vb);
+  T* R = (T*)((char*)ws + 2 * vb);
+  T* P = (T*)((char*)ws + 3 * vb);
+  T* AP = (T*)((char*)ws + 4 * vb);
+  T* Z = (T*)((char*)ws + 5 * vb);
+  (void)vb_;
+  CgState<T>* st = (CgState<T>*)dstate;
+  SX_CHECK(vec_in(ctx, B, b, n * w, mem));
+  if (opt->x0) SX_CHECK(vec_in(ctx, X, opt->x0, n * w, mem));
+  else if (n > 0) SX_CUDA(cudaMemsetAsync(X, 0, n * w, ctx->stream));
+  CgState<T> h;
+  std::memset(&h, 0, sizeof(h));
+  h.c.max_iter = opt->max_iter;
+  h.rtol = (T)opt->rtol;
+  h.atol = (T)opt->atol;
+  SX_CHECK(write_bytes(ctx, st, &h, sizeof(h)));
+  ReduceArea ra;
+  SX_CHECK(ctx_reduce_area(ctx, std::max<int64_t>((n + kBlock - 1) / kBlock, vec_grid(ctx, n)) + 8, &ra));
+  const PrecFused<T> pf = prec_fused<T>(m);
+  // r = b - A x (iterative.rs:78-79)
+  SX_CHECK(launch_apply<T>(ctx, a, X, R, EpiResid<T>{B}));
+  if (pk == PK_GENERAL)
+    SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiPlain<T>{}));
+  SX_CHECK(launch_vec<T>(ctx, n, CgSetup<T>{st, B, R, Z, P, pf}));
+  auto body = [&]() -> int {
+    SX_CHECK(launch_apply<T>(ctx, a, P, AP, EpiCgPap<T>{st, P}));
+    SX_CHECK(launch_vec<T>(ctx, n, CgUpdate<T>{st, X, R, P, AP, pf}));
+    if (pk == PK_GENERAL) {
+      SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiSkip<T, CgState<T>>{st}));
+      SX_CHECK(launch_vec<T>(ctx, n, CgRz<T>{st, R, Z}));
+    }
+    SX_CHECK(launch_vec<T>(ctx, n, CgP<T>{st, P, R, Z, pf}));
+    return SX_OK;
+  };
+  const uint64_t key[8] = {1, (uint64_t)sizeof(T), a->serial, m ? m->serial : 0,
+                           (uint64_t)n, (uint64_t)(uintptr_t)ws, (uint64_t)pk, 0};
+  SX_CHECK(run_loop(ctx, st, key, op_graphable(a) && op_graphable(m), body));
+  SX_CHECK(read_ctl(ctx, st, &h, sizeof(h)));
+  SX_CHECK(vec_out(ctx, x_out, X, n * w, mem));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (res) {
+    res->iterations = h.c.iterations;
+    res->residual_norm = (double)h.result_norm;
+    res->converged = h.c.converged;
+    res->message = h.c.message;
+  }
+  return SX_OK;
+}
+
+// =============================================================== BiCGSTAB
+template <typename T>
+struct BiState {
+  LoopCtl c;
+  T rho, rho_old, alpha, omega, beta, rnorm, tol, rtol, atol, result_norm;
+  int x_is_y, pad2;
+};
+
+// r_hat = r, v = p = 0, ||r||, ||b||, initial exits, first rho
+// (iterative.rs:416-447, 450-465)
+template <typename T>
+struct BiSetup {
+  BiState<T>* st;
+  const T *b, *r;
+  T *rhat, *v, *p;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<T>& a) const {
+    T ri = r[i];
+    rhat[i] = ri;
+    v[i] = T(0);
+    p[i] = T(0);
+    a.a += ri * ri;
+    a.b += b[i] * b[i];
+  }
+  __device__ void finish(const Acc3<T>& t) const {
+    T rnorm = sqrt(t.a);
+    T bnorm = sqrt(t.b);
+    st->rnorm = rnorm;
+    st->result_norm = rnorm;
+    st->tol = fmax(st->atol, st->rtol * bnorm);
+    if (rnorm <= st->tol) {
+      st->c.status = ST_DONE;
+      st->c.converged = 1;
+      st->c.message = MSG_CONVERGED_INITIAL;
+      return;
+    }
+    st->rho_old = T(1);
+    st->alpha = T(0);
+    st->omega = T(1);
+    if (st->c.max_iter == 0) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_MAX_ITER;
+      return;
+    }
+    // rho = (r_hat, r) with r_hat == r: the same products as ||r||^2
+    T rho = t.a;
+    st->rho = rho;
+    if (fabs(rho) < eps_of<T>() * T(10)) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_BD_RHO;
+      return;
+    }
+    st->beta = (rho / st->rho_old) * (st->alpha / st->omega);
+  }
+};
+
+// p = r + beta (p - omega v); p~ = M1 p for fused M1 (iterative.rs:467-475)
+template <typename T>
+struct BiP {
+  BiState<T>* st;
+  T *p, *pt;
+  const T *r, *v;
+  PrecFused<T> pf1;
+  int store_pt;
+  static constexpr bool kReduce = false;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ void elem(int64_t i, Acc3<T>&) const {
+    T pi = add_rn(r[i], mul_rn(st->beta, sub_rn(p[i], mul_rn(st->omega, v[i]))));
+    p[i] = pi;
+    if (store_pt) pt[i] = pf1.apply(i, pi);
+  }
+  __device__ void finish(const Acc3<T>&) const {}
+};
+
+// (r_hat, v), alpha and its exits (iterative.rs:486-507)
+template <typename T>
+struct EpiBiRhoV {
+  BiState<T>* st;
+  const T* rhat;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ T out(int64_t, T ax) const { return ax; }
+  __device__ void acc(int64_t i, T y, Acc3<T>& a) const { a.a += rhat[i] * y; }
+  __device__ void finish(const Acc3<T>& t) const {
+    T den = t.a;
+    if (fabs(den) < eps_of<T>() * T(10)) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_BD_RHAT_V;
+      st->result_norm = st->rnorm;
+      return;
+    }
+    T alpha = st->rho / den;
+    st->alpha = alpha;
+    if (!isfinite(alpha)) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_BD_ALPHA;
+      st->result_norm = st->rnorm;
+    }
+  }
+};
+
+// y = x + alpha p~; s = r - alpha v; ||s|| (iterative.rs:510-533)
+template <typename T>
+struct BiS {
+  BiState<T>* st;
+  const T *x, *pt, *r, *v;
+  T *y, *s, *stl;
+  PrecFused<T> pf1;
+  int store_st;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ void elem(int64_t i, Acc3<T>& a) const {
+    const T alpha = st->alpha;
+    y[i] = add_rn(x[i], mul_rn(alpha, pt[i]));
+    T si = sub_rn(r[i], mul_rn(alpha, v[i]));
+    s[i] = si;
+    if (store_st) stl[i] = pf1.apply(i, si);
+    a.a += si * si;
+  }
+  __device__ void finish(const Acc3<T>& t) const {
+    T snorm = sqrt(t.a);
+    if (snorm <= st->tol) {
+      st->c.status = ST_DONE;
+      st->c.converged = 1;
+      st->c.message = MSG_CONVERGED;
+      st->c.iterations += 1;
+      st->result_norm = snorm;
+      st->x_is_y = 1;
+    }
+  }
+};
+
+// (t, s), (t, t), omega and its exits (iterative.rs:550-574)
+template <typename T>
+struct EpiBiT {
+  BiState<T>* st;
+  const T* s;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ T out(int64_t, T ax) const { return ax; }
+  __device__ void acc(int64_t i, T t, Acc3<T>& a) const {
+    a.a += t * s[i];
+    a.b += t * t;
+  }
+  __device__ void finish(const Acc3<T>& tot) const {
+    const T e10 = eps_of<T>() * T(10);
+    T ts = tot.a, tt = tot.b;
+    if (tt < e10) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_BD_TT;
+      st->result_norm = st->rnorm;
+      return;
+    }
+    T omega = ts / tt;
+    st->omega = omega;
+    if (!isfinite(omega) || fabs(omega) < e10) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_BD_OMEGA;
+      st->result_norm = st->rnorm;
+    }
+  }
+};
+
+// x = y + omega s~ (then M2 x); r = s - omega t; ||r||; next rho and the
+// loop bookkeeping (iterative.rs:577-606, 450-465).  mode 0: whole step;
+// mode 1: updates only (x into xt for a general M2); mode 2: reductions only.
+template <typename T>
+struct BiR {
+  BiState<T>* st;
+  T *x, *r;
+  const T *y, *stl, *s, *t, *rhat;
+  T* xt;
+  PrecFused<T> pf2;
+  int mode;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const {
+    if (st->c.status != ST_RUNNING) {
+      if (mode != 1 && blockIdx.x == 0 && threadIdx.x == 0)
+        set_cond(st->c.use_cond, st->c.cond, 0u);
+      return true;
+    }
+    return false;
+  }
+  __device__ void elem(int64_t i, Acc3<T>& a) const {
+    if (mode != 2) {
+      const T omega = st->omega;
+      T xi = add_rn(y[i], mul_rn(omega, stl[i]));
+      if (mode == 1) xt[i] = xi;
+      else x[i] = pf2.apply(i, xi);
+      r[i] = sub_rn(s[i], mul_rn(omega, t[i]));
+    }
+    if (mode != 1) {
+      T ri = r[i];
+      a.a += ri * ri;
+      a.b += rhat[i] * ri;
+    }
+  }
+  __device__ void finish(const Acc3<T>& tot) const {
+    if (mode == 1) return;
+    T rnorm = sqrt(tot.a);
+    st->rnorm = rnorm;
+    st->result_norm = rnorm;
+    if (rnorm <= st->tol) {
+      st->c.status = ST_DONE;
+      st->c.converged = 1;
+      st->c.message = MSG_CONVERGED;
+      st->c.iterations += 1;
+    } else {
+      st->rho_old = st->rho;
+      st->c.iterations += 1;
+      if (st->c.iterations >= st->c.max_iter) {
+        st->c.status = ST_DONE;
+        st->c.message = MSG_MAX_ITER;
+      } else {
+        T rho = tot.b;
+        st->rho = rho;
+        if (fabs(rho) < eps_of<T>() * T(10)) {
+          st->c.status = ST_DONE;
+          st->c.message = MSG_BD_RHO;
+        } else {
+          st->beta = (rho / st->rho_old) * (st->alpha / st->omega);
+        }
+      }
+    }
+    if (st->c.budget > 0) st->c.budget -= 1;
+    set_cond(st->c.use_cond, st->c.cond,
+             (st->c.status == ST_RUNNING && st->c.budget > 0) ? 1u : 0u);
+  }
+};
+
+template <typename T>
+static int bicgstab_run(sx_ctx ctx, sx_op a, const void* b, const sx_bicgstab_options* opt,
+                        void* x_out, sx_mem mem, sx_iter_result* res) {
+  const int64_t n = a->nrows;
+  sx_op m1 = opt->left_preconditioner, m2 = opt->right_preconditioner;
+  SX_CHECK(check_prec(a, m1));
+  SX_CHECK(check_prec(a, m2));
+  const int k1 = prec_kind(m1), k2 = prec_kind(m2);
+  const size_t w = sizeof(T);
+  const size_t vb = align_up((size_t)std::max<int64_t>(n, 1) * w, 256);
+  void *ws = nullptr, *dstate = nullptr;
+  SX_CHECK(ws_get(ctx, vb * 13, &ws, &dstate));
+  auto V = [&](int i) { return (T*)((char*)ws + (size_t)i * vb); };
+  T *B = V(0), *X = V(1), *R = V(2), *RH = V(3), *P = V(4), *PT = V(5), *VV = V(6), *Y = V(7),
+    *S = V(8), *STL = V(9), *TT = V(10), *TMP = V(11), *XT = V(12);
+  BiState<T>* st = (BiState<T>*)dstate;
+  SX_CHECK(vec_in(ctx, B, b, n * w, mem));
+  if (opt->x0) SX_CHECK(vec_in(ctx, X, opt->x0, n * w, mem));
+  else if (n > 0) SX_CUDA(cudaMemsetAsync(X, 0, n * w, ctx->stream));
+  BiState<T> h;
+  std::memset(&h, 0, sizeof(h));
+  h.c.max_iter = opt->max_iter;
+  h.rtol = (T)opt->rtol;
+  h.atol = (T)opt->atol;
+  SX_CHECK(write_bytes(ctx, st, &h, sizeof(h)));
+  ReduceArea ra;
+  SX_CHECK(ctx_reduce_area(ctx, std::max<int64_t>((n + kBlock - 1) / kBlock, vec_grid(ctx, n)) + 8, &ra));
+  const PrecFused<T> pf1 = prec_fused<T>(m1), pf2 = prec_fused<T>(m2);
+  SX_CHECK(launch_apply<T>(ctx, a, X, R, EpiResid<T>{B}));
+  SX_CHECK(launch_vec<T>(ctx, n, BiSetup<T>{st, B, R, RH, VV, P}));
+  // p~ and s~: the same buffer as p / s when there is no M1
+  T* ptil = (k1 == PK_NONE) ? P : PT;
+  T* stil = (k1 == PK_NONE) ? S : STL;
+  auto body = [&]() -> int {
+    SX_CHECK(launch_vec<T>(ctx, n, BiP<T>{st, P, PT, R, VV, pf1, (k1 == PK_DIAG || k1 == PK_SCALED) ? 1 : 0}));
+    if (k1 == PK_GENERAL) SX_CHECK(launch_apply<T>(ctx, m1, P, PT, EpiSkip<T, BiState<T>>{st}));
+    if (!m2) {
+      SX_CHECK(launch_apply<T>(ctx, a, ptil, VV, EpiBiRhoV<T>{st, RH}));
+    } else {
+      SX_CHECK(launch_apply<T>(ctx, a, ptil, TMP, EpiSkip<T, BiState<T>>{st}));
+      SX_CHECK(launch_apply<T>(ctx, m2, TMP, VV, EpiBiRhoV<T>{st, RH}));
+    }
+    SX_CHECK(launch_vec<T>(ctx, n, BiS<T>{st, X, ptil, R, VV, Y, S, STL, pf1,
+                                          (k1 == PK_DIAG || k1 == PK_SCALED) ? 1 : 0}));
+    if (k1 == PK_GENERAL) SX_CHECK(launch_apply<T>(ctx, m1, S, STL, EpiSkip<T, BiState<T>>{st}));
+    if (!m2) {
+      SX_CHECK(launch_apply<T>(ctx, a, stil, TT, EpiBiT<T>{st, S}));
+    } else {
+      SX_CHECK(launch_apply<T>(ctx, a, stil, TMP, EpiSkip<T, BiState<T>>{st}));
+      SX_CHECK(launch_apply<T>(ctx, m2, TMP, TT, EpiBiT<T>{st, S}));
+    }
+    if (k2 == PK_GENERAL) {
+      SX_CHECK(launch_vec<T>(ctx, n, BiR<T>{st, X, R, Y, stil, S, TT, RH, XT, pf2, 1}));
+      SX_CHECK(launch_apply<T>(ctx, m2, XT, X, EpiSkip<T, BiState<T>>{st}));
+      SX_CHECK(launch_vec<T>(ctx, n, BiR<T>{st, X, R, Y, stil, S, TT, RH, XT, pf2, 2}));
+    } else {
+      SX_CHECK(launch_vec<T>(ctx, n, BiR<T>{st, X, R, Y, stil, S, TT, RH, XT, pf2, 0}));
+    }
+    return SX_OK;
+  };
+  const uint64_t key[8] = {2, (uint64_t)sizeof(T), a->serial, m1 ? m1->serial : 0,
+                           m2 ? m2->serial : 0, (uint64_t)n, (uint64_t)(uintptr_t)ws, 0};
+  SX_CHECK(run_loop(ctx, st, key,
+                    op_graphable(a) && op_graphable(m1) && op_graphable(m2), body));
+  SX_CHECK(read_ctl(ctx, st, &h, sizeof(h)));
+  if (h.x_is_y) {
+    // x = y, then x = M2 x (iterative.rs:519-524)
+    if (m2) SX_CHECK(launch_apply<T>(ctx, m2, Y, X, EpiPlain<T>{}));
+    else if (n > 0) SX_CUDA(cudaMemcpyAsync(X, Y, n * w, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  SX_CHECK(vec_out(ctx, x_out, X, n * w, mem));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (res) {
+    res->iterations = h.c.iterations;
+    res->residual_norm = (double)h.result_norm;
+    res->converged = h.c.converged;
+    res->message = h.c.message;
+  }
+  return SX_OK;
+}
+
+// ================================================================== GMRES
+// One WHILE iteration = one restart cycle (iterative.rs:695-803).  Arnoldi
+// step j is captured as: w = M A v_j; for i = 0..j one fused kernel that
+// finishes the previous projection (w -= h_{i-1,j} v_{i-1}) and forms
+// h_ij = (v_i, w) -- modified Gram-Schmidt in the reference's order; a final
+// kernel subtracts the last projection and forms ||w||, whose finishing
+// block also applies the Givens rotations; then v_{j+1} = w / ||w||.
+// Kernels of step j return at once unless the cycle is still at step j.
+template <typename T>
+struct GmState {
+  LoopCtl c;
+  T rnorm, tol, rtol, atol, hnorm;
+  int restart, j, active;  // j: inner_iter of the current cycle; active: cycle running
+  int pad3;
+  unsigned long long outer;
+};
+
+template <typename T>
+struct GmArrays {
+  T* h;   // (restart+1) x restart, row-major h[i*restart + j]
+  T* cs;  // restart
+  T* sn;  // restart
+  T* s;   // restart + 1
+  T* y;   // restart
+};
+
+// ||r|| and the setup of a cycle: v_0 = r / ||r||, s = [||r||, 0, ...]
+template <typename T>
+struct GmStart {
+  GmState<T>* st;
+  GmArrays<T> g;
+  const T* r;
+  T* v0;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ void elem(int64_t i, Acc3<T>&) const {
+    // iterative.rs:704: v[0] = r / rnorm
+    v0[i] = r[i] / st->rnorm;
+  }
+  __device__ void finish(const Acc3<T>&) const {
+    const int R = st->restart;
+    for (int q = 0; q < (R + 1) * R; ++q) g.h[q] = T(0);
+    for (int q = 0; q < R; ++q) { g.cs[q] = T(0); g.sn[q] = T(0); }
+    for (int q = 0; q <= R; ++q) g.s[q] = T(0);
+    g.s[0] = st->rnorm;
+    st->j = 0;
+    st->active = (R > 0 && st->outer < st->c.max_iter) ? 1 : 0;
+  }
+};
+
+// w = A v_j (then M w) while the cycle is at step jj
+template <typename T>
+struct EpiGmW {
+  GmState<T>* st;
+  int jj;
+  static constexpr bool kReduce = false;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING || !st->active || st->j != jj; }
+  __device__ T out(int64_t, T ax) const { return ax; }
+  __device__ void acc(int64_t, T, Acc3<T>&) const {}
+  __device__ void finish(const Acc3<T>&) const {}
+};
+
+// MGS projection i of step jj: w -= h_{i-1,jj} v_{i-1} (i > 0); h_{i,jj} = (v_i, w)
+template <typename T>
+struct GmMgs {
+  GmState<T>* st;
+  GmArrays<T> g;
+  T* w;
+  const T *vprev, *vi;
+  int i, jj;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING || !st->active || st->j != jj; }
+  __device__ void elem(int64_t k, Acc3<T>& a) const {
+    T wk = w[k];
+    if (i > 0) {
+      wk = sub_rn(wk, mul_rn(g.h[(i - 1) * st->restart + jj], vprev[k]));
+      w[k] = wk;
+    }
+    a.a += vi[k] * wk;
+  }
+  __device__ void finish(const Acc3<T>& t) const { g.h[i * st->restart + jj] = t.a; }
+};
+
+// last projection, ||w||, breakdown, Givens rotations, convergence
+// (iterative.rs:719-768)
+template <typename T>
+struct GmNorm {
+  GmState<T>* st;
+  GmArrays<T> g;
+  T* w;
+  const T* vj;
+  int jj;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING || !st->active || st->j != jj; }
+  __device__ void elem(int64_t k, Acc3<T>& a) const {
+    T wk = sub_rn(w[k], mul_rn(g.h[jj * st->restart + jj], vj[k]));
+    w[k] = wk;
+    a.a += wk * wk;
+  }
+  __device__ void finish(const Acc3<T>& t) const {
+    const int R = st->restart;
+    T* h = g.h;
+    const int j = jj;
+    T hn = sqrt(t.a);
+    h[(j + 1) * R + j] = hn;
+    st->hnorm = hn;
+    if (hn < eps_of<T>() * T(10)) {
+      st->active = 0;  // happy breakdown: column j is dropped
+      return;
+    }
+    for (int i = 0; i < j; ++i) {
+      T a = h[i * R + j], b = h[(i + 1) * R + j];
+      T temp = add_rn(mul_rn(g.cs[i], a), mul_rn(g.sn[i], b));
+      h[(i + 1) * R + j] = add_rn(mul_rn(-g.sn[i], a), mul_rn(g.cs[i], b));
+      h[i * R + j] = temp;
+    }
+    T hjj = h[j * R + j], hj1 = h[(j + 1) * R + j];
+    T rho = sqrt(add_rn(mul_rn(hjj, hjj), mul_rn(hj1, hj1)));
+    g.cs[j] = hjj / rho;
+    g.sn[j] = hj1 / rho;
+    h[j * R + j] = rho;
+    h[(j + 1) * R + j] = T(0);
+    T temp = add_rn(mul_rn(g.cs[j], g.s[j]), mul_rn(g.sn[j], g.s[j + 1]));
+    g.s[j + 1] = add_rn(mul_rn(-g.sn[j], g.s[j]), mul_rn(g.cs[j], g.s[j + 1]));
+    g.s[j] = temp;
+    st->j = j + 1;
+    // v_{j+1} is normalised by the next kernel with st->hnorm
+    st->active = 2;  // normalise pending, then continue
+  }
+};
+
+// v_{j+1} = w / h_{j+1,j}; decide whether the cycle continues
+template <typename T>
+struct GmNormalize {
+  GmState<T>* st;
+  GmArrays<T> g;
+  const T* w;
+  T* vnext;
+  int jj;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const {
+    return st->c.status != ST_RUNNING || st->active != 2 || st->j != jj + 1;
+  }
+  __device__ void elem(int64_t k, Acc3<T>&) const { vnext[k] = w[k] / st->hnorm; }
+  __device__ void finish(const Acc3<T>&) const {
+    const int j = st->j;
+    bool more = j < st->restart && (unsigned long long)j + st->outer < st->c.max_iter;
+    if (fabs(g.s[j]) <= st->tol) more = false;
+    st->active = more ? 1 : 0;
+  }
+};
+
+// back substitution (iterative.rs:771-779), one thread
+template <typename T>
+__global__ void k_gm_backsub(GmState<T>* st, GmArrays<T> g) {
+  if (st->c.status != ST_RUNNING) return;
+  const int R = st->restart, j = st->j;
+  for (int i = j - 1; i >= 0; --i) {
+    T yi = g.s[i];
+    for (int q = i + 1; q < j; ++q) yi = sub_rn(yi, mul_rn(g.h[i * R + q], g.y[q]));
+    g.y[i] = yi / g.h[i * R + i];
+  }
+}
+
+// x += sum_i y_i v_i in the reference's order (iterative.rs:782-786)
+template <typename T>
+struct GmX {
+  GmState<T>* st;
+  GmArrays<T> g;
+  T* x;
+  const T* vbase;
+  size_t vstride;  // elements between basis vectors
+  static constexpr bool kReduce = false;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ void elem(int64_t k, Acc3<T>&) const {
+    const int j = st->j;
+    T xk = x[k];
+    for (int i = 0; i < j; ++i) xk = add_rn(xk, mul_rn(g.y[i], vbase[(size_t)i * vstride + k]));
+    x[k] = xk;
+  }
+  __device__ void finish(const Acc3<T>&) const {}
+};
+
+// ||r|| after a cycle, outer count, loop condition (iterative.rs:789-803)
+template <typename T>
+struct GmEnd {
+  GmState<T>* st;
+  const T* r;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const {
+    if (st->c.status != ST_RUNNING) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(st->c.use_cond, st->c.cond, 0u);
+      return true;
+    }
+    return false;
+  }
+  __device__ void elem(int64_t i, Acc3<T>& a) const { a.a += r[i] * r[i]; }
+  __device__ void finish(const Acc3<T>& t) const {
+    T rnorm = sqrt(t.a);
+    st->rnorm = rnorm;
+    st->outer += (unsigned long long)st->j;
+    st->c.iterations = st->outer;
+    if (rnorm <= st->tol || !(st->outer < st->c.max_iter)) {
+      st->c.status = ST_DONE;
+      st->c.converged = rnorm <= st->tol ? 1 : 0;
+      st->c.message = st->c.converged ? MSG_CONVERGED : MSG_MAX_ITER;
+    }
+    if (st->c.budget > 0) st->c.budget -= 1;
+    set_cond(st->c.use_cond, st->c.cond,
+             (st->c.status == ST_RUNNING && st->c.budget > 0) ? 1u : 0u);
+  }
+};
+
+// initial ||r|| (after the optional M r) and ||b||
+template <typename T>
+struct GmInit {
+  GmState<T>* st;
+  const T *r, *b;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<T>& a) const {
+    a.a += r[i] * r[i];
+    a.b += b[i] * b[i];
+  }
+  __device__ void finish(const Acc3<T>& t) const {
+    st->rnorm = sqrt(t.a);
+    st->tol = fmax(st->atol, st->rtol * sqrt(t.b));
+    st->outer = 0;
+    if (!(0 < st->c.max_iter && st->rnorm > st->tol)) {
+      st->c.status = ST_DONE;
+      st->c.converged = st->rnorm <= st->tol ? 1 : 0;
+      st->c.message = st->c.converged ? MSG_CONVERGED : MSG_MAX_ITER;
+    }
+  }
+};
+
+template <typename T>
+static int gmres_run(sx_ctx ctx, sx_op a, const void* b, const sx_gmres_options* opt, void* x_out,
+                     sx_mem mem, sx_iter_result* res) {
+  const int64_t n = a->nrows;
+  sx_op m = opt->preconditioner;
+  SX_CHECK(check_prec(a, m));
+  const uint64_t restart64 = std::min<uint64_t>(opt->restart, (uint64_t)n);
+  if (restart64 > 4096)
+    return set_error(SX_ERR_VALUE, "Value error: restart above 4096 is not supported on the device");
+  const int R = (int)restart64;
+  const size_t w = sizeof(T);
+  const size_t vb = align_up((size_t)std::max<int64_t>(n, 1) * w, 256);
+  const size_t small = align_up((size_t)((R + 1) * (R + 1) * 2 + 4 * (R + 2)) * w, 256);
+  void *ws = nullptr, *dstate = nullptr;
+  SX_CHECK(ws_get(ctx, vb * (6 + (size_t)R + 1) + small, &ws, &dstate));
+  auto V = [&](size_t i) { return (T*)((char*)ws + i * vb); };
+  T *B = V(0), *X = V(1), *Rv = V(2), *W = V(3), *TMP = V(4), *AX = V(5);
+  T* basis = V(6);  // R + 1 vectors, stride vb / w elements
+  const size_t vstride = vb / w;
+  T* sm = (T*)((char*)ws + vb * (6 + (size_t)R + 1));
+  GmArrays<T> g;
+  g.h = sm;
+  g.cs = g.h + (size_t)(R + 1) * std::max(R, 1);
+  g.sn = g.cs + std::max(R, 1);
+  g.s = g.sn + std::max(R, 1);
+  g.y = g.s + R + 1;
+  (void)AX;
+  GmState<T>* st = (GmState<T>*)dstate;
+  SX_CHECK(vec_in(ctx, B, b, n * w, mem));
+  if (opt->x0) SX_CHECK(vec_in(ctx, X, opt->x0, n * w, mem));
+  else if (n > 0) SX_CUDA(cudaMemsetAsync(X, 0, n * w, ctx->stream));
+  GmState<T> h;
+  std::memset(&h, 0, sizeof(h));
+  h.c.max_iter = opt->max_iter;
+  h.rtol = (T)opt->rtol;
+  h.atol = (T)opt->atol;
+  h.restart = R;
+  SX_CHECK(write_bytes(ctx, st, &h, sizeof(h)));
+  ReduceArea ra;
+  SX_CHECK(ctx_reduce_area(ctx, std::max<int64_t>((n + kBlock - 1) / kBlock, vec_grid(ctx, n)) + 8, &ra));
+  // r = M (b - A x); ||r||; ||b|| (iterative.rs:677-690)
+  if (m) {
+    SX_CHECK(launch_apply<T>(ctx, a, X, TMP, EpiResid<T>{B}));
+    SX_CHECK(launch_apply<T>(ctx, m, TMP, Rv, EpiPlain<T>{}));
+  } else {
+    SX_CHECK(launch_apply<T>(ctx, a, X, Rv, EpiResid<T>{B}));
+  }
+  SX_CHECK(launch_vec<T>(ctx, n, GmInit<T>{st, Rv, B}));
+  {
+    GmState<T> hs;
+    SX_CHECK(read_ctl(ctx, st, &hs, sizeof(hs)));
+    if (hs.c.status == ST_RUNNING && R == 0)
+      return set_error(SX_ERR_VALUE,
+                       "Value error: restart = 0 makes no progress (the reference loops forever)");
+  }
+  auto body = [&]() -> int {
+    SX_CHECK(launch_vec<T>(ctx, n, GmStart<T>{st, g, Rv, basis}));
+    for (int j = 0; j < R; ++j) {
+      T* vj = basis + (size_t)j * vstride;
+      if (m) {
+        SX_CHECK(launch_apply<T>(ctx, a, vj, TMP, EpiGmW<T>{st, j}));
+        SX_CHECK(launch_apply<T>(ctx, m, TMP, W, EpiGmW<T>{st, j}));
+      } else {
+        SX_CHECK(launch_apply<T>(ctx, a, vj, W, EpiGmW<T>{st, j}));
+      }
+      for (int i = 0; i <= j; ++i) {
+        const T* vprev = i > 0 ? basis + (size_t)(i - 1) * vstride : nullptr;
+        SX_CHECK(launch_vec<T>(ctx, n, GmMgs<T>{st, g, W, vprev, basis + (size_t)i * vstride, i, j}));
+      }
+      SX_CHECK(launch_vec<T>(ctx, n, GmNorm<T>{st, g, W, vj, j}));
+      SX_CHECK(launch_vec<T>(ctx, n, GmNormalize<T>{st, g, W, basis + (size_t)(j + 1) * vstride, j}));
+    }
+    k_gm_backsub<T><<<1, 1, 0, ctx->stream>>>(st, g);
+    ctx->launches++;
+    SX_CHECK(launch_vec<T>(ctx, n, GmX<T>{st, g, X, basis, vstride}));
+    if (m) {
+      SX_CHECK(launch_apply<T>(ctx, a, X, TMP, EpiResid<T>{B}));
+      SX_CHECK(launch_apply<T>(ctx, m, TMP, Rv, EpiPlain<T>{}));
+    } else {
+      SX_CHECK(launch_apply<T>(ctx, a, X, Rv, EpiResid<T>{B}));
+    }
+    SX_CHECK(launch_vec<T>(ctx, n, GmEnd<T>{st, Rv}));
+    return SX_OK;
+  };
+  const uint64_t key[8] = {3, (uint64_t)sizeof(T), a->serial, m ? m->serial : 0,
+                           (uint64_t)n, (uint64_t)(uintptr_t)ws, (uint64_t)R, 0};
+  SX_CHECK(run_loop(ctx, st, key, op_graphable(a) && op_graphable(m), body));
+  SX_CHECK(read_ctl(ctx, st, &h, sizeof(h)));
+  SX_CHECK(vec_out(ctx, x_out, X, n * w, mem));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (res) {
+    res->iterations = h.outer;
+    res->residual_norm = (double)h.rnorm;
+    res->converged = h.rnorm <= h.tol ? 1 : 0;
+    res->message = res->converged ? MSG_CONVERGED : MSG_MAX_ITER;
+  }
+  return SX_OK;
+}
+
+}  // namespace sx
+
+using namespace sx;
+
+static int solver_checks(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, void* x_out,
+                         const char* name) {
+  if (!ctx || !a) return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: null ctx/operator");
+  if (a->nrows != a->ncols)
+    return set_error(SX_ERR_VALUE,
+                     std::string("Value error: Matrix must be square for ") + name + " solver");
+  if (b_len != (uint64_t)a->nrows)
+    return set_error(SX_ERR_DIMENSION_MISMATCH,
+                     "Dimension mismatch: expected " + std::to_string(a->nrows) + ", found " +
+                         std::to_string(b_len),
+                     (uint64_t)a->nrows, b_len);
+  if (a->nrows > 0 && (!b || !x_out))
+    return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: null b/x");
+  SX_CUDA(cudaSetDevice(ctx->device));
+  return SX_OK;
+}
+
+extern "C" {
+
+void sx_cg_options_default(sx_cg_options* o) {
+  o->max_iter = 1000;
+  o->rtol = 1e-8;
+  o->atol = 1e-12;
+  o->x0 = nullptr;
+  o->preconditioner = nullptr;
+}
+void sx_bicgstab_options_default(sx_bicgstab_options* o) {
+  o->max_iter = 1000;
+  o->rtol = 1e-8;
+  o->atol = 1e-12;
+  o->x0 = nullptr;
+  o->left_preconditioner = nullptr;
+  o->right_preconditioner = nullptr;
+}
+void sx_gmres_options_default(sx_gmres_options* o) {
+  o->max_iter = 1000;
+  o->restart = 30;
+  o->rtol = 1e-8;
+  o->atol = 1e-12;
+  o->x0 = nullptr;
+  o->preconditioner = nullptr;
+}
+
+int sx_cg(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_cg_options* opt,
+          void* x_out, sx_mem mem, sx_iter_result* res) {
+  SX_CHECK(solver_checks(ctx, a, b, b_len, x_out, "CG"));
+  sx_cg_options d;
+  if (!opt) { sx_cg_options_default(&d); opt = &d; }
+  int rc = a->dtype == SX_F64 ? cg_run<double>(ctx, a, b, opt, x_out, mem, res)
+                              : cg_run<float>(ctx, a, b, opt, x_out, mem, res);
+  return rc == SX_OK ? clear_error() : rc;
+}
+
+int sx_bicgstab(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_bicgstab_options* opt,
+                void* x_out, sx_mem mem, sx_iter_result* res) {
+  SX_CHECK(solver_checks(ctx, a, b, b_len, x_out, "BiCGSTAB"));
+  sx_bicgstab_options d;
+  if (!opt) { sx_bicgstab_options_default(&d); opt = &d; }
+  int rc = a->dtype == SX_F64 ? bicgstab_run<double>(ctx, a, b, opt, x_out, mem, res)
+                              : bicgstab_run<float>(ctx, a, b, opt, x_out, mem, res);
+  return rc == SX_OK ? clear_error() : rc;
+}
+
+int sx_gmres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_gmres_options* opt,
+             void* x_out, sx_mem mem, sx_iter_result* res) {
+  SX_CHECK(solver_checks(ctx, a, b, b_len, x_out, "GMRES"));
+  sx_gmres_options d;
+  if (!opt) { sx_gmres_options_default(&d); opt = &d; }
+  int rc = a->dtype == SX_F64 ? gmres_run<double>(ctx, a, b, opt, x_out, mem, res)
+                              : gmres_run<float>(ctx, a, b, opt, x_out, mem, res);
+  return rc == SX_OK ? clear_error() : rc;
+}
+
+void sx_solver_cache_release(sx_ctx ctx) {
+  if (!ctx || !ctx->solver_cache) return;
+  SolverCache* c = (SolverCache*)ctx->solver_cache;
+  drop_graphs(c);
+  dev_free(c->ws);
+  dev_free(c->state);
+  delete c;
+  ctx->solver_cache = nullptr;
+}
+
+}  // extern "C"

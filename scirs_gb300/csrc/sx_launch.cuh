@@ -1,0 +1,134 @@
+// Launch layer: y = op(x) with a compile-time epilogue for every operator
+// kind of the library.  Included by the translation units that fuse solver
+// scalar updates into operator applications.
+#pragma once
+
+#include "sx_internal.h"
+#include "sx_kernels.cuh"
+
+namespace sx {
+
+// Epilogue that only stores A x.
+template <typename T>
+struct EpiPlain {
+  static constexpr bool kReduce = false;
+  __device__ bool skip() const { return false; }
+  __device__ T out(int64_t, T ax) const { return ax; }
+  __device__ void acc(int64_t, T, Acc3<T>&) const {}
+  __device__ void finish(const Acc3<T>&) const {}
+};
+
+// Elementwise operators: identity, scaled identity, diagonal, Jacobi.  The
+// product is rounded exactly as the reference's `x_i * d_i`
+// (interface.rs:114, :160-163; preconditioners.rs:78-81).
+template <typename T, class Epi>
+__global__ void __launch_bounds__(kBlock) k_diag_apply(int64_t n, int kind, const T* __restrict__ d,
+                                                       T scale, const T* __restrict__ x, T* y,
+                                                       T* partials, unsigned int* counter, Epi epi) {
+  if (epi.skip()) return;
+  Acc3<T> a{T(0), T(0), T(0)};
+  const int64_t stride = (int64_t)gridDim.x * kBlock;
+  for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) {
+    T xi = x[i];
+    T ax = kind == SX_OP_IDENTITY ? xi : (kind == SX_OP_SCALED_IDENTITY ? mul_rn(xi, scale) : mul_rn(xi, d[i]));
+    T v = epi.out(i, ax);
+    y[i] = v;
+    epi.acc(i, v, a);
+  }
+  if constexpr (Epi::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) epi.finish(tot);
+  }
+}
+
+// Epilogue over an already computed y (after a multi-kernel apply).
+template <typename T, class Epi>
+__global__ void __launch_bounds__(kBlock) k_epi_inplace(int64_t n, T* y, T* partials,
+                                                        unsigned int* counter, Epi epi) {
+  if (epi.skip()) return;
+  Acc3<T> a{T(0), T(0), T(0)};
+  const int64_t stride = (int64_t)gridDim.x * kBlock;
+  for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) {
+    T v = epi.out(i, y[i]);
+    y[i] = v;
+    epi.acc(i, v, a);
+  }
+  if constexpr (Epi::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) epi.finish(tot);
+  }
+}
+
+constexpr int kSpmvItems = 8;
+
+// CSR SpMV with epilogue.  Must not allocate or synchronise: it runs inside
+// stream capture.  The reduction area must already hold gridDim blocks.
+template <typename T, class Epi>
+int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
+  if (c.nrows <= 0) return SX_OK;
+  ReduceArea ra;
+  const int64_t blocks = (c.nrows + kBlock - 1) / kBlock;
+  SX_CHECK(ctx_reduce_area(ctx, blocks, &ra));
+  if (c.monotone) {
+    spmv_stream_kernel<T, kSpmvItems, Epi><<<(unsigned)blocks, kBlock, 0, ctx->stream>>>(
+        c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows, (T*)ra.partials, ra.counter, epi);
+  } else {
+    spmv_rowseq_kernel<T, Epi><<<(unsigned)blocks, kBlock, 0, ctx->stream>>>(
+        c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows, (T*)ra.partials, ra.counter, epi);
+  }
+  ctx->launches++;
+  SX_CUDA(cudaGetLastError());
+  return SX_OK;
+}
+
+template <typename T, class Body>
+int launch_vec(sx_ctx ctx, int64_t n, Body body) {
+  ReduceArea ra;
+  const int g = vec_grid(ctx, n);
+  SX_CHECK(ctx_reduce_area(ctx, g, &ra));
+  vec_kernel<T, Body><<<g, kBlock, 0, ctx->stream>>>(n, (T*)ra.partials, ra.counter, body);
+  ctx->launches++;
+  SX_CUDA(cudaGetLastError());
+  return SX_OK;
+}
+
+template <typename T, class Epi>
+int launch_apply(sx_ctx ctx, sx_op op, const T* x, T* y, Epi epi) {
+  switch (op->kind) {
+    case SX_OP_CSR:
+      return launch_csr<T, Epi>(ctx, op->csr, x, y, epi);
+    case SX_OP_IDENTITY:
+    case SX_OP_SCALED_IDENTITY:
+    case SX_OP_DIAGONAL:
+    case SX_OP_JACOBI: {
+      ReduceArea ra;
+      const int g = vec_grid(ctx, op->nrows);
+      SX_CHECK(ctx_reduce_area(ctx, g, &ra));
+      k_diag_apply<T, Epi><<<g, kBlock, 0, ctx->stream>>>(op->nrows, op->kind, (const T*)op->diag,
+                                                          (T)op->scale, x, y, (T*)ra.partials,
+                                                          ra.counter, epi);
+      ctx->launches++;
+      SX_CUDA(cudaGetLastError());
+      return SX_OK;
+    }
+    case SX_OP_FSAI: {
+      // y = G (G^T x): the second SpMV carries the epilogue
+      SX_CHECK(launch_csr<T, EpiPlain<T>>(ctx, op->transpose->csr, x, (T*)op->work, EpiPlain<T>{}));
+      return launch_csr<T, Epi>(ctx, op->csr, (const T*)op->work, y, epi);
+    }
+    default: {
+      // IC0 and host operators: apply, then run the epilogue over y
+      SX_CHECK(apply_general(ctx, op, x, y));
+      ReduceArea ra;
+      const int g = vec_grid(ctx, op->nrows);
+      SX_CHECK(ctx_reduce_area(ctx, g, &ra));
+      k_epi_inplace<T, Epi><<<g, kBlock, 0, ctx->stream>>>(op->nrows, y, (T*)ra.partials,
+                                                           ra.counter, epi);
+      ctx->launches++;
+      SX_CUDA(cudaGetLastError());
+      return SX_OK;
+    }
+  }
+}
+
+}  // namespace sx

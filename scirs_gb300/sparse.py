@@ -1,0 +1,471 @@
+"""Python host mirror of the scirs2-sparse iterative-solve API over the C ABI.
+
+Names and argument meanings follow the reference crate (scirs2-sparse):
+``CsrMatrix::new`` / ``CsrArray::from_triplets`` construction, the
+``LinearOperator`` slot (operators and preconditioners are the same handle
+type), and ``cg`` / ``bicgstab`` / ``gmres`` with their option defaults
+(linalg/iterative.rs:17-35, :348-368, :614-634).  Errors surface as
+``SparseError`` carrying the SparseError variant name, payload and Display
+text (error.rs:9-74).  Every numeric operation runs in the CUDA library;
+nothing here computes on the host.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+
+_VARIANTS = {
+    1: "ComputationError",
+    2: "DimensionMismatch",
+    3: "IndexOutOfBounds",
+    4: "InvalidAxis",
+    5: "InvalidSliceRange",
+    6: "InconsistentData",
+    7: "NotImplemented",
+    8: "SingularMatrix",
+    9: "ValueError",
+    10: "ConversionError",
+    11: "OperationNotSupported",
+    12: "ShapeMismatch",
+    13: "IterativeSolverFailure",
+    14: "IndexCastOverflow",
+    100: "CudaError",
+    101: "DeviceTimeout",
+    102: "InvalidArgument",
+    103: "OutOfMemory",
+}
+
+
+class SparseError(Exception):
+    """A non-zero status of the C ABI, with the SparseError payload."""
+
+    def __init__(self, code: int, message: str, payload: tuple):
+        super().__init__(message)
+        self.code = code
+        self.variant = _VARIANTS.get(code, "Unknown")
+        self.payload = payload
+        self.message = message
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        info = L.ErrorInfo()
+        L.lib.sx_last_error(C.byref(info))
+        raise SparseError(rc, info.message.decode("utf-8", "replace"),
+                          (info.v0, info.v1, info.v2, info.v3))
+
+
+def message_string(code: int) -> str:
+    return L.lib.sx_message_string(code).decode("utf-8")
+
+
+_NP = {L.SX_F32: np.float32, L.SX_F64: np.float64}
+
+
+def _dtype_code(dtype) -> int:
+    dt = np.dtype(dtype)
+    if dt == np.float64:
+        return L.SX_F64
+    if dt == np.float32:
+        return L.SX_F32
+    raise TypeError(f"unsupported value type {dt}")
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data if a.size else 0
+
+
+class Context:
+    """One CUDA stream, scratch and graph caches on one device."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None):
+        h = L.ctx_t()
+        if stream is None:
+            _check(L.lib.sx_ctx_create(device, C.byref(h)))
+        else:
+            _check(L.lib.sx_ctx_create_on_stream(device, C.c_void_p(stream), C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    @property
+    def stream(self) -> int:
+        return L.lib.sx_ctx_stream(self.handle) or 0
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(L.lib.sx_ctx_kernel_launches(self.handle))
+
+    def synchronize(self) -> None:
+        _check(L.lib.sx_ctx_synchronize(self.handle))
+
+    def close(self) -> None:
+        if self.handle:
+            L.lib.sx_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Operator:
+    """A device operator: CSR matrix, identity/diagonal operator or preconditioner."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+        k = C.c_int()
+        _check(L.lib.sx_op_kind_of(handle, C.byref(k)))
+        self.kind = k.value
+        d = C.c_int()
+        _check(L.lib.sx_op_dtype(handle, C.byref(d)))
+        self.dtype_code = d.value
+        r, c = C.c_uint64(), C.c_uint64()
+        _check(L.lib.sx_op_shape(handle, C.byref(r), C.byref(c)))
+        self.shape = (r.value, c.value)
+        self._keep = None
+
+    @property
+    def dtype(self):
+        return _NP[self.dtype_code]
+
+    def close(self) -> None:
+        if self.handle:
+            L.lib.sx_op_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # LinearOperator::matvec / rmatvec
+    def matvec(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=self.dtype)
+        y = np.empty(self.shape[0], dtype=self.dtype)
+        _check(L.lib.sx_op_matvec(self.ctx.handle, self.handle, _ptr(x), x.size, _ptr(y), L.SX_MEM_HOST))
+        return y
+
+    def rmatvec(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=self.dtype)
+        y = np.empty(self.shape[1], dtype=self.dtype)
+        _check(L.lib.sx_op_rmatvec(self.ctx.handle, self.handle, _ptr(x), x.size, _ptr(y), L.SX_MEM_HOST))
+        return y
+
+    # CSR accessors
+    def csr_info(self):
+        r, c, n, s = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_int()
+        _check(L.lib.sx_csr_info(self.handle, C.byref(r), C.byref(c), C.byref(n), C.byref(s)))
+        return r.value, c.value, n.value, bool(s.value)
+
+    @property
+    def nnz(self) -> int:
+        return self.csr_info()[2]
+
+    @property
+    def has_sorted_indices(self) -> bool:
+        return self.csr_info()[3]
+
+    def to_arrays(self):
+        """(indptr, indices, data) as usize-like uint64 arrays and values."""
+        nr, _, nnz, _ = self.csr_info()
+        indptr = np.empty(nr + 1, dtype=np.uint64)
+        indices = np.empty(nnz, dtype=np.uint64)
+        data = np.empty(nnz, dtype=self.dtype)
+        _check(L.lib.sx_csr_download(self.ctx.handle, self.handle, _ptr(indptr), _ptr(indices), _ptr(data)))
+        return indptr, indices, data
+
+    def get(self, i: int, j: int):
+        out = np.zeros(1, dtype=self.dtype)
+        _check(L.lib.sx_csr_get(self.ctx.handle, self.handle, i, j, _ptr(out)))
+        return out[0]
+
+    def transpose(self) -> "Operator":
+        h = L.op_t()
+        _check(L.lib.sx_csr_transpose(self.ctx.handle, self.handle, C.byref(h)))
+        return Operator(self.ctx, h)
+
+    def astype(self, dtype) -> "Operator":
+        h = L.op_t()
+        _check(L.lib.sx_csr_astype(self.ctx.handle, self.handle, _dtype_code(dtype), C.byref(h)))
+        return Operator(self.ctx, h)
+
+    def to_dense(self) -> np.ndarray:
+        indptr, indices, data = self.to_arrays()
+        d = np.zeros(self.shape, dtype=self.dtype)
+        for r in range(self.shape[0]):
+            for k in range(int(indptr[r]), int(indptr[r + 1])):
+                d[r, int(indices[k])] = data[k]
+        return d
+
+
+# ------------------------------------------------------------ construction
+def csr_matrix(ctx: Context, data, rows, cols, shape, dtype=np.float64) -> Operator:
+    """CsrMatrix::new(data, rows, cols, shape) (csr.rs:92-160)."""
+    return _from_triplets(ctx, rows, cols, data, shape, dtype, L.SX_API_CSR_MATRIX, False)
+
+
+def csr_array_from_triplets(ctx: Context, rows, cols, data, shape, sorted=False,
+                            dtype=np.float64) -> Operator:
+    """CsrArray::from_triplets(rows, cols, data, shape, sorted) (csr_array.rs:152-219)."""
+    return _from_triplets(ctx, rows, cols, data, shape, dtype, L.SX_API_CSR_ARRAY, sorted)
+
+
+def _from_triplets(ctx, rows, cols, data, shape, dtype, api, sorted_):
+    data = np.ascontiguousarray(data, dtype=dtype)
+    rows = np.ascontiguousarray(rows, dtype=np.uint64)
+    cols = np.ascontiguousarray(cols, dtype=np.uint64)
+    if not (len(rows) == len(cols) == len(data)):
+        if api == L.SX_API_CSR_MATRIX:
+            found = min(len(rows), len(cols))
+            raise SparseError(2, f"Dimension mismatch: expected {len(data)}, found {found}",
+                              (len(data), found, 0, 0))
+        raise SparseError(6, "Inconsistent data: rows, cols, and data must have the same length",
+                          (0, 0, 0, 0))
+    h = L.op_t()
+    _check(L.lib.sx_csr_from_triplets(ctx.handle, _dtype_code(dtype), api, _ptr(rows), _ptr(cols),
+                                      _ptr(data), len(data), int(shape[0]), int(shape[1]),
+                                      1 if sorted_ else 0, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def csr_matrix_from_raw(ctx: Context, data, indptr, indices, shape, dtype=np.float64) -> Operator:
+    """CsrMatrix::from_raw_csr(data, indptr, indices, shape) (csr.rs:174-227)."""
+    return _from_raw(ctx, data, indptr, indices, shape, dtype, L.SX_API_CSR_MATRIX)
+
+
+def csr_array(ctx: Context, data, indices, indptr, shape, dtype=np.float64) -> Operator:
+    """CsrArray::new(data, indices, indptr, shape) (csr_array.rs:77-136)."""
+    return _from_raw(ctx, data, indptr, indices, shape, dtype, L.SX_API_CSR_ARRAY)
+
+
+def _from_raw(ctx, data, indptr, indices, shape, dtype, api):
+    data = np.ascontiguousarray(data, dtype=dtype)
+    indptr = np.ascontiguousarray(indptr, dtype=np.uint64)
+    indices = np.ascontiguousarray(indices, dtype=np.uint64)
+    if len(data) != len(indices):
+        if api == L.SX_API_CSR_MATRIX:
+            raise SparseError(2, f"Dimension mismatch: expected {len(data)}, found {len(indices)}",
+                              (len(data), len(indices), 0, 0))
+        raise SparseError(6, "Inconsistent data: data and indices must have the same length",
+                          (0, 0, 0, 0))
+    h = L.op_t()
+    _check(L.lib.sx_csr_from_raw(ctx.handle, _dtype_code(dtype), api, _ptr(indptr), len(indptr),
+                                 _ptr(indices), _ptr(data), len(data), int(shape[0]), int(shape[1]),
+                                 C.byref(h)))
+    return Operator(ctx, h)
+
+
+def csr_from_arrays(ctx: Context, indptr, indices, data, shape, dtype=None) -> Operator:
+    """Device-native upload of int64 row pointers / int32 columns (host numpy)."""
+    dtype = dtype or np.asarray(data).dtype
+    indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+    indices = np.ascontiguousarray(indices, dtype=np.int32)
+    data = np.ascontiguousarray(data, dtype=dtype)
+    h = L.op_t()
+    _check(L.lib.sx_csr_from_raw_i32(ctx.handle, _dtype_code(dtype), _ptr(indptr), _ptr(indices),
+                                     _ptr(data), int(shape[0]), int(shape[1]), len(data),
+                                     L.SX_MEM_HOST, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def identity(ctx: Context, n: int, dtype=np.float64) -> Operator:
+    h = L.op_t()
+    _check(L.lib.sx_op_identity(ctx.handle, _dtype_code(dtype), n, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def scaled_identity(ctx: Context, n: int, scale: float, dtype=np.float64) -> Operator:
+    h = L.op_t()
+    _check(L.lib.sx_op_scaled_identity(ctx.handle, _dtype_code(dtype), n, float(scale), C.byref(h)))
+    return Operator(ctx, h)
+
+
+def diagonal(ctx: Context, diag, dtype=np.float64) -> Operator:
+    d = np.ascontiguousarray(diag, dtype=dtype)
+    h = L.op_t()
+    _check(L.lib.sx_op_diagonal(ctx.handle, _dtype_code(dtype), _ptr(d), d.size, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def host_operator(ctx: Context, n: int, fn, dtype=np.float64) -> Operator:
+    """A user LinearOperator whose matvec runs in Python (staged copies)."""
+    npdt = np.dtype(dtype)
+
+    def cb(user, x, y, nn):
+        xs = np.ctypeslib.as_array(C.cast(x, C.POINTER(C.c_double if npdt == np.float64 else C.c_float)), (nn,))
+        ys = np.ctypeslib.as_array(C.cast(y, C.POINTER(C.c_double if npdt == np.float64 else C.c_float)), (n,))
+        ys[:] = fn(xs.copy())
+        return 0
+
+    cfn = L.HOST_MATVEC_FN(cb)
+    h = L.op_t()
+    _check(L.lib.sx_op_host(ctx.handle, _dtype_code(dtype), n, n, cfn, None, C.byref(h)))
+    op = Operator(ctx, h)
+    op._keep = cfn
+    return op
+
+
+def jacobi(ctx: Context, a: Operator) -> Operator:
+    """JacobiPreconditioner::new(&matrix) (preconditioners.rs:21-44)."""
+    h = L.op_t()
+    _check(L.lib.sx_precond_jacobi(ctx.handle, a.handle, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def jacobi_from_diagonal(ctx: Context, diag, dtype=np.float64) -> Operator:
+    """JacobiPreconditioner::from_diagonal (preconditioners.rs:47-62)."""
+    d = np.ascontiguousarray(diag, dtype=dtype)
+    h = L.op_t()
+    _check(L.lib.sx_precond_jacobi_from_diagonal(ctx.handle, _dtype_code(dtype), _ptr(d), d.size, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def ic0(ctx: Context, a: Operator, textbook: bool = False) -> Operator:
+    """IC0Preconditioner::new(&matrix) (ic.rs:22-135); textbook=True gives standard IC(0)."""
+    h = L.op_t()
+    _check(L.lib.sx_precond_ic0(ctx.handle, a.handle,
+                                L.SX_IC0_TEXTBOOK if textbook else L.SX_IC0_REFERENCE, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def fsai(ctx: Context, g: Operator) -> Operator:
+    """M^-1 = G G^T from a lower-triangular CSR G."""
+    h = L.op_t()
+    _check(L.lib.sx_precond_fsai(ctx.handle, g.handle, C.byref(h)))
+    return Operator(ctx, h)
+
+
+# ----------------------------------------------------------------- solvers
+@dataclass
+class IterationResult:
+    """IterationResult (iterative.rs:8-14)."""
+    x: np.ndarray
+    iterations: int
+    residual_norm: float
+    converged: bool
+    message: str
+
+
+def _result(x, r: L.IterResult) -> IterationResult:
+    return IterationResult(x, int(r.iterations), float(r.residual_norm), bool(r.converged),
+                           message_string(r.message))
+
+
+def _prep(a: Operator, b, x0):
+    b = np.ascontiguousarray(b, dtype=a.dtype)
+    x = np.empty(a.shape[0], dtype=a.dtype)
+    x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=a.dtype)
+    if x0a is not None and x0a.size != a.shape[0]:
+        raise SparseError(2, f"Dimension mismatch: expected {a.shape[0]}, found {x0a.size}",
+                          (a.shape[0], x0a.size, 0, 0))
+    return b, x, x0a
+
+
+def cg(a: Operator, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None,
+       preconditioner: Optional[Operator] = None) -> IterationResult:
+    """cg(a, b, CGOptions { .. }) (iterative.rs:40-162)."""
+    b, x, x0a = _prep(a, b, x0)
+    o = L.CGOptions(max_iter, rtol, atol, _ptr(x0a) if x0a is not None else None,
+                    preconditioner.handle if preconditioner else None)
+    r = L.IterResult()
+    _check(L.lib.sx_cg(a.ctx.handle, a.handle, _ptr(b), b.size, C.byref(o), _ptr(x), L.SX_MEM_HOST, C.byref(r)))
+    return _result(x, r)
+
+
+def bicgstab(a: Operator, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None,
+             left_preconditioner: Optional[Operator] = None,
+             right_preconditioner: Optional[Operator] = None) -> IterationResult:
+    """bicgstab(a, b, BiCGSTABOptions { .. }) (iterative.rs:377-611)."""
+    b, x, x0a = _prep(a, b, x0)
+    o = L.BiCGSTABOptions(max_iter, rtol, atol, _ptr(x0a) if x0a is not None else None,
+                          left_preconditioner.handle if left_preconditioner else None,
+                          right_preconditioner.handle if right_preconditioner else None)
+    r = L.IterResult()
+    _check(L.lib.sx_bicgstab(a.ctx.handle, a.handle, _ptr(b), b.size, C.byref(o), _ptr(x), L.SX_MEM_HOST, C.byref(r)))
+    return _result(x, r)
+
+
+def gmres(a: Operator, b, max_iter=1000, restart=30, rtol=1e-8, atol=1e-12, x0=None,
+          preconditioner: Optional[Operator] = None) -> IterationResult:
+    """gmres(a, b, GMRESOptions { .. }) (iterative.rs:641-816)."""
+    b, x, x0a = _prep(a, b, x0)
+    o = L.GMRESOptions(max_iter, restart, rtol, atol, _ptr(x0a) if x0a is not None else None,
+                       preconditioner.handle if preconditioner else None)
+    r = L.IterResult()
+    _check(L.lib.sx_gmres(a.ctx.handle, a.handle, _ptr(b), b.size, C.byref(o), _ptr(x), L.SX_MEM_HOST, C.byref(r)))
+    return _result(x, r)
+
+
+@dataclass
+class IRResult:
+    x: np.ndarray
+    outer_iterations: int
+    inner_iterations: int
+    rel_residual: float
+    converged: bool
+
+
+def cg_mixed(a64: Operator, b, tol=1e-10, inner_rtol=1e-4, max_outer=30, max_inner=10000,
+             x0=None, preconditioner: Optional[Operator] = None,
+             a32: Optional[Operator] = None) -> IRResult:
+    """FP64 iterative refinement around an FP32 PCG (no reference counterpart)."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.empty(a64.shape[0], dtype=np.float64)
+    x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+    o = L.IROptions()
+    L.lib.sx_ir_options_default(C.byref(o))
+    o.max_outer, o.max_inner, o.tol, o.inner_rtol = max_outer, max_inner, tol, inner_rtol
+    o.x0 = _ptr(x0a) if x0a is not None else None
+    o.preconditioner = preconditioner.handle if preconditioner else None
+    o.a32 = a32.handle if a32 else None
+    r = L.IRResult()
+    _check(L.lib.sx_cg_mixed(a64.ctx.handle, a64.handle, _ptr(b), b.size, C.byref(o), _ptr(x),
+                             L.SX_MEM_HOST, C.byref(r)))
+    return IRResult(x, int(r.outer_iterations), int(r.inner_iterations), float(r.rel_residual),
+                    bool(r.converged))
+
+
+def true_rel_residual(a64: Operator, b, x) -> float:
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = C.c_double()
+    _check(L.lib.sx_true_rel_residual(a64.ctx.handle, a64.handle, _ptr(b), _ptr(x), L.SX_MEM_HOST,
+                                      C.byref(out)))
+    return out.value
+
+
+# -------------------------------------------------------------- generators
+GEN_KINDS = {"poisson2d": 0, "laplace3d": 1, "varcoef3d": 2, "varcoef2d": 3, "aniso_q1": 4,
+             "powerlaw": 5}
+
+
+def generate(kind: str, nx: int, ny: int = 1, nz: int = 1, seed: int = 0, param0: float = 0.0,
+             param1: float = 0.0):
+    """Seeded synthetic CSR: returns (indptr int64, indices int32, values float64)."""
+    spec = L.GenSpec(GEN_KINDS[kind], nx, ny, nz, seed, param0, param1)
+    n, nnz = C.c_int64(), C.c_int64()
+    rc = L.lib.sx_gen_matrix(C.byref(spec), C.byref(n), C.byref(nnz), None, None, None)
+    if rc:
+        raise ValueError(f"generator {kind} rejected its arguments ({rc})")
+    indptr = np.empty(n.value + 1, dtype=np.int64)
+    indices = np.empty(nnz.value, dtype=np.int32)
+    vals = np.empty(nnz.value, dtype=np.float64)
+    rc = L.lib.sx_gen_matrix(C.byref(spec), C.byref(n), C.byref(nnz), _ptr(indptr), _ptr(indices), _ptr(vals))
+    if rc:
+        raise ValueError(f"generator {kind} failed ({rc})")
+    return indptr, indices, vals
+
+
+def rhs_normal(seed: int, n: int) -> np.ndarray:
+    b = np.empty(n, dtype=np.float64)
+    L.lib.sx_gen_rhs_normal(seed, n, _ptr(b))
+    return b
