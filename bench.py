@@ -188,7 +188,14 @@ def run_ours(args):
     x_dev = torch.empty(n, dtype=torch.float64, device=dev)
     b_pin = torch.from_numpy(b).pin_memory()
     x_pin = torch.empty(n, dtype=torch.float64).pin_memory()
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    flush = torch.ones(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    flush_out = torch.empty(1, dtype=torch.float32, device=dev)
+
+    def l2_flush():
+        # read 512 MB (4x L2): evicts the previous step's lines without
+        # leaving dirty lines behind for the next kernel to write back
+        torch.sum(flush, dim=0, out=flush_out)
+
     torch.cuda.synchronize()
 
     import ctypes as C
@@ -216,7 +223,7 @@ def run_ours(args):
         times = []
         launches0 = ctx.kernel_launches
         for _ in range(steps):
-            flush.zero_()  # L2 flush between steps (outside the events)
+            l2_flush()  # between steps, outside the events
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -258,7 +265,7 @@ def run_ours(args):
             L.lib.sx_spmv_ex(ctx.handle, op.handle, C.c_void_p(xbuf.data_ptr()), C.c_void_p(ybuf.data_ptr()), 1)
         total = 0.0
         for _ in range(reps):
-            flush.zero_()
+            l2_flush()
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -271,6 +278,20 @@ def run_ours(args):
         return total / reps
 
     peak, peak_kind = load_peaks()
+    # sanity reference for the timing method: a plain device copy of 1 GiB
+    cbuf_a = torch.empty(256 * 1024 * 1024, dtype=torch.float32, device=dev)
+    cbuf_b = torch.empty_like(cbuf_a)
+    for _ in range(3):
+        cbuf_b.copy_(cbuf_a)
+    torch.cuda.synchronize()
+    ce0, ce1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ce0.record()
+    for _ in range(5):
+        cbuf_b.copy_(cbuf_a)
+    ce1.record()
+    ce1.synchronize()
+    copy_gbs = 5 * 2 * cbuf_a.numel() * 4 / (ce0.elapsed_time(ce1) / 1e3) / 1e9
+    del cbuf_a, cbuf_b
     x32 = torch.randn(n, dtype=torch.float32, device=dev)
     y32 = torch.empty(n, dtype=torch.float32, device=dev)
     x64 = torch.randn(n, dtype=torch.float64, device=dev)
@@ -340,6 +361,7 @@ def run_ours(args):
                      "frac": b32 / t32 / 1e9 / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": b32, "traffic": traffic},
         "spmv_sweep": sweep,
+        "copy_gbs_same_run": copy_gbs,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
@@ -353,6 +375,47 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_profile(args):
+    """A few launches of one kernel for ncu (small, self-contained)."""
+    import torch
+
+    import scirs_gb300 as S
+    from scirs_gb300 import _lib as L
+    import ctypes as C
+
+    ctx = S.Context(0)
+    if args.profile == "solve":
+        ip, ix, v, n, b = build_problem()
+        a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+        a32 = a64.astype(np.float32)
+        m32 = S.jacobi(ctx, a32)
+        for _ in range(args.steps):
+            r = S.cg_mixed(a64, b, tol=TOL, inner_rtol=args.inner_rtol, preconditioner=m32, a32=a32)
+        print(json.dumps({"profile": "solve", "n": n, "outer": r.outer_iterations,
+                          "inner": r.inner_iterations, "rel_residual": r.rel_residual}))
+        for op in (m32, a32, a64):
+            op.close()
+        ctx.close()
+        return
+    if args.profile in ("spmv32", "spmv64"):
+        ip, ix, v = S.generate("laplace3d", GRID, GRID, GRID)
+    else:
+        ip, ix, v = S.generate("powerlaw", 4194304, seed=1, param0=16.0, param1=4096.0)
+    n = len(ip) - 1
+    dt = np.float64 if args.profile.endswith("64") else np.float32
+    a = S.csr_from_arrays(ctx, ip, ix, v.astype(dt), (n, n))
+    tdt = torch.float64 if dt == np.float64 else torch.float32
+    x = torch.randn(n, dtype=tdt, device="cuda")
+    y = torch.empty(n, dtype=tdt, device="cuda")
+    for _ in range(args.steps):
+        S.sparse._check(L.lib.sx_spmv_ex(ctx.handle, a.handle, C.c_void_p(x.data_ptr()),
+                                         C.c_void_p(y.data_ptr()), 1))
+    ctx.synchronize()
+    print(json.dumps({"profile": args.profile, "n": n, "nnz": len(v), "launches": args.steps}))
+    a.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -363,8 +426,13 @@ def main():
     ap.add_argument("--no-sweep", dest="sweep", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iters", type=int, default=60)
+    ap.add_argument("--profile", default=None,
+                    choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "solve"],
+                    help="run a few launches of one SpMV for an ncu capture and exit")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -293,6 +293,41 @@ void sx_ir_options_default(sx_ir_options* o);
 int sx_cg_mixed(sx_ctx ctx, sx_op a64, const double* b, uint64_t b_len, const sx_ir_options* opt,
                 double* x_out, sx_mem mem, sx_ir_result* res);
 
+/* --------------------------------------------- batched PCG (no reference
+ * counterpart: batches the one-system-per-call cg of iterative.rs:40-162) */
+/* Thousands of independent SPD systems stored as one block-diagonal CSR
+ * (system s owns rows and columns [sys_ptr[s], sys_ptr[s+1])).  Per system:
+ * FP64 iterative refinement around an FP32 Jacobi-PCG, stopping when
+ * ||b_s - A_s x_s|| <= max(atol, rtol ||b_s||) in FP64.  All systems advance
+ * together in persistent kernels over the blocks of still-running systems,
+ * the iteration loop captured in a CUDA graph. */
+typedef struct {
+  uint64_t max_iter;   /* inner iterations per refinement step, default 10000 */
+  double rtol;         /* default 1e-8 (FP64 true residual, per system) */
+  double atol;         /* default 0 */
+  double inner_rtol;   /* default 1e-4 */
+  uint64_t max_outer;  /* default 30 */
+} sx_batched_options;
+typedef struct {
+  uint64_t inner_iterations;
+  double rel_residual; /* final FP64 true relative residual of the system */
+  int converged;
+} sx_batched_result;
+typedef struct {
+  uint64_t outer_iterations;
+  uint64_t converged_systems;
+  uint64_t max_inner_iterations;
+  uint64_t total_inner_iterations;
+  double worst_rel_residual;
+  uint64_t kernel_launches;
+} sx_batched_summary;
+void sx_batched_options_default(sx_batched_options* o);
+/* a64: FP64 block-diagonal CSR; a32: its FP32 copy (NULL = made inside);
+ * per_system: nsys entries or NULL. */
+int sx_batched_pcg(sx_ctx ctx, sx_op a64, sx_op a32, const int64_t* sys_ptr, uint64_t nsys,
+                   const double* b, double* x, const sx_batched_options* opt, sx_mem mem,
+                   sx_batched_result* per_system, sx_batched_summary* summary);
+
 /* FP64 true relative residual ||b - A x||_2 / ||b||_2 of an FP64 CSR. */
 int sx_true_rel_residual(sx_ctx ctx, sx_op a64, const double* b, const double* x, sx_mem mem,
                          double* out);

@@ -38,6 +38,14 @@ typedef struct {
 int sx_gen_matrix(const sx_gen_spec* spec, int64_t* n_out, int64_t* nnz_out, int64_t* indptr,
                   int32_t* indices, double* vals);
 
+/* A batch of 2D variable-coefficient 5-point systems (SX_GEN_VARCOEF2D
+ * each), square sides uniform in [side_min, side_max], coefficients
+ * exp(sigma N(0,1)), assembled as one block-diagonal CSR.  Call with
+ * indptr == NULL to get the sizes and sys_ptr (nsys + 1 entries). */
+int sx_gen_batch_varcoef2d(uint64_t nsys, int64_t side_min, int64_t side_max, uint64_t seed,
+                           double sigma, int64_t* sys_ptr, int64_t* n_out, int64_t* nnz_out,
+                           int64_t* indptr, int32_t* indices, double* vals);
+
 /* b_i ~ N(0, 1) from the seed. */
 void sx_gen_rhs_normal(uint64_t seed, int64_t n, double* b);
 

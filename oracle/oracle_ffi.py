@@ -138,7 +138,9 @@ def op_csr_i32(indptr, indices, data, shape, f64=True):
     if not f64:
         # an FP32 operator over the same arrays (values rounded to float)
         d32 = d.astype(np.float32)
-        h32 = lib().or_op_csr(0, p(ip.astype(np.uint64)), p(ix.astype(np.uint64)), p(d32), shape[0], shape[1])
+        ip64 = ip.astype(np.uint64)
+        ix64 = ix.astype(np.uint64)
+        h32 = lib().or_op_csr(0, p(ip64), p(ix64), p(d32), shape[0], shape[1])
         return Op(h32, shape[0], False)
     return op
 

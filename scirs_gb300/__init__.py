@@ -6,7 +6,10 @@ sm_103a CUDA kernels behind the C ABI in include/scirs_sparse.h; this
 package is the Python mirror of the reference API over that ABI.
 """
 from .sparse import (  # noqa: F401
+    BatchedResult,
     Context,
+    batched_pcg,
+    generate_batch,
     IRResult,
     IterationResult,
     Operator,

@@ -9,7 +9,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from .build import LIB_PATH
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libscirs_sparse_gpu.so")
 
 if not os.path.exists(LIB_PATH):
     raise ImportError(
@@ -121,6 +121,35 @@ class GenSpec(C.Structure):
     ]
 
 
+class BatchedOptions(C.Structure):
+    _fields_ = [
+        ("max_iter", c_u64),
+        ("rtol", c_dbl),
+        ("atol", c_dbl),
+        ("inner_rtol", c_dbl),
+        ("max_outer", c_u64),
+    ]
+
+
+class BatchedResult(C.Structure):
+    _fields_ = [
+        ("inner_iterations", c_u64),
+        ("rel_residual", c_dbl),
+        ("converged", c_int),
+    ]
+
+
+class BatchedSummary(C.Structure):
+    _fields_ = [
+        ("outer_iterations", c_u64),
+        ("converged_systems", c_u64),
+        ("max_inner_iterations", c_u64),
+        ("total_inner_iterations", c_u64),
+        ("worst_rel_residual", c_dbl),
+        ("kernel_launches", c_u64),
+    ]
+
+
 HOST_MATVEC_FN = C.CFUNCTYPE(c_int, c_vp, c_vp, c_vp, c_u64)
 
 P = C.POINTER
@@ -168,6 +197,10 @@ _SIGS = {
     "sx_true_rel_residual": (c_int, [ctx_t, op_t, c_vp, c_vp, c_int, P(c_dbl)]),
     "sx_gen_matrix": (c_int, [P(GenSpec), P(c_i64), P(c_i64), c_vp, c_vp, c_vp]),
     "sx_gen_rhs_normal": (None, [c_u64, c_i64, c_vp]),
+    "sx_gen_batch_varcoef2d": (c_int, [c_u64, c_i64, c_i64, c_u64, c_dbl, c_vp, P(c_i64), P(c_i64), c_vp, c_vp, c_vp]),
+    "sx_batched_options_default": (None, [P(BatchedOptions)]),
+    "sx_batched_pcg": (c_int, [ctx_t, op_t, op_t, c_vp, c_u64, c_vp, c_vp, P(BatchedOptions), c_int,
+                               c_vp, P(BatchedSummary)]),
 }
 
 MISSING = []

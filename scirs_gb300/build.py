@@ -25,6 +25,7 @@ SOURCES = [
     "sx_krylov.cu",
     "sx_ic0.cu",
     "sx_mixed.cu",
+    "sx_batched.cu",
     "sx_gen.cpp",
 ]
 

@@ -275,6 +275,10 @@ static int scan_exclusive(sx_ctx ctx, const int32_t* in, int64_t m, int32_t* out
   return rc;
 }
 
+int exclusive_scan_i32(sx_ctx ctx, const int32_t* in, int64_t m, int32_t* out) {
+  return scan_exclusive(ctx, in, m, out);
+}
+
 namespace {
 
 // Scatter triplet k into its row's slot range with key (col << 32 | k).
@@ -1261,6 +1265,7 @@ int sx_op_matvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, s
   if (mem == SX_MEM_DEVICE) {
     SX_CHECK(spmv_device(ctx, op, x, y, SX_SPMV_EXACT));
     SX_CUDA(cudaStreamSynchronize(ctx->stream));
+    SX_CHECK(ic0_health(ctx, op));
     return clear_error();
   }
   void *dx = nullptr, *dy = nullptr;
@@ -1273,6 +1278,7 @@ int sx_op_matvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, s
       cudaMemcpyAsync(y, dy, op->nrows * w, cudaMemcpyDeviceToHost, ctx->stream);
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
       if (e != cudaSuccess) rc = cuda_fail(e, "matvec", __FILE__, __LINE__);
+      else rc = ic0_health(ctx, op);
     }
   }
   dev_free(dx);

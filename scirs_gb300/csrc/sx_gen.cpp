@@ -363,4 +363,46 @@ int sx_gen_matrix(const sx_gen_spec* spec, int64_t* n_out, int64_t* nnz_out, int
   }
 }
 
+int sx_gen_batch_varcoef2d(uint64_t nsys, int64_t side_min, int64_t side_max, uint64_t seed,
+                           double sigma, int64_t* sys_ptr, int64_t* n_out, int64_t* nnz_out,
+                           int64_t* indptr, int32_t* indices, double* vals) {
+  if (!sys_ptr || !n_out || !nnz_out || side_min < 1 || side_max < side_min) return 2;
+  std::vector<int64_t> side(nsys), nnz_ptr(nsys + 1, 0);
+  sys_ptr[0] = 0;
+  for (uint64_t s = 0; s < nsys; ++s) {
+    SplitMix64 r(stream_seed(seed, s, 0x5AD));
+    side[s] = side_min + (int64_t)(r.uniform() * (double)(side_max - side_min + 1));
+    if (side[s] > side_max) side[s] = side_max;
+    sys_ptr[s + 1] = sys_ptr[s] + side[s] * side[s];
+    nnz_ptr[s + 1] = nnz_ptr[s] + stencil5_nnz(side[s], side[s]);
+  }
+  *n_out = sys_ptr[nsys];
+  *nnz_out = nnz_ptr[nsys];
+  if (!indptr) return 0;
+  // systems in parallel; each writes its own slice with global numbering
+  unsigned hw = std::thread::hardware_concurrency();
+  int nt = hw ? (int)std::min<unsigned>(hw, 64) : 4;
+  std::vector<std::thread> th;
+  std::vector<int> rc(nt, 0);
+  for (int t = 0; t < nt; ++t) {
+    th.emplace_back([&, t]() {
+      for (uint64_t s = t; s < nsys; s += nt) {
+        sx_gen_spec sp{SX_GEN_VARCOEF2D, side[s], side[s], 1, seed * 0x9E3779B97F4A7C15ull + s + 1, sigma, 0.0};
+        int64_t n = 0, nnz = 0;
+        const int64_t r0 = sys_ptr[s], k0 = nnz_ptr[s];
+        std::vector<int64_t> ip(side[s] * side[s] + 1);
+        int e = sx_gen_matrix(&sp, &n, &nnz, ip.data(), indices + k0, vals + k0);
+        if (e) { rc[t] = e; return; }
+        for (int64_t i = 0; i < n; ++i) indptr[r0 + i] = ip[i] + k0;
+        for (int64_t k = 0; k < nnz; ++k) indices[k0 + k] += (int32_t)r0;
+      }
+    });
+  }
+  for (auto& x : th) x.join();
+  indptr[*n_out] = *nnz_out;
+  for (int e : rc)
+    if (e) return e;
+  return 0;
+}
+
 }  // extern "C"

@@ -123,6 +123,9 @@ int spmv_device(sx_ctx ctx, sx_op a, const void* x, void* y, unsigned flags);
 // for host callbacks.
 int apply_general(sx_ctx ctx, sx_op op, const void* x, void* y);
 
+// Abort flag of an IC(0) operator's bounded waits -> SX_ERR_DEVICE_TIMEOUT.
+int ic0_health(sx_ctx ctx, sx_op op);
+
 // Cached transpose of a CSR operator (rmatvec, FSAI's G^T).
 int ensure_transpose(sx_ctx ctx, sx_op a);
 int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out);

@@ -99,12 +99,35 @@ __device__ __forceinline__ bool grid_reduce3(Acc3<T> v, T* partials, unsigned in
 //   void acc(int64_t row, T y, Acc3<T>& a)   -> per-row reduction terms
 //   static constexpr bool kReduce            -> run the grid reduction
 //   void finish(const Acc3<T>& tot)          -> thread 0 of the last block
+template <typename T>
+struct Vec4 {
+  T v[4];
+};
+
+// 4 consecutive values with 128-bit loads (two for double)
+__device__ __forceinline__ Vec4<float> ld4(const float* p) {
+  float4 a = __ldcs(reinterpret_cast<const float4*>(p));
+  return Vec4<float>{{a.x, a.y, a.z, a.w}};
+}
+__device__ __forceinline__ Vec4<double> ld4(const double* p) {
+  double2 a = __ldcs(reinterpret_cast<const double2*>(p));
+  double2 b = __ldcs(reinterpret_cast<const double2*>(p) + 1);
+  return Vec4<double>{{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ int4 ld4i(const int32_t* p) {
+  return __ldcs(reinterpret_cast<const int4*>(p));
+}
+
 template <typename T, int ITEMS, class Epi>
 __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
     const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
     const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, int64_t nrows,
     T* partials, unsigned int* counter, Epi epi) {
   if (epi.skip()) return;
+  // A tile covers TILE nonzeros starting at a multiple of 4, so every thread
+  // moves 4 consecutive columns and values with 128-bit loads; the products
+  // go to shared memory and each thread then sums its own row in order.
+  constexpr int CH = ITEMS / 4;
   constexpr int TILE = kBlock * ITEMS;
   __shared__ int32_t s_ptr[kBlock + 1];
   __shared__ T s_prod[TILE];
@@ -118,12 +141,27 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
   int32_t my_s = 0, my_e = 0;
   if (tid < nr) { my_s = s_ptr[tid]; my_e = s_ptr[tid + 1]; }
   T acc = T(0);
-  for (int32_t base = s; base < e; base += TILE) {
+  for (int32_t base = s & ~3; base < e; base += TILE) {
     const int32_t tend = min(e, base + TILE);
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-      const int32_t k = base + j * kBlock + tid;
-      if (k < tend) s_prod[k - base] = mul_rn(vals[k], __ldg(x + indices[k]));
+    for (int c = 0; c < CH; ++c) {
+      const int32_t k0 = base + (c * kBlock + tid) * 4;
+      if (k0 < tend) {
+        // k0 + 3 < e implies an in-bounds vector (e <= nnz)
+        if (k0 + 3 < e) {
+          const int4 ci = ld4i(indices + k0);
+          const Vec4<T> cv = ld4(vals + k0);
+          const int cc[4] = {ci.x, ci.y, ci.z, ci.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (k0 + q >= s) s_prod[k0 + q - base] = mul_rn(cv.v[q], __ldg(x + cc[q]));
+        } else {
+          for (int q = 0; q < 4; ++q) {
+            const int32_t k = k0 + q;
+            if (k >= s && k < e) s_prod[k - base] = mul_rn(vals[k], __ldg(x + indices[k]));
+          }
+        }
+      }
     }
     __syncthreads();
     if (tid < nr) {

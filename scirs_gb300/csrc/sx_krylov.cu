@@ -67,17 +67,6 @@ __device__ __forceinline__ void set_cond(int use, cudaGraphConditionalHandle h, 
 template <typename T>
 __device__ __forceinline__ T eps_of() { return sizeof(T) == 8 ? (T)2.220446049250313e-16 : (T)1.1920928955078125e-07f; }
 
-// Epilogue y = b - A x (initial residuals: iterative.rs:78-79, :416-417, :677-678).
-template <typename T>
-struct EpiResid {
-  const T* b;
-  static constexpr bool kReduce = false;
-  __device__ bool skip() const { return false; }
-  __device__ T out(int64_t i, T ax) const { return sub_rn(b[i], ax); }
-  __device__ void acc(int64_t, T, Acc3<T>&) const {}
-  __device__ void finish(const Acc3<T>&) const {}
-};
-
 // Loop control shared by every solver state (first member of each state):
 // the host rewrites only the tail fields (use_cond .. cond) between graph
 // launches; everything else is owned by the device.
@@ -476,6 +465,8 @@ static int cg_run(sx_ctx ctx, sx_op a, const void* b, const sx_cg_options* opt, 
   const uint64_t key[8] = {1, (uint64_t)sizeof(T), a->serial, m ? m->serial : 0,
                            (uint64_t)n, (uint64_t)(uintptr_t)ws, (uint64_t)pk, 0};
   SX_CHECK(run_loop(ctx, st, key, op_graphable(a) && op_graphable(m), body));
+  SX_CHECK(ic0_health(ctx, m));
+  SX_CHECK(ic0_health(ctx, a));
   SX_CHECK(read_ctl(ctx, st, &h, sizeof(h)));
   SX_CHECK(vec_out(ctx, x_out, X, n * w, mem));
   SX_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -783,6 +774,8 @@ static int bicgstab_run(sx_ctx ctx, sx_op a, const void* b, const sx_bicgstab_op
                            m2 ? m2->serial : 0, (uint64_t)n, (uint64_t)(uintptr_t)ws, 0};
   SX_CHECK(run_loop(ctx, st, key,
                     op_graphable(a) && op_graphable(m1) && op_graphable(m2), body));
+  SX_CHECK(ic0_health(ctx, m1));
+  SX_CHECK(ic0_health(ctx, m2));
   SX_CHECK(read_ctl(ctx, st, &h, sizeof(h)));
   if (h.x_is_y) {
     // x = y, then x = M2 x (iterative.rs:519-524)
@@ -1123,6 +1116,7 @@ static int gmres_run(sx_ctx ctx, sx_op a, const void* b, const sx_gmres_options*
   const uint64_t key[8] = {3, (uint64_t)sizeof(T), a->serial, m ? m->serial : 0,
                            (uint64_t)n, (uint64_t)(uintptr_t)ws, (uint64_t)R, 0};
   SX_CHECK(run_loop(ctx, st, key, op_graphable(a) && op_graphable(m), body));
+  SX_CHECK(ic0_health(ctx, m));
   SX_CHECK(read_ctl(ctx, st, &h, sizeof(h)));
   SX_CHECK(vec_out(ctx, x_out, X, n * w, mem));
   SX_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -18,6 +18,17 @@ struct EpiPlain {
   __device__ void finish(const Acc3<T>&) const {}
 };
 
+// Epilogue y = b - A x (initial residuals: iterative.rs:78-79, :416-417, :677-678).
+template <typename T>
+struct EpiResid {
+  const T* b;
+  static constexpr bool kReduce = false;
+  __device__ bool skip() const { return false; }
+  __device__ T out(int64_t i, T ax) const { return sub_rn(b[i], ax); }
+  __device__ void acc(int64_t, T, Acc3<T>&) const {}
+  __device__ void finish(const Acc3<T>&) const {}
+};
+
 // Elementwise operators: identity, scaled identity, diagonal, Jacobi.  The
 // product is rounded exactly as the reference's `x_i * d_i`
 // (interface.rs:114, :160-163; preconditioners.rs:78-81).

@@ -434,6 +434,54 @@ def cg_mixed(a64: Operator, b, tol=1e-10, inner_rtol=1e-4, max_outer=30, max_inn
                     bool(r.converged))
 
 
+@dataclass
+class BatchedResult:
+    x: np.ndarray
+    inner_iterations: np.ndarray
+    rel_residual: np.ndarray
+    converged: np.ndarray
+    outer_iterations: int
+    kernel_launches: int
+
+
+def batched_pcg(a64: Operator, sys_ptr, b, rtol=1e-8, atol=0.0, inner_rtol=1e-4, max_iter=10000,
+                max_outer=30, a32: Optional[Operator] = None) -> BatchedResult:
+    """Batched FP64-refined FP32 Jacobi-PCG over a block-diagonal CSR."""
+    sys_ptr = np.ascontiguousarray(sys_ptr, dtype=np.int64)
+    nsys = len(sys_ptr) - 1
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.empty(a64.shape[0], dtype=np.float64)
+    o = L.BatchedOptions(max_iter, rtol, atol, inner_rtol, max_outer)
+    per = (L.BatchedResult * max(nsys, 1))()
+    summ = L.BatchedSummary()
+    _check(L.lib.sx_batched_pcg(a64.ctx.handle, a64.handle, a32.handle if a32 else None, _ptr(sys_ptr),
+                                nsys, _ptr(b), _ptr(x), C.byref(o), L.SX_MEM_HOST, per, C.byref(summ)))
+    return BatchedResult(x,
+                         np.array([per[i].inner_iterations for i in range(nsys)], dtype=np.int64),
+                         np.array([per[i].rel_residual for i in range(nsys)]),
+                         np.array([bool(per[i].converged) for i in range(nsys)]),
+                         int(summ.outer_iterations), int(summ.kernel_launches))
+
+
+def generate_batch(nsys: int, side_min: int, side_max: int, seed: int = 0, sigma: float = 1.0):
+    """Block-diagonal batch of 2D variable-coefficient systems:
+    (sys_ptr, indptr, indices, values)."""
+    sys_ptr = np.empty(nsys + 1, dtype=np.int64)
+    n, nnz = C.c_int64(), C.c_int64()
+    rc = L.lib.sx_gen_batch_varcoef2d(nsys, side_min, side_max, seed, sigma, _ptr(sys_ptr), C.byref(n),
+                                      C.byref(nnz), None, None, None)
+    if rc:
+        raise ValueError(f"batch generator failed ({rc})")
+    indptr = np.empty(n.value + 1, dtype=np.int64)
+    indices = np.empty(nnz.value, dtype=np.int32)
+    vals = np.empty(nnz.value, dtype=np.float64)
+    rc = L.lib.sx_gen_batch_varcoef2d(nsys, side_min, side_max, seed, sigma, _ptr(sys_ptr), C.byref(n),
+                                      C.byref(nnz), _ptr(indptr), _ptr(indices), _ptr(vals))
+    if rc:
+        raise ValueError(f"batch generator failed ({rc})")
+    return sys_ptr, indptr, indices, vals
+
+
 def true_rel_residual(a64: Operator, b, x) -> float:
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.ascontiguousarray(x, dtype=np.float64)
