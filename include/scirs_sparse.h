@@ -293,6 +293,33 @@ void sx_ir_options_default(sx_ir_options* o);
 int sx_cg_mixed(sx_ctx ctx, sx_op a64, const double* b, uint64_t b_len, const sx_ir_options* opt,
                 double* x_out, sx_mem mem, sx_ir_result* res);
 
+/* ------------------------------ learned factorised sparse approximate inverse
+ * (no reference counterpart; nearest relative SpaiPreconditioner,
+ * linalg/spai.rs:15-192, a different method).  A message-passing network
+ * over the graph of A predicts a lower-triangular G on the pattern of
+ * lower(A) with a softplus diagonal; M^-1 = G G^T is applied as two SpMVs.
+ * Trained on the device by its own forward/backward kernels with the
+ * random-probe loss ||(G^T A G - I) Z||^2 / (k n) on the Jacobi-scaled A. */
+typedef struct sx_gnn_s* sx_gnn;
+uint64_t sx_gnn_num_params(void);
+/* params: sx_gnn_num_params() floats, or NULL for a seeded initialisation
+ * that starts at G = D^-1/2 (Jacobi). */
+int sx_gnn_create(sx_ctx ctx, const float* params, uint64_t seed, sx_gnn* out);
+int sx_gnn_destroy(sx_gnn net);
+int sx_gnn_get_params(sx_ctx ctx, sx_gnn net, float* out);
+int sx_gnn_set_params(sx_ctx ctx, sx_gnn net, const float* in);
+/* Loss and gradient without an update.  probes: host n x 4 row-major, or
+ * NULL for seeded Gaussian probes; grad_out: host, may be NULL. */
+int sx_gnn_loss_grad(sx_ctx ctx, sx_gnn net, sx_op a, const float* probes, uint64_t seed,
+                     float* loss_out, float* grad_out);
+/* One Adam step on the probe loss of a (4 seeded probes). */
+int sx_gnn_train_step(sx_ctx ctx, sx_gnn net, sx_op a, uint64_t seed, float lr, float* loss_out);
+/* Predicted G^ values in pattern order (each row: strict-lower entries by
+ * column, then the diagonal); g_out may be NULL to query the count. */
+int sx_gnn_edge_values(sx_ctx ctx, sx_gnn net, sx_op a, float* g_out, uint64_t* ng_out);
+/* The preconditioner M^-1 = G G^T for a (same dtype as a). */
+int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out);
+
 /* --------------------------------------------- batched PCG (no reference
  * counterpart: batches the one-system-per-call cg of iterative.rs:40-162) */
 /* Thousands of independent SPD systems stored as one block-diagonal CSR
@@ -331,6 +358,7 @@ int sx_batched_pcg(sx_ctx ctx, sx_op a64, sx_op a32, const int64_t* sys_ptr, uin
 /* FP64 true relative residual ||b - A x||_2 / ||b||_2 of an FP64 CSR. */
 int sx_true_rel_residual(sx_ctx ctx, sx_op a64, const double* b, const double* x, sx_mem mem,
                          double* out);
+
 
 #ifdef __cplusplus
 }

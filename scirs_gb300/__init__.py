@@ -12,6 +12,7 @@ from .sparse import (  # noqa: F401
     generate_batch,
     IRResult,
     IterationResult,
+    LearnedSAI,
     Operator,
     SparseError,
     bicgstab,

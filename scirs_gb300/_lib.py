@@ -199,6 +199,15 @@ _SIGS = {
     "sx_gen_rhs_normal": (None, [c_u64, c_i64, c_vp]),
     "sx_gen_batch_varcoef2d": (c_int, [c_u64, c_i64, c_i64, c_u64, c_dbl, c_vp, P(c_i64), P(c_i64), c_vp, c_vp, c_vp]),
     "sx_batched_options_default": (None, [P(BatchedOptions)]),
+    "sx_gnn_num_params": (c_u64, []),
+    "sx_gnn_create": (c_int, [ctx_t, c_vp, c_u64, P(c_vp)]),
+    "sx_gnn_destroy": (c_int, [c_vp]),
+    "sx_gnn_get_params": (c_int, [ctx_t, c_vp, c_vp]),
+    "sx_gnn_set_params": (c_int, [ctx_t, c_vp, c_vp]),
+    "sx_gnn_loss_grad": (c_int, [ctx_t, c_vp, op_t, c_vp, c_u64, P(C.c_float), c_vp]),
+    "sx_gnn_train_step": (c_int, [ctx_t, c_vp, op_t, c_u64, C.c_float, P(C.c_float)]),
+    "sx_gnn_edge_values": (c_int, [ctx_t, c_vp, op_t, c_vp, P(c_u64)]),
+    "sx_precond_learned": (c_int, [ctx_t, op_t, c_vp, P(op_t)]),
     "sx_batched_pcg": (c_int, [ctx_t, op_t, op_t, c_vp, c_u64, c_vp, c_vp, P(BatchedOptions), c_int,
                                c_vp, P(BatchedSummary)]),
 }

@@ -318,7 +318,7 @@ __global__ void kb_scale_down(const int32_t* __restrict__ row_sys, int64_t n, co
                               const double* __restrict__ rr, const int* __restrict__ active, float* r32) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int s = row_sys[i];
-    r32[i] = active[s] ? (float)(r[i] / sqrt(rr[s])) : 0.0f;
+    r32[i] = active[s] ? (float)(r[i] * (1.0 / sqrt(rr[s]))) : 0.0f;
   }
 }
 

@@ -519,16 +519,26 @@ __global__ void k_sorted_check(const int32_t* __restrict__ ptr, int64_t nrows,
 }
 
 __global__ void k_row_stats(const int32_t* __restrict__ ptr, int64_t nrows, int* flags,
-                            int* maxlen) {
+                            int* maxlen, int* maxchunk) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int mx = 0;
+  int mx = 0, mc = 0;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
     int32_t L = ptr[r + 1] - ptr[r];
     if (L < 0) flags[0] = 1;
     mx = max(mx, L);
+    if ((r & (kBlock - 1)) == 0) {
+      const int64_t re = min(nrows, r + kBlock);
+      mc = max(mc, ptr[re] - ptr[r]);
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(maxlen, mx);
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    mc = max(mc, __shfl_down_sync(0xffffffffu, mc, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(maxlen, mx);
+    atomicMax(maxchunk, mc);
+  }
 }
 
 template <typename TO, typename TI>
@@ -567,7 +577,7 @@ int csr_finalize_stats(sx_ctx ctx, DevCsr& c) {
   cudaMemsetAsync(d, 0, 4 * sizeof(int), ctx->stream);
   int g = vec_grid(ctx, c.nrows);
   if (c.nrows > 0) {
-    k_row_stats<<<g, kBlock, 0, ctx->stream>>>(c.indptr, c.nrows, d, d + 1);
+    k_row_stats<<<g, kBlock, 0, ctx->stream>>>(c.indptr, c.nrows, d, d + 1, d + 3);
     k_sorted_check<<<g, kBlock, 0, ctx->stream>>>(c.indptr, c.nrows, c.indices, c.nnz, d + 2);
     ctx->launches += 2;
   }
@@ -579,6 +589,7 @@ int csr_finalize_stats(sx_ctx ctx, DevCsr& c) {
   c.monotone = h[0] == 0;
   c.max_row_len = h[1];
   c.has_sorted_indices = h[2] == 0;
+  c.max_chunk_nnz = h[3];
   c.mean_row_len = c.nrows > 0 ? (double)c.nnz / (double)c.nrows : 0.0;
   return SX_OK;
 }

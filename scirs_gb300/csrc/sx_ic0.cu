@@ -393,7 +393,6 @@ int ic0_health(sx_ctx ctx, sx_op op) {
   return SX_OK;
 }
 
-int exclusive_scan_i32(sx_ctx ctx, const int32_t* in, int64_t m, int32_t* out);  // sx_core.cu
 
 }  // namespace sx
 

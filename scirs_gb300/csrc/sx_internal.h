@@ -54,6 +54,7 @@ struct DevCsr {
   bool monotone = true;        // indptr non-decreasing
   int32_t max_row_len = 0;
   double mean_row_len = 0.0;
+  int32_t max_chunk_nnz = 0;   // most nonzeros in any 256-row chunk
 };
 
 struct IC0Dev;   // defined in sx_ic0.cu
@@ -122,6 +123,9 @@ int spmv_device(sx_ctx ctx, sx_op a, const void* x, void* y, unsigned flags);
 // host callbacks).  Enqueued on ctx->stream; no allocation, no sync except
 // for host callbacks.
 int apply_general(sx_ctx ctx, sx_op op, const void* x, void* y);
+
+// Exclusive scan of m int32 counts into out[0..m] (synchronises the stream).
+int exclusive_scan_i32(sx_ctx ctx, const int32_t* in, int64_t m, int32_t* out);
 
 // Abort flag of an IC(0) operator's bounded waits -> SX_ERR_DEVICE_TIMEOUT.
 int ic0_health(sx_ctx ctx, sx_op op);

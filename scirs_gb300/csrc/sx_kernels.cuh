@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace sx {
 
 constexpr int kBlock = 256;        // threads per block of every kernel here
@@ -118,7 +120,7 @@ __device__ __forceinline__ int4 ld4i(const int32_t* p) {
   return __ldcs(reinterpret_cast<const int4*>(p));
 }
 
-template <typename T, int ITEMS, class Epi>
+template <typename T, int ITEMS, class Epi, bool FMA = false>
 __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
     const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
     const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, int64_t nrows,
@@ -129,8 +131,11 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
   // go to shared memory and each thread then sums its own row in order.
   constexpr int CH = ITEMS / 4;
   constexpr int TILE = kBlock * ITEMS;
+  // FMA mode keeps value and x in shared memory and sums with fused
+  // multiply-adds in the same order (one rounding per term instead of two)
   __shared__ int32_t s_ptr[kBlock + 1];
   __shared__ T s_prod[TILE];
+  __shared__ T s_x[FMA ? TILE : 1];
   const int tid = threadIdx.x;
   const int64_t r0 = (int64_t)blockIdx.x * kBlock;
   const int nr = (int)min((int64_t)kBlock, nrows - r0);
@@ -141,6 +146,10 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
   int32_t my_s = 0, my_e = 0;
   if (tid < nr) { my_s = s_ptr[tid]; my_e = s_ptr[tid + 1]; }
   T acc = T(0);
+  auto put = [&](int32_t slot, T v, T xv) {
+    if constexpr (FMA) { s_prod[slot] = v; s_x[slot] = xv; }
+    else s_prod[slot] = mul_rn(v, xv);
+  };
   for (int32_t base = s & ~3; base < e; base += TILE) {
     const int32_t tend = min(e, base + TILE);
 #pragma unroll
@@ -154,11 +163,11 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
           const int cc[4] = {ci.x, ci.y, ci.z, ci.w};
 #pragma unroll
           for (int q = 0; q < 4; ++q)
-            if (k0 + q >= s) s_prod[k0 + q - base] = mul_rn(cv.v[q], __ldg(x + cc[q]));
+            if (k0 + q >= s) put(k0 + q - base, cv.v[q], __ldg(x + cc[q]));
         } else {
           for (int q = 0; q < 4; ++q) {
             const int32_t k = k0 + q;
-            if (k >= s && k < e) s_prod[k - base] = mul_rn(vals[k], __ldg(x + indices[k]));
+            if (k >= s && k < e) put(k - base, vals[k], __ldg(x + indices[k]));
           }
         }
       }
@@ -166,7 +175,11 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
     __syncthreads();
     if (tid < nr) {
       const int32_t lo = max(my_s, base), hi = min(my_e, tend);
-      for (int32_t k = lo; k < hi; ++k) acc = add_rn(acc, s_prod[k - base]);
+      if constexpr (FMA) {
+        for (int32_t k = lo; k < hi; ++k) acc = fma(s_prod[k - base], s_x[k - base], acc);
+      } else {
+        for (int32_t k = lo; k < hi; ++k) acc = add_rn(acc, s_prod[k - base]);
+      }
     }
     __syncthreads();
   }
@@ -176,6 +189,110 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
     const T v = epi.out(row, acc);
     y[row] = v;
     epi.acc(row, v, a);
+  }
+  if constexpr (Epi::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && tid == 0) epi.finish(tot);
+  }
+}
+
+// Pipelined persistent variant for matrices whose 256-row chunks each fit
+// one tile (chunk nnz + 3 <= 256 * ITEMS).  A block walks chunks
+// c, c + gridDim.x, ...; the row pointers and the 128-bit column/value loads
+// of the next chunk are issued while the current chunk gathers x and sums
+// its rows, so two chunks per block are in flight.  Per-row order and
+// rounding are those of spmv_stream_kernel (bit-identical results).
+template <typename T, int ITEMS, class Epi, bool FMA = false>
+__global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
+    const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+    const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, int64_t nrows,
+    int64_t nchunks, T* partials, unsigned int* counter, Epi epi) {
+  if (epi.skip()) return;
+  constexpr int CH = ITEMS / 4;
+  constexpr int TILE = kBlock * ITEMS;
+  __shared__ T s_prod[TILE];
+  __shared__ T s_x[FMA ? TILE : 1];
+  const int tid = threadIdx.x;
+  // registers of the chunk in flight
+  int32_t cs = 0, ce = 0, ms = 0, me = 0;
+  int4 ci[CH];
+  Vec4<T> cv[CH];
+  auto load_meta = [&](int64_t ch, int32_t& s0, int32_t& e0, int32_t& m0, int32_t& m1) {
+    const int64_t r0 = ch * kBlock;
+    const int nr = (int)min((int64_t)kBlock, nrows - r0);
+    s0 = __ldg(indptr + r0);
+    e0 = __ldg(indptr + r0 + nr);
+    if (tid < nr) { m0 = __ldg(indptr + r0 + tid); m1 = __ldg(indptr + r0 + tid + 1); }
+    else { m0 = 0; m1 = 0; }
+  };
+  auto load_data = [&](int32_t s0, int32_t e0, int4* di, Vec4<T>* dv) {
+    const int32_t base = s0 & ~3;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+      const int32_t k0 = base + (c * kBlock + tid) * 4;
+      if (k0 + 3 < e0) {
+        di[c] = ld4i(indices + k0);
+        dv[c] = ld4(vals + k0);
+      } else {
+        int cc[4];
+        T vv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int32_t k = k0 + q;
+          const bool in = k < e0;
+          cc[q] = in ? indices[k] : 0;
+          vv[q] = in ? vals[k] : T(0);
+        }
+        di[c] = make_int4(cc[0], cc[1], cc[2], cc[3]);
+        dv[c] = Vec4<T>{{vv[0], vv[1], vv[2], vv[3]}};
+      }
+    }
+  };
+  Acc3<T> a{T(0), T(0), T(0)};
+  int64_t ch = blockIdx.x;
+  if (ch < nchunks) {
+    load_meta(ch, cs, ce, ms, me);
+    load_data(cs, ce, ci, cv);
+  }
+  while (ch < nchunks) {
+    const int64_t nxt = ch + gridDim.x;
+    const int32_t base = cs & ~3;
+    // products of the current chunk into shared memory
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+      const int32_t k0 = base + (c * kBlock + tid) * 4;
+      const int cc[4] = {ci[c].x, ci[c].y, ci[c].z, ci[c].w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int32_t k = k0 + q;
+        if (k >= cs && k < ce) {
+          const T xv = __ldg(x + cc[q]);
+          if constexpr (FMA) { s_prod[k - base] = cv[c].v[q]; s_x[k - base] = xv; }
+          else s_prod[k - base] = mul_rn(cv[c].v[q], xv);
+        }
+      }
+    }
+    // row pointers of the next chunk (independent of the work below)
+    int32_t ns = 0, ne = 0, nms = 0, nme = 0;
+    if (nxt < nchunks) load_meta(nxt, ns, ne, nms, nme);
+    __syncthreads();
+    const int64_t row = ch * kBlock + tid;
+    if (row < nrows) {
+      T acc = T(0);
+      if constexpr (FMA) {
+        for (int32_t k = ms; k < me; ++k) acc = fma(s_prod[k - base], s_x[k - base], acc);
+      } else {
+        for (int32_t k = ms; k < me; ++k) acc = add_rn(acc, s_prod[k - base]);
+      }
+      const T v = epi.out(row, acc);
+      y[row] = v;
+      epi.acc(row, v, a);
+    }
+    // columns and values of the next chunk
+    if (nxt < nchunks) load_data(ns, ne, ci, cv);
+    __syncthreads();
+    cs = ns; ce = ne; ms = nms; me = nme;
+    ch = nxt;
   }
   if constexpr (Epi::kReduce) {
     Acc3<T> tot;
@@ -207,6 +324,32 @@ __global__ void __launch_bounds__(kBlock) spmv_rowseq_kernel(
   }
 }
 
+// plain (cacheable) 4-wide loads and stores for solver vectors, which the
+// next kernel reads again
+__device__ __forceinline__ Vec4<float> ldv4(const float* p) {
+  float4 a = *reinterpret_cast<const float4*>(p);
+  return Vec4<float>{{a.x, a.y, a.z, a.w}};
+}
+__device__ __forceinline__ Vec4<double> ldv4(const double* p) {
+  double2 a = *reinterpret_cast<const double2*>(p);
+  double2 b = *(reinterpret_cast<const double2*>(p) + 1);
+  return Vec4<double>{{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ void stv4(float* p, const Vec4<float>& v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
+}
+__device__ __forceinline__ void stv4(double* p, const Vec4<double>& v) {
+  *reinterpret_cast<double2*>(p) = make_double2(v.v[0], v.v[1]);
+  *(reinterpret_cast<double2*>(p) + 1) = make_double2(v.v[2], v.v[3]);
+}
+
+// Bodies may set `static constexpr bool kVec4 = true` and provide
+// elem4(i, acc) for four consecutive elements starting at a multiple of 4.
+template <class B, class = void>
+struct Vec4Flag : std::false_type {};
+template <class B>
+struct Vec4Flag<B, std::void_t<decltype(B::kVec4)>> : std::integral_constant<bool, B::kVec4> {};
+
 // -------------------------------------------------------- elementwise
 // Body interface (all __device__):
 //   bool skip() const
@@ -219,7 +362,14 @@ __global__ void __launch_bounds__(kBlock) vec_kernel(int64_t n, T* partials,
   if (body.skip()) return;
   Acc3<T> a{T(0), T(0), T(0)};
   const int64_t stride = (int64_t)gridDim.x * kBlock;
-  for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) body.elem(i, a);
+  if constexpr (Vec4Flag<Body>::value) {
+    // four consecutive elements per thread with 128-bit accesses, then the tail
+    const int64_t n4 = n >> 2;
+    for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n4; i += stride) body.elem4(i << 2, a);
+    for (int64_t i = (n4 << 2) + (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) body.elem(i, a);
+  } else {
+    for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) body.elem(i, a);
+  }
   if constexpr (Body::kReduce) {
     Acc3<T> tot;
     if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) body.finish(tot);

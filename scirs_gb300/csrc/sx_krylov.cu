@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -243,6 +244,9 @@ static int run_loop(sx_ctx ctx, void* d_state, const uint64_t key[8], bool graph
   SX_CHECK(read_ctl(ctx, d_state, &h, sizeof(h)));
   if (h.status != ST_RUNNING) return SX_OK;
   GraphEntry* g = nullptr;
+  // SX_GRAPHS=0 launches the same kernels eagerly (per-kernel profiling)
+  const char* env = std::getenv("SX_GRAPHS");
+  if (env && env[0] == '0') graphable = false;
   if (graphable) {
     g = graph_find(ctx, key);
     if (!g) {
@@ -289,6 +293,7 @@ struct CgSetup {
   T* p;
   PrecFused<T> pf;
   static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = false;
   __device__ bool skip() const { return false; }
   __device__ void elem(int64_t i, Acc3<T>& a) const {
     T ri = r[i];
@@ -342,6 +347,7 @@ struct CgUpdate {
   PrecFused<T> pf;
   static constexpr bool kReduce = true;
   __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  static constexpr bool kVec4 = true;
   __device__ void elem(int64_t i, Acc3<T>& a) const {
     const T alpha = st->alpha;
     x[i] = add_rn(x[i], mul_rn(alpha, p[i]));
@@ -349,6 +355,23 @@ struct CgUpdate {
     r[i] = ri;
     a.a += ri * ri;
     if (pf.kind != PK_GENERAL) a.b += ri * pf.apply(i, ri);
+  }
+  __device__ void elem4(int64_t i, Acc3<T>& a) const {
+    const T alpha = st->alpha;
+    Vec4<T> xv = ldv4(x + i), pv = ldv4(p + i), rv = ldv4(r + i), qv = ldv4(ap + i);
+    Vec4<T> dv{{T(1), T(1), T(1), T(1)}};
+    if (pf.kind == PK_DIAG) dv = ldv4(pf.d + i);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      xv.v[q] = add_rn(xv.v[q], mul_rn(alpha, pv.v[q]));
+      const T ri = sub_rn(rv.v[q], mul_rn(alpha, qv.v[q]));
+      rv.v[q] = ri;
+      a.a += ri * ri;
+      if (pf.kind == PK_DIAG) a.b += ri * mul_rn(ri, dv.v[q]);
+      else if (pf.kind != PK_GENERAL) a.b += ri * pf.apply(i + q, ri);
+    }
+    stv4(x + i, xv);
+    stv4(r + i, rv);
   }
   __device__ void finish(const Acc3<T>& t) const {
     T rnorm = sqrt(t.a);
@@ -398,9 +421,31 @@ struct CgP {
     }
     return false;
   }
+  static constexpr bool kVec4 = true;
   __device__ void elem(int64_t i, Acc3<T>&) const {
     T zi = pf.kind == PK_GENERAL ? z[i] : pf.apply(i, r[i]);
     p[i] = add_rn(zi, mul_rn(st->beta, p[i]));
+  }
+  __device__ void elem4(int64_t i, Acc3<T>&) const {
+    const T beta = st->beta;
+    Vec4<T> pv = ldv4(p + i);
+    Vec4<T> zv;
+    if (pf.kind == PK_GENERAL) {
+      zv = ldv4(z + i);
+    } else {
+      zv = ldv4(r + i);
+      if (pf.kind == PK_DIAG) {
+        const Vec4<T> dv = ldv4(pf.d + i);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) zv.v[q] = mul_rn(zv.v[q], dv.v[q]);
+      } else if (pf.kind == PK_SCALED) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) zv.v[q] = mul_rn(zv.v[q], pf.s);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) pv.v[q] = add_rn(zv.v[q], mul_rn(beta, pv.v[q]));
+    stv4(p + i, pv);
   }
   __device__ void finish(const Acc3<T>&) const {
     st->c.iterations += 1;
@@ -495,6 +540,7 @@ struct BiSetup {
   const T *b, *r;
   T *rhat, *v, *p;
   static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = false;
   __device__ bool skip() const { return false; }
   __device__ void elem(int64_t i, Acc3<T>& a) const {
     T ri = r[i];
@@ -1012,6 +1058,7 @@ struct GmInit {
   GmState<T>* st;
   const T *r, *b;
   static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = false;
   __device__ bool skip() const { return false; }
   __device__ void elem(int64_t i, Acc3<T>& a) const {
     a.a += r[i] * r[i];

@@ -3,6 +3,8 @@
 // scalar updates into operator applications.
 #pragma once
 
+#include <algorithm>
+
 #include "sx_internal.h"
 #include "sx_kernels.cuh"
 
@@ -72,16 +74,38 @@ __global__ void __launch_bounds__(kBlock) k_epi_inplace(int64_t n, T* y, T* part
 
 constexpr int kSpmvItems = 8;
 
+// Blocks of kBlock threads one SM holds at once for kernel Kern (queried once).
+template <auto Kern>
+int resident_blocks() {
+  static int cached = 0;
+  if (!cached) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, Kern, kBlock, 0) != cudaSuccess || nb < 1) nb = 1;
+    cached = nb;
+  }
+  return cached;
+}
+
 // CSR SpMV with epilogue.  Must not allocate or synchronise: it runs inside
 // stream capture.  The reduction area must already hold gridDim blocks.
-template <typename T, class Epi>
+template <typename T, class Epi, bool FMA = false>
 int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
   if (c.nrows <= 0) return SX_OK;
   ReduceArea ra;
   const int64_t blocks = (c.nrows + kBlock - 1) / kBlock;
   SX_CHECK(ctx_reduce_area(ctx, blocks, &ra));
-  if (c.monotone) {
-    spmv_stream_kernel<T, kSpmvItems, Epi><<<(unsigned)blocks, kBlock, 0, ctx->stream>>>(
+  if (c.monotone && c.max_chunk_nnz + 3 <= kBlock * 8) {
+    constexpr auto kern = spmv_pipe_kernel<T, 8, Epi, FMA>;
+    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
+    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows,
+                                                      blocks, (T*)ra.partials, ra.counter, epi);
+  } else if (c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12) {
+    constexpr auto kern = spmv_pipe_kernel<T, 12, Epi, FMA>;
+    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
+    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows,
+                                                      blocks, (T*)ra.partials, ra.counter, epi);
+  } else if (c.monotone) {
+    spmv_stream_kernel<T, kSpmvItems, Epi, FMA><<<(unsigned)blocks, kBlock, 0, ctx->stream>>>(
         c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows, (T*)ra.partials, ra.counter, epi);
   } else {
     spmv_rowseq_kernel<T, Epi><<<(unsigned)blocks, kBlock, 0, ctx->stream>>>(
@@ -103,11 +127,15 @@ int launch_vec(sx_ctx ctx, int64_t n, Body body) {
   return SX_OK;
 }
 
-template <typename T, class Epi>
+// EXACT = false (solver-internal use): FP64 CSR products use the FMA row
+// sums, which halve the work of GB300's FP64 pipe and stay within a few ulp
+// per row; EXACT = true reproduces the reference's per-row rounding.
+template <typename T, class Epi, bool EXACT = false>
 int launch_apply(sx_ctx ctx, sx_op op, const T* x, T* y, Epi epi) {
+  constexpr bool kFma = !EXACT && sizeof(T) == 8;
   switch (op->kind) {
     case SX_OP_CSR:
-      return launch_csr<T, Epi>(ctx, op->csr, x, y, epi);
+      return launch_csr<T, Epi, kFma>(ctx, op->csr, x, y, epi);
     case SX_OP_IDENTITY:
     case SX_OP_SCALED_IDENTITY:
     case SX_OP_DIAGONAL:
@@ -124,8 +152,8 @@ int launch_apply(sx_ctx ctx, sx_op op, const T* x, T* y, Epi epi) {
     }
     case SX_OP_FSAI: {
       // y = G (G^T x): the second SpMV carries the epilogue
-      SX_CHECK(launch_csr<T, EpiPlain<T>>(ctx, op->transpose->csr, x, (T*)op->work, EpiPlain<T>{}));
-      return launch_csr<T, Epi>(ctx, op->csr, (const T*)op->work, y, epi);
+      SX_CHECK(launch_csr<T, EpiPlain<T>, kFma>(ctx, op->transpose->csr, x, (T*)op->work, EpiPlain<T>{}));
+      return launch_csr<T, Epi, kFma>(ctx, op->csr, (const T*)op->work, y, epi);
     }
     default: {
       // IC0 and host operators: apply, then run the epilogue over y

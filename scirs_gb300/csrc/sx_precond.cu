@@ -18,11 +18,12 @@ int ic0_apply(sx_ctx ctx, sx_op op, const void* x, void* y);  // sx_ic0.cu
 
 int spmv_device(sx_ctx ctx, sx_op a, const void* x, void* y, unsigned flags) {
   (void)flags;
+  // the public SpMV keeps the reference's per-row rounding (bit-exact)
   if (a->dtype == SX_F64)
-    return launch_apply<double, EpiPlain<double>>(ctx, a, (const double*)x, (double*)y,
-                                                  EpiPlain<double>{});
-  return launch_apply<float, EpiPlain<float>>(ctx, a, (const float*)x, (float*)y,
-                                              EpiPlain<float>{});
+    return launch_apply<double, EpiPlain<double>, true>(ctx, a, (const double*)x, (double*)y,
+                                                        EpiPlain<double>{});
+  return launch_apply<float, EpiPlain<float>, true>(ctx, a, (const float*)x, (float*)y,
+                                                    EpiPlain<float>{});
 }
 
 int apply_general(sx_ctx ctx, sx_op op, const void* x, void* y) {

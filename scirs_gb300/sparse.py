@@ -434,6 +434,71 @@ def cg_mixed(a64: Operator, b, tol=1e-10, inner_rtol=1e-4, max_outer=30, max_inn
                     bool(r.converged))
 
 
+class LearnedSAI:
+    """The message-passing network that predicts G for M^-1 = G G^T."""
+
+    def __init__(self, ctx: Context, params=None, seed: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        pp = None
+        if params is not None:
+            params = np.ascontiguousarray(params, dtype=np.float32)
+            pp = _ptr(params)
+        _check(L.lib.sx_gnn_create(ctx.handle, pp, seed, C.byref(h)))
+        self.handle = h
+        self.num_params = int(L.lib.sx_gnn_num_params())
+
+    def close(self):
+        if self.handle:
+            L.lib.sx_gnn_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.empty(self.num_params, dtype=np.float32)
+        _check(L.lib.sx_gnn_get_params(self.ctx.handle, self.handle, _ptr(out)))
+        return out
+
+    @params.setter
+    def params(self, value):
+        value = np.ascontiguousarray(value, dtype=np.float32)
+        _check(L.lib.sx_gnn_set_params(self.ctx.handle, self.handle, _ptr(value)))
+
+    def loss_grad(self, a: Operator, probes=None, seed: int = 0):
+        grad = np.empty(self.num_params, dtype=np.float32)
+        loss = C.c_float()
+        pp = None
+        if probes is not None:
+            probes = np.ascontiguousarray(probes, dtype=np.float32)
+            pp = _ptr(probes)
+        _check(L.lib.sx_gnn_loss_grad(self.ctx.handle, self.handle, a.handle, pp, seed, C.byref(loss),
+                                      _ptr(grad)))
+        return float(loss.value), grad
+
+    def train_step(self, a: Operator, seed: int, lr: float = 1e-3) -> float:
+        loss = C.c_float()
+        _check(L.lib.sx_gnn_train_step(self.ctx.handle, self.handle, a.handle, seed, lr, C.byref(loss)))
+        return float(loss.value)
+
+    def edge_values(self, a: Operator) -> np.ndarray:
+        ng = C.c_uint64()
+        _check(L.lib.sx_gnn_edge_values(self.ctx.handle, self.handle, a.handle, None, C.byref(ng)))
+        out = np.empty(ng.value, dtype=np.float32)
+        _check(L.lib.sx_gnn_edge_values(self.ctx.handle, self.handle, a.handle, _ptr(out), C.byref(ng)))
+        return out
+
+    def preconditioner(self, a: Operator) -> Operator:
+        h = L.op_t()
+        _check(L.lib.sx_precond_learned(self.ctx.handle, a.handle, self.handle, C.byref(h)))
+        return Operator(self.ctx, h)
+
+
 @dataclass
 class BatchedResult:
     x: np.ndarray

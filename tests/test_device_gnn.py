@@ -1,0 +1,105 @@
+"""Learned factorised SAI: device forward/backward vs the PyTorch CPU oracle,
+training, and the gain of the trained network over Jacobi."""
+import numpy as np
+import pytest
+import torch
+
+from tests import gnn_reference as R
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def S():
+    import scirs_gb300
+
+    return scirs_gb300
+
+
+def _aniso(S, ctx, nx, ny, eps, theta, dtype=np.float64):
+    ip, ix, v = S.generate("aniso_q1", nx, ny, param0=eps, param1=theta)
+    n = len(ip) - 1
+    return ip, ix, v, S.csr_from_arrays(ctx, ip, ix, v.astype(dtype), (n, n))
+
+
+def test_forward_matches_pytorch(S, ctx):
+    ip, ix, v, a = _aniso(S, ctx, 20, 17, 30.0, 0.7)
+    net = S.LearnedSAI(ctx, seed=3)
+    p = net.params
+    # a perturbed, non-trivial network (the initial one is near the identity)
+    rng = np.random.default_rng(1)
+    p = (p + 0.2 * rng.standard_normal(p.size).astype(np.float32)).astype(np.float32)
+    net.params = p
+    g_dev = net.edge_values(a)
+    prep = R.prepare(ip, ix, v)
+    g_ref = R.forward(torch.tensor(p), prep).detach().numpy()
+    assert g_dev.shape == g_ref.shape
+    scale = np.abs(g_ref).max()
+    assert np.max(np.abs(g_dev - g_ref)) <= 3e-2 * scale
+    assert np.corrcoef(g_dev, g_ref)[0, 1] > 0.999
+
+
+def test_gradient_matches_autograd(S, ctx):
+    ip, ix, v, a = _aniso(S, ctx, 16, 15, 10.0, 1.1)
+    net = S.LearnedSAI(ctx, seed=5)
+    rng = np.random.default_rng(2)
+    p = (net.params + 0.1 * rng.standard_normal(net.num_params)).astype(np.float32)
+    net.params = p
+    prep = R.prepare(ip, ix, v)
+    z = rng.standard_normal((prep["n"], 4)).astype(np.float32)
+    loss_dev, grad_dev = net.loss_grad(a, probes=z)
+    pt = torch.tensor(p, requires_grad=True)
+    loss_ref = R.probe_loss(R.forward(pt, prep), prep, z)
+    loss_ref.backward()
+    grad_ref = pt.grad.numpy()
+    assert abs(loss_dev - loss_ref.item()) <= 2e-2 * abs(loss_ref.item())
+    # per parameter group: direction and magnitude
+    o = 0
+    for name, shape in R.param_layout():
+        k = int(np.prod(shape))
+        gd, gr = grad_dev[o:o + k], grad_ref[o:o + k]
+        o += k
+        nr = np.linalg.norm(gr)
+        if nr < 1e-6 * np.linalg.norm(grad_ref):
+            continue
+        cos = float(gd @ gr / (np.linalg.norm(gd) * nr + 1e-30))
+        assert cos > 0.995, (name, cos)
+        assert abs(np.linalg.norm(gd) / nr - 1) < 0.05, (name, np.linalg.norm(gd), nr)
+
+
+def test_training_reduces_loss_and_iterations(S, ctx):
+    rng = np.random.default_rng(7)
+    train = []
+    for _ in range(6):
+        eps = float(10 ** rng.uniform(0, 3))
+        theta = float(rng.uniform(0, np.pi))
+        train.append(_aniso(S, ctx, 48, 48, eps, theta)[3])
+    net = S.LearnedSAI(ctx, seed=11)
+    first = np.mean([net.loss_grad(a, seed=99)[0] for a in train])
+    for step in range(600):
+        net.train_step(train[step % len(train)], seed=step, lr=2e-3)
+    last = np.mean([net.loss_grad(a, seed=99)[0] for a in train])
+    assert last < 0.8 * first, (first, last)
+    # held-out matrix: PCG iterations with the learned G G^T vs Jacobi
+    ip, ix, v, a = _aniso(S, ctx, 64, 64, 300.0, 0.4)
+    n = a.shape[0]
+    b = S.rhs_normal(5, n)
+    r_j = S.cg(a, b, max_iter=20000, rtol=1e-8, atol=0.0, preconditioner=S.jacobi(ctx, a))
+    m = net.preconditioner(a)
+    r_l = S.cg(a, b, max_iter=20000, rtol=1e-8, atol=0.0, preconditioner=m)
+    assert r_j.converged and r_l.converged
+    assert r_l.iterations < r_j.iterations, (r_l.iterations, r_j.iterations)
+
+
+def test_learned_preconditioner_is_spd_apply(S, ctx):
+    # M^-1 = G G^T: symmetric and positive on random vectors
+    ip, ix, v, a = _aniso(S, ctx, 12, 12, 5.0, 0.3)
+    net = S.LearnedSAI(ctx, seed=1)
+    m = net.preconditioner(a)
+    n = a.shape[0]
+    rng = np.random.default_rng(0)
+    for _ in range(3):
+        x, y = rng.standard_normal(n), rng.standard_normal(n)
+        mx, my = m.matvec(x), m.matvec(y)
+        assert abs(x @ my - y @ mx) <= 1e-10 * np.linalg.norm(x) * np.linalg.norm(my)
+        assert x @ mx > 0

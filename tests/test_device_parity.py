@@ -187,30 +187,31 @@ def test_cg_max_iter_path(S, ctx):
 
 @pytest.mark.parametrize("prec", ["none", "left", "right", "both"])
 def test_bicgstab_matches_oracle(S, ctx, prec):
-    # non-symmetric: convection added to a variable-coefficient stencil
+    # non-symmetric, diagonally dominant: convection on a variable-coefficient stencil
     ip, ix, v, n, b = _system(S, "varcoef2d", (40, 30, 1), p0=0.5)
     v = v.copy()
     for r in range(n):
         for k in range(ip[r], ip[r + 1]):
             if ix[k] == r + 1:
                 v[k] *= 1.3
+            if ix[k] == r:
+                v[k] *= 1.5
     a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
     oa = O.op_csr_i32(ip, ix, v, (n, n))
     m = S.jacobi(ctx, a)
     om = O.op_jacobi(oa)
     left = m if prec in ("left", "both") else None
     right = m if prec in ("right", "both") else None
-    # rtol 1e-6 keeps the solve clear of the reference's absolute breakdown
-    # thresholds (|rho| < 10 eps), which rounding would trip at random
-    r = S.bicgstab(a, b, max_iter=2000, rtol=1e-6, atol=0.0, left_preconditioner=left,
+    r = S.bicgstab(a, b, max_iter=2000, rtol=1e-8, atol=0.0, left_preconditioner=left,
                    right_preconditioner=right)
-    ro = O.bicgstab(oa, b, max_iter=2000, rtol=1e-6, atol=0.0,
+    ro = O.bicgstab(oa, b, max_iter=2000, rtol=1e-8, atol=0.0,
                     left=om if left else None, right=om if right else None)
-    assert r.converged and ro["converged"] and r.message == ro["message"] == "Converged"
-    assert abs(r.iterations - ro["iterations"]) <= max(3, ro["iterations"] // 10)
-    assert np.linalg.norm(r.x - ro["x"]) / np.linalg.norm(ro["x"]) < 1e-4
-    res = np.linalg.norm(b - oa.matvec(r.x)) / np.linalg.norm(b)
-    assert res < 2e-6
+    # with both, the reference's x = M2 x inside every iteration (iterative.rs:583-585)
+    # derails the solve into a breakdown; the device must report the same
+    assert r.converged == ro["converged"] and r.message == ro["message"]
+    assert abs(r.iterations - ro["iterations"]) <= 2
+    if ro["converged"]:
+        assert np.linalg.norm(r.x - ro["x"]) / np.linalg.norm(ro["x"]) < 1e-6
 
 
 @pytest.mark.parametrize("restart,prec", [(30, False), (10, True), (500, False)])
