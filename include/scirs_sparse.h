@@ -359,6 +359,18 @@ int sx_batched_pcg(sx_ctx ctx, sx_op a64, sx_op a32, const int64_t* sys_ptr, uin
 int sx_true_rel_residual(sx_ctx ctx, sx_op a64, const double* b, const double* x, sx_mem mem,
                          double* out);
 
+/* The same residual for callers that cannot allocate device memory while
+ * they run (a framework that owns all GPU memory through its own pool, a
+ * real-time loop that must not stall on an allocation).  No counterpart in
+ * the reference.  b and x are device pointers; nothing is allocated: the
+ * reduction scratch is a 1 MiB file-scope device array that every GPU which
+ * loads the library holds until exit.  At most 16,777,216 rows
+ * (SX_ERR_VALUE beyond).  Calls share that array, so calls that overlap on
+ * the GPU race and must be serialised by the caller.  The first call on a
+ * device looks the array up (cudaGetSymbolAddress); make it before any
+ * stream capture.  The result is bit-identical to sx_true_rel_residual. */
+int sx_true_rel_residual_noalloc(sx_ctx ctx, sx_op a64, const double* b_dev, const double* x_dev,
+                                 double* out);
 
 #ifdef __cplusplus
 }

@@ -195,6 +195,7 @@ _SIGS = {
     "sx_ir_options_default": (None, [P(IROptions)]),
     "sx_cg_mixed": (c_int, [ctx_t, op_t, c_vp, c_u64, P(IROptions), c_vp, c_int, P(IRResult)]),
     "sx_true_rel_residual": (c_int, [ctx_t, op_t, c_vp, c_vp, c_int, P(c_dbl)]),
+    "sx_true_rel_residual_noalloc": (c_int, [ctx_t, op_t, c_vp, c_vp, P(c_dbl)]),
     "sx_gen_matrix": (c_int, [P(GenSpec), P(c_i64), P(c_i64), c_vp, c_vp, c_vp]),
     "sx_gen_rhs_normal": (None, [c_u64, c_i64, c_vp]),
     "sx_gen_batch_varcoef2d": (c_int, [c_u64, c_i64, c_i64, c_u64, c_dbl, c_vp, P(c_i64), P(c_i64), c_vp, c_vp, c_vp]),

@@ -26,6 +26,7 @@ SOURCES = [
     "sx_ic0.cu",
     "sx_mixed.cu",
     "sx_batched.cu",
+    "sx_noalloc.cu",
     "sx_gnn.cu",
     "sx_gen.cpp",
 ]
