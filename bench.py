@@ -416,6 +416,97 @@ def run_profile(args):
     ctx.close()
 
 
+# ------------------------------------------- learned SAI vs Jacobi (configs[4])
+WEIGHTS = os.path.join(REPO, "scirs_gb300", "weights", "aniso_q1.npz")
+
+
+def eval_learned(ctx, net, side, seeds, max_iter=400000, with_fp64_learned=True, log=None):
+    """Held-out anisotropic Q1 problems: time to FP64 relative residual 1e-8 for
+    FP64 Jacobi-PCG, mixed-precision Jacobi-PCG and mixed-precision learned PCG
+    (falling back to FP64 learned PCG if refinement stagnates)."""
+    import torch
+
+    import scirs_gb300 as S
+    from scirs_gb300 import learned as LR
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return out, e0.elapsed_time(e1) / 1e3
+
+    rows = []
+    for sd in seeds:
+        prob = LR.sample_problem(sd)
+        a64 = LR.build(ctx, prob, side=side)
+        a32 = a64.astype(np.float32)
+        n = a64.shape[0]
+        b = S.rhs_normal(sd, n)
+        row = {"seed": sd, "eps": prob.eps, "theta": prob.theta, "n": n, "nnz": a64.nnz}
+        m64 = S.jacobi(ctx, a64)
+        r, t = timed(lambda: S.cg(a64, b, max_iter=max_iter, rtol=TOL, atol=0.0, preconditioner=m64))
+        row["jacobi_fp64"] = {"s": t, "iters": r.iterations, "conv": r.converged,
+                              "true_res": S.true_rel_residual(a64, b, r.x)}
+        m32 = S.jacobi(ctx, a32)
+        r, t = timed(lambda: S.cg_mixed(a64, b, tol=TOL, inner_rtol=1e-4, max_inner=max_iter,
+                                        preconditioner=m32, a32=a32))
+        row["jacobi_mixed"] = {"s": t, "outer": r.outer_iterations, "inner": r.inner_iterations,
+                               "conv": r.converged, "true_res": r.rel_residual}
+        if net is not None:
+            g32, t_setup = timed(lambda: net.preconditioner(a32))
+            r, t = timed(lambda: S.cg_mixed(a64, b, tol=TOL, inner_rtol=1e-4, max_inner=max_iter,
+                                            preconditioner=g32, a32=a32))
+            row["learned_mixed"] = {"s": t, "setup_s": t_setup, "outer": r.outer_iterations,
+                                    "inner": r.inner_iterations, "conv": r.converged,
+                                    "true_res": r.rel_residual}
+            if with_fp64_learned or not r.converged:
+                g64, t_setup64 = timed(lambda: net.preconditioner(a64))
+                r, t = timed(lambda: S.cg(a64, b, max_iter=max_iter, rtol=TOL, atol=0.0,
+                                          preconditioner=g64))
+                row["learned_fp64"] = {"s": t, "setup_s": t_setup64, "iters": r.iterations,
+                                       "conv": r.converged, "true_res": S.true_rel_residual(a64, b, r.x)}
+                g64.close()
+            g32.close()
+        for op in (m32, m64, a32, a64):
+            op.close()
+        rows.append(row)
+        if log:
+            log(json.dumps(row))
+    return rows
+
+
+def run_learned(args):
+    import scirs_gb300 as S
+    from scirs_gb300 import learned as LR
+
+    ctx = S.Context(0)
+    log = lambda s: print(s, file=sys.stderr, flush=True)  # noqa: E731
+    train_log = None
+    if args.train_gnn:
+        t0 = time.perf_counter()
+        net, train_log = LR.train(ctx, args.train_gnn, seed=args.train_seed, log_every=100)
+        t_train = time.perf_counter() - t0
+        out = os.path.join(REPO, "gpurun_out", "aniso_q1.npz")
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        LR.save_weights(out, net, {"steps": args.train_gnn, "seed": args.train_seed, "train_s": t_train})
+        log(json.dumps({"trained_steps": args.train_gnn, "train_s": t_train, "log": train_log[-5:]}))
+    elif os.path.exists(WEIGHTS):
+        net = LR.load_weights(ctx, WEIGHTS)
+    else:
+        net = None
+    seeds = [int(s) for s in args.eval_seeds.split(",")]
+    rows = eval_learned(ctx, net, args.eval_side, seeds, log=log)
+    print(json.dumps({"eval_side": args.eval_side, "rows": rows}), flush=True)
+    if net is not None:
+        net.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,8 +520,15 @@ def main():
     ap.add_argument("--profile", default=None,
                     choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "solve"],
                     help="run a few launches of one SpMV for an ncu capture and exit")
+    ap.add_argument("--workload", default="laplace3d", choices=["laplace3d", "learned"])
+    ap.add_argument("--train-gnn", type=int, default=0, help="train the network for N steps first")
+    ap.add_argument("--train-seed", type=int, default=0)
+    ap.add_argument("--eval-side", type=int, default=1024)
+    ap.add_argument("--eval-seeds", default="1000001,1000002,1000003,1000004")
     args = ap.parse_args()
-    if args.profile:
+    if args.workload == "learned":
+        run_learned(args)
+    elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args)

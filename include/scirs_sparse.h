@@ -273,6 +273,9 @@ int sx_gmres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_gmres_
  *   x = x0 (FP64); repeat { r = b - A x in FP64; stop when
  *   ||r||_2 <= tol ||b||_2; solve A d = r/||r|| with FP32 PCG to inner_rtol;
  *   x += ||r|| d (FP64) }.
+ * The loop also stops (converged = 0) when a correction fails to halve the
+ * FP64 residual: with kappa(A) * 2^-24 near 1 the FP32 solve cannot help, and
+ * the caller should fall back to an FP64 solve.
  * a64 must be SX_F64; the FP32 copy is made inside (or pass a32). */
 typedef struct {
   uint64_t max_outer;    /* default 30 */

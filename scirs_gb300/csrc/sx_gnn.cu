@@ -609,7 +609,7 @@ __global__ void k_i32_to_i64(const int32_t* __restrict__ in, int64_t n, int64_t*
 int prep_graph(sx_ctx ctx, sx_gnn net, sx_op a, Graph** out) {
   for (auto& g : net->graphs)
     if (g.key == a->serial) { *out = &g; return SX_OK; }
-  if (net->graphs.size() >= 32) {
+  if (net->graphs.size() >= 64) {
     for (auto& g : net->graphs) graph_free(g);
     net->graphs.clear();
   }

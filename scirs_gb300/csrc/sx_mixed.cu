@@ -180,9 +180,13 @@ int sx_cg_mixed(sx_ctx ctx, sx_op a64, const double* b, uint64_t b_len, const sx
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
       if (e != cudaSuccess) { rc = cuda_fail(e, "refinement residual", __FILE__, __LINE__); break; }
       const double rnorm = std::sqrt(h.rr), bnorm = std::sqrt(h.bb);
+      const double prev = rel;
       rel = bnorm > 0 ? rnorm / bnorm : rnorm;
       if (rnorm <= opt->tol * bnorm) { converged = 1; break; }
       if (outer >= opt->max_outer) break;
+      // stagnation: an FP32 correction that no longer halves the FP64
+      // residual (kappa(A) * eps_fp32 is near 1) ends the refinement
+      if (outer > 0 && !(rel < 0.5 * prev)) break;
       if ((rc = launch_vec<double>(ctx, n, ScaleDown{dr, r32, nrm}))) break;
       sx_iter_result ir;
       if ((rc = sx_cg(ctx, a32, r32, (uint64_t)n, &io, d32, SX_MEM_DEVICE, &ir))) break;

@@ -1,0 +1,235 @@
+// The reference crate's own tests of the solve path, written against the C++
+// mirror of its API (include/scirs_sparse.hpp).  Each test names the Rust
+// test it ports; inputs and assertions are the reference's.
+#include <cmath>
+#include <cstdio>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "scirs_sparse.hpp"
+
+using namespace scirs2_sparse;
+
+static int g_failed = 0, g_run = 0;
+#define CHECK(cond)                                                              \
+  do {                                                                           \
+    if (!(cond)) {                                                               \
+      std::printf("  CHECK failed at %s:%d: %s\n", __FILE__, __LINE__, #cond);   \
+      throw std::runtime_error("check failed");                                  \
+    }                                                                            \
+  } while (0)
+#define NEAR(a, b, eps) CHECK(std::fabs((double)(a) - (double)(b)) < (eps))
+
+static void run(const char* name, const std::function<void()>& f) {
+  ++g_run;
+  try {
+    f();
+    std::printf("ok   %s\n", name);
+  } catch (const std::exception& e) {
+    ++g_failed;
+    std::printf("FAIL %s: %s\n", name, e.what());
+  }
+}
+
+static double resid(const LinearOperator<double>& a, const std::vector<double>& x,
+                    const std::vector<double>& b) {
+  auto ax = a.matvec(x);
+  double s = 0;
+  for (size_t i = 0; i < b.size(); ++i) s += (b[i] - ax[i]) * (b[i] - ax[i]);
+  return std::sqrt(s);
+}
+
+int main() {
+  // csr.rs:505-567: test_csr_create / test_csr_to_dense / test_csr_dot
+  run("csr_create_to_dense_dot", [] {
+    auto m = CsrMatrix<double>::create({1, 2, 3, 4, 5}, {0, 0, 1, 2, 2}, {0, 2, 2, 0, 1}, {3, 3});
+    CHECK((m.shape() == std::pair<size_t, size_t>(3, 3)));
+    CHECK(m.nnz() == 5);
+    auto d = m.to_dense();
+    CHECK((d == std::vector<std::vector<double>>{{1, 0, 2}, {0, 0, 3}, {4, 5, 0}}));
+    auto y = m.dot({1, 2, 3});
+    NEAR(y[0], 7, 1e-10); NEAR(y[1], 9, 1e-10); NEAR(y[2], 14, 1e-10);
+  });
+  // csr.rs:570-591: test_csr_transpose
+  run("csr_transpose", [] {
+    auto m = CsrMatrix<double>::create({1, 2, 3, 4, 5}, {0, 0, 1, 2, 2}, {0, 2, 2, 0, 1}, {3, 3});
+    auto t = m.transpose();
+    CHECK(t.nnz() == 5);
+    CHECK((t.to_dense() == std::vector<std::vector<double>>{{1, 0, 4}, {0, 0, 5}, {2, 3, 0}}));
+  });
+  // csr_array.rs:999-1035: construction and from_triplets
+  run("csr_array_construction_and_from_triplets", [] {
+    auto a = CsrArray<double>::create({1, 2, 3, 4, 5}, {0, 2, 1, 0, 2}, {0, 2, 3, 5}, {3, 3});
+    auto b = CsrArray<double>::from_triplets({0, 0, 1, 2, 2}, {0, 2, 1, 0, 2}, {1, 2, 3, 4, 5}, {3, 3}, false);
+    for (auto* m : {&a, &b}) {
+      CHECK(m->nnz() == 5);
+      CHECK(m->get(0, 0) == 1.0); CHECK(m->get(0, 2) == 2.0); CHECK(m->get(1, 1) == 3.0);
+      CHECK(m->get(2, 0) == 4.0); CHECK(m->get(2, 2) == 5.0); CHECK(m->get(0, 1) == 0.0);
+    }
+  });
+  // csr_array.rs:1059-1076: test_csr_array_dot_vector
+  run("csr_array_dot_vector", [] {
+    auto a = CsrArray<double>::create({1, 2, 3, 4, 5}, {0, 2, 1, 0, 2}, {0, 2, 3, 5}, {3, 3});
+    auto y = a.dot_vector({1, 2, 3});
+    NEAR(y[0], 7, 1e-12); NEAR(y[1], 6, 1e-12); NEAR(y[2], 19, 1e-12);
+  });
+  // iterative.rs:842-868: test_cg_identity / test_cg_diagonal
+  run("cg_identity_and_diagonal", [] {
+    IdentityOperator<double> id(3);
+    auto r = cg<double>(id, {1, 2, 3}, CGOptions<double>());
+    CHECK(r.converged);
+    NEAR(r.x[0], 1, 1e-10); NEAR(r.x[1], 2, 1e-10); NEAR(r.x[2], 3, 1e-10);
+    DiagonalOperator<double> dg({2, 3, 4});
+    r = cg<double>(dg, {2, 6, 12}, CGOptions<double>());
+    CHECK(r.converged);
+    NEAR(r.x[0], 1, 1e-10); NEAR(r.x[1], 2, 1e-10); NEAR(r.x[2], 3, 1e-10);
+  });
+  // iterative.rs:870-892: test_cg_sparse_matrix
+  run("cg_sparse_matrix", [] {
+    auto m = CsrMatrix<double>::create({4, -1, -1, -1, 4, -1, -1, -1, 4}, {0, 0, 0, 1, 1, 1, 2, 2, 2},
+                                       {0, 1, 2, 0, 1, 2, 0, 1, 2}, {3, 3});
+    std::vector<double> b{1, 2, 3};
+    auto r = cg<double>(m, b, CGOptions<double>());
+    CHECK(r.converged);
+    auto ax = m.matvec(r.x);
+    for (int i = 0; i < 3; ++i) NEAR(ax[i], b[i], 1e-9);
+  });
+  // iterative.rs:894-944: bicgstab identity / diagonal / non-symmetric
+  run("bicgstab_identity_diagonal_nonsymmetric", [] {
+    IdentityOperator<double> id(3);
+    auto r = bicgstab<double>(id, {1, 2, 3}, BiCGSTABOptions<double>());
+    CHECK(r.converged);
+    NEAR(r.x[0], 1, 1e-10); NEAR(r.x[2], 3, 1e-10);
+    DiagonalOperator<double> dg({2, 3, 4});
+    r = bicgstab<double>(dg, {2, 6, 12}, BiCGSTABOptions<double>());
+    CHECK(r.converged);
+    NEAR(r.x[0], 1, 1e-10); NEAR(r.x[1], 2, 1e-10); NEAR(r.x[2], 3, 1e-10);
+    auto m = CsrMatrix<double>::create({4, -1, -2, -1, 4, -1, 0, -1, 3}, {0, 0, 0, 1, 1, 1, 2, 2, 2},
+                                       {0, 1, 2, 0, 1, 2, 0, 1, 2}, {3, 3});
+    std::vector<double> b{1, 2, 1};
+    r = bicgstab<double>(m, b, BiCGSTABOptions<double>());
+    CHECK(r.converged);
+    auto ax = m.matvec(r.x);
+    for (int i = 0; i < 3; ++i) NEAR(ax[i], b[i], 1e-9);
+  });
+  // tests/linalg_new_tests.rs:5-32: test_cg_solver
+  run("cg_solver_2x2", [] {
+    auto m = CsrMatrix<double>::create({2, -1, -1, 2}, {0, 0, 1, 1}, {0, 1, 0, 1}, {2, 2});
+    auto r = cg<double>(m, {1, 0}, CGOptions<double>());
+    CHECK(r.converged);
+    NEAR(r.x[0], 2.0 / 3.0, 1e-6); NEAR(r.x[1], 1.0 / 3.0, 1e-6);
+  });
+  // tests/preconditioner_tests.rs:7-42: test_cg_with_jacobi_preconditioner
+  run("cg_with_jacobi_preconditioner", [] {
+    auto m = CsrMatrix<double>::create({4, -1, -1, 4, -1, -1, 4}, {0, 0, 1, 1, 1, 2, 2}, {0, 1, 0, 1, 2, 1, 2}, {3, 3});
+    CGOptions<double> o;
+    o.preconditioner = std::make_shared<JacobiPreconditioner<double>>(JacobiPreconditioner<double>::create(m));
+    std::vector<double> b{2, 1, 2};
+    auto r = cg<double>(m, b, o);
+    CHECK(r.converged);
+    CHECK(r.iterations < 20);
+    auto ax = m.matvec(r.x);
+    for (int i = 0; i < 3; ++i) NEAR(ax[i], b[i], 1e-5);
+  });
+  // tests/preconditioner_tests.rs:44-63 and preconditioners.rs:405-419
+  run("jacobi_preconditioner_simple", [] {
+    auto m = CsrMatrix<double>::create({2, 3, 4}, {0, 1, 2}, {0, 1, 2}, {3, 3});
+    auto y = JacobiPreconditioner<double>::create(m).matvec({2, 6, 12});
+    NEAR(y[0], 1, 1e-10); NEAR(y[1], 2, 1e-10); NEAR(y[2], 3, 1e-10);
+    auto z = JacobiPreconditioner<double>::from_diagonal({2, 3, 4}).matvec({2, 6, 12});
+    NEAR(z[0], 1, 1e-10); NEAR(z[1], 2, 1e-10); NEAR(z[2], 3, 1e-10);
+  });
+  // tests/bicgstab_tests.rs:6-53: duplicate (3,3) entry, left Jacobi
+  run("bicgstab_with_preconditioner", [] {
+    auto m = CsrMatrix<double>::create({10, 1, 2, 12, 1, 1, 8, 2, 3, 1, 15, 1},
+                                       {0, 0, 1, 1, 1, 2, 2, 2, 3, 3, 3, 3},
+                                       {0, 1, 0, 1, 2, 1, 2, 3, 0, 2, 3, 3}, {4, 4});
+    std::vector<double> b{11, 15, 11, 20};
+    BiCGSTABOptions<double> o;
+    o.max_iter = 100; o.rtol = 1e-6; o.atol = 1e-8;
+    o.left_preconditioner = std::make_shared<JacobiPreconditioner<double>>(JacobiPreconditioner<double>::create(m));
+    auto r = bicgstab<double>(m, b, o);
+    CHECK(r.converged);
+    CHECK(r.iterations < 50);
+    CHECK(resid(m, r.x, b) < 1e-6);
+  });
+  // tests/bicgstab_tests.rs:55-113: convection-diffusion n = 10
+  run("bicgstab_complex_system", [] {
+    const size_t n = 10;
+    std::vector<size_t> rows, cols;
+    std::vector<double> data;
+    for (size_t i = 0; i < n; ++i) {
+      rows.push_back(i); cols.push_back(i); data.push_back(4.0);
+      if (i > 0) {
+        rows.push_back(i); cols.push_back(i - 1); data.push_back(-1.5);
+        rows.push_back(i - 1); cols.push_back(i); data.push_back(-0.5);
+      }
+    }
+    auto m = CsrMatrix<double>::create(data, rows, cols, {n, n});
+    std::vector<double> b;
+    for (size_t i = 0; i < n; ++i) b.push_back(1.0 + i);
+    BiCGSTABOptions<double> o;
+    o.max_iter = 200; o.rtol = 1e-8; o.atol = 1e-10;
+    auto r = bicgstab<double>(m, b, o);
+    CHECK(r.converged);
+    CHECK(resid(m, r.x, b) < 5e-7);
+  });
+  // tests/bicgstab_tests.rs:115-137: breakdown on a singular system
+  run("bicgstab_breakdown_detection", [] {
+    auto m = CsrMatrix<double>::create({1, 1, 1, 1}, {0, 0, 1, 1}, {0, 1, 0, 1}, {2, 2});
+    auto r = bicgstab<double>(m, {1, 2}, BiCGSTABOptions<double>());
+    CHECK(!r.converged);
+    CHECK(r.message.find("breakdown") != std::string::npos);
+  });
+  // ic.rs:237-271: test_ic0_simple / test_ic0_not_spd
+  run("ic0_simple_and_not_spd", [] {
+    auto m = CsrMatrix<double>::from_raw_csr({4, -1, -1, 4, -1, -1, 4}, {0, 2, 5, 7}, {0, 1, 0, 1, 2, 1, 2}, {3, 3});
+    auto y = IC0Preconditioner<double>::create(m).matvec({1, 2, 3});
+    for (double v : y) CHECK(std::isfinite(v));
+    auto bad = CsrMatrix<double>::from_raw_csr({1, 2, 3, 4}, {0, 2, 4}, {0, 1, 0, 1}, {2, 2});
+    bool threw = false;
+    try {
+      IC0Preconditioner<double>::create(bad);
+    } catch (const SparseError& e) {
+      threw = e.variant() == "ValueError";
+    }
+    CHECK(threw);
+  });
+  // a user-defined operator joins a device solve (host callback)
+  run("user_operator_in_device_cg", [] {
+    struct Tridiag : LinearOperator<double> {
+      std::pair<size_t, size_t> shape() const override { return {5, 5}; }
+      std::vector<double> matvec(const std::vector<double>& x) const override {
+        std::vector<double> y(5);
+        for (int i = 0; i < 5; ++i) y[i] = 4 * x[i] - (i > 0 ? x[i - 1] : 0) - (i < 4 ? x[i + 1] : 0);
+        return y;
+      }
+    } t;
+    std::vector<double> b{1, 2, 3, 4, 5};
+    auto r = cg<double>(t, b, CGOptions<double>());
+    CHECK(r.converged);
+    CHECK(resid(t, r.x, b) < 1e-8);
+  });
+  // gmres: no test in the reference crate; the non-symmetric 3x3 above
+  run("gmres_nonsymmetric", [] {
+    auto m = CsrMatrix<double>::create({4, -1, -2, -1, 4, -1, 0, -1, 3}, {0, 0, 0, 1, 1, 1, 2, 2, 2},
+                                       {0, 1, 2, 0, 1, 2, 0, 1, 2}, {3, 3});
+    std::vector<double> b{1, 2, 1};
+    auto r = gmres<double>(m, b, GMRESOptions<double>());
+    CHECK(r.converged);
+    CHECK(resid(m, r.x, b) < 1e-9);
+  });
+  // errors carry the reference's variants and messages (csr.rs:107-119)
+  run("construction_errors", [] {
+    try {
+      CsrMatrix<double>::create({1, 2}, {0, 3}, {0, 0}, {3, 3});
+      CHECK(false);
+    } catch (const SparseError& e) {
+      CHECK(e.variant() == "ValueError");
+      CHECK(std::string(e.what()) == "Value error: Row index out of bounds");
+    }
+  });
+  std::printf("%d/%d passed\n", g_run - g_failed, g_run);
+  return g_failed ? 1 : 0;
+}
