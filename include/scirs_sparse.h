@@ -179,8 +179,11 @@ int sx_op_rmatvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, 
 
 /* SpMV flags for sx_spmv_ex */
 #define SX_SPMV_EXACT 1u /* per-row sequential sum of rounded products (reference order) */
-/* Device-pointer SpMV with an explicit summation mode (the default of
- * sx_op_matvec is the exact mode). */
+/* Device-pointer SpMV with an explicit summation mode, asynchronous on the
+ * context stream.  flags = SX_SPMV_EXACT: the reference's rounding, bit for
+ * bit (the mode of sx_op_matvec); flags = 0: FP64 rows are summed with fused
+ * multiply-adds in storage order (a few ulp per row, half the FP64 pipe
+ * work); FP32 is always exact. */
 int sx_spmv_ex(sx_ctx ctx, sx_op a, const void* x_dev, void* y_dev, unsigned flags);
 
 /* --------------------------------------------------------- preconditioners */
@@ -269,22 +272,37 @@ int sx_gmres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_gmres_
 
 /* ------------------------------------------- mixed precision (no reference
  * counterpart; nearest dense analogue scirs2-linalg mixed_precision) */
-/* FP64 iterative refinement around an FP32 preconditioned CG:
- *   x = x0 (FP64); repeat { r = b - A x in FP64; stop when
- *   ||r||_2 <= tol ||b||_2; solve A d = r/||r|| with FP32 PCG to inner_rtol;
- *   x += ||r|| d (FP64) }.
- * The loop also stops (converged = 0) when a correction fails to halve the
- * FP64 residual: with kappa(A) * 2^-24 near 1 the FP32 solve cannot help, and
- * the caller should fall back to an FP64 solve.
+/* FP32 preconditioned CG inside an FP64 refinement loop.  FP64 holds the
+ * solution, the true residual r = b - A x and its norms; every Krylov
+ * iteration runs in FP32.  Two outer loops:
+ *   SX_IR_REPLACE (default): one FP32 CG run split into segments.  A segment
+ *     ends when the FP32 recursive residual has fallen by replace_factor;
+ *     then x += x32 (FP64), r = b - A x (FP64) replaces the FP32 residual and
+ *     the search direction continues with beta = r.z / r_old.z_old, so the
+ *     Krylov progress carries over (residual replacement, "reliable
+ *     updates").  outer_iterations counts replacements, max_inner caps each
+ *     segment, inner_rtol is unused.
+ *   SX_IR_RESTART: classic refinement, x = x0; repeat { r = b - A x (FP64);
+ *     solve A d = r/||r|| with FP32 PCG from zero to inner_rtol;
+ *     x += ||r|| d (FP64) }.
+ * Both stop when ||r||_2 <= tol ||b||_2 (FP64 true residual, converged = 1),
+ * and stop unconverged when the FP64 residual stops falling (halving fails
+ * twice for REPLACE, once for RESTART): with kappa(A) * 2^-24 near 1 the
+ * FP32 iteration cannot help and the caller should fall back to an FP64 solve.
  * a64 must be SX_F64; the FP32 copy is made inside (or pass a32). */
+#define SX_IR_REPLACE 0
+#define SX_IR_RESTART 1
 typedef struct {
   uint64_t max_outer;    /* default 30 */
-  uint64_t max_inner;    /* default 10000 */
+  uint64_t max_inner;    /* default 10000 (RESTART: per inner solve; REPLACE: per segment) */
   double tol;            /* default 1e-10 */
-  double inner_rtol;     /* default 1e-4 */
+  double inner_rtol;     /* default 1e-4 (RESTART only) */
   const void* x0;        /* FP64, NULL = zeros */
   sx_op preconditioner;  /* FP32 operator (JACOBI/IC0/FSAI) or NULL = Jacobi of a32 */
   sx_op a32;             /* optional FP32 copy of a64 */
+  int mode;              /* SX_IR_REPLACE (default) or SX_IR_RESTART */
+  int reserved;
+  double replace_factor; /* default 0.1 (REPLACE only): FP32 residual drop per segment */
 } sx_ir_options;
 typedef struct {
   uint64_t outer_iterations;

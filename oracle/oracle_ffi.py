@@ -85,6 +85,8 @@ def lib():
             "or_bicgstab": (ip, [vp, vp, u64, dbl, dbl, vp, vp, vp, vp, C.POINTER(Res), E]),
             "or_gmres": (ip, [vp, vp, u64, u64, dbl, dbl, vp, vp, vp, C.POINTER(Res), E]),
             "or_cg_mixed_ir": (ip, [vp, vp, vp, i64, vp, C.POINTER(IROpt), vp, C.POINTER(IRRes)]),
+            "or_cg_mixed_replace": (ip, [vp, vp, vp, i64, vp, C.POINTER(IROpt), C.c_double, vp,
+                                         C.POINTER(IRRes)]),
             "or_true_rel_residual": (dbl, [vp, vp, vp, i64, vp, vp]),
         }
         for name, (res, args) in sig.items():
@@ -245,6 +247,22 @@ def cg_mixed_ir(indptr, indices, data, b, tol=1e-10, inner_rtol=1e-4, max_outer=
     o = IROpt(max_outer, max_inner, tol, inner_rtol, 1 if jacobi else 0)
     r = IRRes()
     lib().or_cg_mixed_ir(p(indptr), p(indices), p(data), n, p(b), C.byref(o), p(x), C.byref(r))
+    return dict(x=x, outer=int(r.outer_iterations), inner=int(r.inner_iterations),
+                rel_residual=float(r.rel_residual), converged=bool(r.converged))
+
+
+def cg_mixed_replace(indptr, indices, data, b, tol=1e-10, delta=0.1, max_outer=30,
+                     max_inner=10000, jacobi=True):
+    indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+    indices = np.ascontiguousarray(indices, dtype=np.int32)
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = len(indptr) - 1
+    x = np.empty(n, dtype=np.float64)
+    o = IROpt(max_outer, max_inner, tol, 0.0, 1 if jacobi else 0)
+    r = IRRes()
+    lib().or_cg_mixed_replace(p(indptr), p(indices), p(data), n, p(b), C.byref(o), delta, p(x),
+                              C.byref(r))
     return dict(x=x, outer=int(r.outer_iterations), inner=int(r.inner_iterations),
                 rel_residual=float(r.rel_residual), converged=bool(r.converged))
 

@@ -1074,4 +1074,98 @@ int or_cg_mixed_ir(const int64_t* indptr, const int32_t* indices, const double* 
   return 0;
 }
 
+// FP32 PCG with FP64 residual replacement (restates the device loop of
+// sx_cg_mixed, mode SX_IR_REPLACE):
+//   x64 = 0, r = b (FP64); r32 = (float) r; x32 = 0; z = M r32; p = z;
+//   segment: CG iterations on (x32, r32, p) until ||r32|| <= max(atol, delta ||r32_0||)
+//            with atol = 0.5 tol ||b|| (FP32), or pAp <= 0, or max_inner;
+//   then x64 += x32, x32 = 0, r = b - A x64 (FP64); stop if ||r|| <= tol ||b||;
+//   r32 = (float) r; z = M r32; beta = r32.z / rz_old; p = z + beta p; next segment.
+//   Stops unconverged after max_outer replacements or two replacements in a
+//   row that fail to halve the FP64 residual.
+int or_cg_mixed_replace(const int64_t* indptr, const int32_t* indices, const double* data, int64_t n,
+                        const double* b, const or_ir_options* opt, double delta, double* x,
+                        or_ir_result* res) {
+  or_op* a32 = or_op_csr_i32(1, indptr, indices, data, n, n);
+  a32->f64 = 0;
+  or_op* m = nullptr;
+  if (opt->jacobi) {
+    or_err e;
+    m = or_op_jacobi(a32, &e);
+    if (!m) { delete a32; return 1; }
+  }
+  std::vector<double> x64(n, 0.0), r64(n), ax(n);
+  auto true_residual = [&]() {
+    spmv<double>(indptr, indices, data, (uint64_t)n, x64.data(), ax.data());
+    double rr = 0;
+    for (int64_t i = 0; i < n; ++i) { r64[i] = b[i] - ax[i]; rr = rr + r64[i] * r64[i]; }
+    return std::sqrt(rr);
+  };
+  double bb = 0;
+  for (int64_t i = 0; i < n; ++i) bb = bb + b[i] * b[i];
+  const double bnorm = std::sqrt(bb);
+  double rnorm = true_residual();
+  double rel = rnorm / bnorm;
+  uint64_t outer = 0, inner = 0;
+  bool conv = rnorm <= opt->tol * bnorm;
+  if (!conv) {
+    std::vector<float> r(n), x32(n, 0.0f), z, p, ap;
+    for (int64_t i = 0; i < n; ++i) r[i] = (float)r64[i];
+    z = m ? op_apply(m, r) : r;
+    p = z;
+    float rz_old = dot(r, z);
+    const float atol = (float)(0.5 * opt->tol * bnorm);
+    float tol = std::fmax(atol, (float)delta * norm2(r));
+    double prev = rnorm;
+    int stalls = 0;
+    for (;;) {
+      bool not_pd = false;
+      for (uint64_t it = 0; it < opt->max_inner; ++it) {
+        ap = op_apply(a32, p);
+        const float pap = dot(p, ap);
+        if (pap <= 0.0f) { not_pd = true; break; }
+        const float alpha = rz_old / pap;
+        for (int64_t i = 0; i < n; ++i) x32[i] += alpha * p[i];
+        for (int64_t i = 0; i < n; ++i) r[i] -= alpha * ap[i];
+        ++inner;
+        if (norm2(r) <= tol) break;
+        z = m ? op_apply(m, r) : r;
+        const float rz_new = dot(r, z);
+        const float beta = rz_new / rz_old;
+        for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        rz_old = rz_new;
+      }
+      for (int64_t i = 0; i < n; ++i) { x64[i] = x64[i] + (double)x32[i]; x32[i] = 0.0f; }
+      rnorm = true_residual();
+      rel = rnorm / bnorm;
+      ++outer;
+      if (rnorm <= opt->tol * bnorm) { conv = true; break; }
+      if (not_pd || outer >= opt->max_outer) break;
+      if (!(rnorm < 0.5 * prev)) {
+        if (++stalls >= 2) break;
+      } else {
+        stalls = 0;
+      }
+      prev = rnorm;
+      for (int64_t i = 0; i < n; ++i) r[i] = (float)r64[i];
+      z = m ? op_apply(m, r) : r;
+      const float rz = dot(r, z);
+      const float beta = rz / rz_old;
+      rz_old = rz;
+      for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+      tol = std::fmax(atol, (float)delta * norm2(r));
+    }
+  }
+  std::memcpy(x, x64.data(), n * 8);
+  if (res) {
+    res->outer_iterations = outer;
+    res->inner_iterations = inner;
+    res->rel_residual = rel;
+    res->converged = conv ? 1 : 0;
+  }
+  delete m;
+  delete a32;
+  return 0;
+}
+
 }  // extern "C"

@@ -130,6 +130,11 @@ typedef struct {
 } or_ir_result;
 int or_cg_mixed_ir(const int64_t* indptr, const int32_t* indices, const double* data, int64_t n,
                    const double* b, const or_ir_options* opt, double* x, or_ir_result* res);
+/* FP32 PCG with FP64 residual replacement every time the FP32 residual has
+ * fallen by delta (restates sx_cg_mixed, mode SX_IR_REPLACE). */
+int or_cg_mixed_replace(const int64_t* indptr, const int32_t* indices, const double* data, int64_t n,
+                        const double* b, const or_ir_options* opt, double delta, double* x,
+                        or_ir_result* res);
 
 /* FP64 true relative residual ||b - A x|| / ||b|| with sequential sums. */
 double or_true_rel_residual(const int64_t* indptr, const int32_t* indices, const double* data,

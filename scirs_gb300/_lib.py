@@ -97,7 +97,14 @@ class IROptions(C.Structure):
         ("x0", c_vp),
         ("preconditioner", op_t),
         ("a32", op_t),
+        ("mode", c_int),
+        ("reserved", c_int),
+        ("replace_factor", c_dbl),
     ]
+
+
+SX_IR_REPLACE = 0
+SX_IR_RESTART = 1
 
 
 class IRResult(C.Structure):

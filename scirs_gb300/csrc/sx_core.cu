@@ -16,6 +16,7 @@
 #include <atomic>
 #include <climits>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -76,10 +77,11 @@ static int err_arg(const char* what) {
   return set_error(SX_ERR_INVALID_ARGUMENT, std::string("Invalid argument: ") + what);
 }
 
+// Every device array carries 64 bytes of slack past its end: the windowed
+// SpMV's 16-byte copies may read up to 15 bytes past the last element.
 int dev_alloc(void** p, size_t bytes) {
   *p = nullptr;
-  if (bytes == 0) bytes = 16;
-  SX_CUDA(cudaMalloc(p, bytes));
+  SX_CUDA(cudaMalloc(p, align_up(bytes, 16) + 64));
   return SX_OK;
 }
 void dev_free(void* p) {
@@ -571,6 +573,47 @@ __global__ void k_check_cols32(const int32_t* __restrict__ idx, int64_t n, int64
 
 }  // namespace
 
+// tile_row[u] = first row r with indptr[r+1] > u * kUnit: the row holding
+// entry u * kUnit.  Each nonempty row writes the units that start inside it;
+// tile_row[0] = 0 covers leading empty rows and tile_row[units] = nrows.
+__global__ void k_tile_rows(const int32_t* __restrict__ ptr, int64_t nrows, int64_t units, int32_t* tr) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
+    const int64_t lo = ptr[r], hi = ptr[r + 1];
+    if (hi <= lo) continue;
+    int64_t u = (lo + kUnit - 1) / kUnit;
+    if (u == 0) u = 1;
+    for (; u * kUnit < hi; ++u) tr[u] = (int32_t)r;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    tr[0] = 0;
+    tr[units] = (int32_t)nrows;
+  }
+}
+
+int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
+  dev_free(c.tile_row);
+  c.tile_row = nullptr;
+  c.units = 0;
+  if (!c.monotone || c.nnz <= 0 || c.nrows <= 0) return SX_OK;
+  int32_t first = -1;
+  SX_CUDA(cudaMemcpyAsync(&first, c.indptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (first != 0) return SX_OK;
+  const int64_t units = (c.nnz + kUnit - 1) / kUnit;
+  SX_CHECK(dev_alloc((void**)&c.tile_row, (units + 1) * 4));
+  k_tile_rows<<<vec_grid(ctx, c.nrows), kBlock, 0, ctx->stream>>>(c.indptr, c.nrows, units, c.tile_row);
+  ctx->launches++;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    dev_free(c.tile_row);
+    c.tile_row = nullptr;
+    return cuda_fail(e, "tile rows", __FILE__, __LINE__);
+  }
+  c.units = units;
+  return SX_OK;
+}
+
 int csr_finalize_stats(sx_ctx ctx, DevCsr& c) {
   int* d = nullptr;
   SX_CHECK(dev_alloc((void**)&d, 4 * sizeof(int)));
@@ -591,7 +634,7 @@ int csr_finalize_stats(sx_ctx ctx, DevCsr& c) {
   c.has_sorted_indices = h[2] == 0;
   c.max_chunk_nnz = h[3];
   c.mean_row_len = c.nrows > 0 ? (double)c.nnz / (double)c.nrows : 0.0;
-  return SX_OK;
+  return csr_prepare_tiles(ctx, c);
 }
 
 static std::atomic<uint64_t> g_op_serial{1};
@@ -611,9 +654,12 @@ static void free_csr(DevCsr& c) {
   dev_free(c.indptr);
   dev_free(c.indices);
   dev_free(c.vals);
+  dev_free(c.tile_row);
   c.indptr = nullptr;
   c.indices = nullptr;
   c.vals = nullptr;
+  c.tile_row = nullptr;
+  c.units = 0;
 }
 
 }  // namespace sx
@@ -690,6 +736,8 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   c->device = device;
   c->num_sms = sms;
   c->own_stream = own;
+  if (const char* t = std::getenv("SX_WIN")) c->win_mode = std::atoi(t);
+  if (const char* t = std::getenv("SX_WIN_SHAPE")) c->win_shape = std::atoi(t);
   if (own) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -1086,7 +1134,7 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
   if (a->kind != SX_OP_CSR) return err_arg("not a CSR operator");
   SX_CUDA(cudaSetDevice(ctx->device));
   DevCsr c = a->csr;
-  c.indptr = nullptr; c.indices = nullptr; c.vals = nullptr;
+  c.indptr = nullptr; c.indices = nullptr; c.vals = nullptr; c.tile_row = nullptr; c.units = 0;
   const int64_t n = a->csr.nnz;
   int rc = SX_OK;
   do {
@@ -1108,7 +1156,8 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
       }
     }
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) rc = cuda_fail(e, "astype", __FILE__, __LINE__);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "astype", __FILE__, __LINE__); break; }
+    rc = csr_prepare_tiles(ctx, c);
   } while (0);
   if (rc != SX_OK) { free_csr(c); return rc; }
   sx_op op = new_op(ctx, SX_OP_CSR, dtype, a->nrows, a->ncols);

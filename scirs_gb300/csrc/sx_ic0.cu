@@ -41,6 +41,7 @@ void ic0_destroy(IC0Dev* p) {
   dev_free(p->L.indptr);
   dev_free(p->L.indices);
   dev_free(p->L.vals);
+  dev_free(p->L.tile_row);
   if (p->lt) destroy_op_internal(p->lt);
   dev_free(p->dlast);
   dev_free(p->dfirst);

@@ -55,6 +55,10 @@ struct DevCsr {
   int32_t max_row_len = 0;
   double mean_row_len = 0.0;
   int32_t max_chunk_nnz = 0;   // most nonzeros in any 256-row chunk
+  // first row of every 256-entry unit of the nonzeros (units + 1 entries),
+  // set for monotone matrices with indptr[0] == 0 and nnz > 0
+  int32_t* tile_row = nullptr;
+  int64_t units = 0;
 };
 
 struct IC0Dev;   // defined in sx_ic0.cu
@@ -98,6 +102,12 @@ struct sx_ctx_s {
   unsigned int* red_counter = nullptr;
   // solver workspaces and instantiated graphs (sx_krylov.cu)
   void* solver_cache = nullptr;
+  // SpMV kernel choice from SX_WIN: 0 never the windowed kernel, 1 (default)
+  // the windowed kernel for matrices whose 256-row chunks are too long for
+  // the register pipeline, 2 the windowed kernel whenever it applies;
+  // SX_WIN_SHAPE=0|1|2 picks its window shape
+  int win_mode = 1;
+  int win_shape = 0;
 };
 
 namespace sx {
@@ -114,6 +124,10 @@ void dev_free(void* p);
 // Upload host-side CSR arrays (already validated, int32) into a DevCsr and
 // compute row statistics.
 int csr_finalize_stats(sx_ctx ctx, DevCsr& c);
+constexpr int kUnit = 256;  // nonzeros per tile_row entry
+// builds c.tile_row for the windowed SpMV (allocates and synchronises)
+int csr_prepare_tiles(sx_ctx ctx, DevCsr& c);
+
 
 // ------------------------------------------------------------ kernels API
 // Plain device SpMV entry used by the ABI (y = A x, device pointers).

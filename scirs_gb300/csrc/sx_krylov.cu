@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "sx_launch.cuh"
+#include "sx_mixed.cuh"
 
 namespace sx {
 
@@ -521,6 +522,195 @@ static int cg_run(sx_ctx ctx, sx_op a, const void* b, const sx_cg_options* opt, 
     res->converged = h.c.converged;
     res->message = h.c.message;
   }
+  return SX_OK;
+}
+
+// ============================== FP32 CG with FP64 residual replacement
+// One FP32 PCG run split into segments (cg_mixed_replace below).  Between
+// segments the FP32 iterate is folded into the FP64 solution, the FP64 true
+// residual replaces the FP32 one, and the recurrence continues:
+// beta = r'.z' / rz_old, p = z' + beta p.
+
+// x64 += x32; x32 = 0
+struct IrFold {
+  double* x64;
+  float* x32;
+  static constexpr bool kReduce = false;
+  static constexpr bool kVec4 = false;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<double>&) const {
+    x64[i] = x64[i] + (double)x32[i];
+    x32[i] = 0.0f;
+  }
+  __device__ void finish(const Acc3<double>&) const {}
+};
+
+// r32 = (float) r64 (and a second copy, the segment's reference vector)
+struct IrNarrow {
+  const double* r64;
+  float *r32, *copy;
+  static constexpr bool kReduce = false;
+  static constexpr bool kVec4 = false;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<double>&) const {
+    const float v = (float)r64[i];
+    r32[i] = v;
+    if (copy) copy[i] = v;
+  }
+  __device__ void finish(const Acc3<double>&) const {}
+};
+
+// a new segment: beta from the replaced residual, threshold, counters
+__device__ __forceinline__ void ir_restart(CgState<float>* st, float rz, float rr) {
+  st->beta = rz / st->rz_old;
+  st->rz_old = rz;
+  st->rnorm = sqrtf(rr);
+  st->result_norm = st->rnorm;
+  st->tol = fmaxf(st->atol, st->rtol * st->rnorm);
+  st->c.status = ST_RUNNING;
+  st->c.converged = 0;
+  st->c.message = MSG_CONVERGED;
+  st->c.iterations = 0;
+}
+
+// r32 = (float) r64 with r.z (fused elementwise M) and r.r
+struct IrNarrowRz {
+  CgState<float>* st;
+  const double* r64;
+  float* r32;
+  PrecFused<float> pf;
+  static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = false;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<float>& a) const {
+    const float r = (float)r64[i];
+    r32[i] = r;
+    a.a += r * pf.apply(i, r);
+    a.b += r * r;
+  }
+  __device__ void finish(const Acc3<float>& t) const { ir_restart(st, t.a, t.b); }
+};
+
+// r.z and r.r for a general M (z = M r already applied)
+struct IrRz {
+  CgState<float>* st;
+  const float *r, *z;
+  static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = false;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<float>& a) const {
+    a.a += r[i] * z[i];
+    a.b += r[i] * r[i];
+  }
+  __device__ void finish(const Acc3<float>& t) const { ir_restart(st, t.a, t.b); }
+};
+
+// p = z + beta p after a replacement (no iteration counted)
+struct IrP {
+  CgState<float>* st;
+  float* p;
+  const float *r, *z;
+  PrecFused<float> pf;
+  static constexpr bool kReduce = false;
+  static constexpr bool kVec4 = false;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<float>&) const {
+    const float zi = pf.kind == PK_GENERAL ? z[i] : pf.apply(i, r[i]);
+    p[i] = add_rn(zi, mul_rn(st->beta, p[i]));
+  }
+  __device__ void finish(const Acc3<float>&) const {}
+};
+
+int cg_mixed_replace(sx_ctx ctx, sx_op a64, sx_op a32, sx_op m, const double* db, double* dx, double* dr,
+                     IrNorms* nrm, const sx_ir_options* opt, uint64_t* outer, uint64_t* inner,
+                     double* rel, int* converged) {
+  using T = float;
+  const int64_t n = a64->nrows;
+  SX_CHECK(check_prec(a32, m));
+  const int pk = prec_kind(m);
+  const size_t vb = align_up((size_t)std::max<int64_t>(n, 1) * sizeof(T), 256);
+  void *ws = nullptr, *dstate = nullptr;
+  SX_CHECK(ws_get(ctx, vb * 6, &ws, &dstate));
+  // the layout of cg_run: the segment body is the same graph
+  T* B = (T*)((char*)ws + 0 * vb);
+  T* X = (T*)((char*)ws + 1 * vb);
+  T* R = (T*)((char*)ws + 2 * vb);
+  T* P = (T*)((char*)ws + 3 * vb);
+  T* AP = (T*)((char*)ws + 4 * vb);
+  T* Z = (T*)((char*)ws + 5 * vb);
+  CgState<T>* st = (CgState<T>*)dstate;
+  ReduceArea ra;
+  SX_CHECK(ctx_reduce_area(ctx, std::max<int64_t>((n + kBlock - 1) / kBlock, vec_grid(ctx, n)) + 8, &ra));
+  const PrecFused<T> pf = prec_fused<T>(m);
+
+  auto true_residual = [&](IrNorms& h) -> int {
+    // FMA row sums: a few ulp per row, half the FP64 work
+    SX_CHECK(launch_csr<double, EpiIrResid, true>(ctx, a64->csr, dx, dr, EpiIrResid{db, nrm}));
+    SX_CHECK(read_ctl(ctx, nrm, &h, sizeof(h)));
+    return SX_OK;
+  };
+  IrNorms h;
+  SX_CHECK(true_residual(h));
+  const double bnorm = std::sqrt(h.bb);
+  double rnorm = std::sqrt(h.rr);
+  *rel = bnorm > 0 ? rnorm / bnorm : rnorm;
+  if (rnorm <= opt->tol * bnorm) {
+    *converged = 1;
+    return SX_OK;
+  }
+  const double delta = (opt->replace_factor > 0.0 && opt->replace_factor < 1.0) ? opt->replace_factor : 0.1;
+  CgState<T> hs;
+  std::memset(&hs, 0, sizeof(hs));
+  hs.c.max_iter = opt->max_inner;
+  hs.rtol = (T)delta;                            // segment: ||r32|| drops by delta
+  hs.atol = (T)(0.5 * opt->tol * bnorm);         // or reaches half the final target
+  SX_CHECK(write_bytes(ctx, st, &hs, sizeof(hs)));
+  SX_CHECK(launch_vec<double>(ctx, n, IrNarrow{dr, R, B}));
+  if (n > 0) SX_CUDA(cudaMemsetAsync(X, 0, n * sizeof(T), ctx->stream));
+  if (pk == PK_GENERAL) SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiPlain<T>{}));
+  SX_CHECK(launch_vec<T>(ctx, n, CgSetup<T>{st, B, R, Z, P, pf}));
+  auto body = [&]() -> int {
+    SX_CHECK(launch_apply<T>(ctx, a32, P, AP, EpiCgPap<T>{st, P}));
+    SX_CHECK(launch_vec<T>(ctx, n, CgUpdate<T>{st, X, R, P, AP, pf}));
+    if (pk == PK_GENERAL) {
+      SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiSkip<T, CgState<T>>{st}));
+      SX_CHECK(launch_vec<T>(ctx, n, CgRz<T>{st, R, Z}));
+    }
+    SX_CHECK(launch_vec<T>(ctx, n, CgP<T>{st, P, R, Z, pf}));
+    return SX_OK;
+  };
+  const uint64_t key[8] = {1, (uint64_t)sizeof(T), a32->serial, m ? m->serial : 0,
+                           (uint64_t)n, (uint64_t)(uintptr_t)ws, (uint64_t)pk, 0};
+  double prev = rnorm;
+  int stalls = 0;
+  for (;;) {
+    SX_CHECK(run_loop(ctx, st, key, op_graphable(a32) && op_graphable(m), body));
+    SX_CHECK(read_ctl(ctx, st, &hs, sizeof(hs)));
+    *inner += hs.c.iterations;
+    SX_CHECK(launch_vec<double>(ctx, n, IrFold{dx, X}));
+    SX_CHECK(true_residual(h));
+    rnorm = std::sqrt(h.rr);
+    *rel = bnorm > 0 ? rnorm / bnorm : rnorm;
+    *outer += 1;
+    if (rnorm <= opt->tol * bnorm) { *converged = 1; break; }
+    if (hs.c.message == MSG_NOT_PD) break;  // FP32 p.Ap <= 0: no further progress in FP32
+    if (*outer >= opt->max_outer) break;
+    if (!(rnorm < 0.5 * prev)) {
+      if (++stalls >= 2) break;  // FP32 iteration has stagnated
+    } else {
+      stalls = 0;
+    }
+    prev = rnorm;
+    if (pk == PK_GENERAL) {
+      SX_CHECK(launch_vec<double>(ctx, n, IrNarrow{dr, R, nullptr}));
+      SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiPlain<T>{}));
+      SX_CHECK(launch_vec<T>(ctx, n, IrRz{st, R, Z}));
+    } else {
+      SX_CHECK(launch_vec<T>(ctx, n, IrNarrowRz{st, dr, R, pf}));
+    }
+    SX_CHECK(launch_vec<T>(ctx, n, IrP{st, P, R, Z, pf}));
+  }
+  SX_CHECK(ic0_health(ctx, m));
   return SX_OK;
 }
 

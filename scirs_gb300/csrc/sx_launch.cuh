@@ -7,6 +7,7 @@
 
 #include "sx_internal.h"
 #include "sx_kernels.cuh"
+#include "sx_spmv_win.cuh"
 
 namespace sx {
 
@@ -86,6 +87,54 @@ int resident_blocks() {
   return cached;
 }
 
+// Window sizes, ring depths and gather pipelining of the windowed SpMV;
+// SX_WIN_SHAPE selects the variant (0 default).
+template <typename T, int V>
+struct WinShape;
+// (measured on the 4M-row power-law matrix: FP32 best without pipelining,
+// FP64 best with three stages and pipelined gathers)
+template <> struct WinShape<float, 0> { static constexpr int kCap = 256, kStages = 3; static constexpr bool kPipe = false; };
+template <> struct WinShape<float, 1> { static constexpr int kCap = 256, kStages = 3; static constexpr bool kPipe = true; };
+template <> struct WinShape<float, 2> { static constexpr int kCap = 256, kStages = 2; static constexpr bool kPipe = true; };
+template <> struct WinShape<double, 0> { static constexpr int kCap = 256, kStages = 3; static constexpr bool kPipe = true; };
+template <> struct WinShape<double, 1> { static constexpr int kCap = 256, kStages = 2; static constexpr bool kPipe = true; };
+template <> struct WinShape<double, 2> { static constexpr int kCap = 256, kStages = 2; static constexpr bool kPipe = false; };
+
+// Resident blocks per SM of one windowed SpMV variant (opts in to the
+// dynamic shared memory once per instantiation); -1 if it cannot run.
+template <typename T, int V, class Epi, bool FMA>
+int win_resident_blocks() {
+  static int cached = 0;
+  if (!cached) {
+    using Sh = WinShape<T, V>;
+    constexpr auto kern = spmv_win_kernel<T, Sh::kCap, Sh::kStages, Epi, FMA, Sh::kPipe>;
+    constexpr int smem = WinCfg<T, Sh::kCap, Sh::kStages, FMA>::kSmem;
+    int nb = 0;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kBlock, smem) != cudaSuccess || nb < 1)
+      nb = -1;
+    cached = nb;
+  }
+  return cached;
+}
+
+template <typename T, int V, class Epi, bool FMA>
+bool launch_win(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const ReduceArea& ra,
+                int64_t blocks) {
+  const int nb = win_resident_blocks<T, V, Epi, FMA>();
+  if (nb <= 0) return false;
+  using Sh = WinShape<T, V>;
+  constexpr auto kern = spmv_win_kernel<T, Sh::kCap, Sh::kStages, Epi, FMA, Sh::kPipe>;
+  constexpr int smem = WinCfg<T, Sh::kCap, Sh::kStages, FMA>::kSmem;
+  // at least 4 units per warp, at most the resident blocks, at most the reduction area
+  const int64_t by_units = (c.units + (kBlock / 32) * 4 - 1) / ((kBlock / 32) * 4);
+  int64_t grid = std::min<int64_t>((int64_t)ctx->num_sms * nb, by_units);
+  grid = std::max<int64_t>(1, std::min<int64_t>(grid, blocks));
+  kern<<<(unsigned)grid, kBlock, smem, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, c.tile_row, x, y,
+                                                       c.nrows, c.nnz, c.units, (T*)ra.partials, ra.counter, epi);
+  return true;
+}
+
 // CSR SpMV with epilogue.  Must not allocate or synchronise: it runs inside
 // stream capture.  The reduction area must already hold gridDim blocks.
 template <typename T, class Epi, bool FMA = false>
@@ -94,7 +143,18 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
   ReduceArea ra;
   const int64_t blocks = (c.nrows + kBlock - 1) / kBlock;
   SX_CHECK(ctx_reduce_area(ctx, blocks, &ra));
-  if (c.monotone && c.max_chunk_nnz + 3 <= kBlock * 8) {
+  // every 256-row chunk fits the register pipeline: stencil-like matrices
+  const bool pipe_fits = c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12;
+  bool done = false;
+  if (c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) {
+    switch (ctx->win_shape) {
+      case 1: done = launch_win<T, 1, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
+      case 2: done = launch_win<T, 2, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
+      default: done = launch_win<T, 0, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
+    }
+  }
+  if (done) {
+  } else if (c.monotone && c.max_chunk_nnz + 3 <= kBlock * 8) {
     constexpr auto kern = spmv_pipe_kernel<T, 8, Epi, FMA>;
     const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
     kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows,

@@ -1,9 +1,12 @@
-// Mixed precision: FP64 iterative refinement around an FP32 preconditioned
-// CG (no reference counterpart; the nearest relative is the dense
-// scirs2-linalg mixed_precision module).  FP64 is used only for the true
-// residual r = b - A x, its norm, and the solution accumulation; every
-// inner iteration runs in FP32.
+// Mixed precision: FP64 refinement around an FP32 preconditioned CG (no
+// reference counterpart; the nearest relative is the dense scirs2-linalg
+// mixed_precision module).  FP64 is used only for the true residual
+// r = b - A x, its norm, and the solution accumulation; every inner
+// iteration runs in FP32.  This file holds the entry point, the restart
+// loop and the FP64 true residual; the residual-replacement loop shares the
+// CG kernels and graphs of sx_krylov.cu and lives there.
 //
+// restart loop:
 //   x = x0;  loop: r = b - A x (FP64);  stop if ||r|| <= tol ||b||;
 //            solve A d = r / ||r|| with FP32 PCG to inner_rtol;
 //            x += ||r|| d  (FP64)
@@ -13,33 +16,9 @@
 #include <cstring>
 #include <string>
 
-#include "sx_launch.cuh"
+#include "sx_mixed.cuh"
 
 namespace sx {
-
-struct IrNorms {
-  double rr, bb, rnorm, inv_rnorm;
-};
-
-// y = b - A x in FP64 with ||y||^2 and ||b||^2 fused
-struct EpiIrResid {
-  const double* b;
-  IrNorms* norms;
-  static constexpr bool kReduce = true;
-  __device__ bool skip() const { return false; }
-  __device__ double out(int64_t i, double ax) const { return sub_rn(b[i], ax); }
-  __device__ void acc(int64_t i, double y, Acc3<double>& a) const {
-    a.a += y * y;
-    a.b += b[i] * b[i];
-  }
-  __device__ void finish(const Acc3<double>& t) const {
-    norms->rr = t.a;
-    norms->bb = t.b;
-    // one square root and one division here instead of one per element
-    norms->rnorm = sqrt(t.a);
-    norms->inv_rnorm = 1.0 / norms->rnorm;
-  }
-};
 
 struct ScaleDown {
   const double* r;
@@ -81,6 +60,9 @@ void sx_ir_options_default(sx_ir_options* o) {
   o->x0 = nullptr;
   o->preconditioner = nullptr;
   o->a32 = nullptr;
+  o->mode = SX_IR_REPLACE;
+  o->reserved = 0;
+  o->replace_factor = 0.1;
 }
 
 int sx_true_rel_residual(sx_ctx ctx, sx_op a64, const double* b, const double* x, sx_mem mem,
@@ -136,6 +118,8 @@ int sx_cg_mixed(sx_ctx ctx, sx_op a64, const double* b, uint64_t b_len, const sx
                      (uint64_t)a64->nrows, b_len);
   sx_ir_options d;
   if (!opt) { sx_ir_options_default(&d); opt = &d; }
+  if (opt->mode != SX_IR_REPLACE && opt->mode != SX_IR_RESTART)
+    return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: mixed-precision mode");
   SX_CUDA(cudaSetDevice(ctx->device));
   const int64_t n = a64->nrows;
   sx_op a32 = opt->a32, own32 = nullptr, m = opt->preconditioner, ownm = nullptr;
@@ -166,6 +150,15 @@ int sx_cg_mixed(sx_ctx ctx, sx_op a64, const double* b, uint64_t b_len, const sx
     cudaMemcpyAsync(db, b, n * 8, kin, ctx->stream);
     if (opt->x0) cudaMemcpyAsync(dx, opt->x0, n * 8, kin, ctx->stream);
     else cudaMemsetAsync(dx, 0, n * 8, ctx->stream);
+    if (opt->mode != SX_IR_RESTART) {
+      rc = cg_mixed_replace(ctx, a64, a32, m, db, dx, dr, nrm, opt, &outer, &inner, &rel, &converged);
+      if (rc) break;
+      const cudaMemcpyKind kout = mem == SX_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+      cudaMemcpyAsync(x_out, dx, n * 8, kout, ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) rc = cuda_fail(e, "solution copy", __FILE__, __LINE__);
+      break;
+    }
     sx_cg_options io;
     sx_cg_options_default(&io);
     io.max_iter = opt->max_inner;

@@ -8,9 +8,12 @@
 // other work whose memory plan is fixed.  They still need the FP64 residual
 // check that ends a mixed-precision solve.  sx_true_rel_residual allocates a
 // residual vector and reduction space per call; this variant computes the
-// same norms (bit-identical: the same per-row order and the same block
-// reduction tree) with its reduction partials, ticket counter and totals in a
-// file-scope device array, and takes b and x as device pointers.
+// same residual entries (bit-identical: the same per-row order) and their
+// norms with its reduction partials, ticket counter and totals in a
+// file-scope device array, and takes b and x as device pointers.  Its
+// reduction tree is one row per thread, so the norms agree with the
+// allocating entry point's (whose tree follows the SpMV's work split) to the
+// rounding of the summation order.
 //
 // Limits and sharing:
 //  - at most kNoAllocMaxRows rows (the scratch holds one partial pair per

@@ -17,11 +17,15 @@ namespace sx {
 int ic0_apply(sx_ctx ctx, sx_op op, const void* x, void* y);  // sx_ic0.cu
 
 int spmv_device(sx_ctx ctx, sx_op a, const void* x, void* y, unsigned flags) {
-  (void)flags;
-  // the public SpMV keeps the reference's per-row rounding (bit-exact)
-  if (a->dtype == SX_F64)
-    return launch_apply<double, EpiPlain<double>, true>(ctx, a, (const double*)x, (double*)y,
-                                                        EpiPlain<double>{});
+  // SX_SPMV_EXACT keeps the reference's per-row rounding (bit-exact); without
+  // it, FP64 rows are summed with fused multiply-adds (a few ulp per row)
+  if (a->dtype == SX_F64) {
+    if (flags & SX_SPMV_EXACT)
+      return launch_apply<double, EpiPlain<double>, true>(ctx, a, (const double*)x, (double*)y,
+                                                          EpiPlain<double>{});
+    return launch_apply<double, EpiPlain<double>, false>(ctx, a, (const double*)x, (double*)y,
+                                                         EpiPlain<double>{});
+  }
   return launch_apply<float, EpiPlain<float>, true>(ctx, a, (const float*)x, (float*)y,
                                                     EpiPlain<float>{});
 }

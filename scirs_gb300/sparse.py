@@ -416,8 +416,16 @@ class IRResult:
 
 def cg_mixed(a64: Operator, b, tol=1e-10, inner_rtol=1e-4, max_outer=30, max_inner=10000,
              x0=None, preconditioner: Optional[Operator] = None,
-             a32: Optional[Operator] = None) -> IRResult:
-    """FP64 iterative refinement around an FP32 PCG (no reference counterpart)."""
+             a32: Optional[Operator] = None, mode: str = "replace",
+             replace_factor: float = 0.1) -> IRResult:
+    """FP32 PCG inside an FP64 refinement loop (no reference counterpart).
+
+    mode "replace": one FP32 CG run whose residual is replaced by the FP64
+    true residual each time it has fallen by `replace_factor`; mode
+    "restart": classic refinement, a fresh FP32 PCG to `inner_rtol` per
+    correction."""
+    if mode not in ("replace", "restart"):
+        raise ValueError("mode must be 'replace' or 'restart'")
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.empty(a64.shape[0], dtype=np.float64)
     x0a = None if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
@@ -427,6 +435,8 @@ def cg_mixed(a64: Operator, b, tol=1e-10, inner_rtol=1e-4, max_outer=30, max_inn
     o.x0 = _ptr(x0a) if x0a is not None else None
     o.preconditioner = preconditioner.handle if preconditioner else None
     o.a32 = a32.handle if a32 else None
+    o.mode = L.SX_IR_REPLACE if mode == "replace" else L.SX_IR_RESTART
+    o.replace_factor = replace_factor
     r = L.IRResult()
     _check(L.lib.sx_cg_mixed(a64.ctx.handle, a64.handle, _ptr(b), b.size, C.byref(o), _ptr(x),
                              L.SX_MEM_HOST, C.byref(r)))

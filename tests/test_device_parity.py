@@ -231,7 +231,7 @@ def test_gmres_matches_oracle(S, ctx, restart, prec):
 def test_mixed_precision_refinement(S, ctx):
     ip, ix, v, n, b = _system(S, "varcoef3d", (24, 24, 24), p0=1.5)
     a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
-    r = S.cg_mixed(a, b, tol=1e-10, inner_rtol=1e-4)
+    r = S.cg_mixed(a, b, tol=1e-10, inner_rtol=1e-4, mode="restart")
     assert r.converged and r.rel_residual <= 1e-10
     res = O.true_rel_residual(ip, ix, v, b, r.x)
     assert res <= 1.5e-10
@@ -240,6 +240,29 @@ def test_mixed_precision_refinement(S, ctx):
     # both solve to 1e-10: the solutions agree to ~cond * 1e-10
     assert np.linalg.norm(r.x - ro["x"]) / np.linalg.norm(ro["x"]) < 1e-7
     assert abs(S.true_rel_residual(a, b, r.x) - res) <= 1e-3 * res
+
+
+@pytest.mark.parametrize("kind,dims,p0,p1,tol", [
+    ("varcoef3d", (24, 24, 24), 1.5, 0.0, 1e-10),
+    ("aniso_q1", (96, 80, 1), 500.0, 0.6, 1e-8),
+    ("laplace3d", (40, 40, 40), 0.0, 0.0, 1e-10),
+])
+def test_mixed_precision_residual_replacement(S, ctx, kind, dims, p0, p1, tol):
+    ip, ix, v, n, b = _system(S, kind, dims, p0=p0, p1=p1)
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    r = S.cg_mixed(a, b, tol=tol, mode="replace")
+    assert r.converged and r.rel_residual <= tol
+    res = O.true_rel_residual(ip, ix, v, b, r.x)
+    assert res <= 1.5 * tol
+    ro = O.cg_mixed_replace(ip, ix, v, b, tol=tol)
+    assert ro["converged"]
+    # the same algorithm: FP32 rounding of the reductions differs, the
+    # iteration counts stay close
+    assert abs(r.inner_iterations - ro["inner"]) <= 0.15 * ro["inner"] + 5, (r.inner_iterations, ro["inner"])
+    # fewer FP32 iterations than restarted refinement
+    rr = S.cg_mixed(a, b, tol=tol, inner_rtol=1e-4, mode="restart")
+    assert r.inner_iterations <= rr.inner_iterations
+    assert np.linalg.norm(r.x - ro["x"]) / np.linalg.norm(ro["x"]) < 1e-5
 
 
 def test_host_operator_and_rmatvec(S, ctx):

@@ -1,0 +1,141 @@
+"""The windowed SpMV: window, warp and run-over boundaries vs the oracle.
+
+The nonzeros stream through per-warp windows; rows that cross a window or
+a warp's range carry a partial sum.  These matrices put long rows, empty
+rows and one-entry rows across those boundaries.  Bars: exact mode is
+bit-identical to the oracle (and to the other kernels, SX_WIN=0); the FP64
+fused-multiply-add mode stays within a few ulp of sum_k |a_k x_k|.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle_ffi as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def S():
+    import scirs_gb300
+
+    return scirs_gb300
+
+
+def _from_lengths(rng, lengths, ncols):
+    lengths = np.asarray(lengths, dtype=np.int64)
+    ip = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    rows = np.repeat(np.arange(len(lengths)), lengths)
+    ix = rng.integers(0, ncols, ip[-1])
+    ix = ix[np.lexsort((ix, rows))].astype(np.int32)  # sorted within each row
+    v = rng.uniform(-1.0, 1.0, ip[-1])
+    return ip, ix, v
+
+
+def _cases(rng):
+    yield "one_huge_row", [3, 70000, 2, 0, 0, 7]
+    yield "empties_everywhere", [0, 0, 5, 0, 0, 0, 300, 0, 1, 0, 0] * 500
+    yield "empty_tail", [10] * 600 + [0] * 5000
+    yield "leading_empty", [0] * 2000 + [256] * 100 + [0] * 3
+    yield "exact_units", [256] * 400
+    yield "ones", [1] * 300000
+    yield "long_rows_across_warps", list(rng.integers(3000, 4097, 300))
+    yield "powerlaw", list(np.minimum(4096, (rng.pareto(1.2, 20000) + 1).astype(int)))
+    yield "ragged", list(rng.integers(0, 40, 50000))
+    yield "single", [1]
+
+
+def _ctx_with(S, env):
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        return S.Context(0)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+
+
+@pytest.mark.parametrize("shape", ["0", "1", "2"])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_window_boundaries_bit_exact(S, dtype, shape):
+    # SX_WIN=2: the windowed kernel for every matrix, each window shape
+    c = _ctx_with(S, {"SX_WIN": "2", "SX_WIN_SHAPE": shape})
+    rng = np.random.default_rng(17)
+    for name, lengths in _cases(rng):
+        ncols = 8000
+        ip, ix, v = _from_lengths(rng, lengths, ncols)
+        n = len(ip) - 1
+        vals = v.astype(dtype)
+        a = S.csr_from_arrays(c, ip, ix, vals, (n, ncols))
+        x = rng.standard_normal(ncols).astype(dtype)
+        y = a.matvec(x)
+        yr = O.spmv_i32(ip, ix, vals, x)
+        assert np.array_equal(y.view(np.uint8), yr.view(np.uint8)), name
+        a.close()
+    c.close()
+
+
+def test_windowed_kernel_matches_row_kernel(S):
+    # the same products and sums with and without the windowed kernel
+    rng = np.random.default_rng(3)
+    ip, ix, v = S.generate("powerlaw", 200000, 1, 1, seed=4, param0=16.0, param1=4096.0)
+    n = len(ip) - 1
+    x = rng.standard_normal(n)
+    out = {}
+    for mode in ("2", "0"):
+        c = _ctx_with(S, {"SX_WIN": mode})
+        a = S.csr_from_arrays(c, ip, ix, v, (n, n))
+        out[mode] = a.matvec(x)
+        a.close()
+        c.close()
+    assert np.array_equal(out["0"].view(np.uint8), out["2"].view(np.uint8))
+
+
+@pytest.mark.parametrize("win", ["0", "2"])
+@pytest.mark.parametrize("kind,dims", [("laplace3d", (64, 64, 64)), ("powerlaw", (300000, 1, 1))])
+def test_fp64_fma_mode_within_ulps(S, kind, dims, win):
+    ctx = _ctx_with(S, {"SX_WIN": win})
+    import torch
+
+    from scirs_gb300 import _lib as L
+
+    p0, p1 = (16.0, 4096.0) if kind == "powerlaw" else (0.0, 0.0)
+    ip, ix, v = S.generate(kind, *dims, seed=2, param0=p0, param1=p1)
+    n = len(ip) - 1
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    x = np.random.default_rng(8).standard_normal(n)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    S.sparse._check(L.lib.sx_spmv_ex(ctx.handle, a.handle, C.c_void_p(xd.data_ptr()),
+                                     C.c_void_p(yd.data_ptr()), 0))
+    ctx.synchronize()
+    y = yd.cpu().numpy()
+    yr = O.spmv_i32(ip, ix, v, x)
+    rows = np.repeat(np.arange(n), np.diff(ip))
+    mag = np.bincount(rows, weights=np.abs(v * x[ix]), minlength=n)
+    lens = np.diff(ip).astype(np.float64)
+    # sequential summation error bound: (len + 1) * eps * sum |a x|
+    bound = (lens + 1.0) * np.finfo(np.float64).eps * mag
+    assert np.all(np.abs(y - yr) <= bound + 1e-300)
+    # fused multiply-adds: not the exact mode's bits on these values
+    assert not np.array_equal(y, yr)
+    a.close()
+    ctx.close()
+
+
+def test_full_size_laplacian_fp32_bit_exact(S, ctx):
+    ip, ix, v = S.generate("laplace3d", 128, 128, 128)
+    n = len(ip) - 1
+    vals = v.astype(np.float32)
+    a = S.csr_from_arrays(ctx, ip, ix, vals, (n, n))
+    x = S.rhs_normal(5, n).astype(np.float32)
+    y = a.matvec(x)
+    yr = O.spmv_i32(ip, ix, vals, x)
+    assert np.array_equal(y.view(np.uint8), yr.view(np.uint8))
+    a.close()

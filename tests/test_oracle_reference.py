@@ -242,3 +242,4 @@ def test_gmres_solves_small_systems():
     a = op_from_triplets(c["rows"], c["cols"], c["data"], c["shape"])
     r = O.gmres(a, c["b"], restart=4)
     assert r["converged"] and np.linalg.norm(np.asarray(c["b"]) - a.matvec(r["x"])) < 1e-6
+
