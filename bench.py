@@ -1,16 +1,31 @@
 """Benchmark of the scirs2-sparse iterative-solve path on one GB300.
 
-Metric: time to an FP64-verified relative residual of 1e-8 (learned vs
-Jacobi PCG), plus SpMV HBM GB/s.  Workload: 3D 7-point Laplacian on a 128^3
-grid (n = 2,097,152, nnz = 14,581,760), b ~ N(0, 1) from seed 0, x0 = 0.
+Metric: time to an FP64-verified relative residual of 1e-8, learned vs
+Jacobi PCG, plus SpMV HBM GB/s.
 
-A step is one complete solve from b to x.  `value` times the solve with A,
-b and x resident on the device; `e2e` times the same solve through the
-C ABI with b copied from pinned host memory and x copied back inside the
-timed region.  `roofline` times the dominant kernel (the FP32 CSR SpMV of
-the inner solver) alone with CUDA events on the library's stream.
+Headline workload (the learned-SAI evaluation): 2D anisotropic diffusion on
+Q1 elements, 1024 x 1024 grid (n = 1,048,576, nnz = 9,424,900), held-out
+seed 1000001 of the training distribution (eps = 845.08, theta = 0.9632),
+b ~ N(0, 1) from the seed, x0 = 0.  A step is one complete solve from b to
+x including its setup: the FP32 copy of A, the network's forward pass and
+the factor G, and FP32 PCG with FP64 residual replacement until
+||b - A x||_2 <= 1e-8 ||b||_2 in FP64.  `value` times that step with A, b
+and x resident on the device; `e2e` times the same step through the C ABI
+with b copied from pinned host memory and x copied back inside the timed
+region.  `jacobi_pcg_fp64` times plain FP64 Jacobi-PCG (the reference's
+method) on the same problem and device, `speedup_vs_jacobi_fp64` is their
+ratio; IC(0)-PCG (the reference's quirky factorisation and the textbook
+one) is reported beside them.
+
+`roofline` times the dominant kernel of the step, the FP32 CSR SpMV of A,
+alone with CUDA events on the library stream; `spmv_sweep` adds the 3D
+7-point 128^3 Laplacian and the 4M-row power-law matrix in FP32 and FP64.
+`workloads` reports the other configurations once each: 2D Poisson 256^2
+FP64 Jacobi-PCG, the 128^3 Laplacian and the 160^3 variable-coefficient
+problem with mixed precision, and 4096 batched 2D systems.
 `cpu_baseline` times the CPU oracle (a restatement of the reference's cg
-with Jacobi, single-threaded like the reference) on a bounded sample.
+with Jacobi, single-threaded like the reference) on a bounded sample of the
+headline solve.
 
   python bench.py [--steps K] [--warmup W] [--impl reference]
 """
@@ -31,9 +46,14 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 METRIC = "Time to 1e-8 FP64 residual: learned vs Jacobi PCG on GB300; SpMV HBM GB/s"
-GRID = 128
-SEED = 0
 TOL = 1e-8
+SIDE = 1024            # headline grid side
+PROBLEM_SEED = 1000001  # held-out seed of the training distribution
+# FP64 Jacobi-PCG iterations to 1e-8 on the headline problem, counted by a
+# full run of the CPU oracle (the reference arm scales its bounded sample by it)
+JACOBI_ITERS = 5396
+GRID = 128             # 3D Laplacian of the SpMV sweep
+SEED = 0
 
 
 def spmv_bytes(n: int, nnz: int, w: int) -> int:
@@ -41,8 +61,20 @@ def spmv_bytes(n: int, nnz: int, w: int) -> int:
     return nnz * (w + 4) + 4 * (n + 1) + 2 * n * w
 
 
-def workload_desc(n, nnz):
-    return (f"3D 7-point Laplacian {GRID}^3 (n={n:,}, nnz={nnz:,}), b~N(0,1) seed {SEED}, x0=0, "
+def headline_problem():
+    import scirs_gb300 as S
+    from scirs_gb300 import learned as LR
+
+    prob = LR.sample_problem(PROBLEM_SEED)
+    ip, ix, v = S.generate("aniso_q1", SIDE, SIDE, param0=prob.eps, param1=prob.theta)
+    n = len(ip) - 1
+    b = S.rhs_normal(PROBLEM_SEED, n)
+    return prob, ip, ix, v, n, b
+
+
+def workload_desc(prob, n, nnz):
+    return (f"2D anisotropic Q1 diffusion {SIDE}x{SIDE} (n={n:,}, nnz={nnz:,}), eps={prob.eps:.2f}, "
+            f"theta={prob.theta:.4f} (held-out seed {PROBLEM_SEED}), b~N(0,1) from the seed, x0=0, "
             f"stop at FP64 true relative residual {TOL:g}")
 
 
@@ -127,32 +159,31 @@ def cpu_reference_solve(ip, ix, v, n, b, max_iter):
 
 
 def run_reference(args):
+    """The reference's method (cg + Jacobi, FP64, one thread) on the headline
+    problem: each step times a bounded sample of the iterations and scales it
+    to the full count."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    ip, ix, v, n, b = build_problem()
+    prob, ip, ix, v, n, b = headline_problem()
     nnz = len(v)
-    # warm-up: one full solve gives the iteration count at convergence
-    full, t_full = cpu_reference_solve(ip, ix, v, n, b, 100000)
-    iters = full["iterations"]
-    per_iter = t_full / max(iters, 1)
-    sample_iters = iters if t_full <= 20.0 else max(20, int(20.0 / per_iter))
-    for _ in range(max(0, args.warmup - 1)):
-        cpu_reference_solve(ip, ix, v, n, b, sample_iters)
+    sample_iters = min(args.cpu_sample_iters, JACOBI_ITERS)
+    for _ in range(args.warmup):
+        cpu_reference_solve(ip, ix, v, n, b, max(10, sample_iters // 10))
     times = []
     for _ in range(args.steps):
         _, dt = cpu_reference_solve(ip, ix, v, n, b, sample_iters)
-        times.append(dt * iters / sample_iters)
+        times.append(dt * JACOBI_ITERS / sample_iters)
     value = statistics.mean(times)
-    sample = (f"oracle cg+Jacobi FP64 (restatement of iterative.rs:40-162), {sample_iters} of {iters} "
-              f"iterations per step, scaled to {iters}; single thread like the reference")
+    sample = (f"oracle cg+Jacobi FP64 (restatement of iterative.rs:40-162), first {sample_iters} of "
+              f"{JACOBI_ITERS} iterations per step, scaled to {JACOBI_ITERS}; single thread like the reference")
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": workload_desc(n, nnz), "method": "Jacobi-PCG FP64 (reference cg)",
-                   "iterations": iters},
+        "config": {"workload": workload_desc(prob, n, nnz), "method": "Jacobi-PCG FP64 (reference cg)",
+                   "iterations": JACOBI_ITERS},
         "cpu_baseline": {"value": value, "unit": "s", "cores": 1, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -161,10 +192,13 @@ def run_reference(args):
 
 # -------------------------------------------------------------- device arm
 def run_ours(args):
+    import ctypes as C
+
     import torch
 
     import scirs_gb300 as S
     from scirs_gb300 import _lib as L
+    from scirs_gb300 import learned as LR
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -175,21 +209,19 @@ def run_ours(args):
 
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    ip, ix, v, n, b = build_problem()
+    dev = torch.device("cuda", local)
+    prob, ip, ix, v, n, b = headline_problem()
     nnz = len(v)
     ctx = S.Context(local)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
-    a32 = a64.astype(np.float32)
-    m32 = S.jacobi(ctx, a32)
-    m64 = S.jacobi(ctx, a64)
-    dev = torch.device("cuda", local)
+    net = LR.load_weights(ctx, WEIGHTS)
     b_dev = torch.from_numpy(b).to(dev)
     x_dev = torch.empty(n, dtype=torch.float64, device=dev)
     b_pin = torch.from_numpy(b).pin_memory()
     x_pin = torch.empty(n, dtype=torch.float64).pin_memory()
     flush = torch.ones(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    flush_out = torch.empty(1, dtype=torch.float32, device=dev)
+    flush_out = torch.empty((), dtype=torch.float32, device=dev)
 
     def l2_flush():
         # read 512 MB (4x L2): evicts the previous step's lines without
@@ -198,19 +230,36 @@ def run_ours(args):
 
     torch.cuda.synchronize()
 
-    import ctypes as C
-
-    def solve_mixed(b_ptr, x_ptr, mem):
+    def learned_step(b_ptr, x_ptr, mem):
+        """FP32 copy of A, network forward + factor G, FP32 PCG with FP64
+        residual replacement to the FP64 target."""
+        a32 = a64.astype(np.float32)
+        g32 = net.preconditioner(a32)
         o = L.IROptions()
         L.lib.sx_ir_options_default(C.byref(o))
         o.tol = TOL
-        o.inner_rtol = args.inner_rtol
-        o.max_inner = 20000
-        o.preconditioner = m32.handle
+        o.max_inner = 200000
+        o.preconditioner = g32.handle
         o.a32 = a32.handle
+        o.mode = L.SX_IR_REPLACE
         r = L.IRResult()
         rc = L.lib.sx_cg_mixed(ctx.handle, a64.handle, C.c_void_p(b_ptr), n, C.byref(o), C.c_void_p(x_ptr),
                                mem, C.byref(r))
+        g32.close()
+        a32.close()
+        S.sparse._check(rc)
+        return r
+
+    def jacobi_step(b_ptr, x_ptr, mem):
+        """The reference's method on the device: FP64 Jacobi-PCG."""
+        m64 = S.jacobi(ctx, a64)
+        o = L.CGOptions()
+        L.lib.sx_cg_options_default(C.byref(o))
+        o.max_iter, o.rtol, o.atol, o.preconditioner = 200000, TOL, 0.0, m64.handle
+        r = L.IterResult()
+        rc = L.lib.sx_cg(ctx.handle, a64.handle, C.c_void_p(b_ptr), n, C.byref(o), C.c_void_p(x_ptr), mem,
+                         C.byref(r))
+        m64.close()
         S.sparse._check(rc)
         return r
 
@@ -222,6 +271,7 @@ def run_ours(args):
             dist.barrier()
         times = []
         launches0 = ctx.kernel_launches
+        out = None
         for _ in range(steps):
             l2_flush()  # between steps, outside the events
             torch.cuda.synchronize()
@@ -237,142 +287,228 @@ def run_ours(args):
             dist.barrier()
         return times, out, ctx.kernel_launches - launches0
 
-    # device-resident solve (value)
+    dev_b, dev_x = b_dev.data_ptr(), x_dev.data_ptr()
     with ClockSampler(local) as clk:
-        t_dev, res, launches = timed(lambda: solve_mixed(b_dev.data_ptr(), x_dev.data_ptr(), L.SX_MEM_DEVICE),
-                                     args.steps, args.warmup)
-    x = x_dev.cpu().numpy()
-    true_res = S.true_rel_residual(a64, b, x)
-    # end-to-end through the C ABI with host buffers (e2e)
-    t_e2e, res_e2e, _ = timed(lambda: solve_mixed(b_pin.data_ptr(), x_pin.data_ptr(), L.SX_MEM_HOST),
-                              args.steps, max(1, args.warmup // 2))
-    # plain FP64 Jacobi-PCG on the same GPU (the comparison method)
-    def solve_fp64():
-        o = L.CGOptions()
-        L.lib.sx_cg_options_default(C.byref(o))
-        o.max_iter, o.rtol, o.atol, o.preconditioner = 100000, TOL, 0.0, m64.handle
-        r = L.IterResult()
-        S.sparse._check(L.lib.sx_cg(ctx.handle, a64.handle, C.c_void_p(b_dev.data_ptr()), n, C.byref(o),
-                                    C.c_void_p(x_dev.data_ptr()), L.SX_MEM_DEVICE, C.byref(r)))
-        return r
+        t_dev, res, launches = timed(lambda: learned_step(dev_b, dev_x, L.SX_MEM_DEVICE), args.steps,
+                                     args.warmup)
+    x_learned = x_dev.cpu().numpy()
+    true_res = S.true_rel_residual(a64, b, x_learned)
+    # e2e: b from pinned host memory in, x back to pinned host memory, inside the events
+    t_e2e, _, _ = timed(lambda: learned_step(b_pin.data_ptr(), x_pin.data_ptr(), L.SX_MEM_HOST),
+                        max(2, args.steps // 2), 1)
+    # the reference's method on the same device
+    t_jac, r_jac, _ = timed(lambda: jacobi_step(dev_b, dev_x, L.SX_MEM_DEVICE), max(2, args.steps // 2), 1)
+    true_res_jac = S.true_rel_residual(a64, b, x_dev.cpu().numpy())
 
-    t_j64, r_j64, _ = timed(solve_fp64, max(2, args.steps // 2), 1)
-    true_res_j64 = S.true_rel_residual(a64, b, x_dev.cpu().numpy())
+    def once(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return out, e0.elapsed_time(e1) / 1e3
 
-    # roofline: the inner FP32 SpMV alone, CUDA events on the library stream
-    def spmv_time(op, xbuf, ybuf, reps=20):
+    # setup share of the learned step, and the other preconditioners
+    a32 = a64.astype(np.float32)
+    g32, t_setup = once(lambda: net.preconditioner(a32))
+    r_lm, t_lm_solve = once(lambda: S.cg_mixed(a64, b, tol=TOL, max_inner=200000, preconditioner=g32, a32=a32))
+    g32.close()
+    m32 = S.jacobi(ctx, a32)
+    r_jm, t_jm = once(lambda: S.cg_mixed(a64, b, tol=TOL, max_inner=200000, preconditioner=m32, a32=a32))
+    m32.close()
+    ic0 = {}
+    for variant, tb in ((("reference", False), ("textbook", True)) if args.ic0 else ()):
+        try:
+            mi, t_mi = once(lambda: S.ic0(ctx, a64, textbook=tb))
+        except S.SparseError as e:
+            ic0[variant] = {"error": str(e)}
+            continue
+        r_ic, t_ic = once(lambda: S.cg(a64, b, max_iter=args.ic0_max_iter, rtol=TOL, atol=0.0, preconditioner=mi))
+        ic0[variant] = {"s": t_ic + t_mi, "setup_s": t_mi, "iterations": r_ic.iterations,
+                        "converged": r_ic.converged, "fp64_true_rel_residual": S.true_rel_residual(a64, b, r_ic.x)}
+        mi.close()
+
+    # roofline: the dominant kernel of the step, the FP32 SpMV of A, alone
+    peak, peak_kind = load_peaks()
+
+    def spmv_time(op, nn, dt, flags=1, reps=20):
+        tdt = torch.float32 if dt == np.float32 else torch.float64
+        xb = torch.randn(nn, dtype=tdt, device=dev)
+        yb = torch.empty(nn, dtype=tdt, device=dev)
         for _ in range(3):
-            L.lib.sx_spmv_ex(ctx.handle, op.handle, C.c_void_p(xbuf.data_ptr()), C.c_void_p(ybuf.data_ptr()), 1)
-        total = 0.0
+            L.lib.sx_spmv_ex(ctx.handle, op.handle, C.c_void_p(xb.data_ptr()), C.c_void_p(yb.data_ptr()), flags)
+        ts = []
         for _ in range(reps):
             l2_flush()
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            S.sparse._check(L.lib.sx_spmv_ex(ctx.handle, op.handle, C.c_void_p(xbuf.data_ptr()),
-                                             C.c_void_p(ybuf.data_ptr()), 1))
+            S.sparse._check(L.lib.sx_spmv_ex(ctx.handle, op.handle, C.c_void_p(xb.data_ptr()),
+                                             C.c_void_p(yb.data_ptr()), flags))
             e1.record(stream)
             e1.synchronize()
-            total += e0.elapsed_time(e1) / 1e3
-        return total / reps
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return statistics.median(ts)
 
-    peak, peak_kind = load_peaks()
-    # sanity reference for the timing method: a plain device copy of 1 GiB
-    cbuf_a = torch.empty(256 * 1024 * 1024, dtype=torch.float32, device=dev)
-    cbuf_b = torch.empty_like(cbuf_a)
-    for _ in range(3):
-        cbuf_b.copy_(cbuf_a)
-    torch.cuda.synchronize()
-    ce0, ce1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ce0.record()
-    for _ in range(5):
-        cbuf_b.copy_(cbuf_a)
-    ce1.record()
-    ce1.synchronize()
-    copy_gbs = 5 * 2 * cbuf_a.numel() * 4 / (ce0.elapsed_time(ce1) / 1e3) / 1e9
-    del cbuf_a, cbuf_b
-    x32 = torch.randn(n, dtype=torch.float32, device=dev)
-    y32 = torch.empty(n, dtype=torch.float32, device=dev)
-    x64 = torch.randn(n, dtype=torch.float64, device=dev)
-    y64 = torch.empty(n, dtype=torch.float64, device=dev)
-    t32 = spmv_time(a32, x32, y32)
-    t64 = spmv_time(a64, x64, y64)
-    b32 = spmv_bytes(n, nnz, 4)
-    b64 = spmv_bytes(n, nnz, 8)
-    sweep = {
-        "laplace3d_128_fp32": {"GB/s": b32 / t32 / 1e9, "frac": b32 / t32 / 1e9 / peak, "us": t32 * 1e6},
-        "laplace3d_128_fp64": {"GB/s": b64 / t64 / 1e9, "frac": b64 / t64 / 1e9 / peak, "us": t64 * 1e6},
-    }
+    t_a32 = spmv_time(a32, n, np.float32)
+    b_a32 = spmv_bytes(n, nnz, 4)
+    a32.close()
+
+    def sweep_entry(nbytes, t):
+        return {"GB/s": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / peak, "us": t * 1e6}
+
+    sweep = {f"aniso_q1_{SIDE}_fp32": sweep_entry(b_a32, t_a32)}
     if args.sweep:
+        lip, lix, lv = S.generate("laplace3d", GRID, GRID, GRID)
+        ln = len(lip) - 1
+        l64 = S.csr_from_arrays(ctx, lip, lix, lv, (ln, ln))
+        l32 = l64.astype(np.float32)
+        sweep[f"laplace3d_{GRID}_fp32"] = sweep_entry(spmv_bytes(ln, len(lv), 4), spmv_time(l32, ln, np.float32))
+        sweep[f"laplace3d_{GRID}_fp64"] = sweep_entry(spmv_bytes(ln, len(lv), 8), spmv_time(l64, ln, np.float64))
+        sweep[f"laplace3d_{GRID}_fp64_fma"] = sweep_entry(spmv_bytes(ln, len(lv), 8),
+                                                          spmv_time(l64, ln, np.float64, flags=0))
+        l32.close()
+        l64.close()
         pip, pix, pv = S.generate("powerlaw", 4194304, seed=1, param0=16.0, param1=4096.0)
         pn, pnnz = len(pip) - 1, len(pv)
         p64 = S.csr_from_arrays(ctx, pip, pix, pv, (pn, pn))
         p32 = p64.astype(np.float32)
-        px32 = torch.randn(pn, dtype=torch.float32, device=dev)
-        py32 = torch.empty(pn, dtype=torch.float32, device=dev)
-        px64 = torch.randn(pn, dtype=torch.float64, device=dev)
-        py64 = torch.empty(pn, dtype=torch.float64, device=dev)
-        pt32 = spmv_time(p32, px32, py32, 10)
-        pt64 = spmv_time(p64, px64, py64, 10)
-        pb32, pb64 = spmv_bytes(pn, pnnz, 4), spmv_bytes(pn, pnnz, 8)
-        sweep["powerlaw_4M_fp32"] = {"GB/s": pb32 / pt32 / 1e9, "frac": pb32 / pt32 / 1e9 / peak, "us": pt32 * 1e6}
-        sweep["powerlaw_4M_fp64"] = {"GB/s": pb64 / pt64 / 1e9, "frac": pb64 / pt64 / 1e9 / peak, "us": pt64 * 1e6}
+        sweep["powerlaw_4M_fp32"] = sweep_entry(spmv_bytes(pn, pnnz, 4), spmv_time(p32, pn, np.float32, reps=10))
+        sweep["powerlaw_4M_fp64"] = sweep_entry(spmv_bytes(pn, pnnz, 8), spmv_time(p64, pn, np.float64, reps=10))
+        sweep["powerlaw_4M_fp64_fma"] = sweep_entry(spmv_bytes(pn, pnnz, 8),
+                                                    spmv_time(p64, pn, np.float64, flags=0, reps=10))
         p32.close()
         p64.close()
 
+    workloads = run_workloads(ctx, S, once, args) if args.workloads else None
+
     traffic = None
-    prof = os.path.join(REPO, "profiles", "spmv_laplace3d_128_fp32.txt")
+    prof = os.path.join(REPO, "profiles", f"spmv_aniso_q1_{SIDE}_fp32.txt")
     if os.path.exists(prof):
         for line in open(prof):
             if line.startswith("traffic_bytes_per_launch:"):
                 traffic = float(line.split(":")[1])
 
-    # CPU baseline: the oracle on a bounded sample, scaled to the FP64 Jacobi-PCG count
+    # CPU baseline: the oracle on a bounded sample, scaled to the full Jacobi-PCG count
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        iters = int(r_j64.iterations)
-        sample_iters = min(iters, args.cpu_sample_iters)
+        sample_iters = min(JACOBI_ITERS, args.cpu_sample_iters)
         _, dt = cpu_reference_solve(ip, ix, v, n, b, sample_iters)
-        cpu = {"value": dt * iters / sample_iters, "unit": "s", "cores": 1, "kind": "port",
-               "sample": f"oracle cg+Jacobi FP64, first {sample_iters} of {iters} iterations, scaled"}
+        cpu = {"value": dt * JACOBI_ITERS / sample_iters, "unit": "s", "cores": 1, "kind": "port",
+               "sample": f"oracle cg+Jacobi FP64 on the headline problem, first {sample_iters} of "
+                         f"{JACOBI_ITERS} iterations, scaled"}
 
     value = statistics.mean(t_dev)
     if dist:
         tt = torch.tensor([value], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         value = float(tt.item())
-    e2e = statistics.mean(t_e2e)
+    jac = statistics.mean(t_jac)
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
-        "config": {"workload": workload_desc(n, nnz),
-                   "method": "Jacobi-PCG, FP32 inner solve + FP64 iterative refinement",
-                   "inner_rtol": args.inner_rtol, "outer_iterations": int(res.outer_iterations),
-                   "inner_iterations": int(res.inner_iterations), "fp64_true_rel_residual": true_res,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 residual and solution",
+        "data": "synthetic",
+        "config": {"workload": workload_desc(prob, n, nnz),
+                   "method": "learned factorised SAI (GNN weights scirs_gb300/weights/aniso_q1.npz) + FP32 PCG "
+                             "with FP64 residual replacement; step includes the FP32 copy and the network setup",
+                   "outer_iterations": int(res.outer_iterations), "inner_iterations": int(res.inner_iterations),
+                   "fp64_true_rel_residual": true_res,
+                   "setup_s": t_setup, "solve_s": t_lm_solve,
                    "l2": "working set > L2 (129 MB) and a 512 MB L2 flush between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "jacobi_pcg_fp64": {"value": statistics.mean(t_j64), "unit": "s", "iterations": int(r_j64.iterations),
-                            "fp64_true_rel_residual": true_res_j64},
-        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
-        "roofline": {"bound": "hbm", "kernel": "spmv_stream_kernel<float> (laplace3d 128^3)",
-                     "achieved": b32 / t32 / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": b32 / t32 / 1e9 / peak, "peak_source": peak_kind,
-                     "algorithmic_bytes": b32, "traffic": traffic},
+        "jacobi_pcg_fp64": {"value": jac, "unit": "s", "iterations": int(r_jac.iterations),
+                            "fp64_true_rel_residual": true_res_jac},
+        "speedup_vs_jacobi_fp64": jac / value,
+        "jacobi_pcg_mixed": {"value": t_jm, "unit": "s", "outer_iterations": r_jm.outer_iterations,
+                             "inner_iterations": r_jm.inner_iterations, "fp64_true_rel_residual": r_jm.rel_residual},
+        "ic0_pcg_fp64": ic0 if args.ic0 else "not run (--ic0)",
+        "e2e": {"value": statistics.mean(t_e2e), "unit": "s", "h2d_bytes_per_step": n * 8,
+                "d2h_bytes_per_step": n * 8},
+        "roofline": {"bound": "hbm", "kernel": f"FP32 CSR SpMV of A (aniso Q1 {SIDE}^2), spmv_pipe_kernel<float>",
+                     "achieved": b_a32 / t_a32 / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": b_a32 / t_a32 / 1e9 / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes": b_a32, "traffic": traffic},
         "spmv_sweep": sweep,
-        "copy_gbs_same_run": copy_gbs,
+        "workloads": workloads,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    for op in (m64, m32, a32, a64):
-        op.close()
+    net.close()
+    a64.close()
     ctx.close()
     if dist:
         dist.destroy_process_group()
+
+
+def run_workloads(ctx, S, once, args):
+    """The other configurations, one timed run each (FP64 true residuals)."""
+    out = {}
+    # 2D 5-point Poisson 256^2, FP64 Jacobi-PCG (L2-resident, latency-bound)
+    ip, ix, v = S.generate("poisson2d", 256, 256)
+    n = len(ip) - 1
+    b = S.rhs_normal(0, n)
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    m = S.jacobi(ctx, a)
+    S.cg(a, b, max_iter=5000, rtol=TOL, atol=0.0, preconditioner=m)  # graph capture outside the timing
+    r, t = once(lambda: S.cg(a, b, max_iter=5000, rtol=TOL, atol=0.0, preconditioner=m))
+    out["poisson2d_256_jacobi_fp64"] = {"s": t, "iterations": r.iterations, "us_per_iteration": t / max(r.iterations, 1) * 1e6,
+                                        "fp64_true_rel_residual": S.true_rel_residual(a, b, r.x)}
+    m.close()
+    a.close()
+    # 3D 7-point Laplacian 128^3: mixed precision vs FP64 Jacobi-PCG
+    ip, ix, v = S.generate("laplace3d", GRID, GRID, GRID)
+    n = len(ip) - 1
+    b = S.rhs_normal(SEED, n)
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    a32 = a.astype(np.float32)
+    m32, m64 = S.jacobi(ctx, a32), S.jacobi(ctx, a)
+    S.cg_mixed(a, b, tol=TOL, preconditioner=m32, a32=a32)
+    r, t = once(lambda: S.cg_mixed(a, b, tol=TOL, preconditioner=m32, a32=a32))
+    S.cg(a, b, max_iter=20000, rtol=TOL, atol=0.0, preconditioner=m64)
+    r64, t64 = once(lambda: S.cg(a, b, max_iter=20000, rtol=TOL, atol=0.0, preconditioner=m64))
+    out["laplace3d_128_jacobi"] = {"mixed_s": t, "mixed_inner_iterations": r.inner_iterations,
+                                   "mixed_outer_iterations": r.outer_iterations,
+                                   "mixed_fp64_true_rel_residual": r.rel_residual,
+                                   "fp64_s": t64, "fp64_iterations": r64.iterations}
+    for op in (m32, m64, a32, a):
+        op.close()
+    # 3D variable-coefficient 160^3, mixed precision to 1e-10
+    ip, ix, v = S.generate("varcoef3d", 160, 160, 160, seed=SEED, param0=1.5)
+    n = len(ip) - 1
+    b = S.rhs_normal(SEED, n)
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    a32 = a.astype(np.float32)
+    m32 = S.jacobi(ctx, a32)
+    S.cg_mixed(a, b, tol=1e-10, max_inner=100000, preconditioner=m32, a32=a32)
+    r, t = once(lambda: S.cg_mixed(a, b, tol=1e-10, max_inner=100000, preconditioner=m32, a32=a32))
+    out["varcoef3d_160_mixed_1e-10"] = {"s": t, "inner_iterations": r.inner_iterations,
+                                        "outer_iterations": r.outer_iterations, "converged": r.converged,
+                                        "fp64_true_rel_residual": r.rel_residual}
+    m32.close()
+    a32.close()
+    a.close()
+    if args.batched:
+        sys_ptr, ip, ix, v = S.generate_batch(4096, 32, 256, seed=SEED, sigma=1.0)
+        n = len(ip) - 1
+        b = S.rhs_normal(SEED, n)
+        a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+        del ip, ix, v
+        a32 = a.astype(np.float32)
+        r, t = once(lambda: S.batched_pcg(a, sys_ptr, b, rtol=TOL, a32=a32))
+        out["batched_4096_varcoef2d"] = {"s": t, "systems": 4096, "rows": n, "nnz": a.nnz,
+                                         "converged": int(r.converged.sum()),
+                                         "max_rel_residual": float(r.rel_residual.max()),
+                                         "max_inner_iterations": int(r.inner_iterations.max()),
+                                         "outer_iterations": r.outer_iterations}
+        a32.close()
+        a.close()
+    return out
 
 
 def run_profile(args):
@@ -397,8 +533,28 @@ def run_profile(args):
             op.close()
         ctx.close()
         return
+    if args.profile == "learned":
+        from scirs_gb300 import learned as LR
+
+        prob, ip, ix, v, n, b = headline_problem()
+        a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+        net = LR.load_weights(ctx, WEIGHTS)
+        for _ in range(args.steps):
+            a32 = a64.astype(np.float32)
+            g32 = net.preconditioner(a32)
+            r = S.cg_mixed(a64, b, tol=TOL, max_inner=200000, preconditioner=g32, a32=a32)
+            g32.close()
+            a32.close()
+        print(json.dumps({"profile": "learned", "n": n, "outer": r.outer_iterations,
+                          "inner": r.inner_iterations, "rel_residual": r.rel_residual}))
+        net.close()
+        a64.close()
+        ctx.close()
+        return
     if args.profile in ("spmv32", "spmv64"):
         ip, ix, v = S.generate("laplace3d", GRID, GRID, GRID)
+    elif args.profile == "aniso32":
+        _, ip, ix, v, _, _ = headline_problem()
     else:
         ip, ix, v = S.generate("powerlaw", 4194304, seed=1, param0=16.0, param1=4096.0)
     n = len(ip) - 1
@@ -420,7 +576,7 @@ def run_profile(args):
 WEIGHTS = os.path.join(REPO, "scirs_gb300", "weights", "aniso_q1.npz")
 
 
-def eval_learned(ctx, net, side, seeds, max_iter=400000, with_fp64_learned=True, log=None):
+def eval_learned(ctx, net, side, seeds, max_iter=400000, with_fp64_learned=True, log=None, ic0_max_iter=0):
     """Held-out anisotropic Q1 problems: time to FP64 relative residual 1e-8 for
     FP64 Jacobi-PCG, mixed-precision Jacobi-PCG and mixed-precision learned PCG
     (falling back to FP64 learned PCG if refinement stagnates)."""
@@ -452,6 +608,16 @@ def eval_learned(ctx, net, side, seeds, max_iter=400000, with_fp64_learned=True,
         r, t = timed(lambda: S.cg(a64, b, max_iter=max_iter, rtol=TOL, atol=0.0, preconditioner=m64))
         row["jacobi_fp64"] = {"s": t, "iters": r.iterations, "conv": r.converged,
                               "true_res": S.true_rel_residual(a64, b, r.x)}
+        for variant, tb in ((("ic0_reference_fp64", False), ("ic0_textbook_fp64", True)) if ic0_max_iter else ()):
+            try:
+                mi, t_setup = timed(lambda: S.ic0(ctx, a64, textbook=tb))
+            except S.SparseError as e:
+                row[variant] = {"error": str(e)}
+                continue
+            r, t = timed(lambda: S.cg(a64, b, max_iter=ic0_max_iter, rtol=TOL, atol=0.0, preconditioner=mi))
+            row[variant] = {"s": t, "setup_s": t_setup, "iters": r.iterations, "conv": r.converged,
+                            "true_res": S.true_rel_residual(a64, b, r.x)}
+            mi.close()
         m32 = S.jacobi(ctx, a32)
         r, t = timed(lambda: S.cg_mixed(a64, b, tol=TOL, inner_rtol=1e-4, max_inner=max_iter,
                                         preconditioner=m32, a32=a32))
@@ -500,7 +666,8 @@ def run_learned(args):
     else:
         net = None
     seeds = [int(s) for s in args.eval_seeds.split(",")]
-    rows = eval_learned(ctx, net, args.eval_side, seeds, log=log)
+    rows = eval_learned(ctx, net, args.eval_side, seeds, log=log,
+                        ic0_max_iter=args.ic0_max_iter if args.ic0 else 0)
     print(json.dumps({"eval_side": args.eval_side, "rows": rows}), flush=True)
     if net is not None:
         net.close()
@@ -515,10 +682,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--inner-rtol", type=float, default=1e-4)
     ap.add_argument("--no-sweep", dest="sweep", action="store_false")
+    ap.add_argument("--no-workloads", dest="workloads", action="store_false")
+    ap.add_argument("--no-batched", dest="batched", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-iters", type=int, default=60)
+    ap.add_argument("--cpu-sample-iters", type=int, default=300)
+    ap.add_argument("--ic0", action="store_true", help="also time IC(0)-PCG (reference and textbook factors)")
+    ap.add_argument("--ic0-max-iter", type=int, default=3000)
     ap.add_argument("--profile", default=None,
-                    choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "solve"],
+                    choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "aniso32", "solve", "learned"],
                     help="run a few launches of one SpMV for an ncu capture and exit")
     ap.add_argument("--workload", default="laplace3d", choices=["laplace3d", "learned"])
     ap.add_argument("--train-gnn", type=int, default=0, help="train the network for N steps first")

@@ -591,11 +591,87 @@ __global__ void k_tile_rows(const int32_t* __restrict__ ptr, int64_t nrows, int6
   }
 }
 
+// smallest and largest column of every 256-row chunk
+__global__ void k_chunk_span(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t nrows,
+                             int32_t* cmin, int32_t* cmax) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
+    int32_t lo = INT_MAX, hi = -1;
+    for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) {
+      lo = min(lo, idx[k]);
+      hi = max(hi, idx[k]);
+    }
+    if (hi >= 0) {
+      atomicMin(cmin + r / kBlock, lo);
+      atomicMax(cmax + r / kBlock, hi);
+    }
+  }
+}
+// widest chunk span; chunks without entries get base 0
+__global__ void k_chunk_base(int32_t* cmin, const int32_t* __restrict__ cmax, int64_t nchunks, int* wide) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += stride) {
+    if (cmax[c] < 0) { cmin[c] = 0; continue; }
+    if (cmax[c] - cmin[c] > 65535) *wide = 1;
+  }
+}
+__global__ void k_fill_col16(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t nrows,
+                             const int32_t* __restrict__ base, uint16_t* col16) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += stride) {
+    const int32_t b = base[r / kBlock];
+    for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) col16[k] = (uint16_t)(idx[k] - b);
+  }
+}
+
+static int csr_prepare_col16(sx_ctx ctx, DevCsr& c) {
+  const int64_t nchunks = (c.nrows + kBlock - 1) / kBlock;
+  int32_t *cmin = nullptr, *cmax = nullptr;
+  int* wide = nullptr;
+  uint16_t* col16 = nullptr;
+  int rc = SX_OK;
+  do {
+    if ((rc = dev_alloc((void**)&cmin, nchunks * 4))) break;
+    if ((rc = dev_alloc((void**)&cmax, nchunks * 4))) break;
+    if ((rc = dev_alloc((void**)&wide, 4))) break;
+    cudaMemsetAsync(cmin, 0x7f, nchunks * 4, ctx->stream);  // 0x7f7f7f7f > any column
+    cudaMemsetAsync(cmax, 0xff, nchunks * 4, ctx->stream);  // -1
+    cudaMemsetAsync(wide, 0, 4, ctx->stream);
+    k_chunk_span<<<vec_grid(ctx, c.nrows), kBlock, 0, ctx->stream>>>(c.indptr, c.indices, c.nrows, cmin, cmax);
+    k_chunk_base<<<vec_grid(ctx, nchunks), kBlock, 0, ctx->stream>>>(cmin, cmax, nchunks, wide);
+    ctx->launches += 2;
+    int h = 1;
+    cudaMemcpyAsync(&h, wide, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "column spans", __FILE__, __LINE__); break; }
+    if (h) break;  // some chunk spans too many columns: keep the int32 columns only
+    if ((rc = dev_alloc((void**)&col16, c.nnz * 2))) break;
+    k_fill_col16<<<vec_grid(ctx, c.nrows), kBlock, 0, ctx->stream>>>(c.indptr, c.indices, c.nrows, cmin, col16);
+    ctx->launches++;
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "compressed columns", __FILE__, __LINE__); break; }
+    c.col16 = col16;
+    c.chunk_base = cmin;
+    col16 = nullptr;
+    cmin = nullptr;
+  } while (0);
+  dev_free(cmin);
+  dev_free(cmax);
+  dev_free(wide);
+  dev_free(col16);
+  return rc;
+}
+
 int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
   dev_free(c.tile_row);
+  dev_free(c.col16);
+  dev_free(c.chunk_base);
   c.tile_row = nullptr;
+  c.col16 = nullptr;
+  c.chunk_base = nullptr;
   c.units = 0;
   if (!c.monotone || c.nnz <= 0 || c.nrows <= 0) return SX_OK;
+  SX_CHECK(csr_prepare_col16(ctx, c));
   int32_t first = -1;
   SX_CUDA(cudaMemcpyAsync(&first, c.indptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
   SX_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -655,6 +731,10 @@ static void free_csr(DevCsr& c) {
   dev_free(c.indices);
   dev_free(c.vals);
   dev_free(c.tile_row);
+  dev_free(c.col16);
+  dev_free(c.chunk_base);
+  c.col16 = nullptr;
+  c.chunk_base = nullptr;
   c.indptr = nullptr;
   c.indices = nullptr;
   c.vals = nullptr;
@@ -737,6 +817,7 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   c->num_sms = sms;
   c->own_stream = own;
   if (const char* t = std::getenv("SX_WIN")) c->win_mode = std::atoi(t);
+  if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "0") != 0;
   if (const char* t = std::getenv("SX_WIN_SHAPE")) c->win_shape = std::atoi(t);
   if (own) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -1135,6 +1216,7 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
   SX_CUDA(cudaSetDevice(ctx->device));
   DevCsr c = a->csr;
   c.indptr = nullptr; c.indices = nullptr; c.vals = nullptr; c.tile_row = nullptr; c.units = 0;
+  c.col16 = nullptr; c.chunk_base = nullptr;
   const int64_t n = a->csr.nnz;
   int rc = SX_OK;
   do {

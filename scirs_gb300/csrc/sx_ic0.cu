@@ -42,6 +42,8 @@ void ic0_destroy(IC0Dev* p) {
   dev_free(p->L.indices);
   dev_free(p->L.vals);
   dev_free(p->L.tile_row);
+  dev_free(p->L.col16);
+  dev_free(p->L.chunk_base);
   if (p->lt) destroy_op_internal(p->lt);
   dev_free(p->dlast);
   dev_free(p->dfirst);

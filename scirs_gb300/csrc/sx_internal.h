@@ -59,6 +59,10 @@ struct DevCsr {
   // set for monotone matrices with indptr[0] == 0 and nnz > 0
   int32_t* tile_row = nullptr;
   int64_t units = 0;
+  // compressed columns for the register-pipelined SpMV: col = chunk_base[r / 256]
+  // + col16[k]; set when every 256-row chunk spans fewer than 65,536 columns
+  uint16_t* col16 = nullptr;
+  int32_t* chunk_base = nullptr;
 };
 
 struct IC0Dev;   // defined in sx_ic0.cu
@@ -107,6 +111,9 @@ struct sx_ctx_s {
   // the register pipeline, 2 the windowed kernel whenever it applies;
   // SX_WIN_SHAPE=0|1|2 picks its window shape
   int win_mode = 1;
+  // SX_COL16=0: the register-pipelined SpMV reads the int32 columns even
+  // where the 16-bit copy exists
+  bool col16 = true;
   int win_shape = 0;
 };
 
@@ -125,7 +132,9 @@ void dev_free(void* p);
 // compute row statistics.
 int csr_finalize_stats(sx_ctx ctx, DevCsr& c);
 constexpr int kUnit = 256;  // nonzeros per tile_row entry
-// builds c.tile_row for the windowed SpMV (allocates and synchronises)
+// builds c.tile_row for the windowed SpMV and, where the column spans allow,
+// c.col16 / c.chunk_base for the register-pipelined SpMV (allocates and
+// synchronises)
 int csr_prepare_tiles(sx_ctx ctx, DevCsr& c);
 
 

@@ -202,11 +202,14 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
 // of the next chunk are issued while the current chunk gathers x and sums
 // its rows, so two chunks per block are in flight.  Per-row order and
 // rounding are those of spmv_stream_kernel (bit-identical results).
-template <typename T, int ITEMS, class Epi, bool FMA = false>
+// C16: columns come from the compressed copy, col = chunk_base[chunk] +
+// col16[k] (16-bit offsets, 2 bytes per entry instead of 4).
+template <typename T, int ITEMS, class Epi, bool FMA = false, bool C16 = false>
 __global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
     const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
     const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, int64_t nrows,
-    int64_t nchunks, T* partials, unsigned int* counter, Epi epi) {
+    int64_t nchunks, T* partials, unsigned int* counter, Epi epi,
+    const uint16_t* __restrict__ col16 = nullptr, const int32_t* __restrict__ chunk_base = nullptr) {
   if (epi.skip()) return;
   constexpr int CH = ITEMS / 4;
   constexpr int TILE = kBlock * ITEMS;
@@ -217,21 +220,29 @@ __global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
   int32_t cs = 0, ce = 0, ms = 0, me = 0;
   int4 ci[CH];
   Vec4<T> cv[CH];
-  auto load_meta = [&](int64_t ch, int32_t& s0, int32_t& e0, int32_t& m0, int32_t& m1) {
+  // cb: the chunk's column base (C16 only)
+  auto load_meta = [&](int64_t ch, int32_t& s0, int32_t& e0, int32_t& m0, int32_t& m1, int32_t& cb) {
     const int64_t r0 = ch * kBlock;
     const int nr = (int)min((int64_t)kBlock, nrows - r0);
     s0 = __ldg(indptr + r0);
     e0 = __ldg(indptr + r0 + nr);
     if (tid < nr) { m0 = __ldg(indptr + r0 + tid); m1 = __ldg(indptr + r0 + tid + 1); }
     else { m0 = 0; m1 = 0; }
+    if constexpr (C16) cb = __ldg(chunk_base + ch);
   };
-  auto load_data = [&](int32_t s0, int32_t e0, int4* di, Vec4<T>* dv) {
+  auto load_data = [&](int32_t s0, int32_t e0, int32_t cb, int4* di, Vec4<T>* dv) {
     const int32_t base = s0 & ~3;
 #pragma unroll
     for (int c = 0; c < CH; ++c) {
       const int32_t k0 = base + (c * kBlock + tid) * 4;
       if (k0 + 3 < e0) {
-        di[c] = ld4i(indices + k0);
+        if constexpr (C16) {
+          const uint2 o = __ldcs(reinterpret_cast<const uint2*>(col16 + k0));
+          di[c] = make_int4(cb + (int)(o.x & 0xffffu), cb + (int)(o.x >> 16), cb + (int)(o.y & 0xffffu),
+                            cb + (int)(o.y >> 16));
+        } else {
+          di[c] = ld4i(indices + k0);
+        }
         dv[c] = ld4(vals + k0);
       } else {
         int cc[4];
@@ -240,7 +251,8 @@ __global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
         for (int q = 0; q < 4; ++q) {
           const int32_t k = k0 + q;
           const bool in = k < e0;
-          cc[q] = in ? indices[k] : 0;
+          if constexpr (C16) cc[q] = in ? cb + (int)col16[k] : 0;
+          else cc[q] = in ? indices[k] : 0;
           vv[q] = in ? vals[k] : T(0);
         }
         di[c] = make_int4(cc[0], cc[1], cc[2], cc[3]);
@@ -250,9 +262,13 @@ __global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
   };
   Acc3<T> a{T(0), T(0), T(0)};
   int64_t ch = blockIdx.x;
+  // row pointers run two chunks ahead, columns and values one chunk ahead:
+  // the next chunk's loads are in flight while this chunk is summed
+  int32_t ns = 0, ne = 0, nms = 0, nme = 0, cbc = 0, cbn = 0;
   if (ch < nchunks) {
-    load_meta(ch, cs, ce, ms, me);
-    load_data(cs, ce, ci, cv);
+    load_meta(ch, cs, ce, ms, me, cbc);
+    load_data(cs, ce, cbc, ci, cv);
+    if (ch + gridDim.x < nchunks) load_meta(ch + gridDim.x, ns, ne, nms, nme, cbn);
   }
   while (ch < nchunks) {
     const int64_t nxt = ch + gridDim.x;
@@ -272,9 +288,13 @@ __global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
         }
       }
     }
-    // row pointers of the next chunk (independent of the work below)
-    int32_t ns = 0, ne = 0, nms = 0, nme = 0;
-    if (nxt < nchunks) load_meta(nxt, ns, ne, nms, nme);
+    // columns and values of the next chunk, row pointers of the one after
+    // (the registers of this chunk are free once its products are stored)
+    int32_t n2s = 0, n2e = 0, n2ms = 0, n2me = 0, cb2 = 0;
+    if (nxt < nchunks) {
+      load_data(ns, ne, cbn, ci, cv);
+      if (nxt + gridDim.x < nchunks) load_meta(nxt + gridDim.x, n2s, n2e, n2ms, n2me, cb2);
+    }
     __syncthreads();
     const int64_t row = ch * kBlock + tid;
     if (row < nrows) {
@@ -288,10 +308,9 @@ __global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
       y[row] = v;
       epi.acc(row, v, a);
     }
-    // columns and values of the next chunk
-    if (nxt < nchunks) load_data(ns, ne, ci, cv);
     __syncthreads();
     cs = ns; ce = ne; ms = nms; me = nme;
+    ns = n2s; ne = n2e; nms = n2ms; nme = n2me; cbn = cb2;
     ch = nxt;
   }
   if constexpr (Epi::kReduce) {

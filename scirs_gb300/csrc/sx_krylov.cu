@@ -393,14 +393,17 @@ struct CgUpdate {
   }
 };
 
-// r.z and beta for a general preconditioner (iterative.rs:143-144)
+// z = M r with r.z and beta fused into the epilogue of the preconditioner
+// apply (general M: IC(0), FSAI, learned; iterative.rs:143-144); skipped
+// once the solve has ended
 template <typename T>
-struct CgRz {
+struct EpiCgRz {
   CgState<T>* st;
-  const T *r, *z;
+  const T* r;
   static constexpr bool kReduce = true;
   __device__ bool skip() const { return st->c.status != ST_RUNNING; }
-  __device__ void elem(int64_t i, Acc3<T>& a) const { a.a += r[i] * z[i]; }
+  __device__ T out(int64_t, T z) const { return z; }
+  __device__ void acc(int64_t i, T z, Acc3<T>& a) const { a.a += r[i] * z; }
   __device__ void finish(const Acc3<T>& t) const {
     st->beta = t.a / st->rz_old;
     st->rz_old = t.a;
@@ -502,8 +505,7 @@ static int cg_run(sx_ctx ctx, sx_op a, const void* b, const sx_cg_options* opt, 
     SX_CHECK(launch_apply<T>(ctx, a, P, AP, EpiCgPap<T>{st, P}));
     SX_CHECK(launch_vec<T>(ctx, n, CgUpdate<T>{st, X, R, P, AP, pf}));
     if (pk == PK_GENERAL) {
-      SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiSkip<T, CgState<T>>{st}));
-      SX_CHECK(launch_vec<T>(ctx, n, CgRz<T>{st, R, Z}));
+      SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiCgRz<T>{st, R}));
     }
     SX_CHECK(launch_vec<T>(ctx, n, CgP<T>{st, P, R, Z, pf}));
     return SX_OK;
@@ -673,8 +675,7 @@ int cg_mixed_replace(sx_ctx ctx, sx_op a64, sx_op a32, sx_op m, const double* db
     SX_CHECK(launch_apply<T>(ctx, a32, P, AP, EpiCgPap<T>{st, P}));
     SX_CHECK(launch_vec<T>(ctx, n, CgUpdate<T>{st, X, R, P, AP, pf}));
     if (pk == PK_GENERAL) {
-      SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiSkip<T, CgState<T>>{st}));
-      SX_CHECK(launch_vec<T>(ctx, n, CgRz<T>{st, R, Z}));
+      SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiCgRz<T>{st, R}));
     }
     SX_CHECK(launch_vec<T>(ctx, n, CgP<T>{st, P, R, Z, pf}));
     return SX_OK;

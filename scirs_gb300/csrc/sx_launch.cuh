@@ -135,6 +135,14 @@ bool launch_win(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const Re
   return true;
 }
 
+template <typename T, int ITEMS, class Epi, bool FMA, bool C16>
+void launch_pipe(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const ReduceArea& ra, int64_t blocks) {
+  constexpr auto kern = spmv_pipe_kernel<T, ITEMS, Epi, FMA, C16>;
+  const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
+  kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows, blocks,
+                                                    (T*)ra.partials, ra.counter, epi, c.col16, c.chunk_base);
+}
+
 // CSR SpMV with epilogue.  Must not allocate or synchronise: it runs inside
 // stream capture.  The reduction area must already hold gridDim blocks.
 template <typename T, class Epi, bool FMA = false>
@@ -154,16 +162,12 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
     }
   }
   if (done) {
-  } else if (c.monotone && c.max_chunk_nnz + 3 <= kBlock * 8) {
-    constexpr auto kern = spmv_pipe_kernel<T, 8, Epi, FMA>;
-    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
-    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows,
-                                                      blocks, (T*)ra.partials, ra.counter, epi);
-  } else if (c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12) {
-    constexpr auto kern = spmv_pipe_kernel<T, 12, Epi, FMA>;
-    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
-    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows,
-                                                      blocks, (T*)ra.partials, ra.counter, epi);
+  } else if (pipe_fits && c.col16 && ctx->col16) {
+    if (c.max_chunk_nnz + 3 <= kBlock * 8) launch_pipe<T, 8, Epi, FMA, true>(ctx, c, x, y, epi, ra, blocks);
+    else launch_pipe<T, 12, Epi, FMA, true>(ctx, c, x, y, epi, ra, blocks);
+  } else if (pipe_fits) {
+    if (c.max_chunk_nnz + 3 <= kBlock * 8) launch_pipe<T, 8, Epi, FMA, false>(ctx, c, x, y, epi, ra, blocks);
+    else launch_pipe<T, 12, Epi, FMA, false>(ctx, c, x, y, epi, ra, blocks);
   } else if (c.monotone) {
     spmv_stream_kernel<T, kSpmvItems, Epi, FMA><<<(unsigned)blocks, kBlock, 0, ctx->stream>>>(
         c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows, (T*)ra.partials, ra.counter, epi);

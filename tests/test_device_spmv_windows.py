@@ -139,3 +139,42 @@ def test_full_size_laplacian_fp32_bit_exact(S, ctx):
     yr = O.spmv_i32(ip, ix, vals, x)
     assert np.array_equal(y.view(np.uint8), yr.view(np.uint8))
     a.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("kind,dims,p0,p1", [
+    ("laplace3d", (48, 40, 36), 0.0, 0.0),
+    ("aniso_q1", (200, 150, 1), 300.0, 0.5),
+    ("varcoef3d", (30, 30, 30), 1.5, 0.0),
+])
+def test_compressed_columns_bit_exact(S, dtype, kind, dims, p0, p1):
+    # the register-pipelined SpMV with 16-bit column offsets (stencil spans)
+    # and with the int32 columns: both the oracle's bits
+    ip, ix, v = S.generate(kind, *dims, seed=6, param0=p0, param1=p1)
+    n = len(ip) - 1
+    vals = v.astype(dtype)
+    x = np.random.default_rng(2).standard_normal(n).astype(dtype)
+    yr = O.spmv_i32(ip, ix, vals, x)
+    for env in ({}, {"SX_COL16": "0"}):
+        c = _ctx_with(S, env)
+        a = S.csr_from_arrays(c, ip, ix, vals, (n, n))
+        y = a.matvec(x)
+        assert np.array_equal(y.view(np.uint8), yr.view(np.uint8)), env
+        a.close()
+        c.close()
+
+
+def test_compressed_columns_wide_rows_keep_int32(S, ctx):
+    # a chunk spanning more than 65,535 columns: no compressed copy, same bits
+    rng = np.random.default_rng(9)
+    n, ncols = 3000, 200000
+    lengths = rng.integers(1, 9, n)
+    ip = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    rows = np.repeat(np.arange(n), lengths)
+    ix = rng.integers(0, ncols, ip[-1])
+    ix = ix[np.lexsort((ix, rows))].astype(np.int32)
+    v = rng.uniform(-1, 1, ip[-1])
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, ncols))
+    x = rng.standard_normal(ncols)
+    assert np.array_equal(a.matvec(x).view(np.uint8), O.spmv_i32(ip, ix, v, x).view(np.uint8))
+    a.close()
