@@ -138,6 +138,8 @@ int ctx_reduce_area(sx_ctx ctx, int64_t blocks, ReduceArea* out) {
   if (need > ctx->red_bytes) {
     if (ctx->red_partials) {
       SX_CUDA(cudaStreamSynchronize(ctx->stream));
+      // captured solver graphs hold the old address
+      solver_graphs_drop(ctx);
       cudaFree(ctx->red_partials);
       ctx->red_partials = nullptr;
       ctx->red_bytes = 0;
@@ -715,6 +717,11 @@ int csr_finalize_stats(sx_ctx ctx, DevCsr& c) {
 
 static std::atomic<uint64_t> g_op_serial{1};
 
+// Every operator gets a serial never used before in this process: the
+// solvers' graph caches are keyed by serials, and a key that came back after
+// its operator was freed would replay a graph over freed buffers.
+uint64_t next_op_serial() { return g_op_serial.fetch_add(1); }
+
 static sx_op new_op(sx_ctx ctx, int kind, int dtype, int64_t nrows, int64_t ncols) {
   sx_op op = new sx_op_s();
   op->kind = kind;
@@ -722,7 +729,7 @@ static sx_op new_op(sx_ctx ctx, int kind, int dtype, int64_t nrows, int64_t ncol
   op->device = ctx->device;
   op->nrows = nrows;
   op->ncols = ncols;
-  op->serial = g_op_serial.fetch_add(1);
+  op->serial = next_op_serial();
   return op;
 }
 

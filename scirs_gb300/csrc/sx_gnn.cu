@@ -1040,9 +1040,21 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out) {
   *out = nullptr;
   SX_CUDA(cudaSetDevice(ctx->device));
   Graph* g = nullptr;
+  const size_t cached = net->graphs.size();
   SX_CHECK(prep_graph(ctx, net, a, &g));
-  SX_CHECK(acts_ensure(net, g->n, g->ng, kWarpGrid * 8));
-  SX_CHECK(forward(ctx, net, *g));
+  // a matrix seen only here is not kept: its prepared graph is dropped at
+  // the end (training keeps the graphs of its problems)
+  const bool fresh = net->graphs.size() > cached;
+  auto drop_fresh = [&]() {
+    if (fresh && !net->graphs.empty()) {
+      cudaStreamSynchronize(ctx->stream);
+      graph_free(net->graphs.back());
+      net->graphs.pop_back();
+    }
+  };
+  int frc = acts_ensure(net, g->n, g->ng, kWarpGrid * 8);
+  if (frc == SX_OK) frc = forward(ctx, net, *g);
+  if (frc != SX_OK) { drop_fresh(); return frc; }
   const int64_t n = g->n;
   const size_t w = elt_size(a->dtype);
   void* gv = nullptr;
@@ -1065,6 +1077,7 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out) {
   dev_free(gv);
   dev_free(p64);
   if (G) destroy_op_internal(G);
+  drop_fresh();
   return rc == SX_OK ? clear_error() : rc;
 }
 

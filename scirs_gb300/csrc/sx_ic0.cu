@@ -545,7 +545,7 @@ extern "C" int sx_precond_ic0(sx_ctx ctx, sx_op a, int variant, sx_op* out) {
   op->device = ctx->device;
   op->nrows = op->ncols = n;
   op->ic0 = d;
-  op->serial = (uint64_t)(uintptr_t)op ^ 0x1c0;
+  op->serial = next_op_serial();
   *out = op;
   return clear_error();
 }

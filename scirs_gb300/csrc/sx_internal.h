@@ -131,6 +131,11 @@ void dev_free(void* p);
 // Upload host-side CSR arrays (already validated, int32) into a DevCsr and
 // compute row statistics.
 int csr_finalize_stats(sx_ctx ctx, DevCsr& c);
+// a process-unique operator serial (keys of the solvers' graph caches)
+uint64_t next_op_serial();
+// destroys the solvers' cached graphs (sx_krylov.cu); called before a
+// buffer that captured graphs reference is reallocated
+void solver_graphs_drop(sx_ctx ctx);
 constexpr int kUnit = 256;  // nonzeros per tile_row entry
 // builds c.tile_row for the windowed SpMV and, where the column spans allow,
 // c.col16 / c.chunk_base for the register-pipelined SpMV (allocates and

@@ -121,6 +121,10 @@ static void drop_graphs(SolverCache* c) {
   c->graphs.clear();
 }
 
+void solver_graphs_drop(sx_ctx ctx) {
+  if (ctx->solver_cache) drop_graphs((SolverCache*)ctx->solver_cache);
+}
+
 constexpr size_t kStateBytes = 4096;
 
 static int ws_get(sx_ctx ctx, size_t bytes, void** ws, void** state) {

@@ -121,7 +121,7 @@ int sx_precond_jacobi(sx_ctx ctx, sx_op a, sx_op* out) {
   op->dtype = a->dtype;
   op->device = ctx->device;
   op->nrows = op->ncols = n;
-  op->serial = a->serial * 1000003ull + 17;
+  op->serial = next_op_serial();
   int rc = dev_alloc(&op->diag, std::max<int64_t>(n, 1) * elt_size(a->dtype));
   unsigned long long* bad = nullptr;
   if (rc == SX_OK) rc = dev_alloc((void**)&bad, 8);
@@ -154,7 +154,7 @@ int sx_precond_jacobi_from_diagonal(sx_ctx ctx, sx_dtype dtype, const void* diag
   op->dtype = dtype;
   op->device = ctx->device;
   op->nrows = op->ncols = (int64_t)n;
-  op->serial = (uint64_t)(uintptr_t)op;
+  op->serial = next_op_serial();
   void* d = nullptr;
   unsigned long long* bad = nullptr;
   int rc = dev_alloc(&op->diag, std::max<uint64_t>(n, 1) * w);
@@ -194,7 +194,7 @@ int sx_precond_fsai(sx_ctx ctx, sx_op g, sx_op* out) {
   op->dtype = g->dtype;
   op->device = ctx->device;
   op->nrows = op->ncols = g->nrows;
-  op->serial = (uint64_t)(uintptr_t)op ^ 0x5a5a;
+  op->serial = next_op_serial();
   // deep copy of G (the caller keeps its own handle)
   sx_op gt = nullptr;
   int rc = csr_transpose_internal(ctx, g, &gt);

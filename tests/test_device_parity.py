@@ -277,3 +277,33 @@ def test_host_operator_and_rmatvec(S, ctx):
     assert r.converged and np.allclose(r.x, r2.x, rtol=1e-8, atol=1e-10)
     x = np.arange(n, dtype=np.float64)
     assert np.allclose(a.rmatvec(x), dense.T @ x)
+
+
+def test_preconditioners_rebuilt_from_one_matrix(S, ctx):
+    # a fresh Jacobi / IC(0) operator per solve over one matrix: each solve
+    # captures its own graph and gets the same answer
+    ip, ix, v, n, b = _system(S, "poisson2d", (60, 50, 1))
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    out = []
+    for _ in range(3):
+        m = S.jacobi(ctx, a)
+        r = S.cg(a, b, max_iter=2000, rtol=1e-10, atol=0.0, preconditioner=m)
+        m.close()
+        out.append((r.iterations, r.x.copy()))
+    for it, x in out[1:]:
+        assert it == out[0][0] and np.array_equal(x, out[0][1])
+    # a bigger system in between grows the reduction area; the same pair
+    # (a, m) solves before and after it
+    m = S.jacobi(ctx, a)
+    r = S.cg(a, b, max_iter=2000, rtol=1e-10, atol=0.0, preconditioner=m)
+    assert r.iterations == out[0][0]
+    ip2, ix2, v2, n2, b2 = _system(S, "laplace3d", (300, 250, 200))
+    a2 = S.csr_from_arrays(ctx, ip2, ix2, v2, (n2, n2))
+    m2 = S.jacobi(ctx, a2)
+    S.cg(a2, b2, max_iter=3, rtol=1e-10, atol=0.0, preconditioner=m2)
+    m2.close()
+    a2.close()
+    r = S.cg(a, b, max_iter=2000, rtol=1e-10, atol=0.0, preconditioner=m)
+    assert r.iterations == out[0][0] and np.array_equal(r.x, out[0][1])
+    m.close()
+    a.close()
