@@ -21,6 +21,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "sx_internal.h"
 #include "sx_kernels.cuh"
 
@@ -664,6 +666,22 @@ static int csr_prepare_col16(sx_ctx ctx, DevCsr& c) {
   return rc;
 }
 
+__global__ void k_to_half(const float* __restrict__ in, __half* out, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = __float2half_rn(in[i]);
+}
+
+int csr_make_half(sx_ctx ctx, DevCsr& c) {
+  dev_free(c.vals16);
+  c.vals16 = nullptr;
+  if (c.nnz <= 0) return SX_OK;
+  SX_CHECK(dev_alloc(&c.vals16, c.nnz * 2));
+  k_to_half<<<vec_grid(ctx, c.nnz), kBlock, 0, ctx->stream>>>((const float*)c.vals, (__half*)c.vals16, c.nnz);
+  ctx->launches++;
+  SX_CUDA(cudaGetLastError());
+  return SX_OK;
+}
+
 int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
   dev_free(c.tile_row);
   dev_free(c.col16);
@@ -740,8 +758,10 @@ static void free_csr(DevCsr& c) {
   dev_free(c.tile_row);
   dev_free(c.col16);
   dev_free(c.chunk_base);
+  dev_free(c.vals16);
   c.col16 = nullptr;
   c.chunk_base = nullptr;
+  c.vals16 = nullptr;
   c.indptr = nullptr;
   c.indices = nullptr;
   c.vals = nullptr;
@@ -824,7 +844,8 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   c->num_sms = sms;
   c->own_stream = own;
   if (const char* t = std::getenv("SX_WIN")) c->win_mode = std::atoi(t);
-  if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "0") != 0;
+  if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "1") == 0;
+  if (const char* t = std::getenv("SX_MX_FUSED")) c->mx_unfused = std::strcmp(t, "0") == 0;
   if (const char* t = std::getenv("SX_WIN_SHAPE")) c->win_shape = std::atoi(t);
   if (own) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -1223,7 +1244,7 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
   SX_CUDA(cudaSetDevice(ctx->device));
   DevCsr c = a->csr;
   c.indptr = nullptr; c.indices = nullptr; c.vals = nullptr; c.tile_row = nullptr; c.units = 0;
-  c.col16 = nullptr; c.chunk_base = nullptr;
+  c.col16 = nullptr; c.chunk_base = nullptr; c.vals16 = nullptr;
   const int64_t n = a->csr.nnz;
   int rc = SX_OK;
   do {

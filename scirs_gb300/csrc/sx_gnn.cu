@@ -1073,6 +1073,15 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out) {
                                   (uint64_t)g->ng, SX_MEM_DEVICE, &G)))
       break;
     rc = sx_precond_fsai(ctx, G, out);
+    // the factor's values in FP16 for the solvers (the network's output is
+    // already limited by its BF16 weights); FP32 stays for exact applies
+    if (rc == SX_OK && a->dtype == SX_F32) {
+      rc = csr_make_half(ctx, (*out)->csr);
+      if (rc == SX_OK) rc = csr_make_half(ctx, (*out)->transpose->csr);
+      if (rc == SX_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        rc = set_error(SX_ERR_CUDA, "CUDA error in the FP16 factor copy");
+      if (rc != SX_OK) { destroy_op_internal(*out); *out = nullptr; }
+    }
   } while (0);
   dev_free(gv);
   dev_free(p64);

@@ -44,6 +44,7 @@ void ic0_destroy(IC0Dev* p) {
   dev_free(p->L.tile_row);
   dev_free(p->L.col16);
   dev_free(p->L.chunk_base);
+  dev_free(p->L.vals16);
   if (p->lt) destroy_op_internal(p->lt);
   dev_free(p->dlast);
   dev_free(p->dfirst);

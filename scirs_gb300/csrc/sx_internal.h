@@ -63,6 +63,9 @@ struct DevCsr {
   // + col16[k]; set when every 256-row chunk spans fewer than 65,536 columns
   uint16_t* col16 = nullptr;
   int32_t* chunk_base = nullptr;
+  // FP16 copy of FP32 values (__half), read by solver-internal applies of a
+  // learned factor; the exact API path keeps using vals
+  void* vals16 = nullptr;
 };
 
 struct IC0Dev;   // defined in sx_ic0.cu
@@ -111,9 +114,13 @@ struct sx_ctx_s {
   // the register pipeline, 2 the windowed kernel whenever it applies;
   // SX_WIN_SHAPE=0|1|2 picks its window shape
   int win_mode = 1;
-  // SX_COL16=0: the register-pipelined SpMV reads the int32 columns even
-  // where the 16-bit copy exists
-  bool col16 = true;
+  // SX_COL16=1: the register-pipelined SpMV reads the 16-bit column copy
+  // where it exists (fewer bytes, but the decode costs registers and the
+  // kernel is latency bound: slower on GB300, off by default)
+  bool col16 = false;
+  // SX_MX_FUSED=0: the residual-replacement loop runs the plain CG kernels
+  // instead of its fused iteration
+  bool mx_unfused = false;
   int win_shape = 0;
 };
 
@@ -131,6 +138,8 @@ void dev_free(void* p);
 // Upload host-side CSR arrays (already validated, int32) into a DevCsr and
 // compute row statistics.
 int csr_finalize_stats(sx_ctx ctx, DevCsr& c);
+// FP16 copy of an FP32 CSR's values (c.vals16)
+int csr_make_half(sx_ctx ctx, DevCsr& c);
 // a process-unique operator serial (keys of the solvers' graph caches)
 uint64_t next_op_serial();
 // destroys the solvers' cached graphs (sx_krylov.cu); called before a

@@ -8,6 +8,7 @@
 //  - a grid-stride elementwise kernel with the same reduction tail.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -116,6 +117,17 @@ __device__ __forceinline__ Vec4<double> ld4(const double* p) {
   double2 b = __ldcs(reinterpret_cast<const double2*>(p) + 1);
   return Vec4<double>{{a.x, a.y, b.x, b.y}};
 }
+// 4 consecutive FP16 values (one 64-bit load), widened to FP32
+__device__ __forceinline__ Vec4<float> ld4(const __half* p) {
+  const uint2 u = __ldcs(reinterpret_cast<const uint2*>(p));
+  const __half2 a = *reinterpret_cast<const __half2*>(&u.x);
+  const __half2 b = *reinterpret_cast<const __half2*>(&u.y);
+  const float2 fa = __half22float2(a), fb = __half22float2(b);
+  return Vec4<float>{{fa.x, fa.y, fb.x, fb.y}};
+}
+__device__ __forceinline__ float to_val(__half v) { return __half2float(v); }
+__device__ __forceinline__ float to_val(float v) { return v; }
+__device__ __forceinline__ double to_val(double v) { return v; }
 __device__ __forceinline__ int4 ld4i(const int32_t* p) {
   return __ldcs(reinterpret_cast<const int4*>(p));
 }
@@ -203,13 +215,24 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
 // its rows, so two chunks per block are in flight.  Per-row order and
 // rounding are those of spmv_stream_kernel (bit-identical results).
 // C16: columns come from the compressed copy, col = chunk_base[chunk] +
-// col16[k] (16-bit offsets, 2 bytes per entry instead of 4).
-template <typename T, int ITEMS, class Epi, bool FMA = false, bool C16 = false>
-__global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
+// col16[k] (16-bit offsets, 2 bytes per entry instead of 4).  MINB asks the
+// compiler for that many resident blocks per SM (a register budget).  V is
+// the storage type of the values (FP16 for the learned factor, widened to T).
+// Gather supplies the vector entries (x[col], or a vector formed on the fly).
+// x[col]: the plain gather of the SpMV kernels
+template <typename T>
+struct GatherPlain {
+  __device__ __forceinline__ T operator()(const T* __restrict__ x, int col) const { return __ldg(x + col); }
+};
+
+template <typename T, int ITEMS, class Epi, bool FMA = false, bool C16 = false, int MINB = 1, typename V = T,
+          class Gather = GatherPlain<T>>
+__global__ void __launch_bounds__(kBlock, MINB) spmv_pipe_kernel(
     const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-    const T* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, int64_t nrows,
+    const V* __restrict__ vals, const T* __restrict__ x, T* __restrict__ y, int64_t nrows,
     int64_t nchunks, T* partials, unsigned int* counter, Epi epi,
-    const uint16_t* __restrict__ col16 = nullptr, const int32_t* __restrict__ chunk_base = nullptr) {
+    const uint16_t* __restrict__ col16 = nullptr, const int32_t* __restrict__ chunk_base = nullptr,
+    Gather gat = Gather{}) {
   if (epi.skip()) return;
   constexpr int CH = ITEMS / 4;
   constexpr int TILE = kBlock * ITEMS;
@@ -253,7 +276,7 @@ __global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
           const bool in = k < e0;
           if constexpr (C16) cc[q] = in ? cb + (int)col16[k] : 0;
           else cc[q] = in ? indices[k] : 0;
-          vv[q] = in ? vals[k] : T(0);
+          vv[q] = in ? (T)to_val(vals[k]) : T(0);
         }
         di[c] = make_int4(cc[0], cc[1], cc[2], cc[3]);
         dv[c] = Vec4<T>{{vv[0], vv[1], vv[2], vv[3]}};
@@ -282,7 +305,7 @@ __global__ void __launch_bounds__(kBlock) spmv_pipe_kernel(
       for (int q = 0; q < 4; ++q) {
         const int32_t k = k0 + q;
         if (k >= cs && k < ce) {
-          const T xv = __ldg(x + cc[q]);
+          const T xv = gat(x, cc[q]);
           if constexpr (FMA) { s_prod[k - base] = cv[c].v[q]; s_x[k - base] = xv; }
           else s_prod[k - base] = mul_rn(cv[c].v[q], xv);
         }

@@ -627,11 +627,314 @@ struct IrP {
   __device__ void finish(const Acc3<float>&) const {}
 };
 
+// ---- fused FP32 iteration of the residual-replacement loop.  With
+// q = A p kept as its own recurrence (A p_new = A z + beta A p_old), the
+// p update moves into the SpMV epilogue, and for M = G G^T the x/r update
+// moves into the G^T SpMV, whose gathers form r - alpha q on the fly:
+//   K1  w = A z;  p = z + beta p;  q = w + beta q;  p.q -> alpha
+//   K2  (Jacobi) x += alpha p; r -= alpha q; z = D r; ||r||, r.z -> beta
+//   K2  (G G^T) t = G^T (r - alpha q); x += alpha p; r' = r - alpha q; ||r'||
+//   K3  (G G^T) z = G t; r'.z -> beta
+// r ping-pongs between two buffers (G G^T); a captured body runs two
+// iterations so that every buffer keeps its role.
+struct MxState {
+  CgState<float> cg;  // first: the loop control sits at offset 0
+  int rsel, pad;
+};
+
+struct EpiMx1 {
+  CgState<float>* st;
+  const float* z;
+  float *p, *q;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ float out(int64_t i, float w) const {
+    const float b = st->beta;
+    p[i] = add_rn(z[i], mul_rn(b, p[i]));
+    return add_rn(w, mul_rn(b, q[i]));  // stored to q[i]
+  }
+  __device__ void acc(int64_t i, float qi, Acc3<float>& a) const { a.a += p[i] * qi; }
+  __device__ void finish(const Acc3<float>& t) const {
+    st->pap = t.a;
+    if (t.a <= 0.0f) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_NOT_PD;
+      st->result_norm = st->rnorm;
+      return;
+    }
+    st->alpha = st->rz_old / t.a;
+  }
+};
+
+// end of an iteration: count, max_iter, budget, graph condition
+__device__ __forceinline__ void mx_end_iteration(CgState<float>* st) {
+  st->c.iterations += 1;
+  if (st->c.iterations >= st->c.max_iter) {
+    st->c.status = ST_DONE;
+    st->c.message = MSG_MAX_ITER;
+    st->result_norm = st->rnorm;
+  }
+  if (st->c.budget > 0) st->c.budget -= 1;
+  set_cond(st->c.use_cond, st->c.cond, (st->c.status == ST_RUNNING && st->c.budget > 0) ? 1u : 0u);
+}
+__device__ __forceinline__ bool mx_converged(CgState<float>* st, float rnorm) {
+  st->rnorm = rnorm;
+  if (rnorm <= st->tol) {
+    st->c.status = ST_DONE;
+    st->c.converged = 1;
+    st->c.message = MSG_CONVERGED;
+    st->c.iterations += 1;
+    st->result_norm = rnorm;
+    set_cond(st->c.use_cond, st->c.cond, 0u);
+    return true;
+  }
+  return false;
+}
+
+// K2 for Jacobi: x, r, z = D r, ||r||, r.z, beta
+struct MxJacobiUpdate {
+  CgState<float>* st;
+  float *x, *r, *z;
+  const float *p, *q, *d;
+  static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = false;
+  __device__ bool skip() const {
+    if (st->c.status != ST_RUNNING) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(st->c.use_cond, st->c.cond, 0u);
+      return true;
+    }
+    return false;
+  }
+  __device__ void elem(int64_t i, Acc3<float>& a) const {
+    const float al = st->alpha;
+    x[i] = add_rn(x[i], mul_rn(al, p[i]));
+    const float ri = sub_rn(r[i], mul_rn(al, q[i]));
+    r[i] = ri;
+    const float zi = mul_rn(ri, d[i]);
+    z[i] = zi;
+    a.a += ri * ri;
+    a.b += ri * zi;
+  }
+  __device__ void finish(const Acc3<float>& t) const {
+    if (mx_converged(st, sqrtf(t.a))) return;
+    st->beta = t.b / st->rz_old;
+    st->rz_old = t.b;
+    mx_end_iteration(st);
+  }
+};
+
+// K2 for G G^T: gathers r - alpha q, updates x and r' in the epilogue
+struct GatherMxResid {
+  const float *r, *q;
+  const CgState<float>* st;
+  __device__ __forceinline__ float operator()(const float*, int c) const {
+    return sub_rn(__ldg(r + c), mul_rn(st->alpha, __ldg(q + c)));
+  }
+};
+struct EpiMx2 {
+  MxState* ms;
+  float* x;
+  const float *p, *q, *r;
+  float* rn;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return ms->cg.c.status != ST_RUNNING; }
+  __device__ float out(int64_t, float t) const { return t; }
+  __device__ void acc(int64_t i, float, Acc3<float>& a) const {
+    const float al = ms->cg.alpha;
+    x[i] = add_rn(x[i], mul_rn(al, p[i]));
+    const float ri = sub_rn(r[i], mul_rn(al, q[i]));  // the value the gathers formed
+    rn[i] = ri;
+    a.a += ri * ri;
+  }
+  __device__ void finish(const Acc3<float>& t) const {
+    ms->rsel ^= 1;
+    mx_converged(&ms->cg, sqrtf(t.a));
+  }
+};
+// K3 for G G^T: z = G t with r'.z, beta, end of the iteration
+struct EpiMx3 {
+  CgState<float>* st;
+  const float* rn;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const {
+    if (st->c.status != ST_RUNNING) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(st->c.use_cond, st->c.cond, 0u);
+      return true;
+    }
+    return false;
+  }
+  __device__ float out(int64_t, float z) const { return z; }
+  __device__ void acc(int64_t i, float z, Acc3<float>& a) const { a.a += rn[i] * z; }
+  __device__ void finish(const Acc3<float>& t) const {
+    st->beta = t.a / st->rz_old;
+    st->rz_old = t.a;
+    mx_end_iteration(st);
+  }
+};
+
+// a segment start: p = q = 0, beta = 0 (so K1 forms p = z, q = A z), z = D r
+// (Jacobi) or the already applied z, r.z, ||r||, threshold
+struct MxStart {
+  CgState<float>* st;
+  const double* r64;  // non-null: r = (float) r64 first
+  float *r, *z, *p, *q;
+  const float* d;     // Jacobi diagonal, or null (z given)
+  bool restart;       // false: first segment (no beta from a previous r.z)
+  static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = false;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<float>& a) const {
+    float ri = r64 ? (float)r64[i] : r[i];
+    if (r64) r[i] = ri;
+    float zi;
+    if (d) { zi = mul_rn(ri, d[i]); z[i] = zi; }
+    else zi = z[i];
+    if (!restart) { p[i] = 0.0f; q[i] = 0.0f; }
+    a.a += ri * zi;
+    a.b += ri * ri;
+  }
+  __device__ void finish(const Acc3<float>& t) const {
+    if (restart) {
+      ir_restart(st, t.a, t.b);
+    } else {
+      st->beta = 0.0f;
+      st->rz_old = t.a;
+      st->rnorm = sqrtf(t.b);
+      st->result_norm = st->rnorm;
+      st->tol = fmaxf(st->atol, st->rtol * st->rnorm);
+      st->c.status = ST_RUNNING;
+      st->c.converged = 0;
+      st->c.message = MSG_CONVERGED;
+      st->c.iterations = 0;
+    }
+  }
+};
+
+// The fused loop; false (nothing launched) when it does not apply: M must
+// be Jacobi or G G^T with both factors fitting the register pipeline.
+static int cg_mixed_fused(sx_ctx ctx, sx_op a64, sx_op a32, sx_op m, const double* db, double* dx, double* dr,
+                          IrNorms* nrm, const sx_ir_options* opt, uint64_t* outer, uint64_t* inner, double* rel,
+                          int* converged, bool* applied) {
+  *applied = false;
+  const int pk = prec_kind(m);
+  const bool jac = pk == PK_DIAG;
+  const bool gg = m && m->kind == SX_OP_FSAI;
+  if (!jac && !gg) return SX_OK;
+  auto fits = [](const DevCsr& c) { return c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12; };
+  if (!fits(a32->csr) || (gg && !(fits(m->csr) && fits(m->transpose->csr)))) return SX_OK;
+  SX_CHECK(check_prec(a32, m));
+  *applied = true;
+  using T = float;
+  const int64_t n = a64->nrows;
+  const size_t vb = align_up((size_t)std::max<int64_t>(n, 1) * sizeof(T), 256);
+  void *ws = nullptr, *dstate = nullptr;
+  SX_CHECK(ws_get(ctx, vb * 8, &ws, &dstate));
+  auto vec = [&](int k) { return (T*)((char*)ws + k * vb); };
+  T *X = vec(0), *R[2] = {vec(1), vec(2)}, *P = vec(3), *Q = vec(4), *Z = vec(5), *TW = vec(6);
+  MxState* ms = (MxState*)dstate;
+  CgState<T>* st = &ms->cg;
+  ReduceArea ra;
+  SX_CHECK(ctx_reduce_area(ctx, std::max<int64_t>((n + kBlock - 1) / kBlock, vec_grid(ctx, n)) + 8, &ra));
+  const T* dinv = jac ? (const T*)m->diag : nullptr;
+
+  auto true_residual = [&](IrNorms& h) -> int {
+    SX_CHECK(launch_csr<double, EpiIrResid, true>(ctx, a64->csr, dx, dr, EpiIrResid{db, nrm}));
+    SX_CHECK(read_ctl(ctx, nrm, &h, sizeof(h)));
+    return SX_OK;
+  };
+  IrNorms h;
+  SX_CHECK(true_residual(h));
+  const double bnorm = std::sqrt(h.bb);
+  double rnorm = std::sqrt(h.rr);
+  *rel = bnorm > 0 ? rnorm / bnorm : rnorm;
+  if (rnorm <= opt->tol * bnorm) {
+    *converged = 1;
+    return SX_OK;
+  }
+  const double delta = (opt->replace_factor > 0.0 && opt->replace_factor < 1.0) ? opt->replace_factor : 0.1;
+  MxState hs;
+  std::memset(&hs, 0, sizeof(hs));
+  hs.cg.c.max_iter = opt->max_inner;
+  hs.cg.rtol = (T)delta;
+  hs.cg.atol = (T)(0.5 * opt->tol * bnorm);
+  SX_CHECK(write_bytes(ctx, ms, &hs, sizeof(hs)));
+  if (n > 0) SX_CUDA(cudaMemsetAsync(X, 0, n * sizeof(T), ctx->stream));
+  // first segment
+  if (jac) {
+    SX_CHECK(launch_vec<T>(ctx, n, MxStart{st, dr, R[0], Z, P, Q, dinv, false}));
+  } else {
+    SX_CHECK(launch_vec<double>(ctx, n, IrNarrow{dr, R[0], nullptr}));
+    SX_CHECK(launch_apply<T>(ctx, m, R[0], Z, EpiPlain<T>{}));
+    SX_CHECK(launch_vec<T>(ctx, n, MxStart{st, nullptr, R[0], Z, P, Q, nullptr, false}));
+  }
+  auto k1 = [&]() { return launch_apply<T>(ctx, a32, Z, Q, EpiMx1{st, Z, P, Q}); };
+  auto body = [&]() -> int {
+    if (jac) {
+      SX_CHECK(k1());
+      SX_CHECK(launch_vec<T>(ctx, n, MxJacobiUpdate{st, X, R[0], Z, P, Q, dinv}));
+      return SX_OK;
+    }
+    for (int h2 = 0; h2 < 2; ++h2) {  // two iterations: r goes R0 -> R1 -> R0
+      T* rin = R[h2];
+      T* rout = R[h2 ^ 1];
+      SX_CHECK(k1());
+      if (!launch_pipe_gather<T, EpiMx2, GatherMxResid, true>(ctx, m->transpose->csr, nullptr, TW,
+                                                               EpiMx2{ms, X, P, Q, rin, rout},
+                                                               GatherMxResid{rin, Q, st}))
+        return set_error(SX_ERR_CUDA, "CUDA error in the fused G^T step");
+      if (!launch_pipe_gather<T, EpiMx3, GatherPlain<T>, true>(ctx, m->csr, TW, Z, EpiMx3{st, rout},
+                                                                GatherPlain<T>{}))
+        return set_error(SX_ERR_CUDA, "CUDA error in the fused G step");
+    }
+    return SX_OK;
+  };
+  const uint64_t key[8] = {4, (uint64_t)jac, a32->serial, m->serial, (uint64_t)n, (uint64_t)(uintptr_t)ws, 0, 0};
+  double prev = rnorm;
+  int stalls = 0;
+  for (;;) {
+    SX_CHECK(run_loop(ctx, ms, key, true, body));
+    SX_CHECK(read_ctl(ctx, ms, &hs, sizeof(hs)));
+    *inner += hs.cg.c.iterations;
+    SX_CHECK(launch_vec<double>(ctx, n, IrFold{dx, X}));
+    SX_CHECK(true_residual(h));
+    rnorm = std::sqrt(h.rr);
+    *rel = bnorm > 0 ? rnorm / bnorm : rnorm;
+    *outer += 1;
+    if (rnorm <= opt->tol * bnorm) { *converged = 1; break; }
+    if (hs.cg.c.message == MSG_NOT_PD) break;
+    if (*outer >= opt->max_outer) break;
+    if (!(rnorm < 0.5 * prev)) {
+      if (++stalls >= 2) break;
+    } else {
+      stalls = 0;
+    }
+    prev = rnorm;
+    // replace the FP32 residual; p and q carry over (beta from the new r.z)
+    T* rcur = R[jac ? 0 : hs.rsel];
+    if (jac) {
+      SX_CHECK(launch_vec<T>(ctx, n, MxStart{st, dr, rcur, Z, P, Q, dinv, true}));
+    } else {
+      SX_CHECK(launch_vec<double>(ctx, n, IrNarrow{dr, rcur, nullptr}));
+      SX_CHECK(launch_apply<T>(ctx, m, rcur, Z, EpiPlain<T>{}));
+      SX_CHECK(launch_vec<T>(ctx, n, MxStart{st, nullptr, rcur, Z, P, Q, nullptr, true}));
+    }
+  }
+  return SX_OK;
+}
+
 int cg_mixed_replace(sx_ctx ctx, sx_op a64, sx_op a32, sx_op m, const double* db, double* dx, double* dr,
                      IrNorms* nrm, const sx_ir_options* opt, uint64_t* outer, uint64_t* inner,
                      double* rel, int* converged) {
   using T = float;
   const int64_t n = a64->nrows;
+  if (!ctx->mx_unfused) {
+    bool applied = false;
+    SX_CHECK(cg_mixed_fused(ctx, a64, a32, m, db, dx, dr, nrm, opt, outer, inner, rel, converged, &applied));
+    if (applied) {
+      SX_CHECK(ic0_health(ctx, m));
+      return SX_OK;
+    }
+  }
   SX_CHECK(check_prec(a32, m));
   const int pk = prec_kind(m);
   const size_t vb = align_up((size_t)std::max<int64_t>(n, 1) * sizeof(T), 256);

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "sx_internal.h"
 #include "sx_kernels.cuh"
@@ -135,17 +136,67 @@ bool launch_win(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const Re
   return true;
 }
 
+template <typename T, int ITEMS, class Epi, bool FMA, bool C16, int MINB, typename V = T>
+void launch_pipe_minb(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const ReduceArea& ra,
+                      int64_t blocks) {
+  constexpr auto kern = spmv_pipe_kernel<T, ITEMS, Epi, FMA, C16, MINB, V>;
+  const V* vals = std::is_same<V, T>::value ? (const V*)c.vals : (const V*)c.vals16;
+  const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
+  kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, vals, x, y, c.nrows, blocks,
+                                                    (T*)ra.partials, ra.counter, epi, c.col16, c.chunk_base,
+                                                    GatherPlain<T>{});
+}
+
+// The register pipeline with a custom gather (fused solver steps); false
+// when the matrix's chunks do not fit it.  HALF as in launch_csr.
+template <typename T, int ITEMS, class Epi, class Gather, typename V>
+void launch_pipe_gather_v(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, Gather gat,
+                          const ReduceArea& ra, int64_t blocks) {
+  constexpr auto kern = spmv_pipe_kernel<T, ITEMS, Epi, false, false, 1, V, Gather>;
+  const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
+  kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, vals, x, y, c.nrows, blocks,
+                                                    (T*)ra.partials, ra.counter, epi, nullptr, nullptr, gat);
+}
+
+// The register pipeline with a custom gather (fused solver steps); false
+// when the matrix's chunks do not fit it.  HALF as in launch_csr.
+template <typename T, class Epi, class Gather, bool HALF>
+bool launch_pipe_gather(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, Gather gat) {
+  if (c.nrows <= 0) return true;
+  if (!(c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12)) return false;
+  ReduceArea ra;
+  const int64_t blocks = (c.nrows + kBlock - 1) / kBlock;
+  if (ctx_reduce_area(ctx, blocks, &ra) != SX_OK) return false;
+  const bool small = c.max_chunk_nnz + 3 <= kBlock * 8;
+  bool done = false;
+  if constexpr (HALF && sizeof(T) == 4) {
+    if (c.vals16) {
+      if (small) launch_pipe_gather_v<T, 8>(ctx, c, (const __half*)c.vals16, x, y, epi, gat, ra, blocks);
+      else launch_pipe_gather_v<T, 12>(ctx, c, (const __half*)c.vals16, x, y, epi, gat, ra, blocks);
+      done = true;
+    }
+  }
+  if (!done) {
+    if (small) launch_pipe_gather_v<T, 8>(ctx, c, (const T*)c.vals, x, y, epi, gat, ra, blocks);
+    else launch_pipe_gather_v<T, 12>(ctx, c, (const T*)c.vals, x, y, epi, gat, ra, blocks);
+  }
+  ctx->launches++;
+  return cudaGetLastError() == cudaSuccess;
+}
+
+// register budget: 8 resident blocks per SM for FP32 with 8 items per thread
+// (no spills; measured fastest on the 128^3 Laplacian), the compiler's
+// choice otherwise (FP64 spills under a tighter budget)
 template <typename T, int ITEMS, class Epi, bool FMA, bool C16>
 void launch_pipe(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const ReduceArea& ra, int64_t blocks) {
-  constexpr auto kern = spmv_pipe_kernel<T, ITEMS, Epi, FMA, C16>;
-  const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
-  kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, x, y, c.nrows, blocks,
-                                                    (T*)ra.partials, ra.counter, epi, c.col16, c.chunk_base);
+  constexpr int kMinBlocks = (sizeof(T) == 4 && ITEMS == 8) ? 8 : 1;
+  launch_pipe_minb<T, ITEMS, Epi, FMA, C16, kMinBlocks>(ctx, c, x, y, epi, ra, blocks);
 }
 
 // CSR SpMV with epilogue.  Must not allocate or synchronise: it runs inside
 // stream capture.  The reduction area must already hold gridDim blocks.
-template <typename T, class Epi, bool FMA = false>
+// HALF: FP32 values may be read from the FP16 copy where one exists.
+template <typename T, class Epi, bool FMA = false, bool HALF = false>
 int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
   if (c.nrows <= 0) return SX_OK;
   ReduceArea ra;
@@ -159,6 +210,13 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
       case 1: done = launch_win<T, 1, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
       case 2: done = launch_win<T, 2, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
       default: done = launch_win<T, 0, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
+    }
+  }
+  if constexpr (HALF && sizeof(T) == 4) {
+    if (!done && pipe_fits && c.vals16) {
+      if (c.max_chunk_nnz + 3 <= kBlock * 8) launch_pipe_minb<T, 8, Epi, FMA, false, 1, __half>(ctx, c, x, y, epi, ra, blocks);
+      else launch_pipe_minb<T, 12, Epi, FMA, false, 1, __half>(ctx, c, x, y, epi, ra, blocks);
+      done = true;
     }
   }
   if (done) {
@@ -215,9 +273,10 @@ int launch_apply(sx_ctx ctx, sx_op op, const T* x, T* y, Epi epi) {
       return SX_OK;
     }
     case SX_OP_FSAI: {
-      // y = G (G^T x): the second SpMV carries the epilogue
-      SX_CHECK(launch_csr<T, EpiPlain<T>, kFma>(ctx, op->transpose->csr, x, (T*)op->work, EpiPlain<T>{}));
-      return launch_csr<T, Epi, kFma>(ctx, op->csr, (const T*)op->work, y, epi);
+      // y = G (G^T x): the second SpMV carries the epilogue; solver-internal
+      // applies read a learned factor's FP16 values
+      SX_CHECK(launch_csr<T, EpiPlain<T>, kFma, !EXACT>(ctx, op->transpose->csr, x, (T*)op->work, EpiPlain<T>{}));
+      return launch_csr<T, Epi, kFma, !EXACT>(ctx, op->csr, (const T*)op->work, y, epi);
     }
     default: {
       // IC0 and host operators: apply, then run the epilogue over y

@@ -304,3 +304,4 @@ __global__ void __launch_bounds__(kBlock) spmv_win_kernel(
 }
 
 }  // namespace sx
+

@@ -103,3 +103,38 @@ def test_learned_preconditioner_is_spd_apply(S, ctx):
         mx, my = m.matvec(x), m.matvec(y)
         assert abs(x @ my - y @ mx) <= 1e-10 * np.linalg.norm(x) * np.linalg.norm(my)
         assert x @ mx > 0
+
+
+def test_fp16_factor_matches_fp32_factor_iterations(S, ctx):
+    # the learned preconditioner's solver applies read G in FP16; the same G
+    # in FP32 (a user FSAI operator) needs about as many PCG iterations
+    ip, ix, v, a64 = _aniso(S, ctx, 96, 80, 200.0, 0.8)
+    a32 = a64.astype(np.float32)
+    n = a64.shape[0]
+    net = S.LearnedSAI(ctx, seed=4)
+    rng = np.random.default_rng(3)
+    net.params = (net.params + 0.05 * rng.standard_normal(net.num_params)).astype(np.float32)
+    g = net.edge_values(a32)
+    # G pattern: each row's strict-lower columns, then the diagonal
+    lens, cols = [], []
+    for i in range(n):
+        row = ix[ip[i]:ip[i + 1]]
+        low = row[row < i]
+        cols.append(np.concatenate([low, [i]]))
+        lens.append(len(low) + 1)
+    gp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    gi = np.concatenate(cols).astype(np.int32)
+    diag = np.array([v[ip[i]:ip[i + 1]][ix[ip[i]:ip[i + 1]] == i][0] for i in range(n)])
+    dis = 1.0 / np.sqrt(diag.astype(np.float32).astype(np.float64))
+    gv = (g.astype(np.float64) * np.repeat(dis, lens)).astype(np.float32)
+    G = S.csr_from_arrays(ctx, gp, gi, gv, (n, n))
+    m32 = S.fsai(ctx, G)
+    m16 = net.preconditioner(a32)
+    b = S.rhs_normal(2, n).astype(np.float32)
+    r32 = S.cg(a32, b, max_iter=20000, rtol=1e-5, atol=0.0, preconditioner=m32)
+    r16 = S.cg(a32, b, max_iter=20000, rtol=1e-5, atol=0.0, preconditioner=m16)
+    assert r32.converged and r16.converged
+    assert abs(r16.iterations - r32.iterations) <= 0.05 * r32.iterations + 3, (r16.iterations, r32.iterations)
+    for op in (m16, m32, G, a32, a64):
+        op.close()
+    net.close()

@@ -307,3 +307,69 @@ def test_preconditioners_rebuilt_from_one_matrix(S, ctx):
     assert r.iterations == out[0][0] and np.array_equal(r.x, out[0][1])
     m.close()
     a.close()
+
+
+def _ctx_env(S, env):
+    import os
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        return S.Context(0)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+
+
+@pytest.mark.parametrize("kind,dims,p0,p1", [
+    ("aniso_q1", (128, 96, 1), 300.0, 0.6),
+    ("laplace3d", (40, 36, 32), 0.0, 0.0),
+])
+def test_fused_replacement_loop_matches_plain_kernels(S, kind, dims, p0, p1):
+    # the fused FP32 iteration (q = A z + beta q, x/r updates in the SpMV
+    # epilogues) against the plain CG kernels: same algorithm, FP32 rounding
+    # apart; both reach the FP64 target
+    ip, ix, v, n, b = _system(S, kind, dims, p0=p0, p1=p1)
+    res = {}
+    for mode in ("1", "0"):
+        c = _ctx_env(S, {"SX_MX_FUSED": mode})
+        a = S.csr_from_arrays(c, ip, ix, v, (n, n))
+        r = S.cg_mixed(a, b, tol=1e-9)
+        assert r.converged and O.true_rel_residual(ip, ix, v, b, r.x) <= 1.5e-9
+        res[mode] = r.inner_iterations
+        a.close()
+        c.close()
+    assert abs(res["1"] - res["0"]) <= 0.1 * res["0"] + 3, res
+
+
+def test_fused_replacement_loop_with_factored_preconditioner(S):
+    # M = G G^T (FSAI operator): the fused G^T / G steps against the plain ones
+    ip, ix, v, n, b = _system(S, "aniso_q1", (100, 90, 1), p0=50.0, p1=1.2)
+    # G = D^-1/2 on the lower pattern (a Jacobi-like factor with the full pattern)
+    lens, cols, vals = [], [], []
+    for i in range(n):
+        row = ix[ip[i]:ip[i + 1]]
+        low = row[row < i]
+        d = v[ip[i]:ip[i + 1]][row == i][0]
+        cols.append(np.concatenate([low, [i]]))
+        vals.append(np.concatenate([np.full(len(low), -0.05 / np.sqrt(d)), [1.0 / np.sqrt(d)]]))
+        lens.append(len(low) + 1)
+    gp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    gi = np.concatenate(cols).astype(np.int32)
+    gv = np.concatenate(vals).astype(np.float32)
+    res = {}
+    for mode in ("1", "0"):
+        c = _ctx_env(S, {"SX_MX_FUSED": mode})
+        a = S.csr_from_arrays(c, ip, ix, v, (n, n))
+        a32 = a.astype(np.float32)
+        G = S.csr_from_arrays(c, gp, gi, gv, (n, n))
+        m = S.fsai(c, G)
+        r = S.cg_mixed(a, b, tol=1e-9, preconditioner=m, a32=a32)
+        assert r.converged and O.true_rel_residual(ip, ix, v, b, r.x) <= 1.5e-9
+        res[mode] = r.inner_iterations
+        for op in (m, G, a32, a):
+            op.close()
+        c.close()
+    assert abs(res["1"] - res["0"]) <= 0.1 * res["0"] + 3, res

@@ -148,14 +148,14 @@ def test_full_size_laplacian_fp32_bit_exact(S, ctx):
     ("varcoef3d", (30, 30, 30), 1.5, 0.0),
 ])
 def test_compressed_columns_bit_exact(S, dtype, kind, dims, p0, p1):
-    # the register-pipelined SpMV with 16-bit column offsets (stencil spans)
-    # and with the int32 columns: both the oracle's bits
+    # the register-pipelined SpMV with the int32 columns and with the 16-bit
+    # column offsets (stencil spans): both the oracle's bits
     ip, ix, v = S.generate(kind, *dims, seed=6, param0=p0, param1=p1)
     n = len(ip) - 1
     vals = v.astype(dtype)
     x = np.random.default_rng(2).standard_normal(n).astype(dtype)
     yr = O.spmv_i32(ip, ix, vals, x)
-    for env in ({}, {"SX_COL16": "0"}):
+    for env in ({}, {"SX_COL16": "1"}):
         c = _ctx_with(S, env)
         a = S.csr_from_arrays(c, ip, ix, vals, (n, n))
         y = a.matvec(x)
@@ -178,3 +178,4 @@ def test_compressed_columns_wide_rows_keep_int32(S, ctx):
     x = rng.standard_normal(ncols)
     assert np.array_equal(a.matvec(x).view(np.uint8), O.spmv_i32(ip, ix, v, x).view(np.uint8))
     a.close()
+
