@@ -636,7 +636,7 @@ struct IrP {
 //   K2  (G G^T) t = G^T (r - alpha q); x += alpha p; r' = r - alpha q; ||r'||
 //   K3  (G G^T) z = G t; r'.z -> beta
 // r ping-pongs between two buffers (G G^T); a captured body runs two
-// iterations so that every buffer keeps its role.
+// iterations, R[0] -> R[1] -> R[0], so every segment starts from R[0].
 struct MxState {
   CgState<float> cg;  // first: the loop control sits at offset 0
   int rsel, pad;
@@ -909,8 +909,14 @@ static int cg_mixed_fused(sx_ctx ctx, sx_op a64, sx_op a32, sx_op m, const doubl
       stalls = 0;
     }
     prev = rnorm;
-    // replace the FP32 residual; p and q carry over (beta from the new r.z)
-    T* rcur = R[jac ? 0 : hs.rsel];
+    // replace the FP32 residual; p and q carry over (beta from the new r.z).
+    // The captured body starts every pair of iterations from R[0], so the
+    // replaced residual goes there whichever buffer the segment ended in.
+    T* rcur = R[0];
+    if (!jac && hs.rsel != 0) {
+      hs.rsel = 0;
+      SX_CHECK(write_bytes(ctx, &ms->rsel, &hs.rsel, sizeof(int)));
+    }
     if (jac) {
       SX_CHECK(launch_vec<T>(ctx, n, MxStart{st, dr, rcur, Z, P, Q, dinv, true}));
     } else {
