@@ -419,3 +419,60 @@ __global__ void __launch_bounds__(kBlock) vec_kernel(int64_t n, T* partials,
 }
 
 }  // namespace sx
+
+namespace sx {
+
+// Short-row SpMV: one thread per row, the row's K-entry window entirely in
+// registers (no shared memory, no block barrier).  Every column/value load
+// and then every gather of a row is issued before the first is used; the
+// products and the sum then follow storage order (csr.rs:479-497), so the
+// results are those of the other kernels.  Rows longer than K take a
+// sequential tail loop.  Consecutive threads own consecutive rows, so a
+// warp's k-th loads fall in a few consecutive lines that L1 serves to the
+// following loads.
+template <typename T, int K, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>>
+__global__ void __launch_bounds__(kBlock) spmv_short_kernel(
+    const int32_t* __restrict__ indptr, const int32_t* __restrict__ indices, const V* __restrict__ vals,
+    const T* __restrict__ x, T* __restrict__ y, int64_t nrows, T* partials, unsigned int* counter, Epi epi,
+    Gather gat = Gather{}) {
+  if (epi.skip()) return;
+  Acc3<T> a{T(0), T(0), T(0)};
+  const int64_t stride = (int64_t)gridDim.x * kBlock;
+  for (int64_t row = (int64_t)blockIdx.x * kBlock + threadIdx.x; row < nrows; row += stride) {
+    const int32_t s = __ldg(indptr + row), e = __ldg(indptr + row + 1);
+    const int len = e - s;
+    int col[K];
+    T val[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const bool in = j < len;
+      col[j] = in ? __ldg(indices + s + j) : 0;
+      val[j] = in ? (T)to_val(vals[s + j]) : T(0);
+    }
+    T xv[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) xv[j] = j < len ? gat(x, col[j]) : T(0);
+    T acc = T(0);
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (j < len) {
+        if constexpr (FMA) acc = fma(val[j], xv[j], acc);
+        else acc = add_rn(acc, mul_rn(val[j], xv[j]));
+      }
+    }
+    for (int32_t k = s + K; k < e; ++k) {  // rows longer than K
+      const T vk = (T)to_val(vals[k]), xk = gat(x, __ldg(indices + k));
+      if constexpr (FMA) acc = fma(vk, xk, acc);
+      else acc = add_rn(acc, mul_rn(vk, xk));
+    }
+    const T v = epi.out(row, acc);
+    y[row] = v;
+    epi.acc(row, v, a);
+  }
+  if constexpr (Epi::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) epi.finish(tot);
+  }
+}
+
+}  // namespace sx

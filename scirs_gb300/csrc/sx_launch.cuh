@@ -149,6 +149,23 @@ void launch_pipe_minb(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, co
 
 // The register pipeline with a custom gather (fused solver steps); false
 // when the matrix's chunks do not fit it.  HALF as in launch_csr.
+// Short-row SpMV launch: K = 8, 12 or 16 by the longest row (monotone
+// matrices only); false when rows are longer than 16.
+template <typename T, class Epi, bool FMA, typename V = T, class Gather = GatherPlain<T>>
+bool launch_short(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
+                  int64_t blocks, Gather gat = Gather{}) {
+  if (!c.monotone || c.max_row_len > 16) return false;
+  auto go = [&](auto kern) {
+    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 8);
+    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, vals, x, y, c.nrows, (T*)ra.partials,
+                                                      ra.counter, epi, gat);
+  };
+  if (c.max_row_len <= 8) go(spmv_short_kernel<T, 8, Epi, FMA, V, Gather>);
+  else if (c.max_row_len <= 12) go(spmv_short_kernel<T, 12, Epi, FMA, V, Gather>);
+  else go(spmv_short_kernel<T, 16, Epi, FMA, V, Gather>);
+  return true;
+}
+
 template <typename T, int ITEMS, class Epi, class Gather, typename V>
 void launch_pipe_gather_v(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, Gather gat,
                           const ReduceArea& ra, int64_t blocks) {
@@ -169,8 +186,14 @@ bool launch_pipe_gather(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, 
   if (ctx_reduce_area(ctx, blocks, &ra) != SX_OK) return false;
   const bool small = c.max_chunk_nnz + 3 <= kBlock * 8;
   bool done = false;
+  if (ctx->short_rows) {
+    if constexpr (HALF && sizeof(T) == 4) {
+      if (c.vals16) done = launch_short<T, Epi, false, __half, Gather>(ctx, c, (const __half*)c.vals16, x, y, epi, ra, blocks, gat);
+    }
+    if (!done) done = launch_short<T, Epi, false, T, Gather>(ctx, c, (const T*)c.vals, x, y, epi, ra, blocks, gat);
+  }
   if constexpr (HALF && sizeof(T) == 4) {
-    if (c.vals16) {
+    if (!done && c.vals16) {
       if (small) launch_pipe_gather_v<T, 8>(ctx, c, (const __half*)c.vals16, x, y, epi, gat, ra, blocks);
       else launch_pipe_gather_v<T, 12>(ctx, c, (const __half*)c.vals16, x, y, epi, gat, ra, blocks);
       done = true;
@@ -211,6 +234,14 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
       case 2: done = launch_win<T, 2, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
       default: done = launch_win<T, 0, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
     }
+  }
+  if (!done && ctx->short_rows) {
+    bool half = false;
+    if constexpr (HALF && sizeof(T) == 4) half = c.vals16 != nullptr;
+    if constexpr (HALF && sizeof(T) == 4) {
+      if (half) done = launch_short<T, Epi, FMA, __half>(ctx, c, (const __half*)c.vals16, x, y, epi, ra, blocks);
+    }
+    if (!done && !half) done = launch_short<T, Epi, FMA>(ctx, c, (const T*)c.vals, x, y, epi, ra, blocks);
   }
   if constexpr (HALF && sizeof(T) == 4) {
     if (!done && pipe_fits && c.vals16) {

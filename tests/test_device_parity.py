@@ -327,14 +327,15 @@ def _ctx_env(S, env):
     ("aniso_q1", (128, 96, 1), 300.0, 0.6),
     ("laplace3d", (40, 36, 32), 0.0, 0.0),
 ])
-def test_fused_replacement_loop_matches_plain_kernels(S, kind, dims, p0, p1):
+@pytest.mark.parametrize("short", ["0", "1"])
+def test_fused_replacement_loop_matches_plain_kernels(S, kind, dims, p0, p1, short):
     # the fused FP32 iteration (q = A z + beta q, x/r updates in the SpMV
     # epilogues) against the plain CG kernels: same algorithm, FP32 rounding
     # apart; both reach the FP64 target
     ip, ix, v, n, b = _system(S, kind, dims, p0=p0, p1=p1)
     res = {}
     for mode in ("1", "0"):
-        c = _ctx_env(S, {"SX_MX_FUSED": mode})
+        c = _ctx_env(S, {"SX_MX_FUSED": mode, "SX_SHORT": short})
         a = S.csr_from_arrays(c, ip, ix, v, (n, n))
         r = S.cg_mixed(a, b, tol=1e-9)
         assert r.converged and O.true_rel_residual(ip, ix, v, b, r.x) <= 1.5e-9
@@ -344,7 +345,8 @@ def test_fused_replacement_loop_matches_plain_kernels(S, kind, dims, p0, p1):
     assert abs(res["1"] - res["0"]) <= 0.1 * res["0"] + 3, res
 
 
-def test_fused_replacement_loop_with_factored_preconditioner(S):
+@pytest.mark.parametrize("short", ["0", "1"])
+def test_fused_replacement_loop_with_factored_preconditioner(S, short):
     # M = G G^T (FSAI operator): the fused G^T / G steps against the plain ones
     ip, ix, v, n, b = _system(S, "aniso_q1", (100, 90, 1), p0=50.0, p1=1.2)
     # G = D^-1/2 on the lower pattern (a Jacobi-like factor with the full pattern)
@@ -361,7 +363,7 @@ def test_fused_replacement_loop_with_factored_preconditioner(S):
     gv = np.concatenate(vals).astype(np.float32)
     res = {}
     for mode in ("1", "0"):
-        c = _ctx_env(S, {"SX_MX_FUSED": mode})
+        c = _ctx_env(S, {"SX_MX_FUSED": mode, "SX_SHORT": short})
         a = S.csr_from_arrays(c, ip, ix, v, (n, n))
         a32 = a.astype(np.float32)
         G = S.csr_from_arrays(c, gp, gi, gv, (n, n))

@@ -148,14 +148,15 @@ def test_full_size_laplacian_fp32_bit_exact(S, ctx):
     ("varcoef3d", (30, 30, 30), 1.5, 0.0),
 ])
 def test_compressed_columns_bit_exact(S, dtype, kind, dims, p0, p1):
-    # the register-pipelined SpMV with the int32 columns and with the 16-bit
-    # column offsets (stencil spans): both the oracle's bits
+    # the register-pipelined SpMV with the int32 columns, with the 16-bit
+    # column offsets (stencil spans), and the register-only short-row
+    # kernel: all the oracle's bits
     ip, ix, v = S.generate(kind, *dims, seed=6, param0=p0, param1=p1)
     n = len(ip) - 1
     vals = v.astype(dtype)
     x = np.random.default_rng(2).standard_normal(n).astype(dtype)
     yr = O.spmv_i32(ip, ix, vals, x)
-    for env in ({}, {"SX_COL16": "1"}):
+    for env in ({}, {"SX_COL16": "1"}, {"SX_SHORT": "1"}):
         c = _ctx_with(S, env)
         a = S.csr_from_arrays(c, ip, ix, vals, (n, n))
         y = a.matvec(x)
