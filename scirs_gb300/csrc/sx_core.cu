@@ -846,7 +846,7 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   if (const char* t = std::getenv("SX_WIN")) c->win_mode = std::atoi(t);
   if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "1") == 0;
   if (const char* t = std::getenv("SX_MX_FUSED")) c->mx_unfused = std::strcmp(t, "0") == 0;
-  if (const char* t = std::getenv("SX_SHORT")) c->short_rows = std::strcmp(t, "1") == 0;
+  if (const char* t = std::getenv("SX_SHORT")) c->short_rows = std::strcmp(t, "0") != 0;
   if (const char* t = std::getenv("SX_WIN_SHAPE")) c->win_shape = std::atoi(t);
   if (own) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);

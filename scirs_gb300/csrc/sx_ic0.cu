@@ -33,6 +33,10 @@ struct IC0Dev {
   void* z = nullptr;     // forward-solve result
   int* ready = nullptr;  // 2 * n flags (forward, backward)
   int* ctl = nullptr;    // [0] row counter fwd, [1] row counter bwd, [2] abort, [3] spare
+  // rows in dependency-level order (forward: levels of L; backward: of L^T);
+  // the counters hand rows out in this order
+  int32_t* fwd_order = nullptr;
+  int32_t* bwd_order = nullptr;
   int variant = 0;
 };
 
@@ -51,6 +55,8 @@ void ic0_destroy(IC0Dev* p) {
   dev_free(p->z);
   dev_free(p->ready);
   dev_free(p->ctl);
+  dev_free(p->fwd_order);
+  dev_free(p->bwd_order);
   delete p;
 }
 
@@ -120,13 +126,14 @@ enum : int { E_NONE = 0, E_MISSING_DIAG = 1, E_NOT_PD = 2 };
 template <typename T>
 __global__ void k_ic0_factor_ref(const int32_t* __restrict__ lp, const int32_t* __restrict__ li,
                                  T* ld, int64_t n, int* ready, int* ctl, int* err_row,
-                                 int* err_code) {
+                                 int* err_code, const int32_t* __restrict__ order) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t i = 0;
     if (lane == 0) i = atomicAdd(ctl + 0, 1);
     i = __shfl_sync(0xffffffffu, i, 0);
     if (i >= n) return;
+    i = order[i];
     if (lane == 0) {
       const int32_t rs = lp[i], re = lp[i + 1];
       int32_t di = -1;
@@ -177,13 +184,14 @@ __global__ void k_ic0_factor_ref(const int32_t* __restrict__ lp, const int32_t* 
 template <typename T>
 __global__ void k_ic0_factor_textbook(const int32_t* __restrict__ lp, const int32_t* __restrict__ li,
                                       T* ld, int64_t n, int* ready, int* ctl, int* err_row,
-                                      int* err_code) {
+                                      int* err_code, const int32_t* __restrict__ order) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t i = 0;
     if (lane == 0) i = atomicAdd(ctl + 0, 1);
     i = __shfl_sync(0xffffffffu, i, 0);
     if (i >= n) return;
+    i = order[i];
     if (lane == 0) {
       const int32_t rs = lp[i], re = lp[i + 1];
       const int32_t di = re - 1;
@@ -276,13 +284,15 @@ __global__ void k_first_strict_copy(const int32_t* __restrict__ lp, const int32_
 template <typename T>
 __global__ void k_ic0_forward(const int32_t* __restrict__ lp, const int32_t* __restrict__ li,
                               const T* __restrict__ ld, const T* __restrict__ dlast, int64_t n,
-                              const T* __restrict__ x, T* z, int* ready, int* ctl) {
+                              const T* __restrict__ x, T* z, int* ready, int* ctl,
+                              const int32_t* __restrict__ order) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t i = 0;
     if (lane == 0) i = atomicAdd(ctl + 0, 1);
     i = __shfl_sync(0xffffffffu, i, 0);
     if (i >= n) return;
+    i = order[i];
     const int32_t rs = lp[i], re = lp[i + 1];
     T sum = x[i];
     for (int32_t base = rs; base < re; base += 32) {
@@ -317,14 +327,15 @@ __global__ void k_ic0_forward(const int32_t* __restrict__ lp, const int32_t* __r
 template <typename T>
 __global__ void k_ic0_backward(const int32_t* __restrict__ tp, const int32_t* __restrict__ ti,
                                const T* __restrict__ tv, const T* __restrict__ dfirst, int64_t n,
-                               const T* __restrict__ z, T* y, int* ready, int* ctl) {
+                               const T* __restrict__ z, T* y, int* ready, int* ctl,
+                               const int32_t* __restrict__ order) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t q = 0;
     if (lane == 0) q = atomicAdd(ctl + 1, 1);
     q = __shfl_sync(0xffffffffu, q, 0);
     if (q >= n) return;
-    const int64_t i = n - 1 - q;
+    const int64_t i = order[q];
     const int32_t rs = tp[i], re = tp[i + 1];
     T sum = ldv(z + i);
     for (int32_t base = rs; base < re; base += 32) {
@@ -366,19 +377,19 @@ int ic0_apply(sx_ctx ctx, sx_op op, const void* x, void* y) {
   if (op->dtype == SX_F64) {
     k_ic0_forward<double><<<g, kBlock, 0, ctx->stream>>>(L.indptr, L.indices, (const double*)L.vals,
                                                          (const double*)d->dlast, n, (const double*)x,
-                                                         (double*)d->z, d->ready, d->ctl);
+                                                         (double*)d->z, d->ready, d->ctl, d->fwd_order);
     k_ic0_backward<double><<<g, kBlock, 0, ctx->stream>>>(T.indptr, T.indices, (const double*)T.vals,
                                                           (const double*)d->dfirst, n,
                                                           (const double*)d->z, (double*)y,
-                                                          d->ready + n, d->ctl);
+                                                          d->ready + n, d->ctl, d->bwd_order);
   } else {
     k_ic0_forward<float><<<g, kBlock, 0, ctx->stream>>>(L.indptr, L.indices, (const float*)L.vals,
                                                         (const float*)d->dlast, n, (const float*)x,
-                                                        (float*)d->z, d->ready, d->ctl);
+                                                        (float*)d->z, d->ready, d->ctl, d->fwd_order);
     k_ic0_backward<float><<<g, kBlock, 0, ctx->stream>>>(T.indptr, T.indices, (const float*)T.vals,
                                                          (const float*)d->dfirst, n,
                                                          (const float*)d->z, (float*)y,
-                                                         d->ready + n, d->ctl);
+                                                         d->ready + n, d->ctl, d->bwd_order);
   }
   ctx->launches += 2;
   SX_CUDA(cudaGetLastError());
@@ -397,6 +408,39 @@ int ic0_health(sx_ctx ctx, sx_op op) {
   return SX_OK;
 }
 
+
+// Rows sorted by dependency level (a stable counting sort): forward, a row
+// depends on the rows j < i of its pattern; backward, on the rows j > i.  A
+// row's dependencies sit on lower levels, so they are handed out before it.
+static int level_order(sx_ctx ctx, const DevCsr& c, bool forward, int32_t** out) {
+  const int64_t n = c.nrows;
+  std::vector<int32_t> ptr(n + 1), idx(std::max<int64_t>(c.nnz, 1));
+  SX_CUDA(cudaMemcpyAsync(ptr.data(), c.indptr, (n + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (c.nnz > 0)
+    SX_CUDA(cudaMemcpyAsync(idx.data(), c.indices, c.nnz * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<int32_t> lev(n, 0);
+  int32_t maxl = 0;
+  for (int64_t t = 0; t < n; ++t) {
+    const int64_t i = forward ? t : n - 1 - t;
+    int32_t l = 0;
+    for (int32_t k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int32_t j = idx[k];
+      if (forward ? (j < i) : (j > i)) l = std::max(l, lev[j] + 1);
+    }
+    lev[i] = l;
+    maxl = std::max(maxl, l);
+  }
+  std::vector<int64_t> start(maxl + 2, 0);
+  for (int64_t i = 0; i < n; ++i) start[lev[i] + 1]++;
+  for (int32_t l = 0; l <= maxl; ++l) start[l + 1] += start[l];
+  std::vector<int32_t> order(std::max<int64_t>(n, 1));
+  for (int64_t i = 0; i < n; ++i) order[start[lev[i]]++] = (int32_t)i;
+  SX_CHECK(dev_alloc((void**)out, std::max<int64_t>(n, 1) * 4));
+  SX_CUDA(cudaMemcpyAsync(*out, order.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  return SX_OK;
+}
 
 }  // namespace sx
 
@@ -454,6 +498,7 @@ extern "C" int sx_precond_ic0(sx_ctx ctx, sx_op a, int variant, sx_op* out) {
                                                            d->L.indptr, d->L.indices, (float*)d->L.vals);
       ctx->launches++;
     }
+    if ((rc = level_order(ctx, d->L, true, &d->fwd_order))) break;
     if ((rc = dev_alloc((void**)&d->ready, 2 * nb * sizeof(int)))) break;
     if ((rc = dev_alloc((void**)&d->ctl, 4 * sizeof(int)))) break;
     if ((rc = dev_alloc((void**)&err, sizeof(int)))) break;
@@ -467,14 +512,14 @@ extern "C" int sx_precond_ic0(sx_ctx ctx, sx_op a, int variant, sx_op* out) {
       const int sg = solve_grid(ctx);
       if (a->dtype == SX_F64) {
         if (variant == SX_IC0_REFERENCE)
-          k_ic0_factor_ref<double><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (double*)d->L.vals, n, d->ready, d->ctl, err, codes);
+          k_ic0_factor_ref<double><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (double*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order);
         else
-          k_ic0_factor_textbook<double><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (double*)d->L.vals, n, d->ready, d->ctl, err, codes);
+          k_ic0_factor_textbook<double><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (double*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order);
       } else {
         if (variant == SX_IC0_REFERENCE)
-          k_ic0_factor_ref<float><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (float*)d->L.vals, n, d->ready, d->ctl, err, codes);
+          k_ic0_factor_ref<float><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (float*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order);
         else
-          k_ic0_factor_textbook<float><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (float*)d->L.vals, n, d->ready, d->ctl, err, codes);
+          k_ic0_factor_textbook<float><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (float*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order);
       }
       ctx->launches++;
     }
@@ -532,6 +577,7 @@ extern "C" int sx_precond_ic0(sx_ctx ctx, sx_op a, int variant, sx_op* out) {
     rc = csr_transpose_internal(ctx, s, &d->lt);
     destroy_op_internal(s);
     if (rc) break;
+    if ((rc = level_order(ctx, d->lt->csr, false, &d->bwd_order))) break;
     rc = csr_finalize_stats(ctx, d->L);
   } while (0);
   dev_free(cnt); dev_free(scnt); dev_free(sp); dev_free(si); dev_free(sv);

@@ -121,9 +121,9 @@ struct sx_ctx_s {
   // SX_MX_FUSED=0: the residual-replacement loop runs the plain CG kernels
   // instead of its fused iteration
   bool mx_unfused = false;
-  // SX_SHORT=1: matrices whose rows all hold at most 16 entries use the
-  // register-only short-row SpMV
-  bool short_rows = false;
+  // matrices whose rows all hold at most 16 entries use the register-only
+  // short-row SpMV for FP32 and FP64-FMA (SX_SHORT=0: never)
+  bool short_rows = true;
   int win_shape = 0;
 };
 

@@ -235,7 +235,9 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
       default: done = launch_win<T, 0, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
     }
   }
-  if (!done && ctx->short_rows) {
+  // short rows: the register-only kernel for FP32 and for FP64 with fused
+  // multiply-adds (measured faster or equal); exact FP64 keeps the pipeline
+  if (!done && ctx->short_rows && (FMA || sizeof(T) == 4)) {
     bool half = false;
     if constexpr (HALF && sizeof(T) == 4) half = c.vals16 != nullptr;
     if constexpr (HALF && sizeof(T) == 4) {
