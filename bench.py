@@ -352,6 +352,7 @@ def run_ours(args):
             ts.append(e0.elapsed_time(e1) / 1e3)
         return statistics.median(ts)
 
+    kname = S.spmv_kernel(a32)
     t_a32 = spmv_time(a32, n, np.float32)
     b_a32 = spmv_bytes(n, nnz, 4)
     a32.close()
@@ -427,7 +428,7 @@ def run_ours(args):
         "ic0_pcg_fp64": ic0 if args.ic0 else "not run (--ic0)",
         "e2e": {"value": statistics.mean(t_e2e), "unit": "s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8},
-        "roofline": {"bound": "hbm", "kernel": f"FP32 CSR SpMV of A (aniso Q1 {SIDE}^2), spmv_pipe_kernel<float>",
+        "roofline": {"bound": "hbm", "kernel": f"FP32 CSR SpMV of A (aniso Q1 {SIDE}^2), {kname}",
                      "achieved": b_a32 / t_a32 / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": b_a32 / t_a32 / 1e9 / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": b_a32, "traffic": traffic},
@@ -549,6 +550,23 @@ def run_profile(args):
                           "inner": r.inner_iterations, "rel_residual": r.rel_residual}))
         net.close()
         a64.close()
+        ctx.close()
+        return
+    if args.profile in ("jacobi64", "jacobi32mixed"):
+        prob, ip, ix, v, n, b = headline_problem()
+        a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+        a32 = a64.astype(np.float32)
+        m = S.jacobi(ctx, a64 if args.profile == "jacobi64" else a32)
+        for _ in range(args.steps):
+            if args.profile == "jacobi64":
+                r = S.cg(a64, b, max_iter=200000, rtol=TOL, atol=0.0, preconditioner=m)
+                its = r.iterations
+            else:
+                r = S.cg_mixed(a64, b, tol=TOL, max_inner=200000, preconditioner=m, a32=a32)
+                its = r.inner_iterations
+        print(json.dumps({"profile": args.profile, "n": n, "iterations": its}))
+        for op in (m, a32, a64):
+            op.close()
         ctx.close()
         return
     if args.profile in ("spmv32", "spmv64"):
@@ -689,7 +707,8 @@ def main():
     ap.add_argument("--ic0", action="store_true", help="also time IC(0)-PCG (reference and textbook factors)")
     ap.add_argument("--ic0-max-iter", type=int, default=3000)
     ap.add_argument("--profile", default=None,
-                    choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "aniso32", "solve", "learned"],
+                    choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "aniso32", "solve", "learned",
+                             "jacobi64", "jacobi32mixed"],
                     help="run a few launches of one SpMV for an ncu capture and exit")
     ap.add_argument("--workload", default="laplace3d", choices=["laplace3d", "learned"])
     ap.add_argument("--train-gnn", type=int, default=0, help="train the network for N steps first")

@@ -185,6 +185,9 @@ int sx_op_rmatvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, 
  * multiply-adds in storage order (a few ulp per row, half the FP64 pipe
  * work); FP32 is always exact. */
 int sx_spmv_ex(sx_ctx ctx, sx_op a, const void* x_dev, void* y_dev, unsigned flags);
+/* Name of the kernel sx_spmv_ex(flags) launches for `a` (diagnostics; no
+ * reference counterpart), NUL-terminated into buf[len]. */
+int sx_spmv_kernel(sx_ctx ctx, sx_op a, unsigned flags, char* buf, uint64_t len);
 
 /* --------------------------------------------------------- preconditioners */
 /* JacobiPreconditioner::new (preconditioners.rs:21-44): 1/get(i,i) with the

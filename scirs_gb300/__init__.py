@@ -18,6 +18,7 @@ from .sparse import (  # noqa: F401
     bicgstab,
     cg,
     cg_mixed,
+    spmv_kernel,
     csr_array,
     csr_array_from_triplets,
     csr_from_arrays,

@@ -219,6 +219,25 @@ void launch_pipe(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const R
 // CSR SpMV with epilogue.  Must not allocate or synchronise: it runs inside
 // stream capture.  The reduction area must already hold gridDim blocks.
 // HALF: FP32 values may be read from the FP16 copy where one exists.
+// The kernel launch_csr picks for a matrix (its decision order, as a name):
+// keep in step with launch_csr below.
+inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma, bool half_ok) {
+  const bool pipe_fits = c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12;
+  const bool items8 = c.max_chunk_nnz + 3 <= kBlock * 8;
+  if (c.nrows <= 0) return "none";
+  if (c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) return "spmv_win_kernel";
+  if (ctx->short_rows && (fma || w == 4) && c.monotone && c.max_row_len <= 16)
+    return c.max_row_len <= 8 ? "spmv_short_kernel<K=8>"
+                              : (c.max_row_len <= 12 ? "spmv_short_kernel<K=12>" : "spmv_short_kernel<K=16>");
+  if (pipe_fits && half_ok && w == 4 && c.vals16)
+    return items8 ? "spmv_pipe_kernel<ITEMS=8, FP16 values>" : "spmv_pipe_kernel<ITEMS=12, FP16 values>";
+  if (pipe_fits && c.col16 && ctx->col16)
+    return items8 ? "spmv_pipe_kernel<ITEMS=8, 16-bit columns>" : "spmv_pipe_kernel<ITEMS=12, 16-bit columns>";
+  if (pipe_fits) return items8 ? "spmv_pipe_kernel<ITEMS=8>" : "spmv_pipe_kernel<ITEMS=12>";
+  if (c.monotone) return "spmv_stream_kernel";
+  return "spmv_rowseq_kernel";
+}
+
 template <typename T, class Epi, bool FMA = false, bool HALF = false>
 int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
   if (c.nrows <= 0) return SX_OK;

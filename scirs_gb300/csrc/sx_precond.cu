@@ -10,6 +10,9 @@
 #include <string>
 #include <vector>
 
+#include <cstdio>
+#include <string>
+
 #include "sx_launch.cuh"
 
 namespace sx {
@@ -28,6 +31,26 @@ int spmv_device(sx_ctx ctx, sx_op a, const void* x, void* y, unsigned flags) {
   }
   return launch_apply<float, EpiPlain<float>, true>(ctx, a, (const float*)x, (float*)y,
                                                     EpiPlain<float>{});
+}
+
+extern "C" int sx_spmv_kernel(sx_ctx ctx, sx_op a, unsigned flags, char* buf, uint64_t len) {
+  if (!ctx || !a || !buf || len == 0) return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: null");
+  std::string name;
+  const bool exact = (flags & SX_SPMV_EXACT) != 0;
+  const int w = (int)elt_size(a->dtype);
+  const bool fma = !exact && w == 8;
+  switch (a->kind) {
+    case SX_OP_CSR: name = spmv_kernel_name(ctx, a->csr, w, fma, false); break;
+    case SX_OP_FSAI:
+      name = std::string("G^T: ") + spmv_kernel_name(ctx, a->transpose->csr, w, fma, !exact) +
+             "; G: " + spmv_kernel_name(ctx, a->csr, w, fma, !exact);
+      break;
+    case SX_OP_IC0: name = "k_ic0_forward + k_ic0_backward"; break;
+    case SX_OP_HOST: name = "host callback"; break;
+    default: name = "k_diag_apply"; break;
+  }
+  std::snprintf(buf, (size_t)len, "%s", name.c_str());
+  return clear_error();
 }
 
 int apply_general(sx_ctx ctx, sx_op op, const void* x, void* y) {

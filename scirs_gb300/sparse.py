@@ -264,6 +264,13 @@ def _from_raw(ctx, data, indptr, indices, shape, dtype, api):
     return Operator(ctx, h)
 
 
+def spmv_kernel(op: Operator, exact: bool = True) -> str:
+    """Name of the SpMV kernel the library launches for `op` (diagnostics)."""
+    buf = C.create_string_buffer(256)
+    _check(L.lib.sx_spmv_kernel(op.ctx.handle, op.handle, L.SX_SPMV_EXACT if exact else 0, buf, 256))
+    return buf.value.decode()
+
+
 def csr_from_arrays(ctx: Context, indptr, indices, data, shape, dtype=None) -> Operator:
     """Device-native upload of int64 row pointers / int32 columns (host numpy)."""
     dtype = dtype or np.asarray(data).dtype

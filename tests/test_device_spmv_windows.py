@@ -180,3 +180,21 @@ def test_compressed_columns_wide_rows_keep_int32(S, ctx):
     assert np.array_equal(a.matvec(x).view(np.uint8), O.spmv_i32(ip, ix, v, x).view(np.uint8))
     a.close()
 
+
+
+def test_kernel_choice_names(S, ctx):
+    # the dispatch: short rows in registers (FP32, FP64 with FMA), the
+    # register pipeline for exact FP64 stencils, windows for long rows
+    ip, ix, v = S.generate("laplace3d", 20, 20, 20)
+    n = len(ip) - 1
+    a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    a32 = a64.astype(np.float32)
+    assert S.spmv_kernel(a32) == "spmv_short_kernel<K=8>"
+    assert S.spmv_kernel(a64, exact=False) == "spmv_short_kernel<K=8>"
+    assert S.spmv_kernel(a64, exact=True) == "spmv_pipe_kernel<ITEMS=8>"
+    ip, ix, v = S.generate("powerlaw", 50000, 1, 1, seed=2, param0=16.0, param1=4096.0)
+    n = len(ip) - 1
+    p = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    assert S.spmv_kernel(p) == "spmv_win_kernel"
+    for op in (a32, a64, p):
+        op.close()
