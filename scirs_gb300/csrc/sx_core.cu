@@ -691,7 +691,11 @@ int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
   c.chunk_base = nullptr;
   c.units = 0;
   if (!c.monotone || c.nnz <= 0 || c.nrows <= 0) return SX_OK;
-  SX_CHECK(csr_prepare_col16(ctx, c));
+  // only what this context's kernel choice can use: the 16-bit columns when
+  // SX_COL16=1, the unit table when the windowed kernel may run
+  if (ctx->col16) SX_CHECK(csr_prepare_col16(ctx, c));
+  const bool pipe_fits = c.max_chunk_nnz + 3 <= kBlock * 12;
+  if (ctx->win_mode == 0 || (ctx->win_mode == 1 && pipe_fits)) return SX_OK;
   int32_t first = -1;
   SX_CUDA(cudaMemcpyAsync(&first, c.indptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
   SX_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -846,7 +850,7 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   if (const char* t = std::getenv("SX_WIN")) c->win_mode = std::atoi(t);
   if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "1") == 0;
   if (const char* t = std::getenv("SX_MX_FUSED")) c->mx_unfused = std::strcmp(t, "0") == 0;
-  if (const char* t = std::getenv("SX_SHORT")) c->short_rows = std::strcmp(t, "0") != 0;
+  if (const char* t = std::getenv("SX_SHORT")) c->short_rows = std::atoi(t);
   if (const char* t = std::getenv("SX_WIN_SHAPE")) c->win_shape = std::atoi(t);
   if (own) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);

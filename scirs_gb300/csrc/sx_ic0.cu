@@ -71,26 +71,35 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 }
 
 __device__ __forceinline__ int ld_flag(const int* p) { return *(volatile const int*)p; }
-
-// Waits until *flag != 0; false if the wait was abandoned (abort raised).
-__device__ bool wait_flag(const int* flag, int* abort) {
-  if (ld_flag(flag)) return true;
-  const unsigned long long t0 = globaltimer();
-  while (!ld_flag(flag)) {
-    if (ld_flag(abort)) return false;
-    __nanosleep(100);
-    if (globaltimer() - t0 > kWaitNs) {
-      atomicExch(abort, 1);
-      return false;
-    }
-  }
-  __threadfence();
-  return true;
+// acquire load: later loads see what the publisher wrote before its release
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 
+// Waits until *flag != 0; false if the wait was abandoned (abort raised or
+// the 2-s limit passed).  Spins without sleeping first: the wait sits on
+// the critical path of the triangular solves, one wait per dependency level.
+__device__ bool wait_flag(const int* flag, int* abort) {
+  if (ld_acquire(flag)) return true;
+  const unsigned long long t0 = globaltimer();
+  for (unsigned it = 1;; ++it) {
+    if (ld_acquire(flag)) return true;
+    if ((it & 63u) == 0) {
+      if (ld_flag(abort)) return false;
+      if (globaltimer() - t0 > kWaitNs) {
+        atomicExch(abort, 1);
+        return false;
+      }
+    }
+    if (it > 4096u) __nanosleep(128);
+  }
+}
+
+// release store: the row's result is visible before its flag
 __device__ __forceinline__ void publish(int* flag) {
-  __threadfence();
-  atomicExch(flag, 1);
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(flag), "r"(1) : "memory");
 }
 
 template <typename T>

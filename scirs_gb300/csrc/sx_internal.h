@@ -122,8 +122,9 @@ struct sx_ctx_s {
   // instead of its fused iteration
   bool mx_unfused = false;
   // matrices whose rows all hold at most 16 entries use the register-only
-  // short-row SpMV for FP32 and FP64-FMA (SX_SHORT=0: never)
-  bool short_rows = true;
+  // short-row SpMV: 1 (default) for FP64 with fused multiply-adds, 2 also
+  // for FP32, 0 never (SX_SHORT)
+  int short_rows = 1;
   int win_shape = 0;
 };
 
@@ -149,9 +150,9 @@ uint64_t next_op_serial();
 // buffer that captured graphs reference is reallocated
 void solver_graphs_drop(sx_ctx ctx);
 constexpr int kUnit = 256;  // nonzeros per tile_row entry
-// builds c.tile_row for the windowed SpMV and, where the column spans allow,
-// c.col16 / c.chunk_base for the register-pipelined SpMV (allocates and
-// synchronises)
+// builds what the context's SpMV choice can use: c.tile_row for the
+// windowed SpMV, and (SX_COL16=1, where the column spans allow) c.col16 /
+// c.chunk_base for the register pipeline (allocates and synchronises)
 int csr_prepare_tiles(sx_ctx ctx, DevCsr& c);
 
 

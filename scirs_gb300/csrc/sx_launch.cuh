@@ -186,7 +186,7 @@ bool launch_pipe_gather(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, 
   if (ctx_reduce_area(ctx, blocks, &ra) != SX_OK) return false;
   const bool small = c.max_chunk_nnz + 3 <= kBlock * 8;
   bool done = false;
-  if (ctx->short_rows) {
+  if (ctx->short_rows == 2) {
     if constexpr (HALF && sizeof(T) == 4) {
       if (c.vals16) done = launch_short<T, Epi, false, __half, Gather>(ctx, c, (const __half*)c.vals16, x, y, epi, ra, blocks, gat);
     }
@@ -226,7 +226,7 @@ inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma
   const bool items8 = c.max_chunk_nnz + 3 <= kBlock * 8;
   if (c.nrows <= 0) return "none";
   if (c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) return "spmv_win_kernel";
-  if (ctx->short_rows && (fma || w == 4) && c.monotone && c.max_row_len <= 16)
+  if (ctx->short_rows && (fma || (w == 4 && ctx->short_rows == 2)) && c.monotone && c.max_row_len <= 16)
     return c.max_row_len <= 8 ? "spmv_short_kernel<K=8>"
                               : (c.max_row_len <= 12 ? "spmv_short_kernel<K=12>" : "spmv_short_kernel<K=16>");
   if (pipe_fits && half_ok && w == 4 && c.vals16)
@@ -254,9 +254,11 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
       default: done = launch_win<T, 0, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
     }
   }
-  // short rows: the register-only kernel for FP32 and for FP64 with fused
-  // multiply-adds (measured faster or equal); exact FP64 keeps the pipeline
-  if (!done && ctx->short_rows && (FMA || sizeof(T) == 4)) {
+  // short rows: the register-only kernel for FP64 with fused multiply-adds
+  // (faster alone, equal inside the solvers); FP32 and exact FP64 keep the
+  // pipeline, which is equal or faster inside the solvers' graphs
+  // (SX_SHORT=2 extends it to FP32)
+  if (!done && ctx->short_rows && (FMA || (sizeof(T) == 4 && ctx->short_rows == 2))) {
     bool half = false;
     if constexpr (HALF && sizeof(T) == 4) half = c.vals16 != nullptr;
     if constexpr (HALF && sizeof(T) == 4) {

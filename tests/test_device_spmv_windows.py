@@ -156,7 +156,7 @@ def test_compressed_columns_bit_exact(S, dtype, kind, dims, p0, p1):
     vals = v.astype(dtype)
     x = np.random.default_rng(2).standard_normal(n).astype(dtype)
     yr = O.spmv_i32(ip, ix, vals, x)
-    for env in ({}, {"SX_SHORT": "0"}, {"SX_SHORT": "0", "SX_COL16": "1"}):
+    for env in ({}, {"SX_SHORT": "2"}, {"SX_SHORT": "0", "SX_COL16": "1"}):
         c = _ctx_with(S, env)
         a = S.csr_from_arrays(c, ip, ix, vals, (n, n))
         y = a.matvec(x)
@@ -183,13 +183,13 @@ def test_compressed_columns_wide_rows_keep_int32(S, ctx):
 
 
 def test_kernel_choice_names(S, ctx):
-    # the dispatch: short rows in registers (FP32, FP64 with FMA), the
-    # register pipeline for exact FP64 stencils, windows for long rows
+    # the dispatch: short rows in registers for FP64 with FMA, the register
+    # pipeline for FP32 and exact FP64 stencils, windows for long rows
     ip, ix, v = S.generate("laplace3d", 20, 20, 20)
     n = len(ip) - 1
     a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
     a32 = a64.astype(np.float32)
-    assert S.spmv_kernel(a32) == "spmv_short_kernel<K=8>"
+    assert S.spmv_kernel(a32) == "spmv_pipe_kernel<ITEMS=8>"
     assert S.spmv_kernel(a64, exact=False) == "spmv_short_kernel<K=8>"
     assert S.spmv_kernel(a64, exact=True) == "spmv_pipe_kernel<ITEMS=8>"
     ip, ix, v = S.generate("powerlaw", 50000, 1, 1, seed=2, param0=16.0, param1=4096.0)
