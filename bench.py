@@ -318,7 +318,9 @@ def run_ours(args):
     r_jm, t_jm = once(lambda: S.cg_mixed(a64, b, tol=TOL, max_inner=200000, preconditioner=m32, a32=a32))
     m32.close()
     ic0 = {}
-    for variant, tb in ((("reference", False), ("textbook", True)) if args.ic0 else ()):
+    # textbook IC(0) always (54 iterations); the reference's factorisation
+    # needs ~1,400 iterations of a level-scheduled triangular solve (--ic0)
+    for variant, tb in ((("reference", False), ("textbook", True)) if args.ic0 else (("textbook", True),)):
         try:
             mi, t_mi = once(lambda: S.ic0(ctx, a64, textbook=tb))
         except S.SparseError as e:
@@ -425,7 +427,7 @@ def run_ours(args):
         "speedup_vs_jacobi_fp64": jac / value,
         "jacobi_pcg_mixed": {"value": t_jm, "unit": "s", "outer_iterations": r_jm.outer_iterations,
                              "inner_iterations": r_jm.inner_iterations, "fp64_true_rel_residual": r_jm.rel_residual},
-        "ic0_pcg_fp64": ic0 if args.ic0 else "not run (--ic0)",
+        "ic0_pcg_fp64": ic0,
         "e2e": {"value": statistics.mean(t_e2e), "unit": "s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8},
         "roofline": {"bound": "hbm", "kernel": f"FP32 CSR SpMV of A (aniso Q1 {SIDE}^2), {kname}",
@@ -704,7 +706,7 @@ def main():
     ap.add_argument("--no-batched", dest="batched", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iters", type=int, default=300)
-    ap.add_argument("--ic0", action="store_true", help="also time IC(0)-PCG (reference and textbook factors)")
+    ap.add_argument("--ic0", action="store_true", help="also time IC(0)-PCG with the reference's factorisation")
     ap.add_argument("--ic0-max-iter", type=int, default=3000)
     ap.add_argument("--profile", default=None,
                     choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "aniso32", "solve", "learned",

@@ -106,7 +106,10 @@ typedef enum {
   SX_OP_JACOBI = 4,          /* JacobiPreconditioner                   preconditioners.rs:14-92 */
   SX_OP_IC0 = 5,             /* IC0Preconditioner                      ic.rs:15-230 */
   SX_OP_FSAI = 6,            /* M^-1 = G G^T (learned factorised SAI; no reference counterpart) */
-  SX_OP_HOST = 7             /* user operator called back on the host  (dyn LinearOperator) */
+  SX_OP_HOST = 7,            /* user operator called back on the host  (dyn LinearOperator) */
+  SX_OP_ZERO = 8,            /* ZeroOperator                           interface.rs:177-222 */
+  SX_OP_SUM = 9,             /* SumOperator: (A + B) x                 interface.rs:299-349 */
+  SX_OP_PRODUCT = 10         /* ProductOperator: A (B x)               interface.rs:351-402 */
 } sx_op_kind;
 
 /* Which reference constructor's validation and error semantics to follow. */
@@ -172,6 +175,17 @@ int sx_op_destroy(sx_op op);
 /* y = A x (LinearOperator::matvec, interface.rs:18; CSR: interface.rs:257-279,
  * CsrArray::dot_vector csr_array.rs:569-593, CsrMatrix::dot csr.rs:479-497).
  * x has x_len entries (DimensionMismatch otherwise), y has nrows. */
+/* ZeroOperator::new(rows, cols) (interface.rs:184-191): matvec gives zeros. */
+int sx_op_zero(sx_ctx ctx, sx_dtype dtype, uint64_t nrows, uint64_t ncols, sx_op* out);
+/* SumOperator::new(a, b) (interface.rs:306-316; ShapeMismatch when the shapes
+ * differ) and ProductOperator::new(a, b) (interface.rs:358-370;
+ * DimensionMismatch when a's columns differ from b's rows).  The composite
+ * borrows a and b (the reference takes ownership of boxes): they must
+ * outlive it, and destroying it leaves them alone. */
+int sx_op_sum(sx_ctx ctx, sx_op a, sx_op b, sx_op* out);
+int sx_op_product(sx_ctx ctx, sx_op a, sx_op b, sx_op* out);
+/* LinearOperator::has_adjoint (interface.rs:49-51 and each operator). */
+int sx_op_has_adjoint(sx_op op, int* out);
 int sx_op_matvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, sx_mem mem);
 /* y = A^T x (LinearOperator::rmatvec; CSR: interface.rs:281-285, through a
  * cached device transpose instead of a transpose per call). */

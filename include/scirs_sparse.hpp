@@ -5,7 +5,7 @@
 // reference crate (scirs2-sparse, workspace 0.1.0-alpha.6):
 //   CsrMatrix          csr.rs:15-498        (CsrMatrix::new -> CsrMatrix::create)
 //   CsrArray           csr_array.rs:30-625  (CsrArray::new -> CsrArray::create)
-//   LinearOperator     linalg/interface.rs:13-52, operators :55-223
+//   LinearOperator     linalg/interface.rs:13-52, operators :55-223, :299-402
 //   JacobiPreconditioner, IC0Preconditioner  linalg/preconditioners.rs:14-92, linalg/ic.rs:15-230
 //   CGOptions / BiCGSTABOptions / GMRESOptions, cg / bicgstab / gmres,
 //   IterationResult    linalg/iterative.rs:8-816
@@ -170,6 +170,57 @@ class DiagonalOperator : public DeviceOperator<F> {
     return h;
   }
   std::vector<F> diagonal_;
+};
+
+// ZeroOperator (interface.rs:177-222)
+template <class F>
+class ZeroOperator : public DeviceOperator<F> {
+ public:
+  ZeroOperator(size_t rows, size_t cols, Context& c = Context::global())
+      : DeviceOperator<F>(c.get(), make(c.get(), rows, cols)) {}
+
+ private:
+  static sx_op make(sx_ctx ctx, size_t rows, size_t cols) {
+    sx_op h = nullptr;
+    detail::check(sx_op_zero(ctx, detail::dtype_of<F>(), rows, cols, &h));
+    return h;
+  }
+};
+
+// SumOperator (A + B) and ProductOperator (A B) (interface.rs:299-402).  The
+// reference boxes its operands; here the composite keeps shared references
+// to the two device operators, so they live as long as it does.
+template <class F>
+class SumOperator : public DeviceOperator<F> {
+ public:
+  static SumOperator create(std::shared_ptr<DeviceOperator<F>> a, std::shared_ptr<DeviceOperator<F>> b) {
+    sx_op h = nullptr;
+    detail::check(sx_op_sum(a->context(), a->device_op(), b->device_op(), &h));
+    return SumOperator(a->context(), h, a, b);
+  }
+  bool has_adjoint() const override { return a_->has_adjoint() && b_->has_adjoint(); }
+
+ private:
+  SumOperator(sx_ctx ctx, sx_op h, std::shared_ptr<DeviceOperator<F>> a, std::shared_ptr<DeviceOperator<F>> b)
+      : DeviceOperator<F>(ctx, h), a_(std::move(a)), b_(std::move(b)) {}
+  std::shared_ptr<DeviceOperator<F>> a_, b_;
+};
+
+template <class F>
+class ProductOperator : public DeviceOperator<F> {
+ public:
+  static ProductOperator create(std::shared_ptr<DeviceOperator<F>> a, std::shared_ptr<DeviceOperator<F>> b) {
+    sx_op h = nullptr;
+    detail::check(sx_op_product(a->context(), a->device_op(), b->device_op(), &h));
+    return ProductOperator(a->context(), h, a, b);
+  }
+  bool has_adjoint() const override { return a_->has_adjoint() && b_->has_adjoint(); }
+
+ private:
+  ProductOperator(sx_ctx ctx, sx_op h, std::shared_ptr<DeviceOperator<F>> a,
+                  std::shared_ptr<DeviceOperator<F>> b)
+      : DeviceOperator<F>(ctx, h), a_(std::move(a)), b_(std::move(b)) {}
+  std::shared_ptr<DeviceOperator<F>> a_, b_;
 };
 
 // ------------------------------------------------------------------ CSR

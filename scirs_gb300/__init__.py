@@ -19,6 +19,9 @@ from .sparse import (  # noqa: F401
     cg,
     cg_mixed,
     spmv_kernel,
+    sum_operator,
+    product_operator,
+    zero_operator,
     csr_array,
     csr_array_from_triplets,
     csr_from_arrays,

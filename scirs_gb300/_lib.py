@@ -190,6 +190,10 @@ _SIGS = {
     "sx_op_rmatvec": (c_int, [ctx_t, op_t, c_vp, c_u64, c_vp, c_int]),
     "sx_spmv_ex": (c_int, [ctx_t, op_t, c_vp, c_vp, C.c_uint]),
     "sx_spmv_kernel": (c_int, [ctx_t, op_t, C.c_uint, C.c_char_p, c_u64]),
+    "sx_op_zero": (c_int, [ctx_t, c_int, c_u64, c_u64, P(op_t)]),
+    "sx_op_sum": (c_int, [ctx_t, op_t, op_t, P(op_t)]),
+    "sx_op_product": (c_int, [ctx_t, op_t, op_t, P(op_t)]),
+    "sx_op_has_adjoint": (c_int, [op_t, P(c_int)]),
     "sx_precond_jacobi": (c_int, [ctx_t, op_t, P(op_t)]),
     "sx_precond_jacobi_from_diagonal": (c_int, [ctx_t, c_int, c_vp, c_u64, P(op_t)]),
     "sx_precond_ic0": (c_int, [ctx_t, op_t, c_int, P(op_t)]),

@@ -1407,6 +1407,75 @@ int sx_op_host(sx_ctx ctx, sx_dtype dtype, uint64_t nrows, uint64_t ncols, sx_ho
   return clear_error();
 }
 
+int sx_op_zero(sx_ctx ctx, sx_dtype dtype, uint64_t nrows, uint64_t ncols, sx_op* out) {
+  if (!ctx || !out) return err_arg("null argument");
+  if (dtype != SX_F32 && dtype != SX_F64) return err_arg("dtype");
+  if (nrows > kI32Max) return err_cast(nrows);
+  if (ncols > kI32Max) return err_cast(ncols);
+  *out = new_op(ctx, SX_OP_ZERO, dtype, (int64_t)nrows, (int64_t)ncols);
+  return clear_error();
+}
+
+static int make_pair_op(sx_ctx ctx, int kind, sx_op a, sx_op b, int64_t nrows, int64_t ncols,
+                        int64_t work_len, sx_op* out) {
+  if (a->dtype != b->dtype) return err_arg("operand dtypes differ");
+  SX_CUDA(cudaSetDevice(ctx->device));
+  sx_op op = new_op(ctx, kind, a->dtype, nrows, ncols);
+  op->left = a;
+  op->right = b;
+  int rc = dev_alloc(&op->work, std::max<int64_t>(work_len, 1) * elt_size(a->dtype));
+  if (rc) { delete op; return rc; }
+  *out = op;
+  return clear_error();
+}
+
+int sx_op_sum(sx_ctx ctx, sx_op a, sx_op b, sx_op* out) {
+  if (!ctx || !a || !b || !out) return err_arg("null argument");
+  if (a->nrows != b->nrows || a->ncols != b->ncols) {
+    // interface.rs:308-313: ShapeMismatch{expected: a.shape(), found: b.shape()}
+    return set_error(SX_ERR_SHAPE_MISMATCH,
+                     "Shape mismatch: expected (" + std::to_string(a->nrows) + ", " + std::to_string(a->ncols) +
+                         "), found (" + std::to_string(b->nrows) + ", " + std::to_string(b->ncols) + ")",
+                     (uint64_t)a->nrows, (uint64_t)a->ncols, (uint64_t)b->nrows, (uint64_t)b->ncols);
+  }
+  return make_pair_op(ctx, SX_OP_SUM, a, b, a->nrows, a->ncols, a->nrows, out);
+}
+
+int sx_op_product(sx_ctx ctx, sx_op a, sx_op b, sx_op* out) {
+  if (!ctx || !a || !b || !out) return err_arg("null argument");
+  // interface.rs:360-366: DimensionMismatch{expected: a_cols, found: b_rows}
+  if (a->ncols != b->nrows) return err_dim((uint64_t)a->ncols, (uint64_t)b->nrows);
+  return make_pair_op(ctx, SX_OP_PRODUCT, a, b, a->nrows, b->ncols, b->nrows, out);
+}
+
+}  // extern "C"
+
+namespace sx {
+// y = y + t (interface.rs:340-344: a + b elementwise)
+template <typename T>
+__global__ void k_add_inplace(T* y, const T* __restrict__ t, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) y[i] = add_rn(y[i], t[i]);
+}
+}  // namespace sx
+
+extern "C" {
+
+static bool has_adjoint(sx_op op) {
+  switch (op->kind) {
+    case SX_OP_HOST: return false;  // interface.rs:49-51 (the trait's default)
+    case SX_OP_SUM:
+    case SX_OP_PRODUCT: return has_adjoint(op->left) && has_adjoint(op->right);  // :349, :399
+    default: return true;
+  }
+}
+
+int sx_op_has_adjoint(sx_op op, int* out) {
+  if (!op || !out) return err_arg("null argument");
+  *out = has_adjoint(op) ? 1 : 0;
+  return SX_OK;
+}
+
 int sx_op_kind_of(sx_op op, int* kind) {
   if (!op || !kind) return err_arg("null argument");
   *kind = op->kind;
@@ -1481,6 +1550,63 @@ int sx_op_rmatvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, 
       // self-adjoint operators: rmatvec = matvec (interface.rs:86-88,
       // :121-124, :164-167; preconditioners.rs:88-91; ic.rs:227-230)
       return sx_op_matvec(ctx, op, x, x_len, y, mem);
+    case SX_OP_ZERO: {
+      // interface.rs:211-218: zeros of length cols
+      if (x_len != (uint64_t)op->nrows) return err_dim((uint64_t)op->nrows, x_len);
+      SX_CUDA(cudaSetDevice(ctx->device));
+      const size_t bytes = (size_t)op->ncols * elt_size(op->dtype);
+      if (mem == SX_MEM_DEVICE) {
+        SX_CUDA(cudaMemsetAsync(y, 0, bytes, ctx->stream));
+        SX_CUDA(cudaStreamSynchronize(ctx->stream));
+      } else {
+        std::memset(y, 0, bytes);
+      }
+      return clear_error();
+    }
+    case SX_OP_SUM:
+    case SX_OP_PRODUCT: {
+      // interface.rs:332-345 and :382-395: both adjoints or OperationNotSupported;
+      // (A + B)^H x = A^H x + B^H x, (A B)^H x = B^H (A^H x)
+      if (!has_adjoint(op->left) || !has_adjoint(op->right))
+        return set_error(SX_ERR_OPERATION_NOT_SUPPORTED,
+                         "Operation not supported: adjoint not supported for one or both operators");
+      if (x_len != (uint64_t)op->nrows) return err_dim((uint64_t)op->nrows, x_len);
+      SX_CUDA(cudaSetDevice(ctx->device));
+      const size_t w = elt_size(op->dtype);
+      void *dx = nullptr, *t = nullptr, *dy = nullptr;
+      int rc = SX_OK;
+      do {
+        if ((rc = dev_alloc(&dx, std::max<int64_t>(op->nrows, 1) * w))) break;
+        if ((rc = dev_alloc(&dy, std::max<int64_t>(op->ncols, 1) * w))) break;
+        const int64_t tlen = op->kind == SX_OP_SUM ? op->ncols : op->left->ncols;
+        if ((rc = dev_alloc(&t, std::max<int64_t>(tlen, 1) * w))) break;
+        SX_CUDA(cudaMemcpyAsync(dx, x, op->nrows * w,
+                                mem == SX_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                ctx->stream));
+        if (op->kind == SX_OP_SUM) {
+          if ((rc = sx_op_rmatvec(ctx, op->left, dx, op->nrows, dy, SX_MEM_DEVICE))) break;
+          if ((rc = sx_op_rmatvec(ctx, op->right, dx, op->nrows, t, SX_MEM_DEVICE))) break;
+          const int g = vec_grid(ctx, op->ncols);
+          if (op->dtype == SX_F64)
+            k_add_inplace<double><<<g, kBlock, 0, ctx->stream>>>((double*)dy, (const double*)t, op->ncols);
+          else
+            k_add_inplace<float><<<g, kBlock, 0, ctx->stream>>>((float*)dy, (const float*)t, op->ncols);
+          ctx->launches++;
+        } else {
+          if ((rc = sx_op_rmatvec(ctx, op->left, dx, op->nrows, t, SX_MEM_DEVICE))) break;
+          if ((rc = sx_op_rmatvec(ctx, op->right, t, op->left->ncols, dy, SX_MEM_DEVICE))) break;
+        }
+        SX_CUDA(cudaMemcpyAsync(y, dy, op->ncols * w,
+                                mem == SX_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "composite rmatvec", __FILE__, __LINE__);
+      } while (0);
+      dev_free(dx);
+      dev_free(t);
+      dev_free(dy);
+      return rc == SX_OK ? clear_error() : rc;
+    }
     default:
       return set_error(SX_ERR_OPERATION_NOT_SUPPORTED,
                        "Operation not supported: adjoint not implemented for this operator");

@@ -87,7 +87,10 @@ struct sx_op_s {
   sx_op_s* transpose = nullptr;       // cached transpose (rmatvec, FSAI's G^T)
   sx::IC0Dev* ic0 = nullptr;
   sx::HostOp host;
-  void* work = nullptr;               // per-operator temporary vector (FSAI: G^T x)
+  void* work = nullptr;               // per-operator temporary vector (FSAI: G^T x;
+                                      // SUM: B x; PRODUCT: B x)
+  sx_op_s* left = nullptr;            // SUM / PRODUCT operands, borrowed
+  sx_op_s* right = nullptr;
   uint64_t serial = 0;                // unique id, keys the solver graph cache
 };
 

@@ -191,7 +191,13 @@ static int graph_build(sx_ctx ctx, const uint64_t key[8], Rec record, GraphEntry
   return SX_OK;
 }
 
-static bool op_graphable(sx_op op) { return !op || op->kind != SX_OP_HOST; }
+// host callbacks cannot run inside a captured graph, also when they sit
+// inside a sum or a product
+static bool op_graphable(sx_op op) {
+  if (!op) return true;
+  if (op->kind == SX_OP_HOST) return false;
+  return op_graphable(op->left) && op_graphable(op->right);
+}
 
 static int check_prec(sx_op a, sx_op m) {
   if (!m) return SX_OK;

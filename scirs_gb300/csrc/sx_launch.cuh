@@ -44,8 +44,13 @@ __global__ void __launch_bounds__(kBlock) k_diag_apply(int64_t n, int kind, cons
   Acc3<T> a{T(0), T(0), T(0)};
   const int64_t stride = (int64_t)gridDim.x * kBlock;
   for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) {
-    T xi = x[i];
-    T ax = kind == SX_OP_IDENTITY ? xi : (kind == SX_OP_SCALED_IDENTITY ? mul_rn(xi, scale) : mul_rn(xi, d[i]));
+    T ax;
+    if (kind == SX_OP_ZERO) {
+      ax = T(0);  // interface.rs:207: zeros whatever x holds
+    } else {
+      const T xi = x[i];
+      ax = kind == SX_OP_IDENTITY ? xi : (kind == SX_OP_SCALED_IDENTITY ? mul_rn(xi, scale) : mul_rn(xi, d[i]));
+    }
     T v = epi.out(i, ax);
     y[i] = v;
     epi.acc(i, v, a);
@@ -65,6 +70,25 @@ __global__ void __launch_bounds__(kBlock) k_epi_inplace(int64_t n, T* y, T* part
   const int64_t stride = (int64_t)gridDim.x * kBlock;
   for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) {
     T v = epi.out(i, y[i]);
+    y[i] = v;
+    epi.acc(i, v, a);
+  }
+  if constexpr (Epi::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) epi.finish(tot);
+  }
+}
+
+// y = y + w elementwise (SumOperator: a + b, interface.rs:325-329), then the
+// epilogue over y
+template <typename T, class Epi>
+__global__ void __launch_bounds__(kBlock) k_sum_epi(int64_t n, T* y, const T* __restrict__ w, T* partials,
+                                                    unsigned int* counter, Epi epi) {
+  if (epi.skip()) return;
+  Acc3<T> a{T(0), T(0), T(0)};
+  const int64_t stride = (int64_t)gridDim.x * kBlock;
+  for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += stride) {
+    const T v = epi.out(i, add_rn(y[i], w[i]));
     y[i] = v;
     epi.acc(i, v, a);
   }
@@ -312,6 +336,25 @@ int launch_apply(sx_ctx ctx, sx_op op, const T* x, T* y, Epi epi) {
   switch (op->kind) {
     case SX_OP_CSR:
       return launch_csr<T, Epi, kFma>(ctx, op->csr, x, y, epi);
+    case SX_OP_SUM: {
+      // y = A x, w = B x, y = y + w with the epilogue
+      SX_CHECK((launch_apply<T, EpiPlain<T>, EXACT>(ctx, op->left, x, y, EpiPlain<T>{})));
+      SX_CHECK((launch_apply<T, EpiPlain<T>, EXACT>(ctx, op->right, x, (T*)op->work, EpiPlain<T>{})));
+      ReduceArea ra;
+      const int g = vec_grid(ctx, op->nrows);
+      SX_CHECK(ctx_reduce_area(ctx, g, &ra));
+      k_sum_epi<T, Epi><<<g, kBlock, 0, ctx->stream>>>(op->nrows, y, (const T*)op->work, (T*)ra.partials,
+                                                        ra.counter, epi);
+      ctx->launches++;
+      SX_CUDA(cudaGetLastError());
+      return SX_OK;
+    }
+    case SX_OP_PRODUCT: {
+      // w = B x, then y = A w carries the epilogue
+      SX_CHECK((launch_apply<T, EpiPlain<T>, EXACT>(ctx, op->right, x, (T*)op->work, EpiPlain<T>{})));
+      return launch_apply<T, Epi, EXACT>(ctx, op->left, (const T*)op->work, y, epi);
+    }
+    case SX_OP_ZERO:
     case SX_OP_IDENTITY:
     case SX_OP_SCALED_IDENTITY:
     case SX_OP_DIAGONAL:

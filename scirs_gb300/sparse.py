@@ -154,6 +154,12 @@ class Operator:
         _check(L.lib.sx_op_matvec(self.ctx.handle, self.handle, _ptr(x), x.size, _ptr(y), L.SX_MEM_HOST))
         return y
 
+    @property
+    def has_adjoint(self) -> bool:
+        out = C.c_int()
+        _check(L.lib.sx_op_has_adjoint(self.handle, C.byref(out)))
+        return bool(out.value)
+
     def rmatvec(self, x) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=self.dtype)
         y = np.empty(self.shape[1], dtype=self.dtype)
@@ -301,6 +307,33 @@ def diagonal(ctx: Context, diag, dtype=np.float64) -> Operator:
     h = L.op_t()
     _check(L.lib.sx_op_diagonal(ctx.handle, _dtype_code(dtype), _ptr(d), d.size, C.byref(h)))
     return Operator(ctx, h)
+
+
+def zero_operator(ctx: Context, nrows: int, ncols: int, dtype=np.float64) -> Operator:
+    """ZeroOperator::new(rows, cols) (interface.rs:184-191)."""
+    h = L.op_t()
+    _check(L.lib.sx_op_zero(ctx.handle, _dtype_code(dtype), nrows, ncols, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def sum_operator(a: Operator, b: Operator) -> Operator:
+    """SumOperator::new(a, b) (interface.rs:306-316).  The result borrows a
+    and b: keep them open while it is used."""
+    h = L.op_t()
+    _check(L.lib.sx_op_sum(a.ctx.handle, a.handle, b.handle, C.byref(h)))
+    op = Operator(a.ctx, h)
+    op._operands = (a, b)
+    return op
+
+
+def product_operator(a: Operator, b: Operator) -> Operator:
+    """ProductOperator::new(a, b): (A B) x = A (B x) (interface.rs:358-370).
+    The result borrows a and b."""
+    h = L.op_t()
+    _check(L.lib.sx_op_product(a.ctx.handle, a.handle, b.handle, C.byref(h)))
+    op = Operator(a.ctx, h)
+    op._operands = (a, b)
+    return op
 
 
 def host_operator(ctx: Context, n: int, fn, dtype=np.float64) -> Operator:

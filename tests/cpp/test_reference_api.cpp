@@ -220,6 +220,28 @@ int main() {
     CHECK(r.converged);
     CHECK(resid(m, r.x, b) < 1e-9);
   });
+  // ZeroOperator / SumOperator / ProductOperator (interface.rs:177-402)
+  run("zero_sum_product_operators", [] {
+    ZeroOperator<double> z(2, 3);
+    auto zy = z.matvec({1, 2, 3});
+    CHECK((zy == std::vector<double>{0, 0}));
+    auto id = std::make_shared<IdentityOperator<double>>(3);
+    auto dg = std::make_shared<DiagonalOperator<double>>(std::vector<double>{2, 3, 4});
+    auto s = SumOperator<double>::create(id, dg);
+    auto sy = s.matvec({1, 1, 1});
+    NEAR(sy[0], 3, 1e-15); NEAR(sy[1], 4, 1e-15); NEAR(sy[2], 5, 1e-15);
+    auto p = ProductOperator<double>::create(dg, dg);
+    auto py = p.matvec({1, 1, 1});
+    NEAR(py[0], 4, 1e-15); NEAR(py[1], 9, 1e-15); NEAR(py[2], 16, 1e-15);
+    auto zz = std::make_shared<ZeroOperator<double>>(2, 3);
+    bool threw = false;
+    try {
+      SumOperator<double>::create(id, zz);
+    } catch (const SparseError& e) {
+      threw = e.variant() == "ShapeMismatch";
+    }
+    CHECK(threw);
+  });
   // errors carry the reference's variants and messages (csr.rs:107-119)
   run("construction_errors", [] {
     try {
