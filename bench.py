@@ -372,6 +372,19 @@ def run_ours(args):
         sweep[f"laplace3d_{GRID}_fp64"] = sweep_entry(spmv_bytes(ln, len(lv), 8), spmv_time(l64, ln, np.float64))
         sweep[f"laplace3d_{GRID}_fp64_fma"] = sweep_entry(spmv_bytes(ln, len(lv), 8),
                                                           spmv_time(l64, ln, np.float64, flags=0))
+        # the same matrix stored as its lower triangle (SymCsrMatrix): merged
+        # rows read as many bytes as the full CSR; the half-storage product
+        # reads the lower triangle once (its bytes: lower entries, x, y)
+        s64 = S.sym_csr_from_csr(l64)
+        s32 = s64.astype(np.float32)
+        lnnz = s64.nnz_stored()
+        half_b = lambda w: lnnz * (w + 4) + 4 * (ln + 1) + 2 * ln * w  # noqa: E731
+        sweep[f"laplace3d_{GRID}_sym_fp64"] = sweep_entry(spmv_bytes(ln, len(lv), 8), spmv_time(s64, ln, np.float64))
+        sweep[f"laplace3d_{GRID}_sym_fp32"] = sweep_entry(spmv_bytes(ln, len(lv), 4), spmv_time(s32, ln, np.float32))
+        sweep[f"laplace3d_{GRID}_sym_half_fp64"] = sweep_entry(half_b(8), spmv_time(s64, ln, np.float64, flags=2))
+        sweep[f"laplace3d_{GRID}_sym_half_fp32"] = sweep_entry(half_b(4), spmv_time(s32, ln, np.float32, flags=2))
+        s32.close()
+        s64.close()
         l32.close()
         l64.close()
         pip, pix, pv = S.generate("powerlaw", 4194304, seed=1, param0=16.0, param1=4096.0)
@@ -571,7 +584,7 @@ def run_profile(args):
             op.close()
         ctx.close()
         return
-    if args.profile in ("spmv32", "spmv64"):
+    if args.profile in ("spmv32", "spmv64") or args.profile.startswith("sym"):
         ip, ix, v = S.generate("laplace3d", GRID, GRID, GRID)
     elif args.profile == "aniso32":
         _, ip, ix, v, _, _ = headline_problem()
@@ -580,12 +593,19 @@ def run_profile(args):
     n = len(ip) - 1
     dt = np.float64 if args.profile.endswith("64") else np.float32
     a = S.csr_from_arrays(ctx, ip, ix, v.astype(dt), (n, n))
+    flags = 1
+    if args.profile.startswith("sym"):
+        # lower-triangle storage: merged rows (exact) or the half-storage scatter
+        full = a
+        a = S.sym_csr_from_csr(full)
+        full.close()
+        flags = 2 if "half" in args.profile else 1
     tdt = torch.float64 if dt == np.float64 else torch.float32
     x = torch.randn(n, dtype=tdt, device="cuda")
     y = torch.empty(n, dtype=tdt, device="cuda")
     for _ in range(args.steps):
         S.sparse._check(L.lib.sx_spmv_ex(ctx.handle, a.handle, C.c_void_p(x.data_ptr()),
-                                         C.c_void_p(y.data_ptr()), 1))
+                                         C.c_void_p(y.data_ptr()), flags))
     ctx.synchronize()
     print(json.dumps({"profile": args.profile, "n": n, "nnz": len(v), "launches": args.steps}))
     a.close()
@@ -710,7 +730,7 @@ def main():
     ap.add_argument("--ic0-max-iter", type=int, default=3000)
     ap.add_argument("--profile", default=None,
                     choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "aniso32", "solve", "learned",
-                             "jacobi64", "jacobi32mixed"],
+                             "jacobi64", "jacobi32mixed", "sym64", "sym32", "symhalf64", "symhalf32"],
                     help="run a few launches of one SpMV for an ncu capture and exit")
     ap.add_argument("--workload", default="laplace3d", choices=["laplace3d", "learned"])
     ap.add_argument("--train-gnn", type=int, default=0, help="train the network for N steps first")

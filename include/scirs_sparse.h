@@ -109,7 +109,8 @@ typedef enum {
   SX_OP_HOST = 7,            /* user operator called back on the host  (dyn LinearOperator) */
   SX_OP_ZERO = 8,            /* ZeroOperator                           interface.rs:177-222 */
   SX_OP_SUM = 9,             /* SumOperator: (A + B) x                 interface.rs:299-349 */
-  SX_OP_PRODUCT = 10         /* ProductOperator: A (B x)               interface.rs:351-402 */
+  SX_OP_PRODUCT = 10,        /* ProductOperator: A (B x)               interface.rs:351-402 */
+  SX_OP_SYM_CSR = 11         /* SymCsrMatrix (lower triangle stored)   sym_csr.rs:24-337 */
 } sx_op_kind;
 
 /* Which reference constructor's validation and error semantics to follow. */
@@ -172,9 +173,6 @@ int sx_op_shape(sx_op op, uint64_t* nrows, uint64_t* ncols);
 int sx_op_dtype(sx_op op, int* dtype);
 int sx_op_destroy(sx_op op);
 
-/* y = A x (LinearOperator::matvec, interface.rs:18; CSR: interface.rs:257-279,
- * CsrArray::dot_vector csr_array.rs:569-593, CsrMatrix::dot csr.rs:479-497).
- * x has x_len entries (DimensionMismatch otherwise), y has nrows. */
 /* ZeroOperator::new(rows, cols) (interface.rs:184-191): matvec gives zeros. */
 int sx_op_zero(sx_ctx ctx, sx_dtype dtype, uint64_t nrows, uint64_t ncols, sx_op* out);
 /* SumOperator::new(a, b) (interface.rs:306-316; ShapeMismatch when the shapes
@@ -186,6 +184,9 @@ int sx_op_sum(sx_ctx ctx, sx_op a, sx_op b, sx_op* out);
 int sx_op_product(sx_ctx ctx, sx_op a, sx_op b, sx_op* out);
 /* LinearOperator::has_adjoint (interface.rs:49-51 and each operator). */
 int sx_op_has_adjoint(sx_op op, int* out);
+/* y = A x (LinearOperator::matvec, interface.rs:18; CSR: interface.rs:257-279,
+ * CsrArray::dot_vector csr_array.rs:569-593, CsrMatrix::dot csr.rs:479-497).
+ * x has x_len entries (DimensionMismatch otherwise), y has nrows. */
 int sx_op_matvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, sx_mem mem);
 /* y = A^T x (LinearOperator::rmatvec; CSR: interface.rs:281-285, through a
  * cached device transpose instead of a transpose per call). */
@@ -193,15 +194,58 @@ int sx_op_rmatvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, 
 
 /* SpMV flags for sx_spmv_ex */
 #define SX_SPMV_EXACT 1u /* per-row sequential sum of rounded products (reference order) */
+#define SX_SPMV_SYM_HALF 2u /* symmetric operators: read only the stored lower triangle and
+                             * add the transposed terms atomically (order not fixed) */
 /* Device-pointer SpMV with an explicit summation mode, asynchronous on the
  * context stream.  flags = SX_SPMV_EXACT: the reference's rounding, bit for
  * bit (the mode of sx_op_matvec); flags = 0: FP64 rows are summed with fused
  * multiply-adds in storage order (a few ulp per row, half the FP64 pipe
- * work); FP32 is always exact. */
+ * work); FP32 is always exact.  SX_SPMV_SYM_HALF (symmetric operators
+ * only, without SX_SPMV_EXACT) reads each stored entry once and scatters the
+ * transposed terms with atomic adds: fewer bytes, but the summation order
+ * varies from run to run (within a few ulp of the exact result). */
 int sx_spmv_ex(sx_ctx ctx, sx_op a, const void* x_dev, void* y_dev, unsigned flags);
 /* Name of the kernel sx_spmv_ex(flags) launches for `a` (diagnostics; no
  * reference counterpart), NUL-terminated into buf[len]. */
 int sx_spmv_kernel(sx_ctx ctx, sx_op a, unsigned flags, char* buf, uint64_t len);
+
+/* ------------------------------------------- symmetric CSR (lower storage) */
+/* SymCsrMatrix::new(data, indptr, indices, (nrows, ncols)) (sym_csr.rs:64-134):
+ * ValueError "Symmetric matrix must be square", "indptr length (a) must be
+ * equal to rows + 1 (b)", "data length (a) must match indices length (b)",
+ * "Last indptr value (a) must equal nnz (b)", IndexOutOfBounds for a column
+ * >= ncols, ValueError "Symmetric CSR should only store the lower triangular
+ * part"; in that order.  (A decreasing or overrunning indptr, a panic in the
+ * reference, is InconsistentData.)  nnz = indices length.  The operator
+ * applies the full symmetric matrix: sx_op_matvec / sx_spmv_ex give
+ * sym_csr_matvec's result (sym_ops.rs:56-90) bit for bit; it works as A in
+ * every solver and as its own adjoint; sx_csr_get gives SymCsrMatrix::get
+ * (sym_csr.rs:280-298). */
+int sx_sym_csr_new(sx_ctx ctx, sx_dtype dtype, const void* data, uint64_t data_len,
+                   const uint64_t* indptr, uint64_t indptr_len, const uint64_t* indices,
+                   uint64_t nnz, uint64_t nrows, uint64_t ncols, sx_op* out);
+/* SymCsrMatrix::from_csr (sym_csr.rs:149-189): ValueError "Matrix must be
+ * symmetric to convert to SymCSR format" when some stored |a_ij - get(j, i)|
+ * exceeds 100 epsilon; else the col <= row entries in storage order. */
+int sx_sym_csr_from_csr(sx_ctx ctx, sx_op a, sx_op* out);
+/* nnz_stored (sym_csr.rs:241-243) and nnz (sym_csr.rs:254-268: rows that
+ * store a diagonal entry count once, every other stored entry twice). */
+int sx_sym_csr_info(sx_ctx ctx, sx_op a, uint64_t* nnz_stored, uint64_t* nnz_full);
+/* The stored arrays (the public data/indptr/indices fields), as usize. */
+int sx_sym_csr_download(sx_ctx ctx, sx_op a, uint64_t* indptr, uint64_t* indices, void* data);
+/* SymCsrMatrix::to_csr (sym_csr.rs:305-337): a CsrMatrix of the full matrix. */
+int sx_sym_csr_to_csr(sx_ctx ctx, sx_op a, sx_op* out);
+/* sym_csr_trace (sym_ops.rs:317-335) and sym_csr_quadratic_form
+ * (sym_ops.rs:271-283), summed in the reference's sequential order: bit for
+ * bit.  x has x_len entries (DimensionMismatch otherwise). */
+int sx_sym_csr_trace(sx_ctx ctx, sx_op a, void* out_value);
+int sx_sym_csr_quadratic_form(sx_ctx ctx, sx_op a, const void* x, uint64_t x_len, sx_mem mem,
+                              void* out_value);
+/* sym_csr_rank1_update (sym_ops.rs:179-233): A = A + alpha x x^T in place
+ * (lower triangle of the dense sum, zeros dropped; O(n^2) work as in the
+ * reference).  alpha is converted to the operator's value type. */
+int sx_sym_csr_rank1_update(sx_ctx ctx, sx_op a, const void* x, uint64_t x_len, double alpha,
+                            sx_mem mem);
 
 /* --------------------------------------------------------- preconditioners */
 /* JacobiPreconditioner::new (preconditioners.rs:21-44): 1/get(i,i) with the

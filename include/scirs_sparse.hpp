@@ -310,6 +310,8 @@ class CsrMatrix : public CsrBase<F> {
   }
   // CsrMatrix<f64>::dot (csr.rs:479-497)
   std::vector<F> dot(const std::vector<F>& x) const { return this->matvec(x); }
+  // takes ownership of a CSR handle made by another call of the library
+  static CsrMatrix adopt(sx_ctx ctx, sx_op h) { return CsrMatrix(ctx, h); }
 
  private:
   CsrMatrix(sx_ctx ctx, sx_op h) : CsrBase<F>(ctx, h) {}
@@ -364,6 +366,93 @@ class CsrArray : public CsrBase<F> {
 };
 
 // -------------------------------------------------------- preconditioners
+// ------------------------------------------- SymCsrMatrix (sym_csr.rs:24-337)
+// The lower triangle is stored; matvec / get apply the full symmetric matrix.
+template <class F>
+class SymCsrMatrix : public DeviceOperator<F> {
+ public:
+  // SymCsrMatrix::new(data, indptr, indices, shape) (sym_csr.rs:64-134)
+  static SymCsrMatrix create(const std::vector<F>& data, const std::vector<size_t>& indptr,
+                             const std::vector<size_t>& indices, std::pair<size_t, size_t> shape,
+                             Context& c = Context::global()) {
+    std::vector<uint64_t> p(indptr.begin(), indptr.end()), k(indices.begin(), indices.end());
+    sx_op h = nullptr;
+    detail::check(sx_sym_csr_new(c.get(), detail::dtype_of<F>(), data.data(), data.size(), p.data(),
+                                 p.size(), k.data(), k.size(), shape.first, shape.second, &h));
+    return SymCsrMatrix(c.get(), h);
+  }
+  // SymCsrMatrix::from_csr (sym_csr.rs:149-189)
+  static SymCsrMatrix from_csr(const CsrMatrix<F>& m) {
+    sx_op h = nullptr;
+    detail::check(sx_sym_csr_from_csr(m.context(), m.device_op(), &h));
+    return SymCsrMatrix(m.context(), h);
+  }
+  size_t nnz_stored() const { return (size_t)info().first; }
+  size_t nnz() const { return (size_t)info().second; }
+  F get(size_t i, size_t j) const {
+    F v = F(0);
+    detail::check(sx_csr_get(this->ctx_, this->op_->h, i, j, &v));
+    return v;
+  }
+  std::vector<size_t> indptr() const { return arrays().first.first; }
+  std::vector<size_t> indices() const { return arrays().first.second; }
+  std::vector<F> data() const { return arrays().second; }
+  // SymCsrMatrix::to_csr (sym_csr.rs:305-337)
+  CsrMatrix<F> to_csr() const {
+    sx_op h = nullptr;
+    detail::check(sx_sym_csr_to_csr(this->ctx_, this->op_->h, &h));
+    return CsrMatrix<F>::adopt(this->ctx_, h);
+  }
+  // SymCsrMatrix::to_dense (sym_csr.rs:344-366)
+  std::vector<std::vector<F>> to_dense() const {
+    auto a = arrays();
+    const size_t n = this->shape().first;
+    std::vector<std::vector<F>> d(n, std::vector<F>(n, F(0)));
+    for (size_t r = 0; r < n; ++r)
+      for (size_t k = a.first.first[r]; k < a.first.first[r + 1]; ++k) d[r][a.first.second[k]] = a.second[k];
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < i; ++j) d[j][i] = d[i][j];
+    return d;
+  }
+
+ private:
+  SymCsrMatrix(sx_ctx ctx, sx_op h) : DeviceOperator<F>(ctx, h) {}
+  std::pair<uint64_t, uint64_t> info() const {
+    uint64_t a = 0, b = 0;
+    detail::check(sx_sym_csr_info(this->ctx_, this->op_->h, &a, &b));
+    return {a, b};
+  }
+  std::pair<std::pair<std::vector<size_t>, std::vector<size_t>>, std::vector<F>> arrays() const {
+    std::vector<uint64_t> ip(this->shape().first + 1), ix(nnz_stored());
+    std::vector<F> d(nnz_stored());
+    detail::check(sx_sym_csr_download(this->ctx_, this->op_->h, ip.data(), ix.data(), d.data()));
+    return {{std::vector<size_t>(ip.begin(), ip.end()), std::vector<size_t>(ix.begin(), ix.end())}, d};
+  }
+};
+
+// sym_ops.rs:56-90, :179-233, :271-283, :317-335
+template <class F>
+std::vector<F> sym_csr_matvec(const SymCsrMatrix<F>& m, const std::vector<F>& x) {
+  return m.matvec(x);
+}
+template <class F>
+void sym_csr_rank1_update(SymCsrMatrix<F>& m, const std::vector<F>& x, F alpha) {
+  detail::check(sx_sym_csr_rank1_update(m.context(), m.device_op(), x.data(), x.size(), (double)alpha,
+                                        SX_MEM_HOST));
+}
+template <class F>
+F sym_csr_quadratic_form(const SymCsrMatrix<F>& m, const std::vector<F>& x) {
+  F v = F(0);
+  detail::check(sx_sym_csr_quadratic_form(m.context(), m.device_op(), x.data(), x.size(), SX_MEM_HOST, &v));
+  return v;
+}
+template <class F>
+F sym_csr_trace(const SymCsrMatrix<F>& m) {
+  F v = F(0);
+  detail::check(sx_sym_csr_trace(m.context(), m.device_op(), &v));
+  return v;
+}
+
 template <class F>
 class JacobiPreconditioner : public DeviceOperator<F> {
  public:

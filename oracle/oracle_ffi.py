@@ -88,6 +88,19 @@ def lib():
             "or_cg_mixed_replace": (ip, [vp, vp, vp, i64, vp, C.POINTER(IROpt), C.c_double, vp,
                                          C.POINTER(IRRes)]),
             "or_true_rel_residual": (dbl, [vp, vp, vp, i64, vp, vp]),
+            "or_sym_csr_check": (ip, [u64, vp, u64, vp, u64, u64, u64, E]),
+            "or_sym_csr_matvec_f64": (None, [vp, vp, vp, u64, vp, vp]),
+            "or_sym_csr_matvec_f32": (None, [vp, vp, vp, u64, vp, vp]),
+            "or_sym_csr_nnz": (u64, [vp, vp, u64, u64]),
+            "or_sym_csr_get_f64": (dbl, [vp, vp, vp, u64, u64, u64]),
+            "or_sym_csr_trace_f64": (dbl, [vp, vp, vp, u64]),
+            "or_sym_csr_trace_f32": (C.c_float, [vp, vp, vp, u64]),
+            "or_sym_csr_quadratic_form_f64": (dbl, [vp, vp, vp, u64, vp]),
+            "or_sym_csr_quadratic_form_f32": (C.c_float, [vp, vp, vp, u64, vp]),
+            "or_sym_csr_rank1_update_f64": (u64, [vp, vp, vp, u64, vp, dbl, vp, vp, vp]),
+            "or_sym_csr_rank1_update_f32": (u64, [vp, vp, vp, u64, vp, C.c_float, vp, vp, vp]),
+            "or_sym_csr_from_csr_f64": (ip, [vp, vp, vp, u64, u64, vp, vp, vp, E]),
+            "or_sym_csr_from_csr_f32": (ip, [vp, vp, vp, u64, u64, vp, vp, vp, E]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -274,3 +287,85 @@ def true_rel_residual(indptr, indices, data, b, x):
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.ascontiguousarray(x, dtype=np.float64)
     return lib().or_true_rel_residual(p(indptr), p(indices), p(data), len(indptr) - 1, p(b), p(x))
+
+
+# ------------------------------------------------------ symmetric CSR (lower)
+def _sym_arrays(indptr, indices, data):
+    return (np.ascontiguousarray(indptr, dtype=np.uint64), np.ascontiguousarray(indices, dtype=np.uint64),
+            np.ascontiguousarray(data))
+
+
+def sym_check(data_len, indptr, indices, shape):
+    """SymCsrMatrix::new validation: (code, message), code 0 = Ok."""
+    indptr = np.ascontiguousarray(indptr, dtype=np.uint64)
+    indices = np.ascontiguousarray(indices, dtype=np.uint64)
+    e = Err()
+    rc = lib().or_sym_csr_check(data_len, p(indptr), len(indptr), p(indices), len(indices),
+                                int(shape[0]), int(shape[1]), C.byref(e))
+    return rc, e.msg.decode()
+
+
+def sym_matvec(indptr, indices, data, x):
+    indptr, indices, data = _sym_arrays(indptr, indices, data)
+    n = len(indptr) - 1
+    x = np.ascontiguousarray(x, dtype=data.dtype)
+    y = np.empty(n, dtype=data.dtype)
+    f = lib().or_sym_csr_matvec_f64 if data.dtype == np.float64 else lib().or_sym_csr_matvec_f32
+    f(p(indptr), p(indices), p(data), n, p(x), p(y))
+    return y
+
+
+def sym_nnz(indptr, indices):
+    indptr = np.ascontiguousarray(indptr, dtype=np.uint64)
+    indices = np.ascontiguousarray(indices, dtype=np.uint64)
+    return lib().or_sym_csr_nnz(p(indptr), p(indices), len(indices), len(indptr) - 1)
+
+
+def sym_get(indptr, indices, data, i, j):
+    indptr, indices, data = _sym_arrays(indptr, indices, np.asarray(data, dtype=np.float64))
+    return lib().or_sym_csr_get_f64(p(indptr), p(indices), p(data), len(indptr) - 1, i, j)
+
+
+def sym_trace(indptr, indices, data):
+    indptr, indices, data = _sym_arrays(indptr, indices, data)
+    f = lib().or_sym_csr_trace_f64 if data.dtype == np.float64 else lib().or_sym_csr_trace_f32
+    return data.dtype.type(f(p(indptr), p(indices), p(data), len(indptr) - 1))
+
+
+def sym_quadratic_form(indptr, indices, data, x):
+    indptr, indices, data = _sym_arrays(indptr, indices, data)
+    x = np.ascontiguousarray(x, dtype=data.dtype)
+    f = (lib().or_sym_csr_quadratic_form_f64 if data.dtype == np.float64
+         else lib().or_sym_csr_quadratic_form_f32)
+    return data.dtype.type(f(p(indptr), p(indices), p(data), len(indptr) - 1, p(x)))
+
+
+def sym_rank1_update(indptr, indices, data, x, alpha):
+    """New (indptr, indices, data) of sym_csr_rank1_update."""
+    indptr, indices, data = _sym_arrays(indptr, indices, data)
+    n = len(indptr) - 1
+    x = np.ascontiguousarray(x, dtype=data.dtype)
+    f = (lib().or_sym_csr_rank1_update_f64 if data.dtype == np.float64
+         else lib().or_sym_csr_rank1_update_f32)
+    cap = max(n * (n + 1) // 2, 1)
+    ip = np.empty(n + 1, dtype=np.uint64)
+    ix = np.empty(cap, dtype=np.uint64)
+    dv = np.empty(cap, dtype=data.dtype)
+    nnz = f(p(indptr), p(indices), p(data), n, p(x), alpha, p(ip), p(ix), p(dv))
+    return ip, ix[:nnz].copy(), dv[:nnz].copy()
+
+
+def sym_from_csr(indptr, indices, data, shape):
+    """SymCsrMatrix::from_csr on CSR arrays: ((indptr, indices, data), None) or (None, message)."""
+    indptr, indices, data = _sym_arrays(indptr, indices, data)
+    nr = int(shape[0])
+    ip = np.empty(nr + 1, dtype=np.uint64)
+    ix = np.empty(max(len(indices), 1), dtype=np.uint64)
+    dv = np.empty(max(len(indices), 1), dtype=data.dtype)
+    e = Err()
+    f = lib().or_sym_csr_from_csr_f64 if data.dtype == np.float64 else lib().or_sym_csr_from_csr_f32
+    rc = f(p(indptr), p(indices), p(data), nr, int(shape[1]), p(ip), p(ix), p(dv), C.byref(e))
+    if rc:
+        return None, e.msg.decode()
+    nnz = int(ip[-1])
+    return (ip, ix[:nnz].copy(), dv[:nnz].copy()), None

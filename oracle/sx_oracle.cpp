@@ -1169,3 +1169,217 @@ int or_cg_mixed_replace(const int64_t* indptr, const int32_t* indices, const dou
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ symmetric CSR (lower part)
+namespace {
+
+// SymCsrMatrix::new checks, sym_csr.rs:70-126, in that order.
+int sym_check(uint64_t data_len, const uint64_t* indptr, uint64_t indptr_len,
+              const uint64_t* indices, uint64_t nnz, uint64_t rows, uint64_t cols, or_err* err) {
+  if (rows != cols) return set_err(err, E_VALUE, value_msg("Symmetric matrix must be square"));
+  if (indptr_len != rows + 1)
+    return set_err(err, E_VALUE,
+                   value_msg("indptr length (" + std::to_string(indptr_len) +
+                             ") must be equal to rows + 1 (" + std::to_string(rows + 1) + ")"));
+  if (data_len != nnz)
+    return set_err(err, E_VALUE,
+                   value_msg("data length (" + std::to_string(data_len) +
+                             ") must match indices length (" + std::to_string(nnz) + ")"));
+  if (indptr[rows] != nnz)
+    return set_err(err, E_VALUE,
+                   value_msg("Last indptr value (" + std::to_string(indptr[rows]) +
+                             ") must equal nnz (" + std::to_string(nnz) + ")"));
+  for (uint64_t i = 0; i < rows; ++i) {
+    if (indptr[i] > indptr[i + 1] || indptr[i + 1] > nnz)
+      return set_err(err, E_INCONSISTENT_DATA, incons_msg("row pointers must be non-decreasing"));
+    for (uint64_t k = indptr[i]; k < indptr[i + 1]; ++k) {
+      const uint64_t c = indices[k];
+      if (c >= cols)
+        return set_err(err, E_INDEX_OUT_OF_BOUNDS,
+                       "Index (" + std::to_string(i) + ", " + std::to_string(c) +
+                           ") out of bounds for array with shape (" + std::to_string(rows) + ", " +
+                           std::to_string(cols) + ")",
+                       i, c, rows, cols);
+      if (c > i)
+        return set_err(err, E_VALUE,
+                       value_msg("Symmetric CSR should only store the lower triangular part"));
+    }
+  }
+  return ok(err);
+}
+
+// sym_csr_matvec, sym_ops.rs:69-87: y = 0; for each stored (i, j, v) in row
+// order: y_i = y_i + v x_j and, when i != j, y_j = y_j + v x_i.
+template <class T>
+void sym_matvec(const uint64_t* indptr, const uint64_t* indices, const T* data, uint64_t n,
+                const T* x, T* y) {
+  for (uint64_t i = 0; i < n; ++i) y[i] = T(0);
+  for (uint64_t i = 0; i < n; ++i)
+    for (uint64_t k = indptr[i]; k < indptr[i + 1]; ++k) {
+      const uint64_t c = indices[k];
+      const T v = data[k];
+      y[i] = y[i] + v * x[c];
+      if (i != c) y[c] = y[c] + v * x[i];
+    }
+}
+
+// sym_csr_trace, sym_ops.rs:321-334: the first diagonal entry of each row.
+template <class T>
+T sym_trace(const uint64_t* indptr, const uint64_t* indices, const T* data, uint64_t n) {
+  T t = T(0);
+  for (uint64_t i = 0; i < n; ++i)
+    for (uint64_t k = indptr[i]; k < indptr[i + 1]; ++k)
+      if (indices[k] == i) {
+        t = t + data[k];
+        break;
+      }
+  return t;
+}
+
+// sym_csr_quadratic_form, sym_ops.rs:275-282.
+template <class T>
+T sym_quad(const uint64_t* indptr, const uint64_t* indices, const T* data, uint64_t n, const T* x) {
+  std::vector<T> ax(n);
+  sym_matvec<T>(indptr, indices, data, n, x, ax.data());
+  T r = T(0);
+  for (uint64_t i = 0; i < n; ++i) r = r + x[i] * ax[i];
+  return r;
+}
+
+// sym_csr_rank1_update, sym_ops.rs:199-231: dense lower triangle (stored
+// entries, the last duplicate wins), + alpha x_i x_j, non-zeros kept.
+template <class T>
+uint64_t sym_rank1(const uint64_t* indptr, const uint64_t* indices, const T* data, uint64_t n,
+                   const T* x, T alpha, uint64_t* ip, uint64_t* ix, T* dv) {
+  std::vector<T> row(n);
+  uint64_t cnt = 0;
+  if (ip) ip[0] = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    std::fill(row.begin(), row.end(), T(0));
+    for (uint64_t k = indptr[i]; k < indptr[i + 1]; ++k) row[indices[k]] = data[k];
+    for (uint64_t j = 0; j <= i; ++j) {
+      const T update = alpha * x[i] * x[j];
+      const T v = row[j] + update;
+      if (v != T(0)) {
+        if (ix) {
+          ix[cnt] = j;
+          dv[cnt] = v;
+        }
+        ++cnt;
+      }
+    }
+    if (ip) ip[i + 1] = cnt;
+  }
+  return cnt;
+}
+
+// SymCsrMatrix::from_csr, sym_csr.rs:149-189, with is_symmetric (:197-225)
+// reading CsrMatrix::get's first match.
+template <class T>
+int sym_from_csr(const uint64_t* indptr, const uint64_t* indices, const T* data, uint64_t rows,
+                 uint64_t cols, uint64_t* ip, uint64_t* ix, T* dv, or_err* err) {
+  if (rows != cols) return set_err(err, E_VALUE, value_msg("Symmetric matrix must be square"));
+  const T tol = std::numeric_limits<T>::epsilon() * T(100.0);
+  for (uint64_t i = 0; i < rows; ++i)
+    for (uint64_t k = indptr[i]; k < indptr[i + 1]; ++k) {
+      const uint64_t j = indices[k];
+      const T other = csr_get<T>(indptr, indices, data, rows, cols, j, i);
+      const T diff = std::fabs(data[k] - other);
+      if (diff > tol)
+        return set_err(err, E_VALUE,
+                       value_msg("Matrix must be symmetric to convert to SymCSR format"));
+    }
+  uint64_t cnt = 0;
+  ip[0] = 0;
+  for (uint64_t i = 0; i < rows; ++i) {
+    for (uint64_t k = indptr[i]; k < indptr[i + 1]; ++k)
+      if (indices[k] <= i) {
+        ix[cnt] = indices[k];
+        dv[cnt] = data[k];
+        ++cnt;
+      }
+    ip[i + 1] = cnt;
+  }
+  return ok(err);
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_sym_csr_check(uint64_t data_len, const uint64_t* indptr, uint64_t indptr_len,
+                     const uint64_t* indices, uint64_t nnz, uint64_t nrows, uint64_t ncols,
+                     or_err* err) {
+  return sym_check(data_len, indptr, indptr_len, indices, nnz, nrows, ncols, err);
+}
+void or_sym_csr_matvec_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                           uint64_t n, const double* x, double* y) {
+  sym_matvec<double>(indptr, indices, data, n, x, y);
+}
+void or_sym_csr_matvec_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                           uint64_t n, const float* x, float* y) {
+  sym_matvec<float>(indptr, indices, data, n, x, y);
+}
+uint64_t or_sym_csr_nnz(const uint64_t* indptr, const uint64_t* indices, uint64_t nnz_stored,
+                        uint64_t n) {
+  // sym_csr.rs:254-268
+  uint64_t diag = 0;
+  for (uint64_t i = 0; i < n; ++i)
+    for (uint64_t k = indptr[i]; k < indptr[i + 1]; ++k)
+      if (indices[k] == i) {
+        ++diag;
+        break;
+      }
+  return diag + 2 * (nnz_stored - diag);
+}
+double or_sym_csr_get_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                          uint64_t n, uint64_t row, uint64_t col) {
+  // sym_csr.rs:280-298
+  if (row >= n || col >= n) return 0.0;
+  const uint64_t r = row < col ? col : row, c = row < col ? row : col;
+  for (uint64_t k = indptr[r]; k < indptr[r + 1]; ++k)
+    if (indices[k] == c) return data[k];
+  return 0.0;
+}
+double or_sym_csr_trace_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                            uint64_t n) {
+  return sym_trace<double>(indptr, indices, data, n);
+}
+float or_sym_csr_trace_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                           uint64_t n) {
+  return sym_trace<float>(indptr, indices, data, n);
+}
+double or_sym_csr_quadratic_form_f64(const uint64_t* indptr, const uint64_t* indices,
+                                     const double* data, uint64_t n, const double* x) {
+  return sym_quad<double>(indptr, indices, data, n, x);
+}
+float or_sym_csr_quadratic_form_f32(const uint64_t* indptr, const uint64_t* indices,
+                                    const float* data, uint64_t n, const float* x) {
+  return sym_quad<float>(indptr, indices, data, n, x);
+}
+uint64_t or_sym_csr_rank1_update_f64(const uint64_t* indptr, const uint64_t* indices,
+                                     const double* data, uint64_t n, const double* x,
+                                     double alpha, uint64_t* indptr_out, uint64_t* indices_out,
+                                     double* data_out) {
+  return sym_rank1<double>(indptr, indices, data, n, x, alpha, indptr_out, indices_out, data_out);
+}
+uint64_t or_sym_csr_rank1_update_f32(const uint64_t* indptr, const uint64_t* indices,
+                                     const float* data, uint64_t n, const float* x, float alpha,
+                                     uint64_t* indptr_out, uint64_t* indices_out,
+                                     float* data_out) {
+  return sym_rank1<float>(indptr, indices, data, n, x, alpha, indptr_out, indices_out, data_out);
+}
+int or_sym_csr_from_csr_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                            uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
+                            uint64_t* indices_out, double* data_out, or_err* err) {
+  return sym_from_csr<double>(indptr, indices, data, nrows, ncols, indptr_out, indices_out,
+                              data_out, err);
+}
+int or_sym_csr_from_csr_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                            uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
+                            uint64_t* indices_out, float* data_out, or_err* err) {
+  return sym_from_csr<float>(indptr, indices, data, nrows, ncols, indptr_out, indices_out,
+                             data_out, err);
+}
+
+}  // extern "C"

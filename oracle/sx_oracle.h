@@ -140,6 +140,51 @@ int or_cg_mixed_replace(const int64_t* indptr, const int32_t* indices, const dou
 double or_true_rel_residual(const int64_t* indptr, const int32_t* indices, const double* data,
                             int64_t n, const double* b, const double* x);
 
+/* ---- symmetric CSR, lower triangle stored (sym_csr.rs, sym_ops.rs) ---- */
+/* SymCsrMatrix::new validation (sym_csr.rs:64-134); 0 = Ok.  A decreasing
+ * or overrunning indptr (a slice panic in Rust) is InconsistentData. */
+int or_sym_csr_check(uint64_t data_len, const uint64_t* indptr, uint64_t indptr_len,
+                     const uint64_t* indices, uint64_t nnz, uint64_t nrows, uint64_t ncols,
+                     or_err* err);
+/* sym_csr_matvec (sym_ops.rs:56-90). */
+void or_sym_csr_matvec_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                           uint64_t n, const double* x, double* y);
+void or_sym_csr_matvec_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                           uint64_t n, const float* x, float* y);
+/* SymCsrMatrix::nnz (sym_csr.rs:254-268), get (sym_csr.rs:280-298). */
+uint64_t or_sym_csr_nnz(const uint64_t* indptr, const uint64_t* indices, uint64_t nnz_stored,
+                        uint64_t n);
+double or_sym_csr_get_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                          uint64_t n, uint64_t row, uint64_t col);
+/* sym_csr_trace (sym_ops.rs:317-335), sym_csr_quadratic_form (:271-283). */
+double or_sym_csr_trace_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                            uint64_t n);
+float or_sym_csr_trace_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                           uint64_t n);
+double or_sym_csr_quadratic_form_f64(const uint64_t* indptr, const uint64_t* indices,
+                                     const double* data, uint64_t n, const double* x);
+float or_sym_csr_quadratic_form_f32(const uint64_t* indptr, const uint64_t* indices,
+                                    const float* data, uint64_t n, const float* x);
+/* sym_csr_rank1_update (sym_ops.rs:179-233): returns the new nnz; with
+ * indptr_out (n + 1) / indices_out / data_out non-null (room for n(n+1)/2
+ * entries) also the new arrays. */
+uint64_t or_sym_csr_rank1_update_f64(const uint64_t* indptr, const uint64_t* indices,
+                                     const double* data, uint64_t n, const double* x,
+                                     double alpha, uint64_t* indptr_out, uint64_t* indices_out,
+                                     double* data_out);
+uint64_t or_sym_csr_rank1_update_f32(const uint64_t* indptr, const uint64_t* indices,
+                                     const float* data, uint64_t n, const float* x, float alpha,
+                                     uint64_t* indptr_out, uint64_t* indices_out,
+                                     float* data_out);
+/* SymCsrMatrix::from_csr (sym_csr.rs:149-225) on CSR arrays: returns 0 and
+ * the lower part (room for nnz entries) or an error (ValueError). */
+int or_sym_csr_from_csr_f64(const uint64_t* indptr, const uint64_t* indices, const double* data,
+                            uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
+                            uint64_t* indices_out, double* data_out, or_err* err);
+int or_sym_csr_from_csr_f32(const uint64_t* indptr, const uint64_t* indices, const float* data,
+                            uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
+                            uint64_t* indices_out, float* data_out, or_err* err);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,7 +33,9 @@ SX_API_CSR_MATRIX, SX_API_CSR_ARRAY = 0, 1
 SX_OP_CSR, SX_OP_IDENTITY, SX_OP_SCALED_IDENTITY, SX_OP_DIAGONAL = 0, 1, 2, 3
 SX_OP_JACOBI, SX_OP_IC0, SX_OP_FSAI, SX_OP_HOST = 4, 5, 6, 7
 SX_IC0_REFERENCE, SX_IC0_TEXTBOOK = 0, 1
+SX_OP_ZERO, SX_OP_SUM, SX_OP_PRODUCT, SX_OP_SYM_CSR = 8, 9, 10, 11
 SX_SPMV_EXACT = 1
+SX_SPMV_SYM_HALF = 2
 
 
 class ErrorInfo(C.Structure):
@@ -194,6 +196,14 @@ _SIGS = {
     "sx_op_sum": (c_int, [ctx_t, op_t, op_t, P(op_t)]),
     "sx_op_product": (c_int, [ctx_t, op_t, op_t, P(op_t)]),
     "sx_op_has_adjoint": (c_int, [op_t, P(c_int)]),
+    "sx_sym_csr_new": (c_int, [ctx_t, c_int, c_vp, c_u64, c_vp, c_u64, c_vp, c_u64, c_u64, c_u64, P(op_t)]),
+    "sx_sym_csr_from_csr": (c_int, [ctx_t, op_t, P(op_t)]),
+    "sx_sym_csr_info": (c_int, [ctx_t, op_t, P(c_u64), P(c_u64)]),
+    "sx_sym_csr_download": (c_int, [ctx_t, op_t, c_vp, c_vp, c_vp]),
+    "sx_sym_csr_to_csr": (c_int, [ctx_t, op_t, P(op_t)]),
+    "sx_sym_csr_trace": (c_int, [ctx_t, op_t, c_vp]),
+    "sx_sym_csr_quadratic_form": (c_int, [ctx_t, op_t, c_vp, c_u64, c_int, c_vp]),
+    "sx_sym_csr_rank1_update": (c_int, [ctx_t, op_t, c_vp, c_u64, c_dbl, c_int]),
     "sx_precond_jacobi": (c_int, [ctx_t, op_t, P(op_t)]),
     "sx_precond_jacobi_from_diagonal": (c_int, [ctx_t, c_int, c_vp, c_u64, P(op_t)]),
     "sx_precond_ic0": (c_int, [ctx_t, op_t, c_int, P(op_t)]),

@@ -28,6 +28,7 @@ SOURCES = [
     "sx_batched.cu",
     "sx_noalloc.cu",
     "sx_gnn.cu",
+    "sx_sym.cu",
     "sx_gen.cpp",
 ]
 

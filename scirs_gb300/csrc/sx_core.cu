@@ -786,6 +786,7 @@ void destroy_op_internal(sx_op op) {
   dev_free(op->diag);
   dev_free(op->work);
   if (op->transpose) destroy_op_internal(op->transpose);
+  if (op->sym_low) destroy_op_internal(op->sym_low);
   if (op->ic0) ic0_destroy(op->ic0);
   delete op;
 }
@@ -1078,6 +1079,14 @@ int sx_csr_from_raw(sx_ctx ctx, sx_dtype dtype, sx_csr_api api, const uint64_t* 
                         ") must equal data length (" + std::to_string(nnz) + ")");
         break;
       }
+      // CsrArray::new accepts a decreasing indptr; an entry above the data
+      // length would make a row run past the arrays (a slice panic in the
+      // reference at first use), so it is refused here
+      if (hm[1] > nnz) {
+        rc = err_incons("indptr entry (" + std::to_string(hm[1]) + ") exceeds data length (" +
+                        std::to_string(nnz) + ")");
+        break;
+      }
     }
     if (hm[1] > kI32Max) { rc = err_cast(hm[1]); break; }
     if (ncols > kI32Max) { rc = err_cast(ncols); break; }
@@ -1339,7 +1348,8 @@ extern "C" {
 
 int sx_csr_get(sx_ctx ctx, sx_op a, uint64_t i, uint64_t j, void* out) {
   if (!ctx || !a || !out) return err_arg("null argument");
-  if (a->kind != SX_OP_CSR) return err_arg("not a CSR operator");
+  // a symmetric operator's merged rows give SymCsrMatrix::get's first match
+  if (a->kind != SX_OP_CSR && a->kind != SX_OP_SYM_CSR) return err_arg("not a CSR operator");
   const size_t w = elt_size(a->dtype);
   // csr.rs:35-37: out-of-range positions read as zero
   if (i >= (uint64_t)a->csr.nrows || j >= (uint64_t)a->csr.ncols) {
@@ -1547,6 +1557,7 @@ int sx_op_rmatvec(sx_ctx ctx, sx_op op, const void* x, uint64_t x_len, void* y, 
     case SX_OP_JACOBI:
     case SX_OP_IC0:
     case SX_OP_FSAI:
+    case SX_OP_SYM_CSR:
       // self-adjoint operators: rmatvec = matvec (interface.rs:86-88,
       // :121-124, :164-167; preconditioners.rs:88-91; ic.rs:227-230)
       return sx_op_matvec(ctx, op, x, x_len, y, mem);

@@ -91,6 +91,8 @@ struct sx_op_s {
                                       // SUM: B x; PRODUCT: B x)
   sx_op_s* left = nullptr;            // SUM / PRODUCT operands, borrowed
   sx_op_s* right = nullptr;
+  sx_op_s* sym_low = nullptr;         // SYM_CSR: the stored lower triangle (owned);
+                                      // csr holds the merged rows applied by SpMV
   uint64_t serial = 0;                // unique id, keys the solver graph cache
 };
 
@@ -177,6 +179,7 @@ int ic0_health(sx_ctx ctx, sx_op op);
 // Cached transpose of a CSR operator (rmatvec, FSAI's G^T).
 int ensure_transpose(sx_ctx ctx, sx_op a);
 int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out);
+int sym_half_spmv(sx_ctx ctx, sx_op a, const void* x, void* y);  // sx_sym.cu
 void destroy_op_internal(sx_op op);
 
 // Grid geometry for the vector kernels (fixed per device -> deterministic

@@ -100,16 +100,33 @@ __global__ void __launch_bounds__(kBlock) k_sum_epi(int64_t n, T* y, const T* __
 
 constexpr int kSpmvItems = 8;
 
-// Blocks of kBlock threads one SM holds at once for kernel Kern (queried once).
+// Blocks of kBlock threads one SM holds at once for kernel Kern with `smem`
+// bytes of dynamic shared memory, after opting Kern in to that much (queried
+// once per kernel); -1 if it cannot run.  The cache is keyed by the kernel
+// itself: every translation unit that instantiates a kernel template holds
+// its own copy of the kernel, and the shared-memory opt-in belongs to that
+// copy, so a cache shared by all units (keyed by template types) would leave
+// the other units' copies without it.
 template <auto Kern>
-int resident_blocks() {
+int resident_blocks_smem(int smem) {
   static int cached = 0;
   if (!cached) {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, Kern, kBlock, 0) != cudaSuccess || nb < 1) nb = 1;
+    if ((smem > 48 * 1024 && cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                                 cudaSuccess) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, Kern, kBlock, smem) != cudaSuccess || nb < 1) {
+      nb = -1;
+      (void)cudaGetLastError();  // a refused query is a fallback, not an error of the next launch
+    }
     cached = nb;
   }
   return cached;
+}
+// Blocks of kBlock threads one SM holds at once for kernel Kern (queried once).
+template <auto Kern>
+int resident_blocks() {
+  const int nb = resident_blocks_smem<Kern>(0);
+  return nb > 0 ? nb : 1;
 }
 
 // Window sizes, ring depths and gather pipelining of the windowed SpMV;
@@ -129,18 +146,9 @@ template <> struct WinShape<double, 2> { static constexpr int kCap = 256, kStage
 // dynamic shared memory once per instantiation); -1 if it cannot run.
 template <typename T, int V, class Epi, bool FMA>
 int win_resident_blocks() {
-  static int cached = 0;
-  if (!cached) {
-    using Sh = WinShape<T, V>;
-    constexpr auto kern = spmv_win_kernel<T, Sh::kCap, Sh::kStages, Epi, FMA, Sh::kPipe>;
-    constexpr int smem = WinCfg<T, Sh::kCap, Sh::kStages, FMA>::kSmem;
-    int nb = 0;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kBlock, smem) != cudaSuccess || nb < 1)
-      nb = -1;
-    cached = nb;
-  }
-  return cached;
+  using Sh = WinShape<T, V>;
+  constexpr auto kern = spmv_win_kernel<T, Sh::kCap, Sh::kStages, Epi, FMA, Sh::kPipe>;
+  return resident_blocks_smem<kern>(WinCfg<T, Sh::kCap, Sh::kStages, FMA>::kSmem);
 }
 
 template <typename T, int V, class Epi, bool FMA>
@@ -335,6 +343,7 @@ int launch_apply(sx_ctx ctx, sx_op op, const T* x, T* y, Epi epi) {
   constexpr bool kFma = !EXACT && sizeof(T) == 8;
   switch (op->kind) {
     case SX_OP_CSR:
+    case SX_OP_SYM_CSR:  // the merged rows: stored row k, then column k below the diagonal
       return launch_csr<T, Epi, kFma>(ctx, op->csr, x, y, epi);
     case SX_OP_SUM: {
       // y = A x, w = B x, y = y + w with the epilogue

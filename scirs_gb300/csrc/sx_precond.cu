@@ -20,6 +20,8 @@ namespace sx {
 int ic0_apply(sx_ctx ctx, sx_op op, const void* x, void* y);  // sx_ic0.cu
 
 int spmv_device(sx_ctx ctx, sx_op a, const void* x, void* y, unsigned flags) {
+  if (a->kind == SX_OP_SYM_CSR && (flags & SX_SPMV_SYM_HALF) && !(flags & SX_SPMV_EXACT))
+    return sym_half_spmv(ctx, a, x, y);
   // SX_SPMV_EXACT keeps the reference's per-row rounding (bit-exact); without
   // it, FP64 rows are summed with fused multiply-adds (a few ulp per row)
   if (a->dtype == SX_F64) {
@@ -41,6 +43,10 @@ extern "C" int sx_spmv_kernel(sx_ctx ctx, sx_op a, unsigned flags, char* buf, ui
   const bool fma = !exact && w == 8;
   switch (a->kind) {
     case SX_OP_CSR: name = spmv_kernel_name(ctx, a->csr, w, fma, false); break;
+    case SX_OP_SYM_CSR:
+      name = (flags & SX_SPMV_SYM_HALF) && !exact ? std::string("k_sym_half")
+                                                  : spmv_kernel_name(ctx, a->csr, w, fma, false);
+      break;
     case SX_OP_FSAI:
       name = std::string("G^T: ") + spmv_kernel_name(ctx, a->transpose->csr, w, fma, !exact) +
              "; G: " + spmv_kernel_name(ctx, a->csr, w, fma, !exact);

@@ -213,6 +213,106 @@ class Operator:
         return d
 
 
+
+class SymCsrMatrix(Operator):
+    """SymCsrMatrix (sym_csr.rs:24-337): the lower triangle is stored, the
+    operator applies the full symmetric matrix."""
+
+    def nnz_stored(self) -> int:
+        """SymCsrMatrix::nnz_stored (sym_csr.rs:241-243)."""
+        a, _ = self._info()
+        return a
+
+    @property
+    def nnz(self) -> int:
+        """SymCsrMatrix::nnz (sym_csr.rs:254-268)."""
+        _, b = self._info()
+        return b
+
+    def _info(self):
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(L.lib.sx_sym_csr_info(self.ctx.handle, self.handle, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def to_arrays(self):
+        """The stored (indptr, indices, data): the public fields of sym_csr.rs:28-34."""
+        n = self.shape[0]
+        nnz = self.nnz_stored()
+        indptr = np.empty(n + 1, dtype=np.uint64)
+        indices = np.empty(nnz, dtype=np.uint64)
+        data = np.empty(nnz, dtype=self.dtype)
+        _check(L.lib.sx_sym_csr_download(self.ctx.handle, self.handle, _ptr(indptr), _ptr(indices), _ptr(data)))
+        return indptr, indices, data
+
+    def to_csr(self) -> Operator:
+        """SymCsrMatrix::to_csr (sym_csr.rs:305-337)."""
+        h = L.op_t()
+        _check(L.lib.sx_sym_csr_to_csr(self.ctx.handle, self.handle, C.byref(h)))
+        return Operator(self.ctx, h)
+
+    def to_dense(self) -> np.ndarray:
+        """SymCsrMatrix::to_dense (sym_csr.rs:344-366): stored entries (the last
+        duplicate wins), then the upper triangle mirrored from the lower."""
+        indptr, indices, data = self.to_arrays()
+        n = self.shape[0]
+        d = np.zeros((n, n), dtype=self.dtype)
+        for i in range(n):
+            for k in range(int(indptr[i]), int(indptr[i + 1])):
+                d[i, int(indices[k])] = data[k]
+        for i in range(n):
+            for j in range(i):
+                d[j, i] = d[i, j]
+        return d
+
+    def astype(self, dtype) -> "SymCsrMatrix":
+        indptr, indices, data = self.to_arrays()
+        return sym_csr_matrix(self.ctx, data.astype(dtype), indptr, indices, self.shape, dtype=dtype)
+
+
+def sym_csr_matrix(ctx: Context, data, indptr, indices, shape, dtype=np.float64) -> SymCsrMatrix:
+    """SymCsrMatrix::new(data, indptr, indices, shape) (sym_csr.rs:64-134)."""
+    data = np.ascontiguousarray(data, dtype=dtype)
+    indptr = np.ascontiguousarray(indptr, dtype=np.uint64)
+    indices = np.ascontiguousarray(indices, dtype=np.uint64)
+    h = L.op_t()
+    _check(L.lib.sx_sym_csr_new(ctx.handle, _dtype_code(dtype), _ptr(data), len(data), _ptr(indptr),
+                                len(indptr), _ptr(indices), len(indices), int(shape[0]), int(shape[1]),
+                                C.byref(h)))
+    return SymCsrMatrix(ctx, h)
+
+
+def sym_csr_from_csr(a: Operator) -> SymCsrMatrix:
+    """SymCsrMatrix::from_csr(matrix) (sym_csr.rs:149-189)."""
+    h = L.op_t()
+    _check(L.lib.sx_sym_csr_from_csr(a.ctx.handle, a.handle, C.byref(h)))
+    return SymCsrMatrix(a.ctx, h)
+
+
+def sym_csr_matvec(a: SymCsrMatrix, x) -> np.ndarray:
+    """sym_csr_matvec(matrix, x) (sym_ops.rs:56-90), bit for bit."""
+    return a.matvec(x)
+
+
+def sym_csr_quadratic_form(a: SymCsrMatrix, x):
+    """sym_csr_quadratic_form(matrix, x) (sym_ops.rs:271-283), bit for bit."""
+    x = np.ascontiguousarray(x, dtype=a.dtype)
+    out = np.zeros(1, dtype=a.dtype)
+    _check(L.lib.sx_sym_csr_quadratic_form(a.ctx.handle, a.handle, _ptr(x), x.size, L.SX_MEM_HOST, _ptr(out)))
+    return out[0]
+
+
+def sym_csr_trace(a: SymCsrMatrix):
+    """sym_csr_trace(matrix) (sym_ops.rs:317-335), bit for bit."""
+    out = np.zeros(1, dtype=a.dtype)
+    _check(L.lib.sx_sym_csr_trace(a.ctx.handle, a.handle, _ptr(out)))
+    return out[0]
+
+
+def sym_csr_rank1_update(a: SymCsrMatrix, x, alpha) -> None:
+    """sym_csr_rank1_update(matrix, x, alpha) (sym_ops.rs:179-233), in place."""
+    x = np.ascontiguousarray(x, dtype=a.dtype)
+    _check(L.lib.sx_sym_csr_rank1_update(a.ctx.handle, a.handle, _ptr(x), x.size, float(alpha), L.SX_MEM_HOST))
+
 # ------------------------------------------------------------ construction
 def csr_matrix(ctx: Context, data, rows, cols, shape, dtype=np.float64) -> Operator:
     """CsrMatrix::new(data, rows, cols, shape) (csr.rs:92-160)."""
@@ -270,10 +370,11 @@ def _from_raw(ctx, data, indptr, indices, shape, dtype, api):
     return Operator(ctx, h)
 
 
-def spmv_kernel(op: Operator, exact: bool = True) -> str:
+def spmv_kernel(op: Operator, exact: bool = True, sym_half: bool = False) -> str:
     """Name of the SpMV kernel the library launches for `op` (diagnostics)."""
     buf = C.create_string_buffer(256)
-    _check(L.lib.sx_spmv_kernel(op.ctx.handle, op.handle, L.SX_SPMV_EXACT if exact else 0, buf, 256))
+    flags = (L.SX_SPMV_EXACT if exact else 0) | (L.SX_SPMV_SYM_HALF if sym_half else 0)
+    _check(L.lib.sx_spmv_kernel(op.ctx.handle, op.handle, flags, buf, 256))
     return buf.value.decode()
 
 

@@ -242,6 +242,43 @@ int main() {
     }
     CHECK(threw);
   });
+  // sym_csr.rs:498-531 test_sym_csr_creation, sym_ops.rs:387-459 matvec /
+  // rank-1 update / quadratic form / trace / comparison with the full CSR
+  run("sym_csr_creation_and_ops", [] {
+    auto sym = SymCsrMatrix<double>::create({2, 1, 2, 3, 1}, {0, 1, 3, 5}, {0, 0, 1, 1, 2}, {3, 3});
+    CHECK((sym.shape() == std::pair<size_t, size_t>(3, 3)));
+    CHECK(sym.nnz_stored() == 5);
+    CHECK(sym.nnz() == 7);
+    CHECK(sym.get(0, 0) == 2.0 && sym.get(0, 1) == 1.0 && sym.get(1, 0) == 1.0);
+    CHECK(sym.get(1, 1) == 2.0 && sym.get(1, 2) == 3.0 && sym.get(2, 1) == 3.0);
+    auto y = sym_csr_matvec(sym, {1.0, 2.0, 3.0});
+    CHECK((y == std::vector<double>{4, 14, 9}));
+    CHECK(sym_csr_quadratic_form(sym, {1.0, 2.0, 3.0}) == 59.0);
+    CHECK(sym_csr_trace(sym) == 5.0);
+    auto full = sym.to_csr();
+    auto yf = full.matvec({1.0, 2.0, 3.0});
+    for (int i = 0; i < 3; ++i) NEAR(yf[i], y[i], 1e-12);
+    sym_csr_rank1_update(sym, {1.0, 0.0, 0.0}, 3.0);
+    CHECK(sym.get(0, 0) == 5.0 && sym.get(0, 1) == 1.0 && sym.get(1, 1) == 2.0);
+    CHECK(sym.get(1, 2) == 3.0 && sym.get(2, 2) == 1.0);
+  });
+  // sym_csr.rs:534-565 test_sym_csr_from_standard
+  run("sym_csr_from_standard", [] {
+    auto csr = CsrMatrix<double>::create({2, 1, 1, 2, 3, 3, 1}, {0, 0, 1, 1, 1, 2, 2}, {0, 1, 0, 1, 2, 1, 2},
+                                         {3, 3});
+    auto sym = SymCsrMatrix<double>::from_csr(csr);
+    auto dense = sym.to_csr().to_dense();
+    CHECK((dense == std::vector<std::vector<double>>{{2, 1, 0}, {1, 2, 3}, {0, 3, 1}}));
+    auto bad = CsrMatrix<double>::create({2, 1, 1, 2, 3, 3, 1}, {0, 0, 1, 1, 2, 2, 2}, {0, 1, 0, 1, 0, 1, 2},
+                                         {3, 3});
+    try {
+      SymCsrMatrix<double>::from_csr(bad);
+      CHECK(false);
+    } catch (const SparseError& e) {
+      CHECK(e.variant() == "ValueError");
+      CHECK(std::string(e.what()) == "Value error: Matrix must be symmetric to convert to SymCSR format");
+    }
+  });
   // errors carry the reference's variants and messages (csr.rs:107-119)
   run("construction_errors", [] {
     try {
