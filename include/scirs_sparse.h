@@ -277,9 +277,23 @@ typedef enum {
   SX_MSG_BREAKDOWN_RHAT_V = 5,    /* "BiCGSTAB breakdown: (r_hat, v) ≈ 0" */
   SX_MSG_BREAKDOWN_ALPHA = 6,     /* "BiCGSTAB breakdown: alpha is not finite" */
   SX_MSG_BREAKDOWN_TT = 7,        /* "BiCGSTAB breakdown: (t, t) ≈ 0" */
-  SX_MSG_BREAKDOWN_OMEGA = 8      /* "BiCGSTAB breakdown: omega is not finite or too small" */
+  SX_MSG_BREAKDOWN_OMEGA = 8,     /* "BiCGSTAB breakdown: omega is not finite or too small" */
+  SX_MSG_BICG_PQ = 9,             /* "BiCG breakdown: (p_star, q) ≈ 0"       iterative.rs:276 */
+  SX_MSG_BICG_RHO = 10,           /* "BiCG breakdown: rho ≈ 0"               iterative.rs:321 */
+  SX_MSG_CGS_RHO = 11,            /* "CGS breakdown: rho ≈ 0"                cgs.rs:94 */
+  SX_MSG_CGS_SIGMA = 12,          /* "CGS breakdown: sigma ≈ 0"              cgs.rs:131 */
+  SX_MSG_QMR_INITIAL = 13,        /* "Converged at initial guess"            qmr.rs:105 */
+  SX_MSG_QMR_RHO = 14,            /* "Breakdown: rho = 0"                    qmr.rs:124 */
+  SX_MSG_QMR_PQ = 15,             /* "Breakdown: <p_tilde, q> = 0"           qmr.rs:184 */
+  SX_MSG_QMR_CONVERGED = 16,      /* "Converged in {iterations} iterations"  qmr.rs:233 */
+  SX_MSG_QMR_OMEGA = 17,          /* "Breakdown: omega = 0"                  qmr.rs:244 */
+  SX_MSG_QMR_MAX_ITER = 18,       /* "Did not converge in {max_iter} iterations. Residual: {r}" qmr.rs:255 */
+  SX_MSG_ZERO_RHS = 19,           /* "System has zero right-hand side"       minres.rs:99 */
+  SX_MSG_ZERO_RESIDUAL = 20       /* "Initial residual is zero"              minres.rs:128 */
 } sx_message;
-/* The exact message strings of the reference (UTF-8). */
+/* The exact message strings of the reference (UTF-8); the two messages with
+ * fields read "{iterations}" / "{max_iter}" / "{r}" here (sx_iter_message
+ * fills them). */
 const char* sx_message_string(int message);
 
 /* IterationResult (iterative.rs:8-14); x is returned through x_out. */
@@ -289,6 +303,11 @@ typedef struct {
   int converged;
   int message; /* sx_message */
 } sx_iter_result;
+
+/* The result's message as the reference formats it, with the iteration
+ * count and the residual (Rust `{}` formatting of an f64 / f32 by dtype) put
+ * into the two QMR messages; NUL-terminated into buf[len]. */
+int sx_iter_message(const sx_iter_result* res, int dtype, char* buf, uint64_t len);
 
 /* CGOptions (iterative.rs:17-35); defaults: 1000, 1e-8, 1e-12, none, none. */
 typedef struct {
@@ -330,6 +349,62 @@ int sx_bicgstab(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len,
 /* gmres (iterative.rs:641-816). */
 int sx_gmres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_gmres_options* opt,
              void* x_out, sx_mem mem, sx_iter_result* res);
+
+/* BiCGOptions (iterative.rs:164-185), also CGSOptions (cgs.rs:8) and the
+ * fields of QMROptions (qmr.rs:18-38); defaults: 1000, 1e-8, 1e-12, none,
+ * none, none. */
+typedef struct {
+  uint64_t max_iter;
+  double rtol;
+  double atol;
+  const void* x0;
+  sx_op left_preconditioner;
+  sx_op right_preconditioner;
+} sx_bicg_options;
+void sx_bicg_options_default(sx_bicg_options* o);
+/* bicg (iterative.rs:189-345): needs A's adjoint (rmatvec). */
+int sx_bicg(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_bicg_options* opt,
+            void* x_out, sx_mem mem, sx_iter_result* res);
+/* cgs (cgs.rs:15-193): only the right preconditioner is used. */
+int sx_cgs(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_bicg_options* opt,
+           void* x_out, sx_mem mem, sx_iter_result* res);
+/* qmr (qmr.rs:44-259): needs A's adjoint (and the preconditioners').
+ * DimensionMismatch{expected: b_len, found: rows} unless A is b_len x b_len. */
+int sx_qmr(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_bicg_options* opt,
+           void* x_out, sx_mem mem, sx_iter_result* res);
+
+/* MINRESOptions (minres.rs:17-35); defaults: 1000, 1e-8, 1e-12, none, none. */
+typedef struct {
+  uint64_t max_iter;
+  double rtol;
+  double atol;
+  const void* x0;
+  sx_op preconditioner;
+} sx_minres_options;
+void sx_minres_options_default(sx_minres_options* o);
+/* minres (minres.rs:66-257).  ComputationError "Indefinite preconditioner" /
+ * "Non-symmetric matrix" when r' M r < 0. */
+int sx_minres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_minres_options* opt,
+              void* x_out, sx_mem mem, sx_iter_result* res);
+
+/* LGMRESOptions (lgmres.rs:10-38); defaults: 500, 1e-8, 1e-8, 30, 3, none,
+ * none.  outer_k is accepted and, as in the reference, does not change the
+ * iteration (its augmentation vectors are never used). */
+typedef struct {
+  uint64_t max_iter;
+  double rtol;
+  double atol;
+  uint64_t inner_m;
+  uint64_t outer_k;
+  const void* x0;
+  sx_op preconditioner;
+} sx_lgmres_options;
+void sx_lgmres_options_default(sx_lgmres_options* o);
+/* lgmres (lgmres.rs:58-188, inner cycle 191-327): iterations = outer cycles; inner_m <= 64.
+ * LGMRESResult has no message: converged -> SX_MSG_CONVERGED, else
+ * SX_MSG_MAX_ITER. */
+int sx_lgmres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_lgmres_options* opt,
+              void* x_out, sx_mem mem, sx_iter_result* res);
 
 /* ------------------------------------------- mixed precision (no reference
  * counterpart; nearest dense analogue scirs2-linalg mixed_precision) */

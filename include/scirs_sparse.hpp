@@ -530,6 +530,38 @@ struct GMRESOptions {  // iterative.rs:614-634
   OperatorPtr<F> preconditioner;
 };
 
+template <class F>
+struct BiCGOptions {  // iterative.rs:164-185; also CGSOptions (cgs.rs:8) and QMROptions (qmr.rs:18-38)
+  size_t max_iter = 1000;
+  F rtol = F(1e-8);
+  F atol = F(1e-12);
+  std::vector<F> x0;
+  OperatorPtr<F> left_preconditioner;
+  OperatorPtr<F> right_preconditioner;
+};
+template <class F>
+using CGSOptions = BiCGOptions<F>;
+template <class F>
+using QMROptions = BiCGOptions<F>;
+template <class F>
+struct MINRESOptions {  // minres.rs:17-35
+  size_t max_iter = 1000;
+  F rtol = F(1e-8);
+  F atol = F(1e-12);
+  std::vector<F> x0;
+  OperatorPtr<F> preconditioner;
+};
+template <class F>
+struct LGMRESOptions {  // lgmres.rs:10-38
+  size_t max_iter = 500;
+  F rtol = F(1e-8);
+  F atol = F(1e-8);
+  size_t inner_m = 30;
+  size_t outer_k = 3;
+  std::vector<F> x0;
+  OperatorPtr<F> preconditioner;
+};
+
 namespace detail {
 // A device handle for any operator: its own, or a host callback for a
 // user-defined C++ LinearOperator (staged copies; the loop stays on the GPU).
@@ -572,8 +604,31 @@ IterationResult<F> result(std::vector<F>&& x, const sx_iter_result& r) {
   out.iterations = (size_t)r.iterations;
   out.residual_norm = (F)r.residual_norm;
   out.converged = r.converged != 0;
-  out.message = sx_message_string(r.message);
+  char buf[512];
+  check(sx_iter_message(&r, dtype_of<F>(), buf, sizeof(buf)));
+  out.message = buf;
   return out;
+}
+template <class F>
+IterationResult<F> bicg_like(int (*fn)(sx_ctx, sx_op, const void*, uint64_t, const sx_bicg_options*, void*,
+                                       sx_mem, sx_iter_result*),
+                             const LinearOperator<F>& a, const std::vector<F>& b, const BiCGOptions<F>& options,
+                             Context& c) {
+  auto A = device_ref(&a, c.get());
+  auto M1 = device_ref(options.left_preconditioner.get(), c.get());
+  auto M2 = device_ref(options.right_preconditioner.get(), c.get());
+  sx_bicg_options o;
+  sx_bicg_options_default(&o);
+  o.max_iter = options.max_iter;
+  o.rtol = (double)options.rtol;
+  o.atol = (double)options.atol;
+  o.x0 = options.x0.empty() ? nullptr : options.x0.data();
+  o.left_preconditioner = M1.h;
+  o.right_preconditioner = M2.h;
+  std::vector<F> x(a.shape().first);
+  sx_iter_result r;
+  check(fn(c.get(), A.h, b.data(), b.size(), &o, x.data(), SX_MEM_HOST, &r));
+  return result(std::move(x), r);
 }
 }  // namespace detail
 
@@ -634,6 +689,63 @@ IterationResult<F> gmres(const LinearOperator<F>& a, const std::vector<F>& b, GM
   std::vector<F> x(a.shape().first);
   sx_iter_result r;
   detail::check(sx_gmres(c.get(), A.h, b.data(), b.size(), &o, x.data(), SX_MEM_HOST, &r));
+  return detail::result(std::move(x), r);
+}
+
+// bicg (iterative.rs:189-345), cgs (cgs.rs:15-193), qmr (qmr.rs:44-259)
+template <class F>
+IterationResult<F> bicg(const LinearOperator<F>& a, const std::vector<F>& b, BiCGOptions<F> options,
+                        Context& c = Context::global()) {
+  return detail::bicg_like(&sx_bicg, a, b, options, c);
+}
+template <class F>
+IterationResult<F> cgs(const LinearOperator<F>& a, const std::vector<F>& b, CGSOptions<F> options,
+                       Context& c = Context::global()) {
+  return detail::bicg_like(&sx_cgs, a, b, options, c);
+}
+template <class F>
+IterationResult<F> qmr(const LinearOperator<F>& a, const std::vector<F>& b, QMROptions<F> options,
+                       Context& c = Context::global()) {
+  return detail::bicg_like(&sx_qmr, a, b, options, c);
+}
+
+// minres (minres.rs:66-257)
+template <class F>
+IterationResult<F> minres(const LinearOperator<F>& a, const std::vector<F>& b, MINRESOptions<F> options,
+                          Context& c = Context::global()) {
+  auto A = detail::device_ref(&a, c.get());
+  auto M = detail::device_ref(options.preconditioner.get(), c.get());
+  sx_minres_options o;
+  sx_minres_options_default(&o);
+  o.max_iter = options.max_iter;
+  o.rtol = (double)options.rtol;
+  o.atol = (double)options.atol;
+  o.x0 = options.x0.empty() ? nullptr : options.x0.data();
+  o.preconditioner = M.h;
+  std::vector<F> x(a.shape().first);
+  sx_iter_result r;
+  detail::check(sx_minres(c.get(), A.h, b.data(), b.size(), &o, x.data(), SX_MEM_HOST, &r));
+  return detail::result(std::move(x), r);
+}
+
+// lgmres (lgmres.rs:58-327); LGMRESResult carries no message
+template <class F>
+IterationResult<F> lgmres(const LinearOperator<F>& a, const std::vector<F>& b, LGMRESOptions<F> options,
+                          Context& c = Context::global()) {
+  auto A = detail::device_ref(&a, c.get());
+  auto M = detail::device_ref(options.preconditioner.get(), c.get());
+  sx_lgmres_options o;
+  sx_lgmres_options_default(&o);
+  o.max_iter = options.max_iter;
+  o.rtol = (double)options.rtol;
+  o.atol = (double)options.atol;
+  o.inner_m = options.inner_m;
+  o.outer_k = options.outer_k;
+  o.x0 = options.x0.empty() ? nullptr : options.x0.data();
+  o.preconditioner = M.h;
+  std::vector<F> x(a.shape().first);
+  sx_iter_result r;
+  detail::check(sx_lgmres(c.get(), A.h, b.data(), b.size(), &o, x.data(), SX_MEM_HOST, &r));
   return detail::result(std::move(x), r);
 }
 

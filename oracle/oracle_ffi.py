@@ -88,6 +88,11 @@ def lib():
             "or_cg_mixed_replace": (ip, [vp, vp, vp, i64, vp, C.POINTER(IROpt), C.c_double, vp,
                                          C.POINTER(IRRes)]),
             "or_true_rel_residual": (dbl, [vp, vp, vp, i64, vp, vp]),
+            "or_bicg": (ip, [vp, vp, u64, dbl, dbl, vp, vp, vp, vp, C.POINTER(Res), E]),
+            "or_cgs": (ip, [vp, vp, u64, dbl, dbl, vp, vp, vp, C.POINTER(Res), E]),
+            "or_qmr": (ip, [vp, vp, u64, dbl, dbl, vp, vp, vp, vp, C.POINTER(Res), E]),
+            "or_minres": (ip, [vp, vp, u64, dbl, dbl, vp, vp, vp, C.POINTER(Res), E]),
+            "or_lgmres": (ip, [vp, vp, u64, u64, dbl, dbl, vp, vp, vp, C.POINTER(Res), E]),
             "or_sym_csr_check": (ip, [u64, vp, u64, vp, u64, u64, u64, E]),
             "or_sym_csr_matvec_f64": (None, [vp, vp, vp, u64, vp, vp]),
             "or_sym_csr_matvec_f32": (None, [vp, vp, vp, u64, vp, vp]),
@@ -199,7 +204,34 @@ MESSAGES = [
     "BiCGSTAB breakdown: alpha is not finite",
     "BiCGSTAB breakdown: (t, t) ≈ 0",
     "BiCGSTAB breakdown: omega is not finite or too small",
+    "BiCG breakdown: (p_star, q) ≈ 0",
+    "BiCG breakdown: rho ≈ 0",
+    "CGS breakdown: rho ≈ 0",
+    "CGS breakdown: sigma ≈ 0",
+    "Converged at initial guess",
+    "Breakdown: rho = 0",
+    "Breakdown: <p_tilde, q> = 0",
+    "Converged in {iterations} iterations",
+    "Breakdown: omega = 0",
+    "Did not converge in {max_iter} iterations. Residual: {r}",
+    "System has zero right-hand side",
+    "Initial residual is zero",
 ]
+
+
+def rust_display(v) -> str:
+    """Rust's `{}` for an f64 / f32: shortest round-trip digits, no exponent."""
+    if np.isnan(v):
+        return "NaN"
+    if np.isinf(v):
+        return "-inf" if v < 0 else "inf"
+    return np.format_float_positional(v, unique=True, trim="-")
+
+
+def format_message(code, iterations, residual, f64=True):
+    m = MESSAGES[code]
+    r = rust_display(np.float64(residual) if f64 else np.float32(residual))
+    return m.replace("{iterations}", str(iterations)).replace("{max_iter}", str(iterations)).replace("{r}", r)
 
 
 def _solve(kind, a: Op, b, max_iter, rtol, atol, x0, m=None, m2=None, restart=30):
@@ -215,12 +247,23 @@ def _solve(kind, a: Op, b, max_iter, rtol, atol, x0, m=None, m2=None, restart=30
     elif kind == "bicgstab":
         m2h = m2.h if m2 is not None else None
         rc = L.or_bicgstab(a.h, p(b), max_iter, rtol, atol, p(x0a), mh, m2h, p(x), C.byref(r), C.byref(e))
-    else:
+    elif kind == "gmres":
         rc = L.or_gmres(a.h, p(b), max_iter, restart, rtol, atol, p(x0a), mh, p(x), C.byref(r), C.byref(e))
+    elif kind in ("bicg", "qmr"):
+        m2h = m2.h if m2 is not None else None
+        f = L.or_bicg if kind == "bicg" else L.or_qmr
+        rc = f(a.h, p(b), max_iter, rtol, atol, p(x0a), mh, m2h, p(x), C.byref(r), C.byref(e))
+    elif kind == "cgs":
+        rc = L.or_cgs(a.h, p(b), max_iter, rtol, atol, p(x0a), mh, p(x), C.byref(r), C.byref(e))
+    elif kind == "minres":
+        rc = L.or_minres(a.h, p(b), max_iter, rtol, atol, p(x0a), mh, p(x), C.byref(r), C.byref(e))
+    else:
+        rc = L.or_lgmres(a.h, p(b), max_iter, restart, rtol, atol, p(x0a), mh, p(x), C.byref(r), C.byref(e))
     if rc:
         raise ValueError(e.msg.decode())
     return dict(x=x, iterations=int(r.iterations), residual_norm=float(r.residual_norm),
-                converged=bool(r.converged), message=MESSAGES[r.message])
+                converged=bool(r.converged),
+                message=format_message(r.message, int(r.iterations), r.residual_norm, a.f64))
 
 
 def cg(a, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None, preconditioner=None):
@@ -233,6 +276,26 @@ def bicgstab(a, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None, left=None, rig
 
 def gmres(a, b, max_iter=1000, restart=30, rtol=1e-8, atol=1e-12, x0=None, preconditioner=None):
     return _solve("gmres", a, b, max_iter, rtol, atol, x0, preconditioner, restart=restart)
+
+
+def bicg(a, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None, left=None, right=None):
+    return _solve("bicg", a, b, max_iter, rtol, atol, x0, left, right)
+
+
+def cgs(a, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None, right=None):
+    return _solve("cgs", a, b, max_iter, rtol, atol, x0, right)
+
+
+def qmr(a, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None, left=None, right=None):
+    return _solve("qmr", a, b, max_iter, rtol, atol, x0, left, right)
+
+
+def minres(a, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None, preconditioner=None):
+    return _solve("minres", a, b, max_iter, rtol, atol, x0, preconditioner)
+
+
+def lgmres(a, b, max_iter=500, rtol=1e-8, atol=1e-8, inner_m=30, x0=None, preconditioner=None):
+    return _solve("lgmres", a, b, max_iter, rtol, atol, x0, preconditioner, restart=inner_m)
 
 
 def spmv_i32(indptr, indices, data, x):

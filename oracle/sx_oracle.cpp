@@ -56,6 +56,18 @@ enum Msg {
   M_BD_ALPHA = 6,
   M_BD_TT = 7,
   M_BD_OMEGA = 8,
+  M_BICG_PQ = 9,
+  M_BICG_RHO = 10,
+  M_CGS_RHO = 11,
+  M_CGS_SIGMA = 12,
+  M_QMR_INITIAL = 13,
+  M_QMR_RHO = 14,
+  M_QMR_PQ = 15,
+  M_QMR_CONVERGED = 16,
+  M_QMR_OMEGA = 17,
+  M_QMR_MAX_ITER = 18,
+  M_ZERO_RHS = 19,
+  M_ZERO_RESIDUAL = 20,
 };
 
 int set_err(or_err* e, int code, const std::string& msg, uint64_t v0 = 0, uint64_t v1 = 0,
@@ -280,6 +292,11 @@ struct or_op {
   uint64_t nrows = 0, ncols = 0;
   virtual void mv64(const double* x, double* y) const = 0;
   virtual void mv32(const float* x, float* y) const = 0;
+  // rmatvec: the preconditioners and elementwise operators are their own
+  // adjoints (interface.rs:86-88, :121-124, :164-167; preconditioners.rs:88-91;
+  // ic.rs:227-230)
+  virtual void rmv64(const double* x, double* y) const { mv64(x, y); }
+  virtual void rmv32(const float* x, float* y) const { mv32(x, y); }
 };
 
 namespace {
@@ -297,6 +314,13 @@ std::vector<F> op_apply(const or_op* op, const std::vector<F>& x) {
   op_matvec<F>(op, x.data(), y.data());
   return y;
 }
+template <class F>
+std::vector<F> op_rapply(const or_op* op, const std::vector<F>& x) {
+  std::vector<F> y(op->ncols);
+  if constexpr (sizeof(F) == 8) op->rmv64((const double*)x.data(), (double*)y.data());
+  else op->rmv32((const float*)x.data(), (float*)y.data());
+  return y;
+}
 
 // MatrixLinearOperator<F, CsrMatrix<F>> (interface.rs:232-296)
 struct CsrOp : or_op {
@@ -308,6 +332,37 @@ struct CsrOp : or_op {
   }
   void mv32(const float* x, float* y) const override {
     spmv<float>(indptr.data(), indices.data(), d32.data(), nrows, x, y);
+  }
+  // MatrixLinearOperator::rmatvec (interface.rs:281-285): the transposed
+  // matrix's matvec, transpose built once
+  mutable std::vector<uint64_t> tptr, tidx;
+  mutable std::vector<double> t64;
+  mutable std::vector<float> t32;
+  void build_t() const {
+    if (!tptr.empty()) return;
+    const uint64_t nnz = indptr[nrows];
+    tptr.assign(ncols + 1, 0);
+    tidx.resize(nnz);
+    t64.resize(nnz);
+    t32.resize(nnz);
+    for (uint64_t k = 0; k < nnz; ++k) tptr[indices[k] + 1] += 1;
+    for (uint64_t c = 0; c < ncols; ++c) tptr[c + 1] += tptr[c];
+    std::vector<uint64_t> cur(tptr.begin(), tptr.end() - 1);
+    for (uint64_t r = 0; r < nrows; ++r)
+      for (uint64_t k = indptr[r]; k < indptr[r + 1]; ++k) {
+        const uint64_t o = cur[indices[k]]++;
+        tidx[o] = r;
+        t64[o] = d64[k];
+        t32[o] = d32[k];
+      }
+  }
+  void rmv64(const double* x, double* y) const override {
+    build_t();
+    spmv<double>(tptr.data(), tidx.data(), t64.data(), ncols, x, y);
+  }
+  void rmv32(const float* x, float* y) const override {
+    build_t();
+    spmv<float>(tptr.data(), tidx.data(), t32.data(), ncols, x, y);
   }
 };
 
@@ -707,6 +762,355 @@ SolveOut<F> gmres(const or_op* a, const std::vector<F>& b, uint64_t max_iter, ui
   return o;
 }
 
+
+// bicg, iterative.rs:189-345: left preconditioner on r (and on A^T p*),
+// right preconditioner on r* (and on A p); no initial convergence test
+template <class F>
+SolveOut<F> bicg(const or_op* a, const std::vector<F>& b, uint64_t max_iter, F rtol, F atol,
+                 const F* x0, const or_op* m1, const or_op* m2) {
+  const uint64_t n = a->nrows;
+  SolveOut<F> o;
+  std::vector<F> x(n, F(0));
+  if (x0) x.assign(x0, x0 + n);
+  std::vector<F> ax = op_apply(a, x);
+  std::vector<F> r(n);
+  for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - ax[i];
+  std::vector<F> rs = r;
+  std::vector<F> z = m1 ? op_apply(m1, r) : r;
+  std::vector<F> zs = m2 ? op_apply(m2, rs) : rs;
+  std::vector<F> p = z, ps = zs;
+  F rho_old = dot(rs, z);
+  F bnorm = norm2(b);
+  F tol = std::fmax(atol, rtol * bnorm);
+  auto finish = [&](uint64_t it, F res, bool conv, int msg) {
+    o.x = x; o.iterations = it; o.residual_norm = res; o.converged = conv; o.message = msg;
+    return o;
+  };
+  const F e10 = eps10<F>();
+  uint64_t it = 0;
+  while (it < max_iter) {
+    std::vector<F> q = op_apply(a, p);
+    if (m2) q = op_apply(m2, q);
+    std::vector<F> qs = op_rapply(a, ps);
+    if (m1) qs = op_apply(m1, qs);
+    F den = dot(ps, q);
+    if (std::fabs(den) < e10) return finish(it, norm2(r), false, M_BICG_PQ);
+    F alpha = rho_old / den;
+    for (uint64_t i = 0; i < n; ++i) {
+      x[i] += alpha * p[i];
+      r[i] -= alpha * q[i];
+      rs[i] -= alpha * qs[i];
+    }
+    F rnorm = norm2(r);
+    if (rnorm <= tol) return finish(it + 1, rnorm, true, M_CONVERGED);
+    z = m1 ? op_apply(m1, r) : r;
+    zs = m2 ? op_apply(m2, rs) : rs;
+    F rho = dot(rs, z);
+    if (std::fabs(rho) < e10) return finish(it + 1, rnorm, false, M_BICG_RHO);
+    F beta = rho / rho_old;
+    for (uint64_t i = 0; i < n; ++i) {
+      p[i] = z[i] + beta * p[i];
+      ps[i] = zs[i] + beta * ps[i];
+    }
+    rho_old = rho;
+    ++it;
+  }
+  return finish(it, norm2(r), false, M_MAX_ITER);
+}
+
+// cgs, cgs.rs:15-193: right preconditioner applied to p, u + q and q
+template <class F>
+SolveOut<F> cgs(const or_op* a, const std::vector<F>& b, uint64_t max_iter, F rtol, F atol,
+                const F* x0, const or_op* m) {
+  const uint64_t n = a->nrows;
+  SolveOut<F> o;
+  std::vector<F> x(n, F(0));
+  if (x0) x.assign(x0, x0 + n);
+  std::vector<F> ax = op_apply(a, x);
+  std::vector<F> r(n);
+  for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - ax[i];
+  F rnorm = norm2(r);
+  F bnorm = norm2(b);
+  F tol = std::fmax(atol, rtol * bnorm);
+  auto finish = [&](uint64_t it, F res, bool conv, int msg) {
+    o.x = x; o.iterations = it; o.residual_norm = res; o.converged = conv; o.message = msg;
+    return o;
+  };
+  if (rnorm <= tol) return finish(0, rnorm, true, M_CONVERGED_INITIAL);
+  std::vector<F> rt = r, u(n, F(0)), p(n, F(0)), q(n, F(0)), uq(n);
+  F rho = F(1);
+  const F e10 = eps10<F>();
+  uint64_t it = 0;
+  while (it < max_iter) {
+    F rho_new = dot(rt, r);
+    if (std::fabs(rho_new) < e10) return finish(it, rnorm, false, M_CGS_RHO);
+    F beta = it == 0 ? F(0) : rho_new / rho;
+    for (uint64_t i = 0; i < n; ++i) {
+      u[i] = r[i] + beta * q[i];
+      p[i] = u[i] + beta * (q[i] + beta * p[i]);
+    }
+    std::vector<F> pp = m ? op_apply(m, p) : p;
+    std::vector<F> v = op_apply(a, pp);
+    F sigma = dot(rt, v);
+    if (std::fabs(sigma) < e10) return finish(it, rnorm, false, M_CGS_SIGMA);
+    F alpha = rho_new / sigma;
+    for (uint64_t i = 0; i < n; ++i) q[i] = u[i] - alpha * v[i];
+    for (uint64_t i = 0; i < n; ++i) uq[i] = u[i] + q[i];
+    std::vector<F> uqp = m ? op_apply(m, uq) : uq;
+    for (uint64_t i = 0; i < n; ++i) x[i] += alpha * uqp[i];
+    std::vector<F> qp = m ? op_apply(m, q) : q;
+    std::vector<F> aq = op_apply(a, qp);
+    for (uint64_t i = 0; i < n; ++i) r[i] -= alpha * (v[i] + aq[i]);
+    rho = rho_new;
+    ++it;
+    rnorm = norm2(r);
+    if (rnorm <= tol) break;
+  }
+  const bool conv = rnorm <= tol;
+  return finish(it, rnorm, conv, conv ? M_CONVERGED : M_MAX_ITER);
+}
+
+// qmr, qmr.rs:44-259 (a BiCGSTAB-like recurrence with the transposed
+// operator in the shadow sequence); tol = atol + rtol ||b||, strict tests
+template <class F>
+SolveOut<F> qmr(const or_op* a, const std::vector<F>& b, uint64_t max_iter, F rtol, F atol,
+                const F* x0, const or_op* m1, const or_op* m2) {
+  const uint64_t n = a->nrows;
+  SolveOut<F> o;
+  std::vector<F> x(n, F(0));
+  if (x0) x.assign(x0, x0 + n);
+  bool all_zero = true;
+  for (uint64_t i = 0; i < n; ++i) all_zero = all_zero && x[i] == F(0);
+  std::vector<F> r(n);
+  if (!all_zero) {
+    std::vector<F> ax = op_apply(a, x);
+    for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - ax[i];
+  } else {
+    r = b;
+  }
+  if (m1) r = op_apply(m1, r);
+  std::vector<F> rt = r;
+  std::vector<F> p(n, F(0)), pt(n, F(0)), q(n, F(0)), qt(n, F(0)), s(n), t;
+  F rho = F(1), rho_old, alpha = F(0), omega = F(1);
+  F bnorm = norm2(b);
+  F rnorm = norm2(r);
+  F tol = atol + rtol * bnorm;
+  auto finish = [&](uint64_t it, F res, bool conv, int msg) {
+    o.x = x; o.iterations = it; o.residual_norm = res; o.converged = conv; o.message = msg;
+    return o;
+  };
+  if (rnorm < tol) return finish(0, rnorm, true, M_QMR_INITIAL);
+  const F e10 = eps10<F>();
+  for (uint64_t it = 0; it < max_iter; ++it) {
+    rho_old = rho;
+    rho = dot(rt, r);
+    if (std::fabs(rho) < e10) return finish(it, rnorm, false, M_QMR_RHO);
+    F beta = it == 0 ? F(0) : (rho / rho_old) * (alpha / omega);
+    if (it == 0) p = r;
+    else for (uint64_t i = 0; i < n; ++i) p[i] = r[i] + (p[i] - q[i] * omega) * beta;
+    std::vector<F> pp = m2 ? op_apply(m2, p) : p;
+    q = op_apply(a, pp);
+    if (m1) q = op_apply(m1, q);
+    if (it == 0) pt = rt;
+    else for (uint64_t i = 0; i < n; ++i) pt[i] = rt[i] + (pt[i] - qt[i] * omega) * beta;
+    std::vector<F> ptp = m1 ? op_rapply(m1, pt) : pt;
+    qt = op_rapply(a, ptp);
+    if (m2) qt = op_rapply(m2, qt);
+    F dpq = dot(pt, q);
+    if (std::fabs(dpq) < e10) return finish(it, rnorm, false, M_QMR_PQ);
+    alpha = rho / dpq;
+    for (uint64_t i = 0; i < n; ++i) s[i] = r[i] - q[i] * alpha;
+    std::vector<F> sp = m2 ? op_apply(m2, s) : s;
+    t = op_apply(a, sp);
+    if (m1) t = op_apply(m1, t);
+    F tt = dot(t, t);
+    omega = tt == F(0) ? F(0) : dot(t, s) / tt;
+    for (uint64_t i = 0; i < n; ++i) x[i] = x[i] + pp[i] * alpha;
+    for (uint64_t i = 0; i < n; ++i) x[i] = x[i] + sp[i] * omega;
+    for (uint64_t i = 0; i < n; ++i) r[i] = s[i] - t[i] * omega;
+    rnorm = norm2(r);
+    if (rnorm < tol) return finish(it + 1, rnorm, true, M_QMR_CONVERGED);
+    if (std::fabs(omega) < std::numeric_limits<F>::epsilon())
+      return finish(it + 1, rnorm, false, M_QMR_OMEGA);
+  }
+  return finish(max_iter, rnorm, false, M_QMR_MAX_ITER);
+}
+
+// minres, minres.rs:66-257 (Paige-Saunders); error 1: "Indefinite
+// preconditioner", error 2: "Non-symmetric matrix" (ComputationError)
+template <class F>
+SolveOut<F> minres(const or_op* a, const std::vector<F>& b, uint64_t max_iter, F rtol, F atol,
+                   const F* x0, const or_op* m, int* error) {
+  const uint64_t n = a->nrows;
+  SolveOut<F> o;
+  *error = 0;
+  std::vector<F> x(n, F(0));
+  if (x0) x.assign(x0, x0 + n);
+  auto finish = [&](uint64_t it, F res, bool conv, int msg) {
+    o.x = x; o.iterations = it; o.residual_norm = res; o.converged = conv; o.message = msg;
+    return o;
+  };
+  const F bnorm = norm2(b);
+  if (bnorm < atol) return finish(0, F(0), true, M_ZERO_RHS);
+  std::vector<F> ax = op_apply(a, x);
+  std::vector<F> r1(n);
+  for (uint64_t i = 0; i < n; ++i) r1[i] = b[i] - ax[i];
+  std::vector<F> y = m ? op_apply(m, r1) : r1;
+  F beta1_sq = dot(r1, y);
+  if (beta1_sq < F(0)) { *error = 1; return o; }
+  if (beta1_sq == F(0)) return finish(0, F(0), true, M_ZERO_RESIDUAL);
+  F beta1 = std::sqrt(beta1_sq);
+  F oldb = F(0), beta = beta1, dbar = F(0), epsln = F(0), phibar = beta1;
+  F cs = F(-1), sn = F(0);
+  std::vector<F> w(n, F(0)), w2(n, F(0)), r2 = r1, v(n, F(0)), w1;
+  std::fill(r1.begin(), r1.end(), F(0));
+  F tnorm2 = F(0), qrnorm = beta1;
+  const F eps = std::numeric_limits<F>::epsilon();
+  for (uint64_t itn = 0; itn < max_iter; ++itn) {
+    const F s = F(1) / beta;
+    for (uint64_t i = 0; i < n; ++i) v[i] = s * y[i];
+    std::vector<F> yn = op_apply(a, v);
+    if (itn >= 1)
+      for (uint64_t i = 0; i < n; ++i) yn[i] -= (beta / oldb) * r1[i];
+    F alfa = dot(v, yn);
+    for (uint64_t i = 0; i < n; ++i) yn[i] -= (alfa / beta) * r2[i];
+    r1 = r2;
+    r2 = yn;
+    y = m ? op_apply(m, r2) : r2;
+    oldb = beta;
+    F beta_sq = dot(r2, y);
+    if (beta_sq < F(0)) { *error = 2; return o; }
+    beta = std::sqrt(beta_sq);
+    tnorm2 = tnorm2 + alfa * alfa + oldb * oldb + beta * beta;
+    F oldeps = epsln;
+    F delta = cs * dbar + sn * alfa;
+    F gbar = sn * dbar - cs * alfa;
+    epsln = sn * beta;
+    dbar = -cs * beta;
+    F gamma = std::sqrt(gbar * gbar + beta * beta);
+    F gc = gamma > eps ? gamma : eps;
+    cs = gbar / gc;
+    sn = beta / gc;
+    F phi = cs * phibar;
+    phibar = sn * phibar;
+    F denom = F(1) / gc;
+    w1 = w2;
+    w2 = w;
+    for (uint64_t i = 0; i < n; ++i) {
+      w[i] = (v[i] - oldeps * w1[i] - delta * w2[i]) * denom;
+      x[i] += phi * w[i];
+    }
+    qrnorm = phibar;
+    F rnorm = qrnorm;
+    F anorm = std::sqrt(tnorm2);
+    F ynorm = norm2(x);
+    F test1 = (ynorm == F(0) || anorm == F(0)) ? std::numeric_limits<F>::infinity() : rnorm / (anorm * ynorm);
+    if (test1 <= rtol || rnorm <= atol) return finish(itn + 1, rnorm, true, M_CONVERGED);
+  }
+  return finish(max_iter, qrnorm, false, M_MAX_ITER);
+}
+
+// lgmres, lgmres.rs:58-327: restarted left-preconditioned GMRES with
+// classical Gram-Schmidt (each h_ij from the unorthogonalised w); the
+// augmentation vectors are collected but unused, as in the reference
+template <class F>
+SolveOut<F> lgmres(const or_op* a, const std::vector<F>& b, uint64_t max_iter, uint64_t inner_m,
+                   F rtol, F atol, const F* x0, const or_op* m) {
+  const uint64_t n = a->nrows;
+  SolveOut<F> o;
+  std::vector<F> x(n, F(0));
+  if (x0) x.assign(x0, x0 + n);
+  auto finish = [&](uint64_t it, F res, bool conv) {
+    o.x = x; o.iterations = it; o.residual_norm = res; o.converged = conv;
+    o.message = conv ? M_CONVERGED : M_MAX_ITER;
+    return o;
+  };
+  F bnorm = F(0);
+  for (uint64_t i = 0; i < n; ++i) bnorm = bnorm + b[i] * b[i];
+  bnorm = std::sqrt(bnorm);
+  if (bnorm < atol) return finish(0, F(0), true);
+  auto residual = [&]() {
+    std::vector<F> ax = op_apply(a, x);
+    std::vector<F> r(n);
+    for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - ax[i];
+    return m ? op_apply(m, r) : r;
+  };
+  std::vector<F> r = residual();
+  F rn = norm2(r);
+  if (rn < atol || rn / bnorm < rtol) return finish(0, rn, true);
+  const F eps = std::numeric_limits<F>::epsilon();
+  uint64_t total = 0;
+  for (uint64_t outer = 0; outer < max_iter; ++outer) {
+    // inner_gmres (lgmres.rs:191-327)
+    std::vector<F> xi(n, F(0));
+    F r0n = norm2(r);
+    if (!(r0n < eps)) {
+      const uint64_t mm = inner_m;
+      std::vector<std::vector<F>> v(mm + 1, std::vector<F>(n, F(0)));
+      for (uint64_t i = 0; i < n; ++i) v[0][i] = r[i] / r0n;
+      std::vector<std::vector<F>> h(mm + 1, std::vector<F>(mm, F(0)));
+      std::vector<F> sv(mm + 1, F(0)), cv(mm + 1, F(0)), beta(mm + 2, F(0));
+      beta[0] = r0n;
+      uint64_t k = 0;
+      for (uint64_t j = 0; j < mm; ++j) {
+        std::vector<F> w = op_apply(a, v[j]);
+        if (m) w = op_apply(m, w);
+        std::vector<F> wo = w;
+        for (uint64_t i = 0; i <= j; ++i) {
+          F hij = dot(w, v[i]);
+          h[i][j] = hij;
+          for (uint64_t q = 0; q < n; ++q) wo[q] -= hij * v[i][q];
+        }
+        F hn = norm2(wo);
+        if (hn > eps) {
+          h[j + 1][j] = hn;
+          for (uint64_t q = 0; q < n; ++q) v[j + 1][q] = wo[q] / hn;
+        } else {
+          k = j + 1;
+          break;
+        }
+        for (uint64_t i = 0; i < j; ++i) {
+          F temp = cv[i] * h[i][j] + sv[i] * h[i + 1][j];
+          h[i + 1][j] = -sv[i] * h[i][j] + cv[i] * h[i + 1][j];
+          h[i][j] = temp;
+        }
+        F hjj = h[j][j], hj1 = h[j + 1][j];
+        F rho = std::sqrt(hjj * hjj + hj1 * hj1);
+        if (rho > eps) {
+          cv[j] = hjj / rho;
+          sv[j] = hj1 / rho;
+          h[j][j] = cv[j] * hjj + sv[j] * hj1;
+          h[j + 1][j] = F(0);
+          beta[j + 1] = -sv[j] * beta[j];
+          beta[j] = cv[j] * beta[j];
+          k = j + 1;
+          if (std::fabs(beta[j + 1]) < F(1e-10)) break;
+        } else {
+          k = j;
+          break;
+        }
+      }
+      if (k > 0) {
+        std::vector<F> y(k, F(0));
+        for (uint64_t i = k; i-- > 0;) {
+          y[i] = beta[i];
+          for (uint64_t j = i + 1; j < k; ++j) y[i] = y[i] - h[i][j] * y[j];
+          if (std::fabs(h[i][i]) > eps) y[i] /= h[i][i];
+          else y[i] = F(0);
+        }
+        for (uint64_t i = 0; i < k; ++i)
+          for (uint64_t q = 0; q < n; ++q) xi[q] += y[i] * v[i][q];
+      }
+    }
+    for (uint64_t q = 0; q < n; ++q) x[q] += xi[q];
+    ++total;
+    r = residual();
+    rn = norm2(r);
+    if (rn < atol || rn / bnorm < rtol) return finish(total, rn, true);
+  }
+  return finish(total, rn, false);
+}
+
 template <class F>
 void fill_result(const SolveOut<F>& s, void* x_out, or_result* res) {
   std::memcpy(x_out, s.x.data(), s.x.size() * sizeof(F));
@@ -1008,6 +1412,90 @@ int or_gmres(const or_op* a, const void* b, uint64_t max_iter, uint64_t restart,
     std::vector<float> bv((const float*)b, (const float*)b + n);
     auto s = gmres<float>(a, bv, max_iter, restart, (float)rtol, (float)atol, (const float*)x0, m);
     fill_result(s, x_out, res);
+  }
+  return ok(err);
+}
+
+
+int or_bicg(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+            const void* x0, const or_op* m1, const or_op* m2, void* x_out, or_result* res,
+            or_err* err) {
+  if (int rc = check_square_and_len<double>(a, "BiCG", err)) return rc;
+  const uint64_t n = a->nrows;
+  if (a->f64) {
+    std::vector<double> bv((const double*)b, (const double*)b + n);
+    fill_result(bicg<double>(a, bv, max_iter, rtol, atol, (const double*)x0, m1, m2), x_out, res);
+  } else {
+    std::vector<float> bv((const float*)b, (const float*)b + n);
+    fill_result(bicg<float>(a, bv, max_iter, (float)rtol, (float)atol, (const float*)x0, m1, m2), x_out, res);
+  }
+  return ok(err);
+}
+
+int or_cgs(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+           const void* x0, const or_op* m, void* x_out, or_result* res, or_err* err) {
+  if (int rc = check_square_and_len<double>(a, "CGS", err)) return rc;
+  const uint64_t n = a->nrows;
+  if (a->f64) {
+    std::vector<double> bv((const double*)b, (const double*)b + n);
+    fill_result(cgs<double>(a, bv, max_iter, rtol, atol, (const double*)x0, m), x_out, res);
+  } else {
+    std::vector<float> bv((const float*)b, (const float*)b + n);
+    fill_result(cgs<float>(a, bv, max_iter, (float)rtol, (float)atol, (const float*)x0, m), x_out, res);
+  }
+  return ok(err);
+}
+
+int or_qmr(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+           const void* x0, const or_op* m1, const or_op* m2, void* x_out, or_result* res,
+           or_err* err) {
+  // qmr.rs:53-59: DimensionMismatch{expected: b.len(), found: rows}
+  const uint64_t n = a->nrows;
+  if (a->ncols != n)
+    return set_err(err, E_DIMENSION_MISMATCH, dim_msg(n, a->nrows), n, a->nrows);
+  if (a->f64) {
+    std::vector<double> bv((const double*)b, (const double*)b + n);
+    fill_result(qmr<double>(a, bv, max_iter, rtol, atol, (const double*)x0, m1, m2), x_out, res);
+  } else {
+    std::vector<float> bv((const float*)b, (const float*)b + n);
+    fill_result(qmr<float>(a, bv, max_iter, (float)rtol, (float)atol, (const float*)x0, m1, m2), x_out, res);
+  }
+  return ok(err);
+}
+
+int or_minres(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+              const void* x0, const or_op* m, void* x_out, or_result* res, or_err* err) {
+  if (a->nrows != a->ncols)
+    return set_err(err, E_DIMENSION_MISMATCH, dim_msg(a->nrows, a->ncols), a->nrows, a->ncols);
+  const uint64_t n = a->nrows;
+  int e = 0;
+  if (a->f64) {
+    std::vector<double> bv((const double*)b, (const double*)b + n);
+    auto s = minres<double>(a, bv, max_iter, rtol, atol, (const double*)x0, m, &e);
+    if (!e) fill_result(s, x_out, res);
+  } else {
+    std::vector<float> bv((const float*)b, (const float*)b + n);
+    auto s = minres<float>(a, bv, max_iter, (float)rtol, (float)atol, (const float*)x0, m, &e);
+    if (!e) fill_result(s, x_out, res);
+  }
+  if (e == 1) return set_err(err, E_COMPUTATION, "Computation error: Indefinite preconditioner");
+  if (e == 2) return set_err(err, E_COMPUTATION, "Computation error: Non-symmetric matrix");
+  return ok(err);
+}
+
+int or_lgmres(const or_op* a, const void* b, uint64_t max_iter, uint64_t inner_m, double rtol,
+              double atol, const void* x0, const or_op* m, void* x_out, or_result* res,
+              or_err* err) {
+  if (a->nrows != a->ncols)
+    return set_err(err, E_DIMENSION_MISMATCH, dim_msg(a->nrows, a->ncols), a->nrows, a->ncols);
+  const uint64_t n = a->nrows;
+  if (a->f64) {
+    std::vector<double> bv((const double*)b, (const double*)b + n);
+    fill_result(lgmres<double>(a, bv, max_iter, inner_m, rtol, atol, (const double*)x0, m), x_out, res);
+  } else {
+    std::vector<float> bv((const float*)b, (const float*)b + n);
+    fill_result(lgmres<float>(a, bv, max_iter, inner_m, (float)rtol, (float)atol, (const float*)x0, m), x_out,
+                res);
   }
   return ok(err);
 }

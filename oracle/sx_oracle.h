@@ -136,6 +136,22 @@ int or_cg_mixed_replace(const int64_t* indptr, const int32_t* indices, const dou
                         const double* b, const or_ir_options* opt, double delta, double* x,
                         or_ir_result* res);
 
+/* ---- bicg (iterative.rs:189-345), cgs (cgs.rs:15-193), qmr (qmr.rs:44-259),
+ * minres (minres.rs:66-257), lgmres (lgmres.rs:58-327) ---- */
+int or_bicg(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+            const void* x0, const or_op* m1, const or_op* m2, void* x_out, or_result* res,
+            or_err* err);
+int or_cgs(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+           const void* x0, const or_op* m, void* x_out, or_result* res, or_err* err);
+int or_qmr(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+           const void* x0, const or_op* m1, const or_op* m2, void* x_out, or_result* res,
+           or_err* err);
+int or_minres(const or_op* a, const void* b, uint64_t max_iter, double rtol, double atol,
+              const void* x0, const or_op* m, void* x_out, or_result* res, or_err* err);
+int or_lgmres(const or_op* a, const void* b, uint64_t max_iter, uint64_t inner_m, double rtol,
+              double atol, const void* x0, const or_op* m, void* x_out, or_result* res,
+              or_err* err);
+
 /* FP64 true relative residual ||b - A x|| / ||b|| with sequential sums. */
 double or_true_rel_residual(const int64_t* indptr, const int32_t* indices, const double* data,
                             int64_t n, const double* b, const double* x);

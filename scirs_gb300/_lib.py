@@ -90,6 +90,39 @@ class GMRESOptions(C.Structure):
     ]
 
 
+class BiCGOptions(C.Structure):
+    _fields_ = [
+        ("max_iter", c_u64),
+        ("rtol", c_dbl),
+        ("atol", c_dbl),
+        ("x0", c_vp),
+        ("left_preconditioner", op_t),
+        ("right_preconditioner", op_t),
+    ]
+
+
+class MINRESOptions(C.Structure):
+    _fields_ = [
+        ("max_iter", c_u64),
+        ("rtol", c_dbl),
+        ("atol", c_dbl),
+        ("x0", c_vp),
+        ("preconditioner", op_t),
+    ]
+
+
+class LGMRESOptions(C.Structure):
+    _fields_ = [
+        ("max_iter", c_u64),
+        ("rtol", c_dbl),
+        ("atol", c_dbl),
+        ("inner_m", c_u64),
+        ("outer_k", c_u64),
+        ("x0", c_vp),
+        ("preconditioner", op_t),
+    ]
+
+
 class IROptions(C.Structure):
     _fields_ = [
         ("max_outer", c_u64),
@@ -214,6 +247,15 @@ _SIGS = {
     "sx_cg": (c_int, [ctx_t, op_t, c_vp, c_u64, P(CGOptions), c_vp, c_int, P(IterResult)]),
     "sx_bicgstab": (c_int, [ctx_t, op_t, c_vp, c_u64, P(BiCGSTABOptions), c_vp, c_int, P(IterResult)]),
     "sx_gmres": (c_int, [ctx_t, op_t, c_vp, c_u64, P(GMRESOptions), c_vp, c_int, P(IterResult)]),
+    "sx_bicg_options_default": (None, [P(BiCGOptions)]),
+    "sx_minres_options_default": (None, [P(MINRESOptions)]),
+    "sx_lgmres_options_default": (None, [P(LGMRESOptions)]),
+    "sx_bicg": (c_int, [ctx_t, op_t, c_vp, c_u64, P(BiCGOptions), c_vp, c_int, P(IterResult)]),
+    "sx_cgs": (c_int, [ctx_t, op_t, c_vp, c_u64, P(BiCGOptions), c_vp, c_int, P(IterResult)]),
+    "sx_qmr": (c_int, [ctx_t, op_t, c_vp, c_u64, P(BiCGOptions), c_vp, c_int, P(IterResult)]),
+    "sx_minres": (c_int, [ctx_t, op_t, c_vp, c_u64, P(MINRESOptions), c_vp, c_int, P(IterResult)]),
+    "sx_lgmres": (c_int, [ctx_t, op_t, c_vp, c_u64, P(LGMRESOptions), c_vp, c_int, P(IterResult)]),
+    "sx_iter_message": (c_int, [P(IterResult), c_int, C.c_char_p, c_u64]),
     "sx_ir_options_default": (None, [P(IROptions)]),
     "sx_cg_mixed": (c_int, [ctx_t, op_t, c_vp, c_u64, P(IROptions), c_vp, c_int, P(IRResult)]),
     "sx_true_rel_residual": (c_int, [ctx_t, op_t, c_vp, c_vp, c_int, P(c_dbl)]),

@@ -29,6 +29,7 @@ SOURCES = [
     "sx_noalloc.cu",
     "sx_gnn.cu",
     "sx_sym.cu",
+    "sx_krylov2.cu",
     "sx_gen.cpp",
 ]
 

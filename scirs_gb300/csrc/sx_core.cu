@@ -834,6 +834,18 @@ const char* sx_message_string(int m) {
     case MSG_BD_ALPHA: return "BiCGSTAB breakdown: alpha is not finite";
     case MSG_BD_TT: return "BiCGSTAB breakdown: (t, t) \xE2\x89\x88 0";
     case MSG_BD_OMEGA: return "BiCGSTAB breakdown: omega is not finite or too small";
+    case MSG_BICG_PQ: return "BiCG breakdown: (p_star, q) \xE2\x89\x88 0";
+    case MSG_BICG_RHO: return "BiCG breakdown: rho \xE2\x89\x88 0";
+    case MSG_CGS_RHO: return "CGS breakdown: rho \xE2\x89\x88 0";
+    case MSG_CGS_SIGMA: return "CGS breakdown: sigma \xE2\x89\x88 0";
+    case MSG_QMR_INITIAL: return "Converged at initial guess";
+    case MSG_QMR_RHO: return "Breakdown: rho = 0";
+    case MSG_QMR_PQ: return "Breakdown: <p_tilde, q> = 0";
+    case MSG_QMR_CONVERGED: return "Converged in {iterations} iterations";
+    case MSG_QMR_OMEGA: return "Breakdown: omega = 0";
+    case MSG_QMR_MAX_ITER: return "Did not converge in {max_iter} iterations. Residual: {r}";
+    case MSG_ZERO_RHS: return "System has zero right-hand side";
+    case MSG_ZERO_RESIDUAL: return "Initial residual is zero";
     default: return "";
   }
 }

@@ -41,6 +41,18 @@ enum : int {
   MSG_BD_ALPHA = 6,
   MSG_BD_TT = 7,
   MSG_BD_OMEGA = 8,
+  MSG_BICG_PQ = 9,
+  MSG_BICG_RHO = 10,
+  MSG_CGS_RHO = 11,
+  MSG_CGS_SIGMA = 12,
+  MSG_QMR_INITIAL = 13,
+  MSG_QMR_RHO = 14,
+  MSG_QMR_PQ = 15,
+  MSG_QMR_CONVERGED = 16,
+  MSG_QMR_OMEGA = 17,
+  MSG_QMR_MAX_ITER = 18,
+  MSG_ZERO_RHS = 19,
+  MSG_ZERO_RESIDUAL = 20,
 };
 
 // ------------------------------------------------------------ device CSR

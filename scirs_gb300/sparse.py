@@ -497,8 +497,10 @@ class IterationResult:
 
 
 def _result(x, r: L.IterResult) -> IterationResult:
+    buf = C.create_string_buffer(512)
+    _check(L.lib.sx_iter_message(C.byref(r), L.SX_F64 if x.dtype == np.float64 else L.SX_F32, buf, 512))
     return IterationResult(x, int(r.iterations), float(r.residual_norm), bool(r.converged),
-                           message_string(r.message))
+                           buf.value.decode("utf-8"))
 
 
 def _prep(a: Operator, b, x0):
@@ -543,6 +545,61 @@ def gmres(a: Operator, b, max_iter=1000, restart=30, rtol=1e-8, atol=1e-12, x0=N
                        preconditioner.handle if preconditioner else None)
     r = L.IterResult()
     _check(L.lib.sx_gmres(a.ctx.handle, a.handle, _ptr(b), b.size, C.byref(o), _ptr(x), L.SX_MEM_HOST, C.byref(r)))
+    return _result(x, r)
+
+
+def _bicg_like(fn, a: Operator, b, max_iter, rtol, atol, x0, left, right) -> IterationResult:
+    b, x, x0a = _prep(a, b, x0)
+    o = L.BiCGOptions(max_iter, rtol, atol, _ptr(x0a) if x0a is not None else None,
+                      left.handle if left else None, right.handle if right else None)
+    r = L.IterResult()
+    _check(fn(a.ctx.handle, a.handle, _ptr(b), b.size, C.byref(o), _ptr(x), L.SX_MEM_HOST, C.byref(r)))
+    return _result(x, r)
+
+
+def bicg(a: Operator, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None,
+         left_preconditioner: Optional[Operator] = None,
+         right_preconditioner: Optional[Operator] = None) -> IterationResult:
+    """bicg(a, b, BiCGOptions { .. }) (iterative.rs:189-345)."""
+    return _bicg_like(L.lib.sx_bicg, a, b, max_iter, rtol, atol, x0, left_preconditioner, right_preconditioner)
+
+
+def cgs(a: Operator, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None,
+        left_preconditioner: Optional[Operator] = None,
+        right_preconditioner: Optional[Operator] = None) -> IterationResult:
+    """cgs(a, b, CGSOptions { .. }) (cgs.rs:15-193); the left preconditioner is unused."""
+    return _bicg_like(L.lib.sx_cgs, a, b, max_iter, rtol, atol, x0, left_preconditioner, right_preconditioner)
+
+
+def qmr(a: Operator, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None,
+        left_preconditioner: Optional[Operator] = None,
+        right_preconditioner: Optional[Operator] = None) -> IterationResult:
+    """qmr(a, b, QMROptions { .. }) (qmr.rs:44-259)."""
+    return _bicg_like(L.lib.sx_qmr, a, b, max_iter, rtol, atol, x0, left_preconditioner, right_preconditioner)
+
+
+def minres(a: Operator, b, max_iter=1000, rtol=1e-8, atol=1e-12, x0=None,
+           preconditioner: Optional[Operator] = None) -> IterationResult:
+    """minres(a, b, MINRESOptions { .. }) (minres.rs:66-257)."""
+    b, x, x0a = _prep(a, b, x0)
+    o = L.MINRESOptions(max_iter, rtol, atol, _ptr(x0a) if x0a is not None else None,
+                        preconditioner.handle if preconditioner else None)
+    r = L.IterResult()
+    _check(L.lib.sx_minres(a.ctx.handle, a.handle, _ptr(b), b.size, C.byref(o), _ptr(x), L.SX_MEM_HOST,
+                           C.byref(r)))
+    return _result(x, r)
+
+
+def lgmres(a: Operator, b, max_iter=500, rtol=1e-8, atol=1e-8, inner_m=30, outer_k=3, x0=None,
+           preconditioner: Optional[Operator] = None) -> IterationResult:
+    """lgmres(a, b, LGMRESOptions { .. }) (lgmres.rs:58-327).  LGMRESResult has no
+    message; the returned one is "Converged" or "Maximum iterations reached"."""
+    b, x, x0a = _prep(a, b, x0)
+    o = L.LGMRESOptions(max_iter, rtol, atol, inner_m, outer_k, _ptr(x0a) if x0a is not None else None,
+                        preconditioner.handle if preconditioner else None)
+    r = L.IterResult()
+    _check(L.lib.sx_lgmres(a.ctx.handle, a.handle, _ptr(b), b.size, C.byref(o), _ptr(x), L.SX_MEM_HOST,
+                           C.byref(r)))
     return _result(x, r)
 
 

@@ -113,6 +113,79 @@ int main() {
     auto ax = m.matvec(r.x);
     for (int i = 0; i < 3; ++i) NEAR(ax[i], b[i], 1e-9);
   });
+  // tests/linalg_new_tests.rs:34-79: test_bicg_solver
+  run("bicg_solver_2x2", [] {
+    auto m = CsrMatrix<double>::create({2, -1, 1, 3}, {0, 0, 1, 1}, {0, 1, 0, 1}, {2, 2});
+    BiCGOptions<double> o;
+    o.atol = 1e-8;
+    o.rtol = 1e-8;
+    auto r = bicg<double>(m, {3, 2}, o);
+    NEAR(r.x[0], 11.0 / 7.0, 1e-5); NEAR(r.x[1], 1.0 / 7.0, 1e-5);
+  });
+  // tests/cgs_revised_tests.rs:6-26 and :182-209
+  run("cgs_identity_and_spd", [] {
+    auto id = CsrMatrix<double>::create({1, 1, 1}, {0, 1, 2}, {0, 1, 2}, {3, 3});
+    auto r = cgs<double>(id, {1, 2, 3}, CGSOptions<double>());
+    CHECK(r.converged && r.iterations == 1);
+    auto m = CsrMatrix<double>::create({4, -1, -1, -1, 4, -1, -1, -1, 4}, {0, 0, 0, 1, 1, 1, 2, 2, 2},
+                                       {0, 1, 2, 0, 1, 2, 0, 1, 2}, {3, 3});
+    r = cgs<double>(m, {2, 2, 2}, CGSOptions<double>());
+    CHECK(r.converged);
+    for (int i = 0; i < 3; ++i) NEAR(r.x[i], 1, 1e-6);
+  });
+  // qmr.rs:298-382: identity, diagonal, initial guess, max iterations
+  run("qmr_reference_tests", [] {
+    IdentityOperator<double> id(3);
+    auto r = qmr<double>(id, {1, 2, 3}, QMROptions<double>());
+    CHECK(r.converged && r.iterations == 1);
+    CHECK(r.message == "Converged in 1 iterations");
+    DiagonalOperator<double> dg({2, 3, 4});
+    QMROptions<double> o;
+    o.rtol = 1e-10;
+    o.atol = 1e-12;
+    r = qmr<double>(dg, {2, 6, 8}, o);
+    CHECK(r.converged && r.iterations <= 10);
+    NEAR(r.x[0], 1, 1e-9); NEAR(r.x[1], 2, 1e-9); NEAR(r.x[2], 2, 1e-9);
+    o.x0 = {0.9, 1.9, 2.9};
+    r = qmr<double>(id, {1, 2, 3}, o);
+    CHECK(r.converged && r.iterations <= 1);
+    DiagonalOperator<double> ill({1e-8, 1, 1});
+    QMROptions<double> o2;
+    o2.max_iter = 5;
+    o2.rtol = 1e-10;
+    o2.atol = 1e-12;
+    r = qmr<double>(ill, {1, 1, 1}, o2);
+    if (!r.converged) CHECK(r.iterations == 5 && r.message.find("Did not converge") != std::string::npos);
+  });
+  // minres.rs:287-401
+  run("minres_reference_tests", [] {
+    IdentityOperator<double> id(3);
+    auto r = minres<double>(id, {1, 2, 3}, MINRESOptions<double>());
+    CHECK(r.converged);
+    NEAR(r.x[0], 1, 1e-10); NEAR(r.x[2], 3, 1e-10);
+    DiagonalOperator<double> dg({2, -3, 4});
+    r = minres<double>(dg, {2, -6, 12}, MINRESOptions<double>());
+    CHECK(r.converged);
+    NEAR(r.x[0], 1, 1e-9); NEAR(r.x[1], 2, 1e-9); NEAR(r.x[2], 3, 1e-9);
+    auto m = CsrMatrix<double>::create({4, -1, -1, 4, -1, -1, 4}, {0, 0, 1, 1, 1, 2, 2}, {0, 1, 0, 1, 2, 1, 2}, {3, 3});
+    MINRESOptions<double> o;
+    o.preconditioner = std::make_shared<DiagonalOperator<double>>(std::vector<double>{0.25, 0.25, 0.25});
+    std::vector<double> b{1, 2, 3};
+    r = minres<double>(m, b, o);
+    CHECK(r.converged);
+    auto ax = m.matvec(r.x);
+    for (int i = 0; i < 3; ++i) NEAR(ax[i], b[i], 1e-9);
+  });
+  // lgmres.rs:335-366
+  run("lgmres_reference_tests", [] {
+    IdentityOperator<double> id(3);
+    auto r = lgmres<double>(id, {1, 2, 3}, LGMRESOptions<double>());
+    CHECK(r.converged);
+    NEAR(r.x[1], 2, 1e-10);
+    auto m = CsrMatrix<double>::from_raw_csr({4, -1, -1, 4, -1, -1, 4}, {0, 2, 5, 7}, {0, 1, 0, 1, 2, 1, 2}, {3, 3});
+    r = lgmres<double>(m, {1, 2, 3}, LGMRESOptions<double>());
+    CHECK(r.converged && r.residual_norm < 1e-8);
+  });
   // tests/linalg_new_tests.rs:5-32: test_cg_solver
   run("cg_solver_2x2", [] {
     auto m = CsrMatrix<double>::create({2, -1, -1, 2}, {0, 0, 1, 1}, {0, 1, 0, 1}, {2, 2});

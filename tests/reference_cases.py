@@ -80,3 +80,67 @@ def dense_of(rows, cols, data, shape):
     for r, c, v in zip(rows, cols, data):
         d[r, c] += v
     return d
+
+
+# ---------------------------------------------------- bicg / cgs / qmr / minres / lgmres
+# tests/linalg_new_tests.rs:34-79 -- bicg on [[2,-1],[1,3]], b = [3, 2] -> [11/7, 1/7] (1e-5)
+BICG_2X2 = dict(rows=[0, 0, 1, 1], cols=[0, 1, 0, 1], data=[2.0, -1.0, 1.0, 3.0], shape=(2, 2),
+                b=[3.0, 2.0], atol=1e-8, rtol=1e-8, x=[11.0 / 7.0, 1.0 / 7.0], tol=1e-5, resid=1e-5)
+
+# tests/cgs_revised_tests.rs:6-26 -- identity: converged in exactly 1 iteration
+CGS_IDENTITY = dict(rows=[0, 1, 2], cols=[0, 1, 2], data=[1.0, 1.0, 1.0], shape=(3, 3), b=[1.0, 2.0, 3.0],
+                    iterations=1, tol=1e-10)
+# tests/cgs_revised_tests.rs:28-61 -- diagonally dominant non-symmetric 3x3, true residual < 1e-8
+CGS_WELL = dict(rows=[0, 0, 0, 1, 1, 1, 2, 2, 2], cols=[0, 1, 2, 0, 1, 2, 0, 1, 2],
+                data=[4.0, 0.5, 0.5, 0.5, 4.0, 0.5, 0.0, 0.5, 4.0], shape=(3, 3), b=[5.0, 5.0, 4.5],
+                rtol=1e-8, atol=1e-10, resid=1e-8)
+# tests/cgs_revised_tests.rs:63-108 -- 4x4 with / without right Jacobi (rtol 1e-6, 100 its)
+CGS_PRECOND = dict(rows=[r for r in range(4) for _ in range(4)], cols=[c for _ in range(4) for c in range(4)],
+                   data=[10.0, 1.0, 0.5, 0.0, 1.0, 8.0, 0.5, 0.5, 0.5, 0.5, 6.0, 1.0, 0.0, 0.5, 1.0, 4.0],
+                   shape=(4, 4), b=[11.5, 10.0, 8.0, 5.5], max_iter=100, rtol=1e-6)
+# tests/cgs_revised_tests.rs:182-209 -- SPD 3x3: converged, x = [1, 1, 1] (1e-6)
+CGS_SPD = dict(rows=[0, 0, 0, 1, 1, 1, 2, 2, 2], cols=[0, 1, 2, 0, 1, 2, 0, 1, 2],
+               data=[4.0, -1.0, -1.0, -1.0, 4.0, -1.0, -1.0, -1.0, 4.0], shape=(3, 3), b=[2.0, 2.0, 2.0],
+               rtol=1e-8, x=[1.0, 1.0, 1.0], tol=1e-6)
+
+
+# tests/cgs_revised_tests.rs:110-180 -- 5x5-grid Laplacian (25 x 25), b = 1..25,
+# max_iter 200, rtol 1e-5, atol 1e-7: if converged, relative true residual < 1e-4
+def cgs_laplacian(n=5):
+    rows, cols, data = [], [], []
+    for i in range(n):
+        for j in range(n):
+            idx = i * n + j
+            rows.append(idx); cols.append(idx); data.append(4.0)
+            if i > 0:
+                rows.append(idx); cols.append((i - 1) * n + j); data.append(-1.0)
+            if i < n - 1:
+                rows.append(idx); cols.append((i + 1) * n + j); data.append(-1.0)
+            if j > 0:
+                rows.append(idx); cols.append(i * n + (j - 1)); data.append(-1.0)
+            if j < n - 1:
+                rows.append(idx); cols.append(i * n + (j + 1)); data.append(-1.0)
+    return dict(rows=rows, cols=cols, data=data, shape=(n * n, n * n), b=[float(i + 1) for i in range(n * n)],
+                max_iter=200, rtol=1e-5, atol=1e-7, rel=1e-4)
+
+
+# qmr.rs:298-382 -- identity (1 iteration), diagonal, initial guess, max iterations
+QMR_IDENTITY = dict(b=[1.0, 2.0, 3.0], iterations=1, tol=1e-10)
+QMR_DIAG = dict(diag=[2.0, 3.0, 4.0], b=[2.0, 6.0, 8.0], x=[1.0, 2.0, 2.0], rtol=1e-10, atol=1e-12,
+                max_iterations=10, tol=1e-9)
+QMR_GUESS = dict(b=[1.0, 2.0, 3.0], x0=[0.9, 1.9, 2.9], rtol=1e-10, atol=1e-12, max_iterations=1, tol=1e-10)
+QMR_MAXIT = dict(diag=[1e-8, 1.0, 1.0], b=[1.0, 1.0, 1.0], max_iter=5, rtol=1e-10, atol=1e-12)
+
+# minres.rs:287-401 -- identity, indefinite diagonal, symmetric 3x3, Jacobi-like diagonal M
+MINRES_IDENTITY = dict(b=[1.0, 2.0, 3.0], tol=1e-10)
+MINRES_DIAG = dict(diag=[2.0, -3.0, 4.0], b=[2.0, -6.0, 12.0], x=[1.0, 2.0, 3.0], tol=1e-9)
+MINRES_SYM = dict(rows=[0, 0, 1, 1, 1, 2, 2], cols=[0, 1, 0, 1, 2, 1, 2],
+                  data=[4.0, -1.0, -1.0, 2.0, -1.0, -1.0, 4.0], shape=(3, 3), b=[1.0, 0.0, 1.0], tol=1e-9)
+MINRES_PREC = dict(rows=[0, 0, 1, 1, 1, 2, 2], cols=[0, 1, 0, 1, 2, 1, 2],
+                   data=[4.0, -1.0, -1.0, 4.0, -1.0, -1.0, 4.0], shape=(3, 3), b=[1.0, 2.0, 3.0],
+                   prec=[0.25, 0.25, 0.25], tol=1e-9)
+
+# lgmres.rs:335-366 -- identity (x = b, 1e-10) and from_raw_csr SPD (residual < 1e-8)
+LGMRES_IDENTITY = dict(b=[1.0, 2.0, 3.0], tol=1e-10)
+LGMRES_SPD = dict(data=[4.0, -1.0, -1.0, 4.0, -1.0, -1.0, 4.0], indptr=[0, 2, 5, 7],
+                  indices=[0, 1, 0, 1, 2, 1, 2], b=[1.0, 2.0, 3.0], resid=1e-8)

@@ -1,0 +1,280 @@
+"""bicg / cgs / qmr / minres / lgmres on the device vs the reference's tests and the oracle.
+
+The reference's own assertions (tests/reference_cases.py) run through the C
+ABI; larger problems compare the device with the oracle's restatement: the
+same exit and message, iteration counts within a few percent (the device's
+dot products are tree sums, the oracle's are sequential), and solutions
+within the solver tolerance.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle_ffi as O
+from tests import reference_cases as R
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def S():
+    import scirs_gb300
+
+    return scirs_gb300
+
+
+def dev_csr(S, ctx, c, dtype=np.float64):
+    return S.csr_matrix(ctx, c["data"], c["rows"], c["cols"], c["shape"], dtype=dtype)
+
+
+def true_resid(c, x):
+    a = R.dense_of(c["rows"], c["cols"], c["data"], c["shape"])
+    return np.linalg.norm(np.asarray(c["b"]) - a @ x)
+
+
+# ------------------------------------------------------ the reference's tests
+def test_bicg_2x2(S, ctx):
+    c = R.BICG_2X2
+    r = S.bicg(dev_csr(S, ctx, c), c["b"], rtol=c["rtol"], atol=c["atol"])
+    assert true_resid(c, r.x) < c["resid"]
+    assert np.allclose(r.x, c["x"], atol=c["tol"])
+
+
+def test_cgs_reference_cases(S, ctx):
+    c = R.CGS_IDENTITY
+    r = S.cgs(dev_csr(S, ctx, c), c["b"])
+    assert r.converged and r.iterations == c["iterations"]
+    assert np.allclose(r.x, c["b"], atol=c["tol"])
+    c = R.CGS_WELL
+    r = S.cgs(dev_csr(S, ctx, c), c["b"], rtol=c["rtol"], atol=c["atol"])
+    assert true_resid(c, r.x) < c["resid"]
+    c = R.CGS_SPD
+    r = S.cgs(dev_csr(S, ctx, c), c["b"], rtol=c["rtol"])
+    assert r.converged and np.allclose(r.x, c["x"], atol=c["tol"])
+    c = R.cgs_laplacian()
+    r = S.cgs(dev_csr(S, ctx, c), c["b"], max_iter=c["max_iter"], rtol=c["rtol"], atol=c["atol"])
+    if r.converged:
+        assert true_resid(c, r.x) / np.linalg.norm(c["b"]) < c["rel"]
+    c = R.CGS_PRECOND
+    a = dev_csr(S, ctx, c)
+    r0 = S.cgs(a, c["b"], max_iter=c["max_iter"], rtol=c["rtol"])
+    r1 = S.cgs(a, c["b"], max_iter=c["max_iter"], rtol=c["rtol"], right_preconditioner=S.jacobi(ctx, a))
+    if r0.converged and r1.converged:
+        assert r1.iterations <= r0.iterations
+
+
+def test_qmr_reference_cases(S, ctx):
+    c = R.QMR_IDENTITY
+    r = S.qmr(S.identity(ctx, 3), c["b"])
+    assert r.converged and r.iterations == c["iterations"]
+    assert r.message == "Converged in 1 iterations"
+    assert np.allclose(r.x, c["b"], atol=c["tol"])
+    c = R.QMR_DIAG
+    r = S.qmr(S.diagonal(ctx, c["diag"]), c["b"], rtol=c["rtol"], atol=c["atol"])
+    assert r.converged and r.iterations <= c["max_iterations"]
+    assert np.allclose(r.x, c["x"], atol=c["tol"])
+    c = R.QMR_GUESS
+    r = S.qmr(S.identity(ctx, 3), c["b"], rtol=c["rtol"], atol=c["atol"], x0=c["x0"])
+    assert r.converged and r.iterations <= c["max_iterations"]
+    assert np.allclose(r.x, c["b"], atol=c["tol"])
+    c = R.QMR_MAXIT
+    r = S.qmr(S.diagonal(ctx, c["diag"]), c["b"], max_iter=c["max_iter"], rtol=c["rtol"], atol=c["atol"])
+    if not r.converged:
+        assert r.iterations == c["max_iter"] and "Did not converge" in r.message
+        # the residual is formatted like Rust's `{}`
+        assert r.message == f"Did not converge in 5 iterations. Residual: {O.rust_display(np.float64(r.residual_norm))}"
+
+
+def test_minres_reference_cases(S, ctx):
+    c = R.MINRES_IDENTITY
+    r = S.minres(S.identity(ctx, 3), c["b"])
+    assert r.converged and np.allclose(r.x, c["b"], atol=c["tol"])
+    c = R.MINRES_DIAG
+    r = S.minres(S.diagonal(ctx, c["diag"]), c["b"])
+    assert r.converged and np.allclose(r.x, c["x"], atol=c["tol"])
+    for c in (R.MINRES_SYM, R.MINRES_PREC):
+        a = dev_csr(S, ctx, c)
+        m = S.diagonal(ctx, c["prec"]) if "prec" in c else None
+        r = S.minres(a, c["b"], preconditioner=m)
+        assert r.converged
+        assert np.all(np.abs(a.matvec(r.x) - c["b"]) < c["tol"])
+
+
+def test_lgmres_reference_cases(S, ctx):
+    c = R.LGMRES_IDENTITY
+    r = S.lgmres(S.identity(ctx, 3), c["b"])
+    assert r.converged and np.allclose(r.x, c["b"], atol=c["tol"])
+    c = R.LGMRES_SPD
+    a = S.csr_matrix_from_raw(ctx, c["data"], c["indptr"], c["indices"], (3, 3))
+    r = S.lgmres(a, c["b"])
+    assert r.converged and r.residual_norm < c["resid"]
+
+
+# --------------------------------------------------------------- error paths
+def test_errors(S, ctx):
+    rect = S.csr_matrix(ctx, [1.0, 2.0], [0, 1], [0, 1], (2, 3))
+    with pytest.raises(S.SparseError, match="Value error: Matrix must be square for BiCG solver"):
+        S.bicg(rect, [1.0, 1.0])
+    with pytest.raises(S.SparseError, match="Value error: Matrix must be square for CGS solver"):
+        S.cgs(rect, [1.0, 1.0])
+    with pytest.raises(S.SparseError, match="Dimension mismatch: expected 2, found 3"):
+        S.minres(rect, [1.0, 1.0])
+    with pytest.raises(S.SparseError, match="Dimension mismatch: expected 2, found 3"):
+        S.lgmres(rect, [1.0, 1.0])
+    sq = S.identity(ctx, 3)
+    with pytest.raises(S.SparseError, match="Dimension mismatch: expected 2, found 3"):
+        S.qmr(sq, [1.0, 1.0])
+    with pytest.raises(S.SparseError, match="Computation error: Indefinite preconditioner"):
+        S.minres(sq, [1.0, 2.0, 3.0], preconditioner=S.diagonal(ctx, [-1.0, -1.0, -1.0]))
+    r = S.minres(sq, [0.0, 0.0, 0.0])
+    assert r.converged and r.iterations == 0 and r.message == "System has zero right-hand side"
+    host = S.host_operator(ctx, 3, lambda x: 2.0 * x)
+    with pytest.raises(S.SparseError, match="adjoint not implemented for this operator"):
+        S.bicg(host, [1.0, 2.0, 3.0])
+    # a host operator needs no adjoint in cgs / minres / lgmres
+    r = S.lgmres(host, [2.0, 4.0, 6.0])
+    assert r.converged and np.allclose(r.x, [1.0, 2.0, 3.0])
+
+
+# ------------------------------------------------------- parity with the oracle
+def _problems(S):
+    ip, ix, v = S.generate("poisson2d", 48, 48)
+    yield "poisson48", ip, ix, v
+    c = R.convection_diffusion(3000)
+    rows = np.asarray(c["rows"])
+    order = np.lexsort((np.asarray(c["cols"]), rows))
+    cols = np.asarray(c["cols"])[order]
+    data = np.asarray(c["data"])[order]
+    cnt = np.bincount(rows, minlength=3000)
+    yield "convdiff3000", np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64), cols.astype(np.int32), data
+
+
+def _agree(d, o, its_rel=0.05, its_abs=2):
+    assert d.converged == o["converged"] and d.message.split(" in ")[0] == o["message"].split(" in ")[0], (d, o["message"])
+    assert abs(d.iterations - o["iterations"]) <= max(its_abs, its_rel * o["iterations"]), (d.iterations, o["iterations"])
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+def test_parity_with_oracle(S, ctx, dt):
+    tol = 1e-8 if dt == np.float64 else 1e-4
+    for name, ip, ix, v in _problems(S):
+        n = len(ip) - 1
+        a = S.csr_from_arrays(ctx, ip, ix, v.astype(dt), (n, n))
+        oa = O.op_csr_i32(ip, ix, v.astype(dt), (n, n), f64=dt == np.float64)
+        b = S.rhs_normal(7, n).astype(dt)
+        ad = None
+        for solver in ("bicg", "qmr", "lgmres") + (("minres",) if name.startswith("poisson") else ()):
+            kw = dict(rtol=tol, atol=0.0 if solver != "lgmres" else 1e-30)
+            d = getattr(S, solver)(a, b, max_iter=3000 if solver != "lgmres" else 200, **kw)
+            o = getattr(O, solver)(oa, b, max_iter=3000 if solver != "lgmres" else 200, **kw)
+            if solver == "qmr" and name.startswith("poisson"):
+                # the reference's qmr is chaotic on this SPD system: a 4e-16
+                # relative change of b moves the oracle from 1,961 iterations
+                # to no convergence in 3,000; only the FP64 outcome is compared
+                # (in FP32 its recursive residual drifts from the true one)
+                if dt == np.float64:
+                    assert d.converged
+                    assert np.linalg.norm(b - a.matvec(d.x)) <= 10 * tol * np.linalg.norm(b)
+                continue
+            _agree(d, o, its_rel=0.05 if dt == np.float64 else 0.15)
+            if d.converged:
+                scale = np.linalg.norm(o["x"])
+                assert np.linalg.norm(d.x - o["x"]) <= (1e-6 if dt == np.float64 else 5e-2) * scale, (name, solver)
+        # cgs: one iteration is the method; the reference's later updates
+        # stagnate, which both sides reproduce
+        d = S.cgs(a, b, max_iter=50, rtol=tol, atol=0.0)
+        o = O.cgs(oa, b, max_iter=50, rtol=tol, atol=0.0)
+        assert d.converged == o["converged"] and d.message == o["message"]
+        d1 = S.cgs(a, b, max_iter=1, rtol=tol, atol=0.0)
+        o1 = O.cgs(oa, b, max_iter=1, rtol=tol, atol=0.0)
+        assert np.linalg.norm(d1.x - o1["x"]) <= (1e-12 if dt == np.float64 else 1e-5) * np.linalg.norm(o1["x"])
+
+
+def test_parity_with_preconditioners(S, ctx):
+    # bicg, minres and lgmres with Jacobi on a 2D Poisson matrix; qmr on the
+    # convection-diffusion matrix (on SPD systems the reference's qmr is
+    # chaotic: a 4e-16 change of b changes its iteration count by thousands)
+    ip, ix, v = S.generate("poisson2d", 40, 40)
+    cases = [("poisson", ip, ix, v, ("bicg", "minres", "lgmres"))]
+    name, cip, cix, cv = list(_problems(S))[1]
+    cases.append((name, cip, cix, cv, ("qmr",)))
+    for name, ip, ix, v, solvers in cases:
+        n = len(ip) - 1
+        a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+        oa = O.op_csr_i32(ip, ix, v, (n, n))
+        m, om = S.jacobi(ctx, a), O.op_jacobi(oa)
+        b = S.rhs_normal(3, n)
+        for solver in solvers:
+            if solver in ("bicg", "qmr"):
+                variants = ((dict(left_preconditioner=m), dict(left=om)),
+                            (dict(right_preconditioner=m), dict(right=om)))
+            else:
+                variants = ((dict(preconditioner=m), dict(preconditioner=om)),)
+            for kw_d, kw_o in variants:
+                atol = 0.0 if solver != "lgmres" else 1e-30
+                d = getattr(S, solver)(a, b, rtol=1e-9, atol=atol, **kw_d)
+                o = getattr(O, solver)(oa, b, rtol=1e-9, atol=atol, **kw_o)
+                _agree(d, o)
+                # the reference's bicg applies a single preconditioner to only
+                # one of its two sequences (iterative.rs:232-242, :255-262),
+                # so it does not converge here; both sides agree on that
+                if o["converged"]:
+                    assert np.linalg.norm(d.x - o["x"]) <= 1e-6 * np.linalg.norm(o["x"]), (name, solver)
+                else:
+                    assert solver == "bicg", (name, solver)
+
+
+def test_minres_symmetric_indefinite(S, ctx):
+    # 2D Laplacian shifted into indefiniteness: minres still converges
+    ip, ix, v = S.generate("poisson2d", 32, 32)
+    n = len(ip) - 1
+    rows = np.repeat(np.arange(n), np.diff(ip))
+    v = v.copy()
+    v[ix == rows] -= 1.0  # eigenvalues of the 4/-1 stencil span (0, 8): now some are negative
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    oa = O.op_csr_i32(ip, ix, v, (n, n))
+    b = S.rhs_normal(5, n)
+    d = S.minres(a, b, max_iter=5000, rtol=1e-10, atol=0.0)
+    o = O.minres(oa, b, max_iter=5000, rtol=1e-10, atol=0.0)
+    _agree(d, o, its_rel=0.1)
+    assert d.converged
+    assert np.linalg.norm(a.matvec(d.x) - b) <= 1e-6 * np.linalg.norm(b)
+
+
+def test_lgmres_inner_sizes(S, ctx):
+    c = R.convection_diffusion(2000)
+    a = S.csr_matrix(ctx, c["data"], c["rows"], c["cols"], c["shape"])
+    ip, ix, dd = a.to_arrays()
+    oa = O.op_csr(ip, ix, dd, c["shape"])
+    b = np.asarray(c["b"])
+    for m in (1, 5, 30, 64):
+        d = S.lgmres(a, b, inner_m=m, rtol=1e-10, atol=1e-30)
+        o = O.lgmres(oa, b, inner_m=m, rtol=1e-10, atol=1e-30)
+        _agree(d, o, its_abs=1)
+        assert np.linalg.norm(d.x - o["x"]) <= 1e-7 * np.linalg.norm(o["x"]), m
+    with pytest.raises(S.SparseError, match="inner_m"):
+        S.lgmres(a, b, inner_m=65)
+
+
+def test_bicg_and_qmr_on_composite_operators(S, ctx):
+    # A = B + 2 I as a sum operator: its adjoint is B^T + 2 I (a composite of
+    # the operands' adjoints); the solves match those with A as one CSR matrix
+    ip, ix, v = S.generate("poisson2d", 24, 24)
+    n = len(ip) - 1
+    rng = np.random.default_rng(1)
+    vv = v * (1.0 + 0.2 * rng.standard_normal(len(v)))  # non-symmetric values
+    bm = S.csr_from_arrays(ctx, ip, ix, vv, (n, n))
+    dg = S.diagonal(ctx, np.full(n, 2.0))
+    s = S.sum_operator(bm, dg)
+    rows = np.repeat(np.arange(n), np.diff(ip))
+    full = vv.copy()
+    full[ix == rows] += 2.0
+    f = S.csr_from_arrays(ctx, ip, ix, full, (n, n))
+    b = S.rhs_normal(2, n)
+    # bicg's breakdown test is absolute (|rho| < 10 eps), so it stops with a
+    # breakdown near 1e-10; rtol 1e-6 ends it by convergence
+    for solver, rtol in (("bicg", 1e-6), ("qmr", 1e-10)):
+        rs = getattr(S, solver)(s, b, rtol=rtol, atol=0.0)
+        rf = getattr(S, solver)(f, b, rtol=rtol, atol=0.0)
+        assert rs.converged and rf.converged, solver
+        assert abs(rs.iterations - rf.iterations) <= 2
+        assert np.linalg.norm(rs.x - rf.x) <= 10 * rtol * np.linalg.norm(rf.x)
