@@ -110,7 +110,9 @@ typedef enum {
   SX_OP_ZERO = 8,            /* ZeroOperator                           interface.rs:177-222 */
   SX_OP_SUM = 9,             /* SumOperator: (A + B) x                 interface.rs:299-349 */
   SX_OP_PRODUCT = 10,        /* ProductOperator: A (B x)               interface.rs:351-402 */
-  SX_OP_SYM_CSR = 11         /* SymCsrMatrix (lower triangle stored)   sym_csr.rs:24-337 */
+  SX_OP_SYM_CSR = 11,        /* SymCsrMatrix (lower triangle stored)   sym_csr.rs:24-337 */
+  SX_OP_ILU0 = 12,           /* ILU0Preconditioner                     preconditioners.rs:194-399 */
+  SX_OP_SSOR = 13            /* SSORPreconditioner                     preconditioners.rs:94-192 */
 } sx_op_kind;
 
 /* Which reference constructor's validation and error semantics to follow. */
@@ -262,6 +264,21 @@ typedef enum {
 } sx_ic0_variant;
 /* IC0Preconditioner::new (ic.rs:22-135) and its apply (ic.rs:143-220). */
 int sx_precond_ic0(sx_ctx ctx, sx_op a, int variant, sx_op* out);
+
+/* ILU0Preconditioner::new (preconditioners.rs:209-324) and its apply
+ * (:331-375): the reference's factorisation order and rounding, bit for bit
+ * (rows factorised in dependency order on the device); ValueError "Missing
+ * diagonal element at row k" / "Zero pivot at position k" for the first
+ * failing row.  The apply solves L y = x (unit diagonal), then U z = y
+ * dividing by the last diagonal entry of each row.  Not self-adjoint:
+ * rmatvec is OperationNotSupported.  A must be square (DimensionMismatch). */
+int sx_precond_ilu0(sx_ctx ctx, sx_op a, sx_op* out);
+/* SSORPreconditioner::new(matrix, omega) (preconditioners.rs:103-131) and
+ * its apply (:140-187): forward sweep (D + omega L) y = x, z = y * D (as the
+ * reference writes it), backward sweep (D + omega U) w = z; ValueError
+ * "Relaxation parameter omega must be in (0, 2)" / "Zero diagonal element
+ * at position i" (first diagonal entry, |d| < epsilon).  Not self-adjoint. */
+int sx_precond_ssor(sx_ctx ctx, sx_op a, double omega, sx_op* out);
 
 /* Factorised approximate inverse M^-1 = G G^T from a lower-triangular CSR G
  * (no reference counterpart; apply = two SpMVs through a cached G^T). */

@@ -76,6 +76,8 @@ def lib():
             "or_op_jacobi_from_diagonal": (vp, [ip, vp, u64, E]),
             "or_op_ic0": (vp, [vp, ip, E]),
             "or_op_fsai": (vp, [vp]),
+            "or_op_ilu0": (vp, [vp, E]),
+            "or_op_ssor": (vp, [vp, dbl, E]),
             "or_op_destroy": (None, [vp]),
             "or_op_matvec": (ip, [vp, vp, vp]),
             "or_op_rows": (u64, [vp]),
@@ -188,6 +190,24 @@ def op_ic0(a: Op, fast=True):
     if not h:
         raise ValueError(e.msg.decode())
     return Op(h, a.n, a.f64)
+
+
+def op_ilu0(a: Op):
+    e = Err()
+    h = lib().or_op_ilu0(a.h, C.byref(e))
+    if not h:
+        raise ValueError(e.msg.decode())
+    return Op(h, a.n, a.f64)
+
+
+def op_ssor(a: Op, omega: float):
+    e = Err()
+    h = lib().or_op_ssor(a.h, omega, C.byref(e))
+    if not h:
+        raise ValueError(e.msg.decode())
+    op = Op(h, a.n, a.f64)
+    op._base = a  # the SSOR operator reads a's arrays
+    return op
 
 
 def op_fsai(g: Op):

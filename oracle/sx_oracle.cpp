@@ -539,6 +539,115 @@ struct IC0Op : or_op {
   void mv32(const float* x, float* y) const override { ic0_apply(l32, nrows, x, y, fast); }
 };
 
+// ILU0Preconditioner (preconditioners.rs:194-399): factorisation with k
+// outermost as the reference writes it, then the L / U split and the two
+// substitutions.
+template <class F>
+struct ILU0Data {
+  std::vector<uint64_t> lp, li, up, ui;
+  std::vector<F> ld, ud;
+};
+template <class F>
+int ilu0_factor(const CsrOp* a, ILU0Data<F>& out, or_err* err) {
+  const uint64_t n = a->nrows;
+  const auto& indptr = a->indptr;
+  const auto& indices = a->indices;
+  std::vector<F> data(indices.size());
+  for (size_t q = 0; q < data.size(); ++q) data[q] = sizeof(F) == 8 ? (F)a->d64[q] : (F)a->d32[q];
+  const F eps = std::numeric_limits<F>::epsilon();
+  for (uint64_t k = 0; k < n; ++k) {
+    // find_diagonal_index (preconditioners.rs:382-399)
+    int64_t kd = -1;
+    for (uint64_t q = indptr[k]; q < indptr[k + 1]; ++q)
+      if (indices[q] == k) { kd = (int64_t)q; break; }
+    if (kd < 0) return set_err(err, E_VALUE, value_msg("Missing diagonal element at row " + std::to_string(k)));
+    const F kdiag = data[kd];
+    if (std::fabs(kdiag) < eps) return set_err(err, E_VALUE, value_msg("Zero pivot at position " + std::to_string(k)));
+    for (uint64_t i = k + 1; i < n; ++i) {
+      const uint64_t rs = indptr[i], re = indptr[i + 1];
+      int64_t kpos = -1;
+      for (uint64_t q = rs; q < re; ++q) {
+        if (indices[q] == k) { kpos = (int64_t)q; break; }
+        if (indices[q] > k) break;
+      }
+      if (kpos < 0) continue;
+      const F mult = data[kpos] / kdiag;
+      data[kpos] = mult;
+      for (uint64_t kj = indptr[k]; kj < indptr[k + 1]; ++kj) {
+        const uint64_t j = indices[kj];
+        if (j <= k) continue;
+        for (uint64_t ij = rs; ij < re; ++ij)
+          if (indices[ij] == j) { data[ij] = data[ij] - mult * data[kj]; break; }
+      }
+    }
+  }
+  out.lp.assign(1, 0);
+  out.up.assign(1, 0);
+  for (uint64_t i = 0; i < n; ++i) {
+    for (uint64_t q = indptr[i]; q < indptr[i + 1]; ++q) {
+      if (indices[q] < i) { out.li.push_back(indices[q]); out.ld.push_back(data[q]); }
+      else { out.ui.push_back(indices[q]); out.ud.push_back(data[q]); }
+    }
+    out.lp.push_back(out.li.size());
+    out.up.push_back(out.ui.size());
+  }
+  return ok(err);
+}
+template <class F>
+void ilu0_apply(const ILU0Data<F>& f, uint64_t n, const F* x, F* z) {
+  std::vector<F> y(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    y[i] = x[i];
+    for (uint64_t q = f.lp[i]; q < f.lp[i + 1]; ++q) y[i] = y[i] - f.ld[q] * y[f.li[q]];
+  }
+  for (uint64_t t = n; t-- > 0;) {
+    z[t] = y[t];
+    F dv = F(1);
+    for (uint64_t q = f.up[t]; q < f.up[t + 1]; ++q) {
+      const uint64_t c = f.ui[q];
+      if (c == t) dv = f.ud[q];
+      else if (c > t) z[t] = z[t] - f.ud[q] * z[c];
+    }
+    z[t] /= dv;
+  }
+}
+struct ILU0Op : or_op {
+  ILU0Data<double> f64d;
+  ILU0Data<float> f32d;
+  void mv64(const double* x, double* y) const override { ilu0_apply(f64d, nrows, x, y); }
+  void mv32(const float* x, float* y) const override { ilu0_apply(f32d, nrows, x, y); }
+};
+
+// SSORPreconditioner (preconditioners.rs:94-192)
+template <class F>
+void ssor_apply(const CsrOp* a, const std::vector<F>& dg, F omega, const F* x, F* w) {
+  const uint64_t n = a->nrows;
+  auto val = [&](uint64_t q) -> F { return sizeof(F) == 8 ? (F)a->d64[q] : (F)a->d32[q]; };
+  std::vector<F> y(n), z(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    F sum = x[i];
+    for (uint64_t q = a->indptr[i]; q < a->indptr[i + 1]; ++q)
+      if (a->indices[q] < i) sum -= omega * val(q) * y[a->indices[q]];
+    y[i] = sum / dg[i];
+  }
+  for (uint64_t i = 0; i < n; ++i) z[i] = y[i] * dg[i];
+  for (uint64_t t = n; t-- > 0;) {
+    F sum = z[t];
+    for (uint64_t q = a->indptr[t]; q < a->indptr[t + 1]; ++q)
+      if (a->indices[q] > t) sum -= omega * val(q) * w[a->indices[q]];
+    w[t] = sum / dg[t];
+  }
+}
+struct SSOROp : or_op {
+  const CsrOp* a = nullptr;
+  std::vector<double> d64;
+  std::vector<float> d32;
+  double om64 = 1;
+  float om32 = 1;
+  void mv64(const double* x, double* y) const override { ssor_apply<double>(a, d64, om64, x, y); }
+  void mv32(const float* x, float* y) const override { ssor_apply<float>(a, d32, om32, x, y); }
+};
+
 // M^-1 = G G^T: y = G (G^T x), G^T kept explicitly through the counting-sort
 // transpose; both products are plain CSR SpMVs.
 struct FsaiOp : or_op {
@@ -1286,6 +1395,42 @@ or_op* or_op_jacobi(const or_op* csr_base, or_err* err) {
   ok(err);
   return op;
 }
+or_op* or_op_ilu0(const or_op* csr_base, or_err* err) {
+  const CsrOp* a = dynamic_cast<const CsrOp*>(csr_base);
+  if (!a) { set_err(err, E_NOT_SUPPORTED, "Operation not supported: not a CSR operator"); return nullptr; }
+  auto* op = new ILU0Op();
+  op->f64 = a->f64; op->nrows = op->ncols = a->nrows;
+  const int rc = a->f64 ? ilu0_factor<double>(a, op->f64d, err) : ilu0_factor<float>(a, op->f32d, err);
+  if (rc) { delete op; return nullptr; }
+  return op;
+}
+
+or_op* or_op_ssor(const or_op* csr_base, double omega, or_err* err) {
+  const CsrOp* a = dynamic_cast<const CsrOp*>(csr_base);
+  if (!a) { set_err(err, E_NOT_SUPPORTED, "Operation not supported: not a CSR operator"); return nullptr; }
+  const bool bad = a->f64 ? (omega <= 0.0 || omega >= 2.0) : ((float)omega <= 0.0f || (float)omega >= 2.0f);
+  if (bad) { set_err(err, E_VALUE, value_msg("Relaxation parameter omega must be in (0, 2)")); return nullptr; }
+  auto* op = new SSOROp();
+  op->a = a; op->f64 = a->f64; op->nrows = op->ncols = a->nrows;
+  op->om64 = omega; op->om32 = (float)omega;
+  op->d64.resize(a->nrows); op->d32.resize(a->nrows);
+  for (uint64_t i = 0; i < a->nrows; ++i) {
+    const double d = csr_get<double>(a->indptr.data(), a->indices.data(), a->d64.data(), a->nrows, a->ncols, i, i);
+    const float d32 = csr_get<float>(a->indptr.data(), a->indices.data(), a->d32.data(), a->nrows, a->ncols, i, i);
+    const bool zero = a->f64 ? std::fabs(d) < std::numeric_limits<double>::epsilon()
+                             : std::fabs(d32) < std::numeric_limits<float>::epsilon();
+    if (zero) {
+      delete op;
+      set_err(err, E_VALUE, value_msg("Zero diagonal element at position " + std::to_string(i)));
+      return nullptr;
+    }
+    op->d64[i] = d;
+    op->d32[i] = d32;
+  }
+  ok(err);
+  return op;
+}
+
 or_op* or_op_jacobi_from_diagonal(int f64, const void* diag, uint64_t n, or_err* err) {
   auto* op = new DiagOp();
   op->f64 = f64; op->nrows = op->ncols = n;

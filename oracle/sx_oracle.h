@@ -152,6 +152,11 @@ int or_lgmres(const or_op* a, const void* b, uint64_t max_iter, uint64_t inner_m
               double atol, const void* x0, const or_op* m, void* x_out, or_result* res,
               or_err* err);
 
+/* ILU0Preconditioner::new (preconditioners.rs:209-324) and SSORPreconditioner::new
+ * (:103-131) on a CSR operator; NULL with err set on failure.  The SSOR
+ * operator refers to the CSR operator, which must outlive it. */
+or_op* or_op_ilu0(const or_op* a, or_err* err);
+or_op* or_op_ssor(const or_op* a, double omega, or_err* err);
 /* FP64 true relative residual ||b - A x|| / ||b|| with sequential sums. */
 double or_true_rel_residual(const int64_t* indptr, const int32_t* indices, const double* data,
                             int64_t n, const double* b, const double* x);

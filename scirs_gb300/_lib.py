@@ -34,6 +34,7 @@ SX_OP_CSR, SX_OP_IDENTITY, SX_OP_SCALED_IDENTITY, SX_OP_DIAGONAL = 0, 1, 2, 3
 SX_OP_JACOBI, SX_OP_IC0, SX_OP_FSAI, SX_OP_HOST = 4, 5, 6, 7
 SX_IC0_REFERENCE, SX_IC0_TEXTBOOK = 0, 1
 SX_OP_ZERO, SX_OP_SUM, SX_OP_PRODUCT, SX_OP_SYM_CSR = 8, 9, 10, 11
+SX_OP_ILU0, SX_OP_SSOR = 12, 13
 SX_SPMV_EXACT = 1
 SX_SPMV_SYM_HALF = 2
 
@@ -241,6 +242,8 @@ _SIGS = {
     "sx_precond_jacobi_from_diagonal": (c_int, [ctx_t, c_int, c_vp, c_u64, P(op_t)]),
     "sx_precond_ic0": (c_int, [ctx_t, op_t, c_int, P(op_t)]),
     "sx_precond_fsai": (c_int, [ctx_t, op_t, P(op_t)]),
+    "sx_precond_ilu0": (c_int, [ctx_t, op_t, P(op_t)]),
+    "sx_precond_ssor": (c_int, [ctx_t, op_t, c_dbl, P(op_t)]),
     "sx_cg_options_default": (None, [P(CGOptions)]),
     "sx_bicgstab_options_default": (None, [P(BiCGSTABOptions)]),
     "sx_gmres_options_default": (None, [P(GMRESOptions)]),

@@ -30,6 +30,7 @@ SOURCES = [
     "sx_gnn.cu",
     "sx_sym.cu",
     "sx_krylov2.cu",
+    "sx_ilu.cu",
     "sx_gen.cpp",
 ]
 

@@ -788,6 +788,7 @@ void destroy_op_internal(sx_op op) {
   if (op->transpose) destroy_op_internal(op->transpose);
   if (op->sym_low) destroy_op_internal(op->sym_low);
   if (op->ic0) ic0_destroy(op->ic0);
+  if (op->tri) tri_destroy(op->tri);
   delete op;
 }
 }  // namespace sx
@@ -1486,6 +1487,8 @@ extern "C" {
 static bool has_adjoint(sx_op op) {
   switch (op->kind) {
     case SX_OP_HOST: return false;  // interface.rs:49-51 (the trait's default)
+    case SX_OP_ILU0:                // preconditioners.rs:378-380
+    case SX_OP_SSOR: return false;  // preconditioners.rs:189-191
     case SX_OP_SUM:
     case SX_OP_PRODUCT: return has_adjoint(op->left) && has_adjoint(op->right);  // :349, :399
     default: return true;

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "sx_launch.cuh"
+#include "sx_sync.cuh"
 
 namespace sx {
 
@@ -61,72 +62,6 @@ void ic0_destroy(IC0Dev* p) {
 }
 
 namespace {
-
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
-
-__device__ __forceinline__ unsigned long long globaltimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ int ld_flag(const int* p) { return *(volatile const int*)p; }
-// acquire load: later loads see what the publisher wrote before its release
-__device__ __forceinline__ int ld_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-// Waits until *flag != 0; false if the wait was abandoned (abort raised or
-// the 2-s limit passed).  Spins without sleeping first: the wait sits on
-// the critical path of the triangular solves, one wait per dependency level.
-__device__ bool wait_flag(const int* flag, int* abort) {
-  if (ld_acquire(flag)) return true;
-  const unsigned long long t0 = globaltimer();
-  for (unsigned it = 1;; ++it) {
-    if (ld_acquire(flag)) return true;
-    if ((it & 63u) == 0) {
-      if (ld_flag(abort)) return false;
-      if (globaltimer() - t0 > kWaitNs) {
-        atomicExch(abort, 1);
-        return false;
-      }
-    }
-    if (it > 4096u) __nanosleep(128);
-  }
-}
-
-// release store: the row's result is visible before its flag
-__device__ __forceinline__ void publish(int* flag) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(flag), "r"(1) : "memory");
-}
-
-template <typename T>
-__device__ __forceinline__ T ldv(const T* p) { return __ldcg(p); }
-
-// ---- building L: lower entries (col <= row) in storage order (ic.rs:32-49)
-__global__ void k_lower_count(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                              int64_t n, int32_t* cnt) {
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    int32_t c = 0;
-    for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) c += idx[k] <= (int32_t)r;
-    cnt[r] = c;
-  }
-}
-
-template <typename T>
-__global__ void k_lower_copy(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                             const T* __restrict__ val, int64_t n, const int32_t* __restrict__ lp,
-                             int32_t* li, T* lv) {
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    int32_t o = lp[r];
-    for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k)
-      if (idx[k] <= (int32_t)r) { li[o] = idx[k]; lv[o] = val[k]; ++o; }
-  }
-}
 
 // per-row error record: err[0] = smallest failing row (or INT_MAX), err_code[row]
 enum : int { E_NONE = 0, E_MISSING_DIAG = 1, E_NOT_PD = 2 };
@@ -406,14 +341,21 @@ int ic0_apply(sx_ctx ctx, sx_op op, const void* x, void* y) {
 }
 
 // abort flag of an IC(0) operator: a wait that gave up
+// (also of the ILU(0) and SSOR sweeps, which use the same waits)
 int ic0_health(sx_ctx ctx, sx_op op) {
-  if (!op || op->kind != SX_OP_IC0 || !op->ic0) return SX_OK;
+  if (!op) return SX_OK;
+  const int* ctl = nullptr;
+  if (op->kind == SX_OP_IC0 && op->ic0) ctl = op->ic0->ctl;
+  else if (op->kind == SX_OP_ILU0 || op->kind == SX_OP_SSOR) ctl = tri_ctl(op);
+  if (!ctl) return SX_OK;
   int h[4] = {0, 0, 0, 0};
-  SX_CUDA(cudaMemcpyAsync(h, op->ic0->ctl, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  SX_CUDA(cudaMemcpyAsync(h, ctl, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   SX_CUDA(cudaStreamSynchronize(ctx->stream));
   if (h[2])
     return set_error(SX_ERR_DEVICE_TIMEOUT,
-                     "Device timeout: an IC(0) dependency wait exceeded its time limit");
+                     op->kind == SX_OP_IC0
+                         ? "Device timeout: an IC(0) dependency wait exceeded its time limit"
+                         : "Device timeout: a triangular-sweep dependency wait exceeded its time limit");
   return SX_OK;
 }
 
@@ -421,7 +363,7 @@ int ic0_health(sx_ctx ctx, sx_op op) {
 // Rows sorted by dependency level (a stable counting sort): forward, a row
 // depends on the rows j < i of its pattern; backward, on the rows j > i.  A
 // row's dependencies sit on lower levels, so they are handed out before it.
-static int level_order(sx_ctx ctx, const DevCsr& c, bool forward, int32_t** out) {
+int level_order(sx_ctx ctx, const DevCsr& c, bool forward, int32_t** out) {
   const int64_t n = c.nrows;
   std::vector<int32_t> ptr(n + 1), idx(std::max<int64_t>(c.nnz, 1));
   SX_CUDA(cudaMemcpyAsync(ptr.data(), c.indptr, (n + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));

@@ -81,6 +81,8 @@ struct DevCsr {
 };
 
 struct IC0Dev;   // defined in sx_ic0.cu
+struct TriDev;   // ILU(0) / SSOR, defined in sx_ilu.cu
+void tri_destroy(TriDev* p);
 struct HostOp {
   sx_host_matvec_fn fn = nullptr;
   void* user = nullptr;
@@ -98,6 +100,7 @@ struct sx_op_s {
   double scale = 1.0;                 // SCALED_IDENTITY
   sx_op_s* transpose = nullptr;       // cached transpose (rmatvec, FSAI's G^T)
   sx::IC0Dev* ic0 = nullptr;
+  sx::TriDev* tri = nullptr;          // ILU0 / SSOR
   sx::HostOp host;
   void* work = nullptr;               // per-operator temporary vector (FSAI: G^T x;
                                       // SUM: B x; PRODUCT: B x)
@@ -192,6 +195,12 @@ int ic0_health(sx_ctx ctx, sx_op op);
 int ensure_transpose(sx_ctx ctx, sx_op a);
 int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out);
 int sym_half_spmv(sx_ctx ctx, sx_op a, const void* x, void* y);  // sx_sym.cu
+// rows in dependency-level order (forward: on the rows j < i of the pattern;
+// backward: on j > i), on the device (sx_ic0.cu)
+int level_order(sx_ctx ctx, const DevCsr& c, bool forward, int32_t** out);
+// ILU(0) / SSOR (sx_ilu.cu): apply, and the abort flag of their waits
+int tri_apply(sx_ctx ctx, sx_op op, const void* x, void* y);
+int* tri_ctl(sx_op op);
 void destroy_op_internal(sx_op op);
 
 // Grid geometry for the vector kernels (fixed per device -> deterministic

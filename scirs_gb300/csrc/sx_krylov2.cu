@@ -42,6 +42,8 @@ int adjoint_op(sx_ctx ctx, sx_op op, sx_op* out) {
       *out = op->transpose;
       return SX_OK;
     case SX_OP_HOST:
+    case SX_OP_ILU0:  // preconditioners.rs:189-191, :378-380
+    case SX_OP_SSOR:
       return set_error(SX_ERR_OPERATION_NOT_SUPPORTED,
                        "Operation not supported: adjoint not implemented for this operator");
     case SX_OP_ZERO:

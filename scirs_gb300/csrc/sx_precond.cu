@@ -52,6 +52,8 @@ extern "C" int sx_spmv_kernel(sx_ctx ctx, sx_op a, unsigned flags, char* buf, ui
              "; G: " + spmv_kernel_name(ctx, a->csr, w, fma, !exact);
       break;
     case SX_OP_IC0: name = "k_ic0_forward + k_ic0_backward"; break;
+    case SX_OP_ILU0:
+    case SX_OP_SSOR: name = "k_tri_sweep (forward) + k_tri_sweep (backward)"; break;
     case SX_OP_HOST: name = "host callback"; break;
     default: name = "k_diag_apply"; break;
   }
@@ -64,6 +66,9 @@ int apply_general(sx_ctx ctx, sx_op op, const void* x, void* y) {
   switch (op->kind) {
     case SX_OP_IC0:
       return ic0_apply(ctx, op, x, y);
+    case SX_OP_ILU0:
+    case SX_OP_SSOR:
+      return tri_apply(ctx, op, x, y);
     case SX_OP_FSAI:
       return spmv_device(ctx, op, x, y, 0);
     case SX_OP_HOST: {

@@ -478,6 +478,20 @@ def ic0(ctx: Context, a: Operator, textbook: bool = False) -> Operator:
     return Operator(ctx, h)
 
 
+def ilu0(ctx: Context, a: Operator) -> Operator:
+    """ILU0Preconditioner::new(&matrix) (preconditioners.rs:209-324)."""
+    h = L.op_t()
+    _check(L.lib.sx_precond_ilu0(ctx.handle, a.handle, C.byref(h)))
+    return Operator(ctx, h)
+
+
+def ssor(ctx: Context, a: Operator, omega: float) -> Operator:
+    """SSORPreconditioner::new(matrix, omega) (preconditioners.rs:103-131)."""
+    h = L.op_t()
+    _check(L.lib.sx_precond_ssor(ctx.handle, a.handle, float(omega), C.byref(h)))
+    return Operator(ctx, h)
+
+
 def fsai(ctx: Context, g: Operator) -> Operator:
     """M^-1 = G G^T from a lower-triangular CSR G."""
     h = L.op_t()
