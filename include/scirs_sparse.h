@@ -143,6 +143,18 @@ int sx_csr_from_raw_i32(sx_ctx ctx, sx_dtype dtype, const int64_t* indptr, const
                         const void* data, uint64_t nrows, uint64_t ncols, uint64_t nnz,
                         sx_mem mem, sx_op* out);
 
+/* save_npz (io.rs:49-177) of a CSR operator: the reference's little-endian
+ * "csr_array" record (format marker, shape, data, indices, indptr), not a
+ * SciPy zip archive.  I/O failures: ComputationError "IO error: ...". */
+int sx_csr_save_npz(sx_ctx ctx, sx_op a, const char* path);
+/* load_npz (io.rs:197-269) of a "csr_array" record into a device CSR, with
+ * CsrArray::new's validation (csr_array.rs:77-136); values are read in
+ * `dtype`'s width, as load_npz::<T> does.  Other known markers (csc_array,
+ * coo_array, dok_array) are NotImplemented; unknown ones ConversionError
+ * "Unknown format: ..."; short files ComputationError "IO error: failed to
+ * fill whole buffer". */
+int sx_csr_load_npz(sx_ctx ctx, sx_dtype dtype, const char* path, sx_op* out);
+
 /* Counting-sort transpose, bit-exact with CsrMatrix::transpose
  * (csr.rs:289-326) and CsrArray::transpose (csr_array.rs:595-625). */
 int sx_csr_transpose(sx_ctx ctx, sx_op a, sx_op* out);

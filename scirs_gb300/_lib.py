@@ -210,6 +210,8 @@ _SIGS = {
     "sx_csr_from_raw": (c_int, [ctx_t, c_int, c_int, c_vp, c_u64, c_vp, c_vp, c_u64, c_u64, c_u64, P(op_t)]),
     "sx_csr_from_raw_i32": (c_int, [ctx_t, c_int, c_vp, c_vp, c_vp, c_u64, c_u64, c_u64, c_int, P(op_t)]),
     "sx_csr_transpose": (c_int, [ctx_t, op_t, P(op_t)]),
+    "sx_csr_save_npz": (c_int, [ctx_t, op_t, C.c_char_p]),
+    "sx_csr_load_npz": (c_int, [ctx_t, c_int, C.c_char_p, P(op_t)]),
     "sx_csr_astype": (c_int, [ctx_t, op_t, c_int, P(op_t)]),
     "sx_csr_info": (c_int, [op_t, P(c_u64), P(c_u64), P(c_u64), P(c_int)]),
     "sx_csr_download": (c_int, [ctx_t, op_t, c_vp, c_vp, c_vp]),

@@ -31,6 +31,7 @@ SOURCES = [
     "sx_sym.cu",
     "sx_krylov2.cu",
     "sx_ilu.cu",
+    "sx_io.cu",
     "sx_gen.cpp",
 ]
 

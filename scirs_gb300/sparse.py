@@ -12,6 +12,7 @@ nothing here computes on the host.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 from typing import Optional
 
@@ -367,6 +368,18 @@ def _from_raw(ctx, data, indptr, indices, shape, dtype, api):
     _check(L.lib.sx_csr_from_raw(ctx.handle, _dtype_code(dtype), api, _ptr(indptr), len(indptr),
                                  _ptr(indices), _ptr(data), len(data), int(shape[0]), int(shape[1]),
                                  C.byref(h)))
+    return Operator(ctx, h)
+
+
+def save_npz(a: Operator, path) -> None:
+    """save_npz(&array, path) (io.rs:49-177): the reference's "csr_array" record."""
+    _check(L.lib.sx_csr_save_npz(a.ctx.handle, a.handle, os.fsencode(path)))
+
+
+def load_npz(ctx: Context, path, dtype=np.float64) -> Operator:
+    """load_npz::<T, _>(path) (io.rs:197-269) of a "csr_array" record, onto the device."""
+    h = L.op_t()
+    _check(L.lib.sx_csr_load_npz(ctx.handle, _dtype_code(dtype), os.fsencode(path), C.byref(h)))
     return Operator(ctx, h)
 
 
