@@ -674,10 +674,18 @@ __global__ void k_to_half(const float* __restrict__ in, __half* out, int64_t n) 
 int csr_make_half(sx_ctx ctx, DevCsr& c) {
   dev_free(c.vals16);
   c.vals16 = nullptr;
+  dev_free(c.dia_vals16);
+  c.dia_vals16 = nullptr;
   if (c.nnz <= 0) return SX_OK;
   SX_CHECK(dev_alloc(&c.vals16, c.nnz * 2));
   k_to_half<<<vec_grid(ctx, c.nnz), kBlock, 0, ctx->stream>>>((const float*)c.vals, (__half*)c.vals16, c.nnz);
   ctx->launches++;
+  if (c.dia_vals) {
+    const int64_t m = (int64_t)c.dia_n * c.dia_ld;
+    SX_CHECK(dev_alloc(&c.dia_vals16, m * 2));
+    k_to_half<<<vec_grid(ctx, m), kBlock, 0, ctx->stream>>>((const float*)c.dia_vals, (__half*)c.dia_vals16, m);
+    ctx->launches++;
+  }
   SX_CUDA(cudaGetLastError());
   return SX_OK;
 }
@@ -714,7 +722,131 @@ int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
   return SX_OK;
 }
 
-int csr_finalize_stats(sx_ctx ctx, DevCsr& c) {
+// ---- diagonal layout -------------------------------------------------
+// flags[0]: more than kDiaMax distinct offsets; flags[1]: a row whose
+// columns do not strictly increase, or a row longer than kDiaMax
+__global__ void k_dia_offsets(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n,
+                              int* table, int* flags) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int32_t s = ptr[r], e = ptr[r + 1];
+    if (e - s > kDiaMax) {
+      flags[1] = 1;
+      continue;
+    }
+    int32_t prev = INT_MIN;
+    for (int32_t k = s; k < e; ++k) {
+      const int32_t c = idx[k];
+      if (c <= prev) flags[1] = 1;
+      prev = c;
+      const int off = c - (int)r;
+      bool found = false;
+      for (int q = 0; q < kDiaMax && !found; ++q) {
+        const int v = table[q];
+        if (v == off) {
+          found = true;
+        } else if (v == INT_MIN) {
+          const int old = atomicCAS(table + q, INT_MIN, off);
+          found = old == INT_MIN || old == off;
+        }
+      }
+      if (!found) flags[0] = 1;
+    }
+  }
+}
+
+struct DiaTable {
+  int32_t off[kDiaMax];
+};
+
+template <typename T>
+__global__ void k_dia_fill(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                           const T* __restrict__ val, int64_t n, DiaTable tab, int nd, int64_t ld, T* dv,
+                           uint16_t* mask) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    unsigned m = 0;
+    for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) {
+      const int off = idx[k] - (int)r;
+      int d = 0;
+      while (d < nd && tab.off[d] != off) ++d;
+      if (d == nd) continue;  // cannot happen once every offset is in the table
+      dv[(int64_t)d * ld + r] = val[k];
+      m |= 1u << d;
+    }
+    mask[r] = (uint16_t)m;
+  }
+}
+
+static void free_dia(DevCsr& c) {
+  dev_free(c.dia_vals);
+  dev_free(c.dia_vals16);
+  dev_free(c.dia_mask);
+  c.dia_vals = nullptr;
+  c.dia_vals16 = nullptr;
+  c.dia_mask = nullptr;
+  c.dia_n = 0;
+  c.dia_ld = 0;
+}
+
+// Builds the diagonal layout when it fits (at most kDiaMax diagonals, rows
+// strictly increasing, at most 25 % padding); otherwise leaves none.
+int csr_prepare_dia(sx_ctx ctx, DevCsr& c, int w) {
+  free_dia(c);
+  if (!ctx->dia || w == 0 || !c.monotone || c.nnz <= 0 || c.nrows <= 0 || c.nrows != c.ncols ||
+      c.max_row_len > kDiaMax)
+    return SX_OK;
+  int* d = nullptr;
+  SX_CHECK(dev_alloc((void**)&d, (kDiaMax + 2) * sizeof(int)));
+  std::vector<int> init(kDiaMax + 2, INT_MIN);
+  init[kDiaMax] = init[kDiaMax + 1] = 0;
+  SX_CUDA(cudaMemcpyAsync(d, init.data(), init.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  k_dia_offsets<<<vec_grid(ctx, c.nrows), kBlock, 0, ctx->stream>>>(c.indptr, c.indices, c.nrows, d, d + kDiaMax);
+  ctx->launches++;
+  std::vector<int> h(kDiaMax + 2);
+  SX_CUDA(cudaMemcpyAsync(h.data(), d, h.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  dev_free(d);
+  if (e != cudaSuccess) return cuda_fail(e, "diagonal offsets", __FILE__, __LINE__);
+  if (h[kDiaMax] || h[kDiaMax + 1]) return SX_OK;
+  std::vector<int32_t> offs;
+  for (int q = 0; q < kDiaMax; ++q)
+    if (h[q] != INT_MIN) offs.push_back(h[q]);
+  std::sort(offs.begin(), offs.end());
+  const int nd = (int)offs.size();
+  // row stride of the diagonals: a multiple of 32 rows plus an odd number of
+  // 32-row groups, so the diagonals (read together) do not start at the same
+  // offset of a power-of-two span of memory
+  const int64_t ld = (c.nrows + 31) / 32 * 32 + 32 * 37;
+  if ((double)nd * (double)c.nrows > 1.25 * (double)c.nnz) return SX_OK;
+  DiaTable tab;
+  for (int q = 0; q < kDiaMax; ++q) tab.off[q] = q < nd ? offs[q] : 0;
+  SX_CHECK(dev_alloc(&c.dia_vals, (size_t)nd * ld * w));
+  int rc = dev_alloc((void**)&c.dia_mask, (size_t)c.nrows * 2);
+  if (rc != SX_OK) {
+    free_dia(c);
+    return rc;
+  }
+  SX_CUDA(cudaMemsetAsync(c.dia_vals, 0, (size_t)nd * ld * w, ctx->stream));
+  if (w == 8)
+    k_dia_fill<double><<<vec_grid(ctx, c.nrows), kBlock, 0, ctx->stream>>>(
+        c.indptr, c.indices, (const double*)c.vals, c.nrows, tab, nd, ld, (double*)c.dia_vals, c.dia_mask);
+  else
+    k_dia_fill<float><<<vec_grid(ctx, c.nrows), kBlock, 0, ctx->stream>>>(
+        c.indptr, c.indices, (const float*)c.vals, c.nrows, tab, nd, ld, (float*)c.dia_vals, c.dia_mask);
+  ctx->launches++;
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    free_dia(c);
+    return cuda_fail(e, "diagonal layout", __FILE__, __LINE__);
+  }
+  c.dia_n = nd;
+  c.dia_ld = ld;
+  for (int q = 0; q < kDiaMax; ++q) c.dia_off[q] = tab.off[q];
+  return SX_OK;
+}
+
+int csr_finalize_stats(sx_ctx ctx, DevCsr& c, int w) {
   int* d = nullptr;
   SX_CHECK(dev_alloc((void**)&d, 4 * sizeof(int)));
   cudaMemsetAsync(d, 0, 4 * sizeof(int), ctx->stream);
@@ -734,7 +866,8 @@ int csr_finalize_stats(sx_ctx ctx, DevCsr& c) {
   c.has_sorted_indices = h[2] == 0;
   c.max_chunk_nnz = h[3];
   c.mean_row_len = c.nrows > 0 ? (double)c.nnz / (double)c.nrows : 0.0;
-  return csr_prepare_tiles(ctx, c);
+  SX_CHECK(csr_prepare_tiles(ctx, c));
+  return csr_prepare_dia(ctx, c, w);
 }
 
 static std::atomic<uint64_t> g_op_serial{1};
@@ -756,6 +889,7 @@ static sx_op new_op(sx_ctx ctx, int kind, int dtype, int64_t nrows, int64_t ncol
 }
 
 static void free_csr(DevCsr& c) {
+  free_dia(c);
   dev_free(c.indptr);
   dev_free(c.indices);
   dev_free(c.vals);
@@ -862,6 +996,7 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   c->num_sms = sms;
   c->own_stream = own;
   if (const char* t = std::getenv("SX_WIN")) c->win_mode = std::atoi(t);
+  if (const char* t = std::getenv("SX_DIA")) c->dia = std::atoi(t);
   if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "1") == 0;
   if (const char* t = std::getenv("SX_MX_FUSED")) c->mx_unfused = std::strcmp(t, "0") == 0;
   if (const char* t = std::getenv("SX_SHORT")) c->short_rows = std::atoi(t);
@@ -1011,7 +1146,7 @@ int sx_csr_from_triplets(sx_ctx ctx, sx_dtype dtype, sx_csr_api api, const uint6
       cudaMemcpyAsync(c.indices, cols32, n * 4, cudaMemcpyDeviceToDevice, ctx->stream);
       cudaMemcpyAsync(c.vals, d_data, n * w, cudaMemcpyDeviceToDevice, ctx->stream);
     }
-    if ((rc = csr_finalize_stats(ctx, c))) break;
+    if ((rc = csr_finalize_stats(ctx, c, (int)elt_size(dtype)))) break;
   } while (0);
   cleanup();
   if (rc != SX_OK) {
@@ -1106,7 +1241,7 @@ int sx_csr_from_raw(sx_ctx ctx, sx_dtype dtype, sx_csr_api api, const uint64_t* 
     c.nrows = (int64_t)nrows;
     c.ncols = (int64_t)ncols;
     c.nnz = n;
-    if ((rc = csr_finalize_stats(ctx, c))) break;
+    if ((rc = csr_finalize_stats(ctx, c, (int)w))) break;
   } while (0);
   dev_free(d_ptr); dev_free(d_idx); dev_free(flags); dev_free(maxes);
   if (rc != SX_OK) {
@@ -1167,7 +1302,7 @@ int sx_csr_from_raw_i32(sx_ctx ctx, sx_dtype dtype, const int64_t* indptr, const
     c.nrows = m;
     c.ncols = (int64_t)ncols;
     c.nnz = n;
-    if ((rc = csr_finalize_stats(ctx, c))) break;
+    if ((rc = csr_finalize_stats(ctx, c, (int)w))) break;
     if (!c.monotone) { rc = err_value("Row pointer array must be monotonically increasing"); break; }
   } while (0);
   dev_free(d_ptr64);
@@ -1231,7 +1366,7 @@ static int csr_transpose_dev(sx_ctx ctx, const DevCsr& a, int dtype, DevCsr& t) 
             keys, n, (const float*)a.vals, t.indices, (float*)t.vals);
       ctx->launches++;
     }
-    rc = csr_finalize_stats(ctx, t);
+    rc = csr_finalize_stats(ctx, t, (int)elt_size(dtype));
   } while (0);
   dev_free(cnt);
   dev_free(cursor);
@@ -1272,6 +1407,7 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
   DevCsr c = a->csr;
   c.indptr = nullptr; c.indices = nullptr; c.vals = nullptr; c.tile_row = nullptr; c.units = 0;
   c.col16 = nullptr; c.chunk_base = nullptr; c.vals16 = nullptr;
+  c.dia_vals = nullptr; c.dia_vals16 = nullptr; c.dia_mask = nullptr;
   const int64_t n = a->csr.nnz;
   int rc = SX_OK;
   do {
@@ -1291,6 +1427,26 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
         k_convert<double, float><<<g, kBlock, 0, ctx->stream>>>((const float*)a->csr.vals, (double*)c.vals, n);
         ctx->launches++;
       }
+    }
+    // the diagonal layout converts along (same positions, new value type)
+    if (a->csr.dia_vals && ctx->dia) {
+      const int64_t m = (int64_t)c.dia_n * c.dia_ld;
+      if ((rc = dev_alloc(&c.dia_vals, m * elt_size(dtype)))) break;
+      if ((rc = dev_alloc((void**)&c.dia_mask, c.nrows * 2))) break;
+      cudaMemcpyAsync(c.dia_mask, a->csr.dia_mask, c.nrows * 2, cudaMemcpyDeviceToDevice, ctx->stream);
+      const int g = vec_grid(ctx, m);
+      if (a->dtype == dtype) {
+        cudaMemcpyAsync(c.dia_vals, a->csr.dia_vals, m * elt_size(dtype), cudaMemcpyDeviceToDevice, ctx->stream);
+      } else if (dtype == SX_F32) {
+        k_convert<float, double><<<g, kBlock, 0, ctx->stream>>>((const double*)a->csr.dia_vals, (float*)c.dia_vals, m);
+        ctx->launches++;
+      } else {
+        k_convert<double, float><<<g, kBlock, 0, ctx->stream>>>((const float*)a->csr.dia_vals, (double*)c.dia_vals, m);
+        ctx->launches++;
+      }
+    } else {
+      c.dia_n = 0;
+      c.dia_ld = 0;
     }
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) { rc = cuda_fail(e, "astype", __FILE__, __LINE__); break; }

@@ -78,7 +78,20 @@ struct DevCsr {
   // FP16 copy of FP32 values (__half), read by solver-internal applies of a
   // learned factor; the exact API path keeps using vals
   void* vals16 = nullptr;
+  // diagonal layout, set when the nonzeros lie on at most kDiaMax diagonals,
+  // every row's columns strictly increase and the padding is small:
+  // dia_vals[d * dia_ld + row] = the entry of `row` on diagonal d (offset
+  // dia_off[d], ascending), zero where absent; bit d of dia_mask[row] says
+  // whether the row stores that entry.  Ascending offsets are the storage
+  // order of a sorted row, so a row's sum keeps the CSR order.
+  int32_t dia_n = 0;
+  int32_t dia_off[16] = {0};
+  int64_t dia_ld = 0;
+  void* dia_vals = nullptr;
+  void* dia_vals16 = nullptr;  // FP16 copy, with vals16
+  uint16_t* dia_mask = nullptr;
 };
+constexpr int kDiaMax = 16;
 
 struct IC0Dev;   // defined in sx_ic0.cu
 struct TriDev;   // ILU(0) / SSOR, defined in sx_ilu.cu
@@ -145,6 +158,9 @@ struct sx_ctx_s {
   // short-row SpMV: 1 (default) for FP64 with fused multiply-adds, 2 also
   // for FP32, 0 never (SX_SHORT)
   int short_rows = 1;
+  // diagonal layout (SX_DIA): 0 never built or used; 1 (default) used for
+  // FP64 matrices and FP16 value copies; 2 used for every matrix that has it
+  int dia = 1;
   int win_shape = 0;
 };
 
@@ -161,7 +177,9 @@ void dev_free(void* p);
 
 // Upload host-side CSR arrays (already validated, int32) into a DevCsr and
 // compute row statistics.
-int csr_finalize_stats(sx_ctx ctx, DevCsr& c);
+// w: bytes per value (4 or 8) to also build the diagonal layout; 0 skips it
+int csr_finalize_stats(sx_ctx ctx, DevCsr& c, int w = 0);
+int csr_prepare_dia(sx_ctx ctx, DevCsr& c, int w);
 // FP16 copy of an FP32 CSR's values (c.vals16)
 int csr_make_half(sx_ctx ctx, DevCsr& c);
 // a process-unique operator serial (keys of the solvers' graph caches)

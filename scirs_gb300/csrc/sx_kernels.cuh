@@ -125,6 +125,25 @@ __device__ __forceinline__ Vec4<float> ld4(const __half* p) {
   const float2 fa = __half22float2(a), fb = __half22float2(b);
   return Vec4<float>{{fa.x, fa.y, fb.x, fb.y}};
 }
+template <typename T>
+struct DiaVec {
+  static constexpr int kVec = 16 / (int)sizeof(T);
+};
+__device__ __forceinline__ void vload(const float* p, float (&o)[4]) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+}
+__device__ __forceinline__ void vload(const double* p, double (&o)[2]) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+  o[0] = a.x; o[1] = a.y;
+}
+__device__ __forceinline__ void vload(const __half* p, float (&o)[4]) {
+  const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+  const float2 fa = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+  const float2 fb = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+  o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
+}
+
 __device__ __forceinline__ float to_val(__half v) { return __half2float(v); }
 __device__ __forceinline__ float to_val(float v) { return v; }
 __device__ __forceinline__ double to_val(double v) { return v; }
@@ -223,6 +242,9 @@ __global__ void __launch_bounds__(kBlock) spmv_stream_kernel(
 template <typename T>
 struct GatherPlain {
   __device__ __forceinline__ T operator()(const T* __restrict__ x, int col) const { return __ldg(x + col); }
+  // 16 bytes at an aligned column (the diagonal-layout kernel)
+  template <int VEC>
+  __device__ __forceinline__ void vec(const T* __restrict__ x, int col, T (&o)[VEC]) const { vload(x + col, o); }
 };
 
 template <typename T, int ITEMS, class Epi, bool FMA = false, bool C16 = false, int MINB = 1, typename V = T,
@@ -421,6 +443,114 @@ __global__ void __launch_bounds__(kBlock) vec_kernel(int64_t n, T* partials,
 }  // namespace sx
 
 namespace sx {
+
+// Diagonal-layout SpMV.  The entries of row r sit at vals[d * ld + r] on the
+// diagonals d whose bit is set in mask[r]; no column indices are read.  A
+// thread owns VEC consecutive rows (4 in FP32, 2 in FP64): for every
+// diagonal it reads the rows' values with one vector load and their x
+// operands with one or two aligned vector loads (two when the diagonal's
+// offset is not a multiple of VEC, then shifted in registers).  The
+// diagonals ascend in offset, which is the storage order of the sorted CSR
+// row, and each row's sum runs over its stored diagonals in that order
+// (from zero, rounded products, or fused multiply-adds for FMA), so the
+// result is that of the CSR kernels.  Groups near the ends of the matrix,
+// where a vector load could leave [0, n), take the row-by-row path.
+struct DiaOffs {
+  int32_t off[16];
+};
+
+// x operands of VEC rows starting at column c: aligned loads at c - s and,
+// when s = c mod VEC is not zero, at c - s + VEC
+template <typename T, int VEC, class Gather>
+__device__ __forceinline__ void dia_xvec(const Gather& gat, const T* x, int c, int s, T (&o)[VEC]) {
+  T a[VEC];
+  gat.vec(x, c - s, a);
+  if (s == 0) {
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) o[j] = a[j];
+    return;
+  }
+  T b[VEC];
+  gat.vec(x, c - s + VEC, b);
+#pragma unroll
+  for (int sh = 1; sh < VEC; ++sh)
+    if (s == sh) {
+#pragma unroll
+      for (int j = 0; j < VEC; ++j) o[j] = j + sh < VEC ? a[j + sh] : b[j + sh - VEC];
+    }
+}
+
+template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>>
+__global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ vals,
+                                                          const uint16_t* __restrict__ mask, int64_t ld,
+                                                          DiaOffs offs, int nd, const T* __restrict__ x,
+                                                          T* __restrict__ y, int64_t nrows, T* partials,
+                                                          unsigned int* counter, Epi epi, Gather gat = Gather{}) {
+  if (epi.skip()) return;
+  constexpr int VEC = DiaVec<T>::kVec;
+  Acc3<T> a{T(0), T(0), T(0)};
+  const int n = (int)nrows;
+  const int omin = offs.off[0], omax = offs.off[nd - 1];
+  const int groups = (n + VEC - 1) / VEC;
+  const int stride = (int)gridDim.x * kBlock;
+  for (int g = (int)blockIdx.x * kBlock + (int)threadIdx.x; g < groups; g += stride) {
+    const int r0 = g * VEC;
+    T acc[VEC];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) acc[j] = T(0);
+    const bool inner = r0 + omin - VEC >= 0 && r0 + omax + 2 * VEC <= n && r0 + VEC <= n;
+    if (inner) {
+      unsigned m[VEC];
+#pragma unroll
+      for (int j = 0; j < VEC; ++j) m[j] = __ldg(mask + r0 + j);
+#pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        if (d < nd) {
+          T v[VEC], xv[VEC];
+          vload(vals + (int64_t)d * ld + r0, v);
+          const int c = r0 + offs.off[d];
+          dia_xvec<T, VEC>(gat, x, c, c & (VEC - 1), xv);
+#pragma unroll
+          for (int j = 0; j < VEC; ++j) {
+            if ((m[j] >> d) & 1u) {
+              if constexpr (FMA) acc[j] = fma(v[j], xv[j], acc[j]);
+              else acc[j] = add_rn(acc[j], mul_rn(v[j], xv[j]));
+            }
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < VEC; ++j) {
+        const int row = r0 + j;
+        if (row < n) {
+          const unsigned m = __ldg(mask + row);
+          for (int d = 0; d < nd; ++d) {
+            if ((m >> d) & 1u) {
+              const T v = (T)to_val(vals[(int64_t)d * ld + row]);
+              const T xd = gat(x, row + offs.off[d]);
+              if constexpr (FMA) acc[j] = fma(v, xd, acc[j]);
+              else acc[j] = add_rn(acc[j], mul_rn(v, xd));
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+      const int row = r0 + j;
+      if (row < n) {
+        const T v = epi.out(row, acc[j]);
+        y[row] = v;
+        epi.acc(row, v, a);
+      }
+    }
+  }
+  if constexpr (Epi::kReduce) {
+    Acc3<T> tot;
+    if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) epi.finish(tot);
+  }
+}
 
 // Short-row SpMV: one thread per row, the row's K-entry window entirely in
 // registers (no shared memory, no block barrier).  Every column/value load

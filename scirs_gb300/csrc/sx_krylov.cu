@@ -477,6 +477,16 @@ struct GatherMxResid {
   __device__ __forceinline__ float operator()(const float*, int c) const {
     return sub_rn(__ldg(r + c), mul_rn(st->alpha, __ldg(q + c)));
   }
+  // the same values for four aligned columns (the diagonal-layout kernel)
+  template <int VEC>
+  __device__ __forceinline__ void vec(const float*, int c, float (&o)[VEC]) const {
+    float rv[VEC], qv[VEC];
+    vload(r + c, rv);
+    vload(q + c, qv);
+    const float al = st->alpha;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) o[j] = sub_rn(rv[j], mul_rn(al, qv[j]));
+  }
 };
 struct EpiMx2 {
   MxState* ms;

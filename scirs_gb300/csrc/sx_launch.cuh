@@ -181,6 +181,37 @@ void launch_pipe_minb(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, co
 
 // The register pipeline with a custom gather (fused solver steps); false
 // when the matrix's chunks do not fit it.  HALF as in launch_csr.
+// Diagonal-layout SpMV launch (values of type V: T, or the FP16 copy);
+// false when the matrix has no diagonal layout.
+template <typename T, class Epi, bool FMA, typename V = T, class Gather = GatherPlain<T>>
+bool launch_dia(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
+                int64_t blocks, Gather gat = Gather{}) {
+  if (!ctx->dia || !vals || c.dia_n <= 0 || !c.dia_mask) return false;
+  // SX_DIA=1 (default): FP64 matrices and FP16 value copies, where it was
+  // measured faster than the CSR kernels; SX_DIA=2: every matrix that has it
+  if (ctx->dia == 1 && sizeof(T) == 4 && sizeof(V) == 4) return false;
+  DiaOffs offs;
+  for (int q = 0; q < 16; ++q) offs.off[q] = c.dia_off[q];
+
+  if (c.dia_n <= 8) {
+    constexpr auto kern = spmv_dia_kernel<T, 8, Epi, FMA, V, Gather>;
+    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
+    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
+                                                      (T*)ra.partials, ra.counter, epi, gat);
+  } else if (c.dia_n <= 12) {
+    constexpr auto kern = spmv_dia_kernel<T, 12, Epi, FMA, V, Gather>;
+    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
+    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
+                                                      (T*)ra.partials, ra.counter, epi, gat);
+  } else {
+    constexpr auto kern = spmv_dia_kernel<T, 16, Epi, FMA, V, Gather>;
+    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
+    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
+                                                      (T*)ra.partials, ra.counter, epi, gat);
+  }
+  return true;
+}
+
 // Short-row SpMV launch: K = 8, 12 or 16 by the longest row (monotone
 // matrices only); false when rows are longer than 16.
 template <typename T, class Epi, bool FMA, typename V = T, class Gather = GatherPlain<T>>
@@ -218,7 +249,12 @@ bool launch_pipe_gather(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, 
   if (ctx_reduce_area(ctx, blocks, &ra) != SX_OK) return false;
   const bool small = c.max_chunk_nnz + 3 <= kBlock * 8;
   bool done = false;
-  if (ctx->short_rows == 2) {
+  if constexpr (HALF && sizeof(T) == 4) {
+    if (c.dia_vals16)
+      done = launch_dia<T, Epi, false, __half, Gather>(ctx, c, (const __half*)c.dia_vals16, x, y, epi, ra, blocks, gat);
+  }
+  if (!done) done = launch_dia<T, Epi, false, T, Gather>(ctx, c, (const T*)c.dia_vals, x, y, epi, ra, blocks, gat);
+  if (!done && ctx->short_rows == 2) {
     if constexpr (HALF && sizeof(T) == 4) {
       if (c.vals16) done = launch_short<T, Epi, false, __half, Gather>(ctx, c, (const __half*)c.vals16, x, y, epi, ra, blocks, gat);
     }
@@ -257,6 +293,13 @@ inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma
   const bool pipe_fits = c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12;
   const bool items8 = c.max_chunk_nnz + 3 <= kBlock * 8;
   if (c.nrows <= 0) return "none";
+  const bool dia_ok = ctx->dia == 2 || (ctx->dia == 1 && (w == 8 || (half_ok && c.dia_vals16)));
+  if (ctx->dia && c.dia_n > 0 && dia_ok) {
+    if (half_ok && w == 4 && c.dia_vals16)
+        return c.dia_n <= 8 ? "spmv_dia_kernel<ND=8, FP16 values>"
+                          : (c.dia_n <= 12 ? "spmv_dia_kernel<ND=12, FP16 values>" : "spmv_dia_kernel<ND=16, FP16 values>");
+    return c.dia_n <= 8 ? "spmv_dia_kernel<ND=8>" : (c.dia_n <= 12 ? "spmv_dia_kernel<ND=12>" : "spmv_dia_kernel<ND=16>");
+  }
   if (c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) return "spmv_win_kernel";
   if (ctx->short_rows && (fma || (w == 4 && ctx->short_rows == 2)) && c.monotone && c.max_row_len <= 16)
     return c.max_row_len <= 8 ? "spmv_short_kernel<K=8>"
@@ -279,7 +322,12 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
   // every 256-row chunk fits the register pipeline: stencil-like matrices
   const bool pipe_fits = c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12;
   bool done = false;
-  if (c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) {
+  // the diagonal layout first (stencil matrices: no column indices to read)
+  if constexpr (HALF && sizeof(T) == 4) {
+    if (c.dia_vals16) done = launch_dia<T, Epi, FMA, __half>(ctx, c, (const __half*)c.dia_vals16, x, y, epi, ra, blocks);
+  }
+  if (!done) done = launch_dia<T, Epi, FMA>(ctx, c, (const T*)c.dia_vals, x, y, epi, ra, blocks);
+  if (!done && c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) {
     switch (ctx->win_shape) {
       case 1: done = launch_win<T, 1, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;
       case 2: done = launch_win<T, 2, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;

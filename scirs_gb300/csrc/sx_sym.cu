@@ -340,7 +340,7 @@ int build_merged(sx_ctx ctx, sx_op low, DevCsr& C) {
       ctx->launches++;
     }
     if ((rc = sync_check(ctx, "symmetric merge"))) break;
-    rc = csr_finalize_stats(ctx, C);
+    rc = csr_finalize_stats(ctx, C, (int)sizeof(T));
   } while (0);
   if (s) destroy_op_internal(s);
   if (st) destroy_op_internal(st);

@@ -96,10 +96,11 @@ def test_windowed_kernel_matches_row_kernel(S):
     assert np.array_equal(out["0"].view(np.uint8), out["2"].view(np.uint8))
 
 
-@pytest.mark.parametrize("win", ["0", "2"])
+@pytest.mark.parametrize("env", [{"SX_WIN": "0", "SX_DIA": "0"}, {"SX_WIN": "2", "SX_DIA": "0"}, {}])
 @pytest.mark.parametrize("kind,dims", [("laplace3d", (64, 64, 64)), ("powerlaw", (300000, 1, 1))])
-def test_fp64_fma_mode_within_ulps(S, kind, dims, win):
-    ctx = _ctx_with(S, {"SX_WIN": win})
+def test_fp64_fma_mode_within_ulps(S, kind, dims, env):
+    # the CSR kernels (row-wise, windowed) and, for the stencil, the diagonal layout
+    ctx = _ctx_with(S, env)
     import torch
 
     from scirs_gb300 import _lib as L
@@ -156,7 +157,8 @@ def test_compressed_columns_bit_exact(S, dtype, kind, dims, p0, p1):
     vals = v.astype(dtype)
     x = np.random.default_rng(2).standard_normal(n).astype(dtype)
     yr = O.spmv_i32(ip, ix, vals, x)
-    for env in ({}, {"SX_SHORT": "2"}, {"SX_SHORT": "0", "SX_COL16": "1"}):
+    for env in ({}, {"SX_DIA": "2"}, {"SX_DIA": "0"}, {"SX_DIA": "0", "SX_SHORT": "2"},
+                {"SX_DIA": "0", "SX_SHORT": "0", "SX_COL16": "1"}):
         c = _ctx_with(S, env)
         a = S.csr_from_arrays(c, ip, ix, vals, (n, n))
         y = a.matvec(x)
@@ -183,18 +185,85 @@ def test_compressed_columns_wide_rows_keep_int32(S, ctx):
 
 
 def test_kernel_choice_names(S, ctx):
-    # the dispatch: short rows in registers for FP64 with FMA, the register
-    # pipeline for FP32 and exact FP64 stencils, windows for long rows
+    # the dispatch: the diagonal layout for stencils; without it (SX_DIA=0)
+    # short rows in registers for FP64 with FMA and the register pipeline for
+    # FP32 and exact FP64; windows for long rows
     ip, ix, v = S.generate("laplace3d", 20, 20, 20)
     n = len(ip) - 1
     a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
     a32 = a64.astype(np.float32)
+    # default (SX_DIA=1): the diagonal layout for FP64, the CSR pipeline for FP32
     assert S.spmv_kernel(a32) == "spmv_pipe_kernel<ITEMS=8>"
-    assert S.spmv_kernel(a64, exact=False) == "spmv_short_kernel<K=8>"
-    assert S.spmv_kernel(a64, exact=True) == "spmv_pipe_kernel<ITEMS=8>"
+    assert S.spmv_kernel(a64, exact=False) == "spmv_dia_kernel<ND=8>"
+    assert S.spmv_kernel(a64, exact=True) == "spmv_dia_kernel<ND=8>"
+    c2 = _ctx_with(S, {"SX_DIA": "2"})
+    d32 = S.csr_from_arrays(c2, ip, ix, v.astype(np.float32), (n, n))
+    assert S.spmv_kernel(d32) == "spmv_dia_kernel<ND=8>"
+    d32.close()
+    c2.close()
+    c = _ctx_with(S, {"SX_DIA": "0"})
+    b64 = S.csr_from_arrays(c, ip, ix, v, (n, n))
+    b32 = b64.astype(np.float32)
+    assert S.spmv_kernel(b32) == "spmv_pipe_kernel<ITEMS=8>"
+    assert S.spmv_kernel(b64, exact=False) == "spmv_short_kernel<K=8>"
+    assert S.spmv_kernel(b64, exact=True) == "spmv_pipe_kernel<ITEMS=8>"
     ip, ix, v = S.generate("powerlaw", 50000, 1, 1, seed=2, param0=16.0, param1=4096.0)
     n = len(ip) - 1
     p = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
     assert S.spmv_kernel(p) == "spmv_win_kernel"
-    for op in (a32, a64, p):
+    for op in (a32, a64, b32, b64, p):
         op.close()
+    c.close()
+
+
+def _diag_cases(rng):
+    # (name, indptr, indices, values, expect the diagonal layout)
+    n = 4000
+    offs = [-37, -1, 0, 1, 5, 300]
+    rows, cols = [], []
+    for i in range(n):
+        for o in offs:
+            j = i + o
+            if 0 <= j < n and rng.uniform() < 0.9:  # ragged: absent entries inside the band
+                rows.append(i)
+                cols.append(j)
+    rows, cols = np.asarray(rows), np.asarray(cols)
+    ip = np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=n))]).astype(np.int64)
+    v = rng.uniform(-1, 1, len(cols))
+    yield "banded_ragged", ip, cols.astype(np.int32), v, True
+    # the same rows with one pair of columns swapped: not strictly increasing
+    c2 = cols.copy()
+    k = int(ip[100])
+    c2[k], c2[k + 1] = c2[k + 1], c2[k]
+    yield "unsorted_row", ip, c2.astype(np.int32), v, False
+    # a duplicate entry
+    c3 = cols.copy()
+    c3[k + 1] = c3[k]
+    yield "duplicate", ip, c3.astype(np.int32), v, False
+    # 17 diagonals
+    offs17 = list(range(-8, 9))
+    rows = np.repeat(np.arange(n), len(offs17))
+    cols = (rows + np.tile(offs17, n))
+    keep = (cols >= 0) & (cols < n)
+    rows, cols = rows[keep], cols[keep]
+    ip = np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=n))]).astype(np.int64)
+    yield "seventeen_diagonals", ip, cols.astype(np.int32), rng.uniform(-1, 1, len(cols)), False
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_diagonal_layout_bit_exact(S, dtype):
+    rng = np.random.default_rng(12)
+    ctx = _ctx_with(S, {"SX_DIA": "2"})  # the layout for FP32 too
+    for name, ip, ix, v, expect in _diag_cases(rng):
+        n = len(ip) - 1
+        vals = v.astype(dtype)
+        a = S.csr_from_arrays(ctx, ip, ix, vals, (n, n))
+        assert S.spmv_kernel(a).startswith("spmv_dia_kernel") == expect, name
+        x = rng.standard_normal(n).astype(dtype)
+        # one infinite x: the rows that store its column give +-inf; a padded
+        # (absent) entry multiplied into it would give NaN
+        x[n // 2] = np.inf
+        y = a.matvec(x)
+        assert np.array_equal(y.view(np.uint8), O.spmv_i32(ip, ix, vals, x).view(np.uint8)), name
+        a.close()
+    ctx.close()
