@@ -1072,7 +1072,8 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out) {
     if ((rc = sx_csr_from_raw_i32(ctx, (sx_dtype)a->dtype, p64, g->gi, gv, (uint64_t)n, (uint64_t)n,
                                   (uint64_t)g->ng, SX_MEM_DEVICE, &G)))
       break;
-    rc = sx_precond_fsai(ctx, G, out);
+    rc = fsai_adopt(ctx, G, out);
+    G = nullptr;
     // the factor's values in FP16 for the solvers (the network's output is
     // already limited by its BF16 weights); FP32 stays for exact applies
     if (rc == SX_OK && a->dtype == SX_F32) {

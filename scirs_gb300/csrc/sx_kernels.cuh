@@ -454,24 +454,17 @@ namespace sx {
 // row, and each row's sum runs over its stored diagonals in that order
 // (from zero, rounded products, or fused multiply-adds for FMA), so the
 // result is that of the CSR kernels.  Groups near the ends of the matrix,
-// where a vector load could leave [0, n), take the row-by-row path.
+// where a vector load could leave [0, n), read element by element.
 struct DiaOffs {
   int32_t off[16];
 };
 
-// x operands of VEC rows starting at column c: aligned loads at c - s and,
-// when s = c mod VEC is not zero, at c - s + VEC
-template <typename T, int VEC, class Gather>
-__device__ __forceinline__ void dia_xvec(const Gather& gat, const T* x, int c, int s, T (&o)[VEC]) {
-  T a[VEC];
-  gat.vec(x, c - s, a);
-  if (s == 0) {
+// x operands of VEC rows from the two aligned vectors a (columns c - s ..)
+// and b (the next VEC columns), s = c mod VEC
+template <typename T, int VEC>
+__device__ __forceinline__ void dia_shift(const T (&a)[VEC], const T (&b)[VEC], int s, T (&o)[VEC]) {
 #pragma unroll
-    for (int j = 0; j < VEC; ++j) o[j] = a[j];
-    return;
-  }
-  T b[VEC];
-  gat.vec(x, c - s + VEC, b);
+  for (int j = 0; j < VEC; ++j) o[j] = a[j];
 #pragma unroll
   for (int sh = 1; sh < VEC; ++sh)
     if (s == sh) {
@@ -479,6 +472,12 @@ __device__ __forceinline__ void dia_xvec(const Gather& gat, const T* x, int c, i
       for (int j = 0; j < VEC; ++j) o[j] = j + sh < VEC ? a[j + sh] : b[j + sh - VEC];
     }
 }
+
+// Diagonals per batch of loads: every load of a batch is issued before the
+// first product, with no condition on them (batch slots past the last
+// diagonal re-read it and are masked off), so a thread waits for memory
+// once per batch rather than once per diagonal.
+constexpr int kDiaBatch = 4;
 
 template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>>
 __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ vals,
@@ -488,6 +487,7 @@ __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ 
                                                           unsigned int* counter, Epi epi, Gather gat = Gather{}) {
   if (epi.skip()) return;
   constexpr int VEC = DiaVec<T>::kVec;
+  constexpr int KB = ND < kDiaBatch ? ND : kDiaBatch;
   Acc3<T> a{T(0), T(0), T(0)};
   const int n = (int)nrows;
   const int omin = offs.off[0], omax = offs.off[nd - 1];
@@ -498,39 +498,76 @@ __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ 
     T acc[VEC];
 #pragma unroll
     for (int j = 0; j < VEC; ++j) acc[j] = T(0);
+    // every aligned x vector of the group stays inside [0, n)
     const bool inner = r0 + omin - VEC >= 0 && r0 + omax + 2 * VEC <= n && r0 + VEC <= n;
     if (inner) {
-      unsigned m[VEC];
+      unsigned m[VEC];  // one 8- or 4-byte load (r0 is a multiple of VEC)
+      if constexpr (VEC == 4) {
+        const uint2 u = __ldg(reinterpret_cast<const uint2*>(mask + r0));
+        m[0] = u.x & 0xFFFFu; m[1] = u.x >> 16; m[2] = u.y & 0xFFFFu; m[3] = u.y >> 16;
+      } else {
+        static_assert(VEC == 2, "DIA groups are 2 or 4 rows");
+        const unsigned u = __ldg(reinterpret_cast<const unsigned*>(mask + r0));
+        m[0] = u & 0xFFFFu; m[1] = u >> 16;
+      }
 #pragma unroll
-      for (int j = 0; j < VEC; ++j) m[j] = __ldg(mask + r0 + j);
+      for (int d0 = 0; d0 < ND; d0 += KB) {
+        if (d0 < nd) {
+          T v[KB][VEC], xa[KB][VEC], xb[KB][VEC];
 #pragma unroll
-      for (int d = 0; d < ND; ++d) {
-        if (d < nd) {
-          T v[VEC], xv[VEC];
-          vload(vals + (int64_t)d * ld + r0, v);
-          const int c = r0 + offs.off[d];
-          dia_xvec<T, VEC>(gat, x, c, c & (VEC - 1), xv);
+          for (int t = 0; t < KB; ++t) {
+            const int d = min(d0 + t, nd - 1);
+            vload(vals + (int64_t)d * ld + r0, v[t]);
+            const int c = r0 + offs.off[d] - (offs.off[d] & (VEC - 1));
+            gat.vec(x, c, xa[t]);
+            gat.vec(x, c + VEC, xb[t]);
+          }
 #pragma unroll
-          for (int j = 0; j < VEC; ++j) {
-            if ((m[j] >> d) & 1u) {
-              if constexpr (FMA) acc[j] = fma(v[j], xv[j], acc[j]);
-              else acc[j] = add_rn(acc[j], mul_rn(v[j], xv[j]));
+          for (int t = 0; t < KB; ++t) {
+            const int d = d0 + t;
+            T xv[VEC];
+            dia_shift<T, VEC>(xa[t], xb[t], offs.off[min(d, nd - 1)] & (VEC - 1), xv);
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+              if (d < nd && ((m[j] >> d) & 1u)) {
+                if constexpr (FMA) acc[j] = fma(v[t][j], xv[j], acc[j]);
+                else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[j]));
+              }
             }
           }
         }
       }
     } else {
+      // groups near the ends: element loads at clamped rows and columns
+      // (in bounds for every slot; the slots of absent entries are masked
+      // off), batched like the vector path so that they too are in flight
+      // together
+      unsigned m[VEC];
 #pragma unroll
-      for (int j = 0; j < VEC; ++j) {
-        const int row = r0 + j;
-        if (row < n) {
-          const unsigned m = __ldg(mask + row);
-          for (int d = 0; d < nd; ++d) {
-            if ((m >> d) & 1u) {
-              const T v = (T)to_val(vals[(int64_t)d * ld + row]);
-              const T xd = gat(x, row + offs.off[d]);
-              if constexpr (FMA) acc[j] = fma(v, xd, acc[j]);
-              else acc[j] = add_rn(acc[j], mul_rn(v, xd));
+      for (int j = 0; j < VEC; ++j) m[j] = r0 + j < n ? __ldg(mask + r0 + j) : 0u;
+#pragma unroll
+      for (int d0 = 0; d0 < ND; d0 += KB) {
+        if (d0 < nd) {
+          T v[KB][VEC], xv[KB][VEC];
+#pragma unroll
+          for (int t = 0; t < KB; ++t) {
+            const int d = min(d0 + t, nd - 1);
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+              const int row = min(r0 + j, n - 1);
+              v[t][j] = (T)to_val(vals[(int64_t)d * ld + row]);
+              xv[t][j] = gat(x, min(max(row + offs.off[d], 0), n - 1));
+            }
+          }
+#pragma unroll
+          for (int t = 0; t < KB; ++t) {
+            const int d = d0 + t;
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+              if (d < nd && ((m[j] >> d) & 1u)) {
+                if constexpr (FMA) acc[j] = fma(v[t][j], xv[t][j], acc[j]);
+                else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[t][j]));
+              }
             }
           }
         }

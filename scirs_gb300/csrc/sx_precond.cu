@@ -212,6 +212,35 @@ int sx_precond_jacobi_from_diagonal(sx_ctx ctx, sx_dtype dtype, const void* diag
   return jacobi_finish(ctx, bad, op, out);
 }
 
+}  // extern "C"
+
+namespace sx {
+// FSAI operator that takes over the CSR arrays of g (a temporary the caller
+// no longer needs): one transpose for G^T instead of the public entry's
+// copy.  g's shell is destroyed whatever the outcome.
+int fsai_adopt(sx_ctx ctx, sx_op g, sx_op* out) {
+  *out = nullptr;
+  sx_op op = new sx_op_s();
+  op->kind = SX_OP_FSAI;
+  op->dtype = g->dtype;
+  op->device = ctx->device;
+  op->nrows = op->ncols = g->nrows;
+  op->serial = next_op_serial();
+  int rc = csr_transpose_internal(ctx, g, &op->transpose);
+  if (rc == SX_OK) {
+    op->csr = g->csr;
+    g->csr = DevCsr();
+    rc = dev_alloc(&op->work, std::max<int64_t>(g->nrows, 1) * elt_size(g->dtype));
+  }
+  destroy_op_internal(g);
+  if (rc != SX_OK) { destroy_op_internal(op); return rc; }
+  *out = op;
+  return SX_OK;
+}
+}  // namespace sx
+
+extern "C" {
+
 int sx_precond_fsai(sx_ctx ctx, sx_op g, sx_op* out) {
   if (!ctx || !g || !out) return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: null");
   if (g->kind != SX_OP_CSR) return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: not CSR");
