@@ -819,6 +819,7 @@ int csr_prepare_dia(sx_ctx ctx, DevCsr& c, int w) {
   // offset of a power-of-two span of memory
   const int64_t ld = (c.nrows + 31) / 32 * 32 + 32 * 37;
   if ((double)nd * (double)c.nrows > 1.25 * (double)c.nnz) return SX_OK;
+  if ((int64_t)nd * ld >= ((int64_t)1 << 31)) return SX_OK;  // the kernels index with 32 bits
   DiaTable tab;
   for (int q = 0; q < kDiaMax; ++q) tab.off[q] = q < nd ? offs[q] : 0;
   SX_CHECK(dev_alloc(&c.dia_vals, (size_t)nd * ld * w));

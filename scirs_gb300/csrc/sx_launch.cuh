@@ -179,36 +179,32 @@ void launch_pipe_minb(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, co
                                                     GatherPlain<T>{});
 }
 
-// The register pipeline with a custom gather (fused solver steps); false
-// when the matrix's chunks do not fit it.  HALF as in launch_csr.
+// One diagonal-layout launch: as many blocks as the row groups need, at
+// most the resident blocks of every SM.
+template <auto Kern, typename T, typename V, class Epi, class Gather>
+void dia_go(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
+            Gather gat, const DiaOffs& offs, int64_t units) {
+  const int64_t grid =
+      std::min<int64_t>((units + kBlock - 1) / kBlock, (int64_t)ctx->num_sms * resident_blocks<Kern>());
+  Kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
+                                                    (T*)ra.partials, ra.counter, epi, gat);
+}
+
 // Diagonal-layout SpMV launch (values of type V: T, or the FP16 copy);
 // false when the matrix has no diagonal layout.
 template <typename T, class Epi, bool FMA, typename V = T, class Gather = GatherPlain<T>>
 bool launch_dia(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
-                int64_t blocks, Gather gat = Gather{}) {
+                int64_t /*blocks*/, Gather gat = Gather{}) {
   if (!ctx->dia || !vals || c.dia_n <= 0 || !c.dia_mask) return false;
   // SX_DIA=1 (default): FP64 matrices and FP16 value copies, where it was
   // measured faster than the CSR kernels; SX_DIA=2: every matrix that has it
   if (ctx->dia == 1 && sizeof(T) == 4 && sizeof(V) == 4) return false;
   DiaOffs offs;
   for (int q = 0; q < 16; ++q) offs.off[q] = c.dia_off[q];
-
-  if (c.dia_n <= 8) {
-    constexpr auto kern = spmv_dia_kernel<T, 8, Epi, FMA, V, Gather>;
-    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
-    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
-                                                      (T*)ra.partials, ra.counter, epi, gat);
-  } else if (c.dia_n <= 12) {
-    constexpr auto kern = spmv_dia_kernel<T, 12, Epi, FMA, V, Gather>;
-    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
-    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
-                                                      (T*)ra.partials, ra.counter, epi, gat);
-  } else {
-    constexpr auto kern = spmv_dia_kernel<T, 16, Epi, FMA, V, Gather>;
-    const int64_t grid = std::min<int64_t>(blocks, (int64_t)ctx->num_sms * resident_blocks<kern>());
-    kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
-                                                      (T*)ra.partials, ra.counter, epi, gat);
-  }
+  const int64_t groups = (c.nrows + DiaVec<T>::kVec - 1) / DiaVec<T>::kVec;
+  if (c.dia_n <= 8) dia_go<spmv_dia_kernel<T, 8, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  else if (c.dia_n <= 12) dia_go<spmv_dia_kernel<T, 12, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  else dia_go<spmv_dia_kernel<T, 16, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   return true;
 }
 
