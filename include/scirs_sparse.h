@@ -435,6 +435,50 @@ void sx_lgmres_options_default(sx_lgmres_options* o);
 int sx_lgmres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_lgmres_options* opt,
               void* x_out, sx_mem mem, sx_iter_result* res);
 
+/* ------------------------------------------------ eigenpairs (eigen.rs)
+ * Both take a symmetric CSR operator (sx_sym_csr_*), as the reference takes
+ * a SymCsrMatrix.  x0 / v0 (NULL: e_0, as the reference) and the
+ * eigenvector output are host or device memory per `mem`; eigenvalues and
+ * residuals are host arrays of the operator's value type.  Device sums are
+ * tree reductions: results agree with the reference's sequential sums to
+ * rounding.  Where the reference panics (a subspace of size 0, fewer
+ * eigenvalues or eigenvector entries than the requested count) the call
+ * returns SX_ERR_COMPUTATION with a message that names the panic. */
+typedef struct {
+  uint64_t iterations;
+  int converged;
+  uint64_t num_eigenvalues; /* entries written to eigenvalues */
+  uint64_t num_columns;     /* residuals and eigenvector columns */
+} sx_eigen_result;
+/* PowerIterationOptions (eigen.rs:16-34): 100, 1e-8, normalize */
+typedef struct {
+  uint64_t max_iter;
+  double tol;
+  int normalize;
+} sx_power_options;
+void sx_power_options_default(sx_power_options* o);
+/* power_iteration (eigen.rs:124-293): largest eigenvalue by magnitude
+ * growth; eigenvector (n entries, may be NULL) and ||A x - lambda x||.
+ * DimensionMismatch{expected: n, found: x0_len} for a wrong x0 length. */
+int sx_power_iteration(sx_ctx ctx, sx_op a, const sx_power_options* opt, const void* x0, uint64_t x0_len,
+                       sx_mem mem, void* eigenvalue, void* eigenvector, void* residual, sx_eigen_result* result);
+/* LanczosOptions (eigen.rs:37-61): 1000, 20, 1e-8, 1, eigenvectors */
+typedef struct {
+  uint64_t max_iter;
+  uint64_t max_subspace_size;
+  double tol;
+  uint64_t num_eigenvalues;
+  int compute_eigenvectors;
+} sx_lanczos_options;
+void sx_lanczos_options_default(sx_lanczos_options* o);
+/* lanczos (eigen.rs:295-494, tridiagonal solvers :512-952).  Room needed:
+ * eigenvalues and residuals min(num_eigenvalues, subspace) entries,
+ * eigenvectors n x that many (row-major, column k = Ritz vector k; may be
+ * NULL; ignored without compute_eigenvectors).  The Lanczos basis lives on
+ * the device (subspace x n values; max_subspace_size <= 4096). */
+int sx_lanczos(sx_ctx ctx, sx_op a, const sx_lanczos_options* opt, const void* v0, uint64_t v0_len, sx_mem mem,
+               void* eigenvalues, void* eigenvectors, void* residuals, sx_eigen_result* result);
+
 /* ------------------------------------------- mixed precision (no reference
  * counterpart; nearest dense analogue scirs2-linalg mixed_precision) */
 /* FP32 preconditioned CG inside an FP64 refinement loop.  FP64 holds the

@@ -749,4 +749,77 @@ IterationResult<F> lgmres(const LinearOperator<F>& a, const std::vector<F>& b, L
   return detail::result(std::move(x), r);
 }
 
+// ---------------------------------------------------------- eigenpairs
+// EigenResult (eigen.rs:64-78); eigenvectors is n x k row-major (column k =
+// pair k), empty when not computed.
+template <class F>
+struct EigenResult {
+  std::vector<F> eigenvalues;
+  std::vector<F> eigenvectors;
+  std::size_t rows = 0, cols = 0;
+  std::size_t iterations = 0;
+  std::vector<F> residuals;
+  bool converged = false;
+};
+struct PowerIterationOptions {  // eigen.rs:16-34
+  std::size_t max_iter = 100;
+  double tol = 1e-8;
+  bool normalize = true;
+};
+struct LanczosOptions {  // eigen.rs:37-61
+  std::size_t max_iter = 1000;
+  std::size_t max_subspace_size = 20;
+  double tol = 1e-8;
+  std::size_t num_eigenvalues = 1;
+  bool compute_eigenvectors = true;
+};
+
+// power_iteration (eigen.rs:124-293); an empty initial guess means e_0
+template <class F>
+EigenResult<F> power_iteration(const SymCsrMatrix<F>& m, const PowerIterationOptions& options,
+                               const std::vector<F>& initial_guess = {}) {
+  const std::size_t n = m.shape().first;
+  sx_power_options o{options.max_iter, options.tol, options.normalize ? 1 : 0};
+  EigenResult<F> r;
+  r.eigenvalues.assign(1, F(0));
+  r.residuals.assign(1, F(0));
+  r.eigenvectors.assign(n, F(0));
+  sx_eigen_result e;
+  detail::check(sx_power_iteration(m.context(), m.device_op(), &o,
+                                   initial_guess.empty() ? nullptr : initial_guess.data(), initial_guess.size(),
+                                   SX_MEM_HOST, r.eigenvalues.data(), r.eigenvectors.data(), r.residuals.data(), &e));
+  r.rows = n;
+  r.cols = 1;
+  r.iterations = e.iterations;
+  r.converged = e.converged != 0;
+  return r;
+}
+
+// lanczos (eigen.rs:295-494)
+template <class F>
+EigenResult<F> lanczos(const SymCsrMatrix<F>& m, const LanczosOptions& options,
+                       const std::vector<F>& initial_guess = {}) {
+  const std::size_t n = m.shape().first;
+  const std::size_t k = std::max<std::size_t>(
+      std::min(options.num_eigenvalues, std::min(options.max_subspace_size, n)), 1);
+  sx_lanczos_options o{options.max_iter, options.max_subspace_size, options.tol, options.num_eigenvalues,
+                       options.compute_eigenvectors ? 1 : 0};
+  EigenResult<F> r;
+  r.eigenvalues.assign(k, F(0));
+  r.residuals.assign(k, F(0));
+  if (options.compute_eigenvectors) r.eigenvectors.assign(n * k, F(0));
+  sx_eigen_result e;
+  detail::check(sx_lanczos(m.context(), m.device_op(), &o, initial_guess.empty() ? nullptr : initial_guess.data(),
+                           initial_guess.size(), SX_MEM_HOST, r.eigenvalues.data(),
+                           options.compute_eigenvectors ? r.eigenvectors.data() : nullptr, r.residuals.data(), &e));
+  r.eigenvalues.resize(e.num_eigenvalues);
+  r.residuals.resize(e.num_columns);
+  if (options.compute_eigenvectors) r.eigenvectors.resize(n * e.num_columns);
+  r.rows = n;
+  r.cols = options.compute_eigenvectors ? e.num_columns : 0;
+  r.iterations = e.iterations;
+  r.converged = e.converged != 0;
+  return r;
+}
+
 }  // namespace scirs2_sparse

@@ -33,6 +33,10 @@ class Res(C.Structure):
                 ("message", C.c_int)]
 
 
+class EigInfo(C.Structure):
+    _fields_ = [("iterations", C.c_uint64), ("converged", C.c_int), ("count", C.c_uint64), ("num", C.c_uint64)]
+
+
 class IROpt(C.Structure):
     _fields_ = [("max_outer", C.c_uint64), ("max_inner", C.c_uint64), ("tol", C.c_double),
                 ("inner_rtol", C.c_double), ("jacobi", C.c_int)]
@@ -108,6 +112,16 @@ def lib():
             "or_sym_csr_rank1_update_f32": (u64, [vp, vp, vp, u64, vp, C.c_float, vp, vp, vp]),
             "or_sym_csr_from_csr_f64": (ip, [vp, vp, vp, u64, u64, vp, vp, vp, E]),
             "or_sym_csr_from_csr_f32": (ip, [vp, vp, vp, u64, u64, vp, vp, vp, E]),
+            "or_power_iteration_f64": (ip, [vp, vp, vp, u64, u64, dbl, ip, vp, u64, vp, vp, vp,
+                                            C.POINTER(EigInfo), E]),
+            "or_power_iteration_f32": (ip, [vp, vp, vp, u64, u64, dbl, ip, vp, u64, vp, vp, vp,
+                                            C.POINTER(EigInfo), E]),
+            "or_lanczos_f64": (ip, [vp, vp, vp, u64, u64, u64, dbl, u64, ip, vp, u64, vp, vp, vp,
+                                    C.POINTER(EigInfo), E]),
+            "or_lanczos_f32": (ip, [vp, vp, vp, u64, u64, u64, dbl, u64, ip, vp, u64, vp, vp, vp,
+                                    C.POINTER(EigInfo), E]),
+            "or_tridiag_eig_f64": (ip, [vp, vp, u64, u64, u64, vp, vp, vp, E]),
+            "or_solve_cubic_f64": (u64, [dbl, dbl, dbl, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -452,3 +466,78 @@ def sym_from_csr(indptr, indices, data, shape):
         return None, e.msg.decode()
     nnz = int(ip[-1])
     return (ip, ix[:nnz].copy(), dv[:nnz].copy()), None
+
+
+# ---------------------------------------------------------------- eigen
+class OracleError(Exception):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+def power_iteration(indptr, indices, data, max_iter=100, tol=1e-8, normalize=True, initial_guess=None):
+    """power_iteration (eigen.rs:124-293) on SymCsrMatrix arrays."""
+    indptr, indices, data = _sym_arrays(indptr, indices, data)
+    n = len(indptr) - 1
+    f64 = data.dtype == np.float64
+    x0 = None if initial_guess is None else np.ascontiguousarray(initial_guess, dtype=data.dtype)
+    lam = np.zeros(1, dtype=data.dtype)
+    res = np.zeros(1, dtype=data.dtype)
+    vec = np.zeros(max(n, 1), dtype=data.dtype)
+    info, e = EigInfo(), Err()
+    f = lib().or_power_iteration_f64 if f64 else lib().or_power_iteration_f32
+    rc = f(p(indptr), p(indices), p(data), n, max_iter, tol, 1 if normalize else 0, p(x0),
+           0 if x0 is None else x0.size, p(lam), p(vec), p(res), C.byref(info), C.byref(e))
+    if rc:
+        raise OracleError(rc, e.msg.decode())
+    return {"eigenvalues": lam, "eigenvectors": vec[:n].reshape(n, 1), "iterations": info.iterations,
+            "residuals": res, "converged": bool(info.converged)}
+
+
+def lanczos(indptr, indices, data, max_iter=1000, max_subspace_size=20, tol=1e-8, num_eigenvalues=1,
+            compute_eigenvectors=True, initial_guess=None):
+    """lanczos (eigen.rs:295-494) on SymCsrMatrix arrays."""
+    indptr, indices, data = _sym_arrays(indptr, indices, data)
+    n = len(indptr) - 1
+    f64 = data.dtype == np.float64
+    x0 = None if initial_guess is None else np.ascontiguousarray(initial_guess, dtype=data.dtype)
+    k = max(min(num_eigenvalues, max_subspace_size, n), 1)
+    vals = np.zeros(max(k, 3), dtype=data.dtype)
+    res = np.zeros(k, dtype=data.dtype)
+    vecs = np.zeros(max(n * k, 1), dtype=data.dtype)
+    info, e = EigInfo(), Err()
+    f = lib().or_lanczos_f64 if f64 else lib().or_lanczos_f32
+    rc = f(p(indptr), p(indices), p(data), n, max_iter, max_subspace_size, tol, num_eigenvalues,
+           1 if compute_eigenvectors else 0, p(x0), 0 if x0 is None else x0.size, p(vals), p(vecs), p(res),
+           C.byref(info), C.byref(e))
+    if rc:
+        raise OracleError(rc, e.msg.decode())
+    cols = int(info.num)
+    return {"eigenvalues": vals[: int(info.count)].copy(),
+            "eigenvectors": vecs[: n * cols].reshape(n, cols) if compute_eigenvectors else None,
+            "iterations": info.iterations, "residuals": res[:cols].copy(), "converged": bool(info.converged)}
+
+
+def tridiag_eig(alpha, beta, num):
+    """solve_tridiagonal_eigenproblem (eigen.rs:512-646): (values, vectors) with
+    vectors[k] the k-th eigenvector, or OracleError."""
+    alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    m = len(alpha)
+    vals = np.zeros(max(m, 3))
+    vecs = np.zeros(max(m * max(m, 3), 1))
+    cnt = C.c_uint64()
+    e = Err()
+    rc = lib().or_tridiag_eig_f64(p(alpha), p(beta) if len(beta) else None, m, len(beta), num, p(vals), p(vecs),
+                                  C.byref(cnt), C.byref(e))
+    if rc:
+        raise OracleError(rc, e.msg.decode())
+    c = int(cnt.value)
+    return vals[:c].copy(), [vecs[k * m:(k + 1) * m].copy() for k in range(c)]
+
+
+def solve_cubic(p_, q, r):
+    """solve_cubic (eigen.rs:890-952): the roots it returns (1 or 3)."""
+    roots = np.zeros(3)
+    k = lib().or_solve_cubic_f64(p_, q, r, p(roots))
+    return roots[:k].copy()

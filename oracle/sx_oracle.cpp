@@ -2016,3 +2016,457 @@ int or_sym_csr_from_csr_f32(const uint64_t* indptr, const uint64_t* indices, con
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ eigen
+// scirs2-sparse/src/linalg/eigen.rs: power_iteration (:124-293), lanczos
+// (:295-494) and their tridiagonal helpers (:512-936), restated with the
+// reference's arithmetic order and its quirks:
+//   - lanczos never updates beta_j after the first step (the update at
+//     :441-443 binds a new variable that dies at once), so every Lanczos
+//     vector is w / beta_1 and every off-diagonal entry is beta_1;
+//   - the QL sweep (:551-632) leaves its loop after one sweep for l >= 1
+//     (the `i < l` test at :617 fires whenever the sweep runs to its end);
+//   - Ritz vectors and the Kaniel-Paige bound index the eigenvector list as
+//     eigvecs[j][k] (:459, :485), i.e. the transpose of the list returned;
+//   - where the reference would panic (an index past the end of a list, a
+//     subspace of size 0) the restatement returns a ComputationError that
+//     names the panic.
+namespace {
+
+template <class T>
+T fold_dot(const std::vector<T>& a, const std::vector<T>& b) {
+  T s = T(0);
+  for (size_t i = 0; i < a.size(); ++i) s = s + a[i] * b[i];
+  return s;
+}
+
+// solve_cubic, eigen.rs:890-952
+template <class T>
+std::vector<T> solve_cubic(T p, T q, T r) {
+  const T p3 = p / T(3.0);
+  const T p3sq = p3 * p3;
+  const T a = q - p * p3;
+  const T b = r + p3 * (T(2.0) * p3sq - q);
+  const T disc = T(4.0) * a * a * a + T(27.0) * b * b;
+  std::vector<T> roots;
+  if (disc == T(0)) {
+    if (a == T(0)) {
+      roots.assign(3, -p3);
+    } else {
+      const T x1 = T(3.0) * b / a;
+      const T x2 = -x1 / T(2.0);
+      roots = {x1 - p3, x2 - p3, x2 - p3};
+    }
+  } else if (disc > T(0)) {
+    const T sd = std::sqrt(disc);
+    const T c1 = (-b + sd * T(0.5)) / T(2.0);
+    const T c2 = (-b - sd * T(0.5)) / T(2.0);
+    const T third = (T)(1.0 / 3.0);
+    const T c1r = std::pow(std::fabs(c1), third) * (c1 >= T(0) ? T(1) : T(-1));
+    const T c2r = std::pow(std::fabs(c2), third) * (c2 >= T(0) ? T(1) : T(-1));
+    roots.push_back(c1r + c2r - p3);
+  } else {
+    const T ps = std::sqrt(-a / T(3.0));
+    const T theta = std::acos(b / (T(2.0) * ps * ps * ps));
+    for (int k = 0; k < 3; ++k) {
+      const T ang = (T)(3.141592653589793 * (2.0 * (double)k) / 3.0);
+      roots.push_back(T(2.0) * ps * std::cos(ang - theta / T(3.0)) - p3);
+    }
+  }
+  return roots;
+}
+
+// descending order of partial_cmp with incomparable pairs Equal (a stable
+// sort, as Rust's sort_by)
+template <class T>
+bool desc_less(T x, T y) { return x > y; }
+
+const char* kPanicIndex = "panic: index out of bounds in the reference's eigenvector lists";
+
+// solve_small_tridiagonal, eigen.rs:650-886
+template <class T>
+int small_tridiag(const std::vector<T>& alpha, const std::vector<T>& beta, size_t num, std::vector<T>& vals,
+                  std::vector<std::vector<T>>& vecs, or_err* err) {
+  const size_t n = alpha.size();
+  vals.clear();
+  vecs.clear();
+  if (n == 1) {
+    vals = {alpha[0]};
+    vecs = {{T(1)}};
+    return ok(err);
+  }
+  if (n == 2) {
+    const T a = alpha[0], b = alpha[1], c = beta[0];
+    const T trace = a + b;
+    const T det = a * b - c * c;
+    const T disc = std::sqrt(trace * trace - T(4.0) * det);
+    T l1 = (trace + disc) * T(0.5), l2 = (trace - disc) * T(0.5);
+    if (!(l1 >= l2)) std::swap(l1, l2);
+    std::vector<T> v1(2, T(0)), v2(2, T(0));
+    if (c != T(0)) {
+      v1[0] = c; v1[1] = l1 - a;
+      v2[0] = c; v2[1] = l2 - a;
+      const T n1 = std::sqrt(v1[0] * v1[0] + v1[1] * v1[1]);
+      const T n2 = std::sqrt(v2[0] * v2[0] + v2[1] * v2[1]);
+      if (n1 != T(0)) { v1[0] = v1[0] / n1; v1[1] = v1[1] / n1; }
+      if (n2 != T(0)) { v2[0] = v2[0] / n2; v2[1] = v2[1] / n2; }
+    } else if (a >= b) {
+      v1 = {T(1), T(0)}; v2 = {T(0), T(1)};
+    } else {
+      v1 = {T(0), T(1)}; v2 = {T(1), T(0)};
+    }
+    vals = {l1, l2};
+    vecs = {v1, v2};
+    if (vals.size() > num) vals.resize(num);
+    if (vecs.size() > num) vecs.resize(num);
+    return ok(err);
+  }
+  // n == 3: characteristic polynomial and Vieta's roots
+  const T a = alpha[0], b = alpha[1], c = alpha[2], d = beta[0], e = beta[1];
+  const T p = -(a + b + c);
+  const T q = a * b + a * c + b * c - d * d - e * e;
+  const T r = -(a * b * c - a * e * e - c * d * d);
+  std::vector<T> sorted = solve_cubic<T>(p, q, r);
+  std::stable_sort(sorted.begin(), sorted.end(), desc_less<T>);
+  const size_t take = std::min<size_t>(num, 3);
+  if (take > sorted.size()) return set_err(err, E_COMPUTATION, "panic: slice index out of range for the cubic's roots");
+  for (size_t t = 0; t < take; ++t) {
+    const T lambda = sorted[t];
+    T m00 = a - lambda, m01 = d, m02 = T(0);
+    T m10 = d, m11 = b - lambda, m12 = e;
+    T m20 = T(0), m21 = e, m22 = c - lambda;
+    const T r0 = std::sqrt(m00 * m00 + m01 * m01 + m02 * m02);
+    const T r1 = std::sqrt(m10 * m10 + m11 * m11 + m12 * m12);
+    const T r2 = std::sqrt(m20 * m20 + m21 * m21 + m22 * m22);
+    std::vector<T> v(3, T(0));
+    if (r0 >= r1 && r0 >= r2 && r0 != T(0)) {
+      const T s = T(1) / r0;
+      m00 = m00 * s; m01 = m01 * s; m02 = m02 * s;
+      T f = m10 / m00;
+      m11 = m11 - f * m01; m12 = m12 - f * m02;
+      f = m20 / m00;
+      m21 = m21 - f * m01; m22 = m22 - f * m02;
+      v[2] = T(1);
+      v[1] = -m12 * v[2] / m11;
+      v[0] = -(m01 * v[1] + m02 * v[2]) / m00;
+    } else if (r1 >= r0 && r1 >= r2 && r1 != T(0)) {
+      const T s = T(1) / r1;
+      m10 = m10 * s; m11 = m11 * s; m12 = m12 * s;
+      T f = m01 / m11;
+      m00 = m00 - f * m10; m02 = m02 - f * m12;
+      f = m21 / m11;
+      m20 = m20 - f * m10; m22 = m22 - f * m12;
+      v[2] = T(1);
+      v[0] = -m02 * v[2] / m00;
+      v[1] = -(m10 * v[0] + m12 * v[2]) / m11;
+    } else if (r2 != T(0)) {
+      const T s = T(1) / r2;
+      m20 = m20 * s; m21 = m21 * s; m22 = m22 * s;
+      T f = m02 / m22;
+      m00 = m00 - f * m20; m01 = m01 - f * m21;
+      f = m12 / m22;
+      m10 = m10 - f * m20; m11 = m11 - f * m21;
+      v[0] = T(1);
+      v[1] = -m10 * v[0] / m11;
+      v[2] = -(m20 * v[0] + m21 * v[1]) / m22;
+    } else {
+      if (num >= 1) v[0] = T(1);
+      else if (num >= 2) v[1] = T(1);
+      else v[2] = T(1);
+    }
+    const T nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (nv != T(0)) { v[0] = v[0] / nv; v[1] = v[1] / nv; v[2] = v[2] / nv; }
+    vecs.push_back(v);
+  }
+  if (sorted.size() > num) sorted.resize(num);
+  vals = sorted;
+  return ok(err);
+}
+
+// solve_tridiagonal_eigenproblem, eigen.rs:512-646
+template <class T>
+int tridiag_eig(const std::vector<T>& alpha, const std::vector<T>& beta, size_t num, std::vector<T>& vals,
+                std::vector<std::vector<T>>& vecs, or_err* err) {
+  const size_t n = alpha.size();
+  if (n == 0) return set_err(err, E_VALUE, value_msg("Empty tridiagonal matrix"));
+  if (beta.size() != n - 1) return set_err(err, E_DIMENSION_MISMATCH, dim_msg(n - 1, beta.size()), n - 1, beta.size());
+  if (n <= 3) return small_tridiag<T>(alpha, beta, num, vals, vecs, err);
+  std::vector<T> d = alpha, e = beta;
+  e.push_back(T(0));
+  std::vector<std::vector<T>> z(n, std::vector<T>(n, T(0)));
+  for (size_t i = 0; i < n; ++i) z[i][i] = T(1);
+  const T small = (T)1e-12;
+  for (size_t l = 0; l < n; ++l) {
+    int iter = 0;
+    for (;;) {
+      size_t m = l;
+      while (m < n - 1) {
+        if (std::fabs(e[m]) <= small * (std::fabs(d[m]) + std::fabs(d[m + 1]))) break;
+        ++m;
+      }
+      if (m == l) break;
+      if (iter >= 30) return set_err(err, E_SOLVER_FAILURE, "Iterative solver failure: QL algorithm did not converge");
+      T g = (d[l + 1] - d[l]) * T(0.5) / e[l];
+      const T r = std::sqrt(g * g + T(1));
+      g = d[m] - d[l] + e[l] / (g + (g >= T(0) ? r : -r));
+      T s = T(1), c = T(1), p = T(0);
+      size_t i = m - 1;
+      while (i >= l && i < n) {
+        const T f = s * e[i];
+        const T b = c * e[i];
+        const T rr = std::sqrt(f * f + g * g);
+        e[i + 1] = rr;
+        if (rr == T(0)) {
+          d[i + 1] = d[i + 1] - p;
+          e[m] = T(0);
+          break;
+        }
+        s = f / rr;
+        c = g / rr;
+        p = s * (d[i] - d[i + 1]) + c * b;
+        d[i + 1] = d[i + 1] + p;
+        g = c * s - b;
+        for (size_t k = 0; k < n; ++k) {
+          const T t = z[k][i + 1];
+          z[k][i + 1] = s * z[k][i] + c * t;
+          z[k][i] = c * z[k][i] - s * t;
+        }
+        if (i == 0) break;
+        i -= 1;
+      }
+      if ((int32_t)i < (int32_t)l || i >= n) break;
+      if (r == T(0)) {  // unreachable: r >= 1 (kept as written)
+        if ((int32_t)m == (int32_t)(l + 1)) break;
+        d[l] = d[l] - p;
+        e[l] = g;
+        e[m - 1] = T(0);
+      }
+      ++iter;
+    }
+  }
+  std::vector<size_t> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return d[i] > d[j]; });
+  vals.clear();
+  vecs.clear();
+  for (size_t k = 0; k < std::min(num, n); ++k) {
+    vals.push_back(d[idx[k]]);
+    std::vector<T> v(n);
+    for (size_t i = 0; i < n; ++i) v[i] = z[i][idx[k]];
+    vecs.push_back(v);
+  }
+  return ok(err);
+}
+
+struct SymArrays {
+  const uint64_t* indptr;
+  const uint64_t* indices;
+  uint64_t n;
+};
+
+// power_iteration, eigen.rs:124-293
+template <class T>
+int power_iteration(const SymArrays& A, const T* data, uint64_t max_iter, double tol, int normalize, const T* x0,
+                    uint64_t x0_len, T* lambda_out, T* vec_out, T* resid_out, or_eig_info* info, or_err* err) {
+  const uint64_t n = A.n;
+  std::vector<T> x(n, T(0));
+  if (x0) {
+    if (x0_len != n) return set_err(err, E_DIMENSION_MISMATCH, dim_msg(n, x0_len), n, x0_len);
+    for (uint64_t i = 0; i < n; ++i) x[i] = x0[i];
+  } else if (n > 0) {
+    x[0] = T(1);
+  }
+  if (normalize) {
+    const T nrm = std::sqrt(fold_dot(x, x));
+    if (nrm != T(0))
+      for (auto& v : x) v = v / nrm;
+  }
+  const T ttol = (T)tol;
+  T lambda = T(0), prev = T(0);
+  bool conv = false;
+  uint64_t it = 0;
+  std::vector<T> y(n);
+  while (it < max_iter) {
+    sym_matvec<T>(A.indptr, A.indices, data, n, x.data(), y.data());
+    const T num = fold_dot(x, y);
+    if (normalize) {
+      lambda = num;
+      if (std::fabs(lambda - prev) < ttol) { conv = true; break; }
+      const T nrm = std::sqrt(fold_dot(y, y));
+      if (nrm != T(0))
+        for (uint64_t i = 0; i < n; ++i) x[i] = y[i] / nrm;
+    } else {
+      x = y;
+      const T nx = std::sqrt(fold_dot(x, x));
+      if (nx != T(0)) lambda = num / (nx * nx);
+      if (std::fabs(lambda - prev) < ttol) { conv = true; break; }
+    }
+    prev = lambda;
+    ++it;
+  }
+  sym_matvec<T>(A.indptr, A.indices, data, n, x.data(), y.data());
+  T rs = T(0);
+  for (uint64_t i = 0; i < n; ++i) {
+    const T ri = y[i] - lambda * x[i];
+    rs = rs + ri * ri;
+  }
+  *lambda_out = lambda;
+  if (vec_out) for (uint64_t i = 0; i < n; ++i) vec_out[i] = x[i];
+  *resid_out = std::sqrt(rs);
+  info->iterations = it;
+  info->converged = conv ? 1 : 0;
+  info->count = 1;
+  return ok(err);
+}
+
+// lanczos, eigen.rs:295-494
+template <class T>
+int lanczos(const SymArrays& A, const T* data, uint64_t max_iter, uint64_t max_subspace, double tol,
+            uint64_t num_eigenvalues, int compute_vecs, const T* v0, uint64_t v0_len, T* vals_out, T* vecs_out,
+            T* resid_out, or_eig_info* info, or_err* err) {
+  const uint64_t n = A.n;
+  const uint64_t sub = std::min(max_subspace, n);
+  const uint64_t num = std::min(num_eigenvalues, sub);
+  std::vector<T> v(n, T(0));
+  if (v0) {
+    if (v0_len != n) return set_err(err, E_DIMENSION_MISMATCH, dim_msg(n, v0_len), n, v0_len);
+    for (uint64_t i = 0; i < n; ++i) v[i] = v0[i];
+  } else if (n > 0) {
+    v[0] = T(1);
+  }
+  if (sub == 0) return set_err(err, E_COMPUTATION, "panic: capacity overflow (subspace size 0)");
+  const T nrm = std::sqrt(fold_dot(v, v));
+  if (nrm != T(0))
+    for (auto& t : v) t = t / nrm;
+  std::vector<std::vector<T>> V{v};
+  std::vector<T> alpha, beta;
+  std::vector<T> w(n);
+  sym_matvec<T>(A.indptr, A.indices, data, n, v.data(), w.data());
+  const T a0 = fold_dot(v, w);
+  alpha.push_back(a0);
+  for (uint64_t i = 0; i < n; ++i) w[i] = w[i] - a0 * v[i];
+  const T beta_j = std::sqrt(fold_dot(w, w));  // never updated (see above)
+  uint64_t it = 1;
+  bool conv = false;
+  const T ttol = (T)tol;
+  std::vector<T> ev;
+  std::vector<std::vector<T>> evec;
+  while (it < max_iter && alpha.size() < sub) {
+    if (beta_j == T(0)) break;
+    beta.push_back(beta_j);
+    std::vector<T> vn(n);
+    for (uint64_t i = 0; i < n; ++i) vn[i] = w[i] / beta_j;
+    V.push_back(vn);
+    sym_matvec<T>(A.indptr, A.indices, data, n, vn.data(), w.data());
+    for (const auto& vj : V) {
+      const T proj = fold_dot(vj, w);
+      for (uint64_t i = 0; i < n; ++i) w[i] = w[i] - proj * vj[i];
+    }
+    const T aj = fold_dot(vn, w);
+    alpha.push_back(aj);
+    for (uint64_t i = 0; i < n; ++i) w[i] = w[i] - aj * vn[i];
+    const T bnext = std::sqrt(fold_dot(w, w));
+    if (alpha.size() >= num) {
+      int rc = tridiag_eig<T>(alpha, beta, num, ev, evec, err);
+      if (rc) return rc;
+      if (ev.empty()) return set_err(err, E_COMPUTATION, "panic: index out of bounds (no eigenvalue to test)");
+      if (bnext < ttol * std::fabs(ev[0])) { conv = true; break; }
+    }
+    ++it;
+  }
+  int rc = tridiag_eig<T>(alpha, beta, num, ev, evec, err);
+  if (rc) return rc;
+  std::vector<T> ritz;
+  if (compute_vecs) {
+    ritz.assign(n * num, T(0));
+    for (uint64_t k = 0; k < num; ++k)
+      for (uint64_t i = 0; i < n; ++i) {
+        T s = T(0);
+        for (size_t j = 0; j < V.size(); ++j)
+          if (j < evec.size()) {
+            if (k >= evec[j].size()) return set_err(err, E_COMPUTATION, kPanicIndex);
+            s = s + evec[j][k] * V[j][i];
+          }
+        ritz[i * num + k] = s;
+      }
+  }
+  std::vector<T> res(num, T(0));
+  if (compute_vecs) {
+    std::vector<T> e(n), ax(n);
+    for (uint64_t k = 0; k < num; ++k) {
+      if (k >= ev.size()) return set_err(err, E_COMPUTATION, kPanicIndex);
+      for (uint64_t i = 0; i < n; ++i) e[i] = ritz[i * num + k];
+      sym_matvec<T>(A.indptr, A.indices, data, n, e.data(), ax.data());
+      T s = T(0);
+      for (uint64_t i = 0; i < n; ++i) {
+        const T ri = ax[i] - ev[k] * e[i];
+        s = s + ri * ri;
+      }
+      res[k] = std::sqrt(s);
+    }
+  } else {
+    for (uint64_t k = 0; k < num; ++k)
+      if (k < evec.size() && !beta.empty()) {
+        if (k >= evec.back().size()) return set_err(err, E_COMPUTATION, kPanicIndex);
+        res[k] = beta.back() * std::fabs(evec.back()[k]);
+      }
+  }
+  for (size_t k = 0; k < ev.size(); ++k) vals_out[k] = ev[k];
+  for (uint64_t k = 0; k < num; ++k) resid_out[k] = res[k];
+  if (compute_vecs && vecs_out)
+    for (uint64_t q = 0; q < n * num; ++q) vecs_out[q] = ritz[q];
+  info->iterations = it;
+  info->converged = conv ? 1 : 0;
+  info->count = ev.size();
+  info->num = num;
+  return ok(err);
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_power_iteration_f64(const uint64_t* indptr, const uint64_t* indices, const double* data, uint64_t n,
+                           uint64_t max_iter, double tol, int normalize, const double* x0, uint64_t x0_len,
+                           double* lambda, double* vec, double* resid, or_eig_info* info, or_err* err) {
+  return power_iteration<double>({indptr, indices, n}, data, max_iter, tol, normalize, x0, x0_len, lambda, vec, resid,
+                                 info, err);
+}
+int or_power_iteration_f32(const uint64_t* indptr, const uint64_t* indices, const float* data, uint64_t n,
+                           uint64_t max_iter, double tol, int normalize, const float* x0, uint64_t x0_len,
+                           float* lambda, float* vec, float* resid, or_eig_info* info, or_err* err) {
+  return power_iteration<float>({indptr, indices, n}, data, max_iter, tol, normalize, x0, x0_len, lambda, vec, resid,
+                                info, err);
+}
+int or_lanczos_f64(const uint64_t* indptr, const uint64_t* indices, const double* data, uint64_t n,
+                   uint64_t max_iter, uint64_t max_subspace, double tol, uint64_t num_eigenvalues, int compute_vecs,
+                   const double* v0, uint64_t v0_len, double* vals, double* vecs, double* resids, or_eig_info* info,
+                   or_err* err) {
+  return lanczos<double>({indptr, indices, n}, data, max_iter, max_subspace, tol, num_eigenvalues, compute_vecs, v0,
+                         v0_len, vals, vecs, resids, info, err);
+}
+int or_lanczos_f32(const uint64_t* indptr, const uint64_t* indices, const float* data, uint64_t n, uint64_t max_iter,
+                   uint64_t max_subspace, double tol, uint64_t num_eigenvalues, int compute_vecs, const float* v0,
+                   uint64_t v0_len, float* vals, float* vecs, float* resids, or_eig_info* info, or_err* err) {
+  return lanczos<float>({indptr, indices, n}, data, max_iter, max_subspace, tol, num_eigenvalues, compute_vecs, v0,
+                        v0_len, vals, vecs, resids, info, err);
+}
+int or_tridiag_eig_f64(const double* alpha, const double* beta, uint64_t m, uint64_t beta_len, uint64_t num,
+                       double* vals, double* vecs, uint64_t* count, or_err* err) {
+  std::vector<double> a(alpha, alpha + m), b(beta, beta + beta_len), ev;
+  std::vector<std::vector<double>> evec;
+  const int rc = tridiag_eig<double>(a, b, num, ev, evec, err);
+  if (rc) return rc;
+  *count = ev.size();
+  for (size_t k = 0; k < ev.size(); ++k) vals[k] = ev[k];
+  for (size_t k = 0; k < evec.size(); ++k)
+    for (size_t i = 0; i < evec[k].size(); ++i) vecs[k * m + i] = evec[k][i];
+  return 0;
+}
+uint64_t or_solve_cubic_f64(double p, double q, double r, double* roots) {
+  const std::vector<double> v = solve_cubic<double>(p, q, r);
+  for (size_t k = 0; k < v.size(); ++k) roots[k] = v[k];
+  return v.size();
+}
+
+}  // extern "C"

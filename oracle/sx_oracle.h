@@ -206,6 +206,37 @@ int or_sym_csr_from_csr_f32(const uint64_t* indptr, const uint64_t* indices, con
                             uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,
                             uint64_t* indices_out, float* data_out, or_err* err);
 
+/* ---- eigen (linalg/eigen.rs) ---- */
+typedef struct {
+  uint64_t iterations;
+  int converged;
+  uint64_t count; /* eigenvalues returned */
+  uint64_t num;   /* min(num_eigenvalues, subspace): residual / vector columns */
+} or_eig_info;
+/* power_iteration (eigen.rs:124-293) on a SymCsrMatrix's arrays; x0 may be
+ * NULL (then e_0); vec: n entries. */
+int or_power_iteration_f64(const uint64_t* indptr, const uint64_t* indices, const double* data, uint64_t n,
+                           uint64_t max_iter, double tol, int normalize, const double* x0, uint64_t x0_len,
+                           double* lambda, double* vec, double* resid, or_eig_info* info, or_err* err);
+int or_power_iteration_f32(const uint64_t* indptr, const uint64_t* indices, const float* data, uint64_t n,
+                           uint64_t max_iter, double tol, int normalize, const float* x0, uint64_t x0_len,
+                           float* lambda, float* vec, float* resid, or_eig_info* info, or_err* err);
+/* lanczos (eigen.rs:295-494): vals and resids have room for num_eigenvalues,
+ * vecs for n * num (row-major, column k = Ritz vector k) when compute_vecs. */
+int or_lanczos_f64(const uint64_t* indptr, const uint64_t* indices, const double* data, uint64_t n,
+                   uint64_t max_iter, uint64_t max_subspace, double tol, uint64_t num_eigenvalues, int compute_vecs,
+                   const double* v0, uint64_t v0_len, double* vals, double* vecs, double* resids, or_eig_info* info,
+                   or_err* err);
+int or_lanczos_f32(const uint64_t* indptr, const uint64_t* indices, const float* data, uint64_t n, uint64_t max_iter,
+                   uint64_t max_subspace, double tol, uint64_t num_eigenvalues, int compute_vecs, const float* v0,
+                   uint64_t v0_len, float* vals, float* vecs, float* resids, or_eig_info* info, or_err* err);
+/* solve_tridiagonal_eigenproblem (eigen.rs:512-646): vecs (count x m) holds
+ * eigenvector k at vecs[k * m .. k * m + m). */
+int or_tridiag_eig_f64(const double* alpha, const double* beta, uint64_t m, uint64_t beta_len, uint64_t num,
+                       double* vals, double* vecs, uint64_t* count, or_err* err);
+/* solve_cubic (eigen.rs:890-952): returns the number of roots written. */
+uint64_t or_solve_cubic_f64(double p, double q, double r, double* roots);
+
 #ifdef __cplusplus
 }
 #endif

@@ -124,6 +124,29 @@ class LGMRESOptions(C.Structure):
     ]
 
 
+class EigenResult(C.Structure):
+    _fields_ = [
+        ("iterations", c_u64),
+        ("converged", C.c_int),
+        ("num_eigenvalues", c_u64),
+        ("num_columns", c_u64),
+    ]
+
+
+class PowerOptions(C.Structure):
+    _fields_ = [("max_iter", c_u64), ("tol", c_dbl), ("normalize", C.c_int)]
+
+
+class LanczosOptions(C.Structure):
+    _fields_ = [
+        ("max_iter", c_u64),
+        ("max_subspace_size", c_u64),
+        ("tol", c_dbl),
+        ("num_eigenvalues", c_u64),
+        ("compute_eigenvectors", C.c_int),
+    ]
+
+
 class IROptions(C.Structure):
     _fields_ = [
         ("max_outer", c_u64),
@@ -260,6 +283,11 @@ _SIGS = {
     "sx_qmr": (c_int, [ctx_t, op_t, c_vp, c_u64, P(BiCGOptions), c_vp, c_int, P(IterResult)]),
     "sx_minres": (c_int, [ctx_t, op_t, c_vp, c_u64, P(MINRESOptions), c_vp, c_int, P(IterResult)]),
     "sx_lgmres": (c_int, [ctx_t, op_t, c_vp, c_u64, P(LGMRESOptions), c_vp, c_int, P(IterResult)]),
+    "sx_power_options_default": (None, [P(PowerOptions)]),
+    "sx_power_iteration": (c_int, [ctx_t, op_t, P(PowerOptions), c_vp, c_u64, c_int, c_vp, c_vp, c_vp,
+                                   P(EigenResult)]),
+    "sx_lanczos_options_default": (None, [P(LanczosOptions)]),
+    "sx_lanczos": (c_int, [ctx_t, op_t, P(LanczosOptions), c_vp, c_u64, c_int, c_vp, c_vp, c_vp, P(EigenResult)]),
     "sx_iter_message": (c_int, [P(IterResult), c_int, C.c_char_p, c_u64]),
     "sx_ir_options_default": (None, [P(IROptions)]),
     "sx_cg_mixed": (c_int, [ctx_t, op_t, c_vp, c_u64, P(IROptions), c_vp, c_int, P(IRResult)]),

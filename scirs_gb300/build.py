@@ -32,11 +32,12 @@ SOURCES = [
     "sx_krylov2.cu",
     "sx_ilu.cu",
     "sx_io.cu",
+    "sx_eigen.cu",
     "sx_gen.cpp",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
 def _nvcc() -> str:

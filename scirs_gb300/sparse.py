@@ -630,6 +630,52 @@ def lgmres(a: Operator, b, max_iter=500, rtol=1e-8, atol=1e-8, inner_m=30, outer
     return _result(x, r)
 
 
+# ----------------------------------------------------------- eigenpairs
+@dataclass
+class EigenResult:
+    """EigenResult (eigen.rs:64-78): eigenvectors is n x k (column k = pair k)."""
+    eigenvalues: np.ndarray
+    eigenvectors: Optional[np.ndarray]
+    iterations: int
+    residuals: np.ndarray
+    converged: bool
+
+
+def power_iteration(a: SymCsrMatrix, max_iter=100, tol=1e-8, normalize=True, initial_guess=None) -> EigenResult:
+    """power_iteration(matrix, PowerIterationOptions { .. }, initial_guess)
+    (eigen.rs:124-293)."""
+    n = a.shape[0]
+    x0 = None if initial_guess is None else np.ascontiguousarray(initial_guess, dtype=a.dtype)
+    o = L.PowerOptions(max_iter, tol, 1 if normalize else 0)
+    lam = np.zeros(1, dtype=a.dtype)
+    res = np.zeros(1, dtype=a.dtype)
+    vec = np.zeros(n, dtype=a.dtype)
+    r = L.EigenResult()
+    _check(L.lib.sx_power_iteration(a.ctx.handle, a.handle, C.byref(o), _ptr(x0) if x0 is not None else None,
+                                    0 if x0 is None else x0.size, L.SX_MEM_HOST, _ptr(lam), _ptr(vec), _ptr(res),
+                                    C.byref(r)))
+    return EigenResult(lam, vec.reshape(n, 1), int(r.iterations), res, bool(r.converged))
+
+
+def lanczos(a: SymCsrMatrix, max_iter=1000, max_subspace_size=20, tol=1e-8, num_eigenvalues=1,
+            compute_eigenvectors=True, initial_guess=None) -> EigenResult:
+    """lanczos(matrix, LanczosOptions { .. }, initial_guess) (eigen.rs:295-494)."""
+    n = a.shape[0]
+    x0 = None if initial_guess is None else np.ascontiguousarray(initial_guess, dtype=a.dtype)
+    o = L.LanczosOptions(max_iter, max_subspace_size, tol, num_eigenvalues, 1 if compute_eigenvectors else 0)
+    k = max(min(num_eigenvalues, max_subspace_size, n), 1)
+    vals = np.zeros(k, dtype=a.dtype)
+    res = np.zeros(k, dtype=a.dtype)
+    vecs = np.zeros(n * k, dtype=a.dtype) if compute_eigenvectors else None
+    r = L.EigenResult()
+    _check(L.lib.sx_lanczos(a.ctx.handle, a.handle, C.byref(o), _ptr(x0) if x0 is not None else None,
+                            0 if x0 is None else x0.size, L.SX_MEM_HOST, _ptr(vals),
+                            _ptr(vecs) if vecs is not None else None, _ptr(res), C.byref(r)))
+    cols = int(r.num_columns)
+    ev = vecs[: n * cols].reshape(n, cols) if vecs is not None else None
+    return EigenResult(vals[: int(r.num_eigenvalues)], ev, int(r.iterations), res[:cols], bool(r.converged))
+
+
 @dataclass
 class IRResult:
     x: np.ndarray

@@ -352,6 +352,39 @@ int main() {
       CHECK(std::string(e.what()) == "Value error: Matrix must be symmetric to convert to SymCSR format");
     }
   });
+  // eigen.rs:996-1066 on the same matrix.  The reference's tests assert
+  // eigenvalues 5, 1, -1, which the matrix does not have (its largest is
+  // 4.7577); these check what its power iteration and two-step Lanczos
+  // compute instead.
+  run("eigen_power_iteration_and_lanczos", [] {
+    auto sym = SymCsrMatrix<double>::create({2, 1, 2, 3, 1}, {0, 1, 3, 5}, {0, 0, 1, 1, 2}, {3, 3});
+    PowerIterationOptions po;
+    po.tol = 1e-10;
+    auto r = power_iteration(sym, po);
+    CHECK(r.converged);
+    NEAR(r.eigenvalues[0], 4.757701765444642, 1e-8);
+    double nrm = 0;
+    for (double v : r.eigenvectors) nrm += v * v;
+    NEAR(std::sqrt(nrm), 1.0, 1e-8);
+    LanczosOptions lo;
+    lo.max_subspace_size = 2;
+    lo.num_eigenvalues = 2;
+    auto l = lanczos(sym, lo);
+    // alpha = [2, 0], beta = [1]: eigenvalues 1 +- sqrt(2)
+    CHECK(l.eigenvalues.size() == 2 && l.rows == 3 && l.cols == 2);
+    NEAR(l.eigenvalues[0], 1.0 + std::sqrt(2.0), 1e-12);
+    NEAR(l.eigenvalues[1], 1.0 - std::sqrt(2.0), 1e-12);
+    lo.max_subspace_size = 6;
+    try {
+      auto big = SymCsrMatrix<double>::create({4, -1, 4, -1, 4, -1, 4, -1, 4}, {0, 1, 3, 5, 7, 9},
+                                              {0, 0, 1, 1, 2, 2, 3, 3, 4}, {5, 5});
+      lanczos(big, lo);
+      CHECK(false);
+    } catch (const SparseError& e) {
+      CHECK(e.variant() == "IterativeSolverFailure");
+      CHECK(std::string(e.what()) == "Iterative solver failure: QL algorithm did not converge");
+    }
+  });
   // errors carry the reference's variants and messages (csr.rs:107-119)
   run("construction_errors", [] {
     try {
