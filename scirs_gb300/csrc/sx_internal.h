@@ -159,8 +159,9 @@ struct sx_ctx_s {
   // for FP32, 0 never (SX_SHORT)
   int short_rows = 1;
   // diagonal layout (SX_DIA): 0 never built or used; 1 (default) used for
-  // FP64 matrices and FP16 value copies; 2 used for every matrix that has it
+  // every matrix that has it
   int dia = 1;
+  bool dia_nd6 = true;  // SX_DIA_ND6=0: five or six diagonals take the 8-slot kernel
   int win_shape = 0;
 };
 

@@ -487,7 +487,8 @@ __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ 
                                                           unsigned int* counter, Epi epi, Gather gat = Gather{}) {
   if (epi.skip()) return;
   constexpr int VEC = DiaVec<T>::kVec;
-  constexpr int KB = ND < kDiaBatch ? ND : kDiaBatch;
+  // up to six diagonals in one batch (the learned factors have five)
+  constexpr int KB = ND <= 6 ? ND : kDiaBatch;
   Acc3<T> a{T(0), T(0), T(0)};
   const int n = (int)nrows;
   const int omin = offs.off[0], omax = offs.off[nd - 1];

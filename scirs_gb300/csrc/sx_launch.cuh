@@ -196,13 +196,12 @@ template <typename T, class Epi, bool FMA, typename V = T, class Gather = Gather
 bool launch_dia(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
                 int64_t /*blocks*/, Gather gat = Gather{}) {
   if (!ctx->dia || !vals || c.dia_n <= 0 || !c.dia_mask) return false;
-  // SX_DIA=1 (default): FP64 matrices and FP16 value copies, where it was
-  // measured faster than the CSR kernels; SX_DIA=2: every matrix that has it
-  if (ctx->dia == 1 && sizeof(T) == 4 && sizeof(V) == 4) return false;
   DiaOffs offs;
   for (int q = 0; q < 16; ++q) offs.off[q] = c.dia_off[q];
   const int64_t groups = (c.nrows + DiaVec<T>::kVec - 1) / DiaVec<T>::kVec;
-  if (c.dia_n <= 8) dia_go<spmv_dia_kernel<T, 8, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  if (c.dia_n <= 6 && ctx->dia_nd6)
+    dia_go<spmv_dia_kernel<T, 6, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  else if (c.dia_n <= 8) dia_go<spmv_dia_kernel<T, 8, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   else if (c.dia_n <= 12) dia_go<spmv_dia_kernel<T, 12, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   else dia_go<spmv_dia_kernel<T, 16, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   return true;
@@ -289,12 +288,12 @@ inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma
   const bool pipe_fits = c.monotone && c.max_chunk_nnz + 3 <= kBlock * 12;
   const bool items8 = c.max_chunk_nnz + 3 <= kBlock * 8;
   if (c.nrows <= 0) return "none";
-  const bool dia_ok = ctx->dia == 2 || (ctx->dia == 1 && (w == 8 || (half_ok && c.dia_vals16)));
-  if (ctx->dia && c.dia_n > 0 && dia_ok) {
-    if (half_ok && w == 4 && c.dia_vals16)
-        return c.dia_n <= 8 ? "spmv_dia_kernel<ND=8, FP16 values>"
-                          : (c.dia_n <= 12 ? "spmv_dia_kernel<ND=12, FP16 values>" : "spmv_dia_kernel<ND=16, FP16 values>");
-    return c.dia_n <= 8 ? "spmv_dia_kernel<ND=8>" : (c.dia_n <= 12 ? "spmv_dia_kernel<ND=12>" : "spmv_dia_kernel<ND=16>");
+  if (ctx->dia && c.dia_n > 0 && c.dia_mask) {
+    const bool h = half_ok && w == 4 && c.dia_vals16;
+    if (c.dia_n <= 6 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=6, FP16 values>" : "spmv_dia_kernel<ND=6>";
+    if (c.dia_n <= 8) return h ? "spmv_dia_kernel<ND=8, FP16 values>" : "spmv_dia_kernel<ND=8>";
+    if (c.dia_n <= 12) return h ? "spmv_dia_kernel<ND=12, FP16 values>" : "spmv_dia_kernel<ND=12>";
+    return h ? "spmv_dia_kernel<ND=16, FP16 values>" : "spmv_dia_kernel<ND=16>";
   }
   if (c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) return "spmv_win_kernel";
   if (ctx->short_rows && (fma || (w == 4 && ctx->short_rows == 2)) && c.monotone && c.max_row_len <= 16)

@@ -157,7 +157,7 @@ def test_compressed_columns_bit_exact(S, dtype, kind, dims, p0, p1):
     vals = v.astype(dtype)
     x = np.random.default_rng(2).standard_normal(n).astype(dtype)
     yr = O.spmv_i32(ip, ix, vals, x)
-    for env in ({}, {"SX_DIA": "2"}, {"SX_DIA": "0"}, {"SX_DIA": "0", "SX_SHORT": "2"},
+    for env in ({}, {"SX_DIA_ND6": "0"}, {"SX_DIA": "0"}, {"SX_DIA": "0", "SX_SHORT": "2"},
                 {"SX_DIA": "0", "SX_SHORT": "0", "SX_COL16": "1"}):
         c = _ctx_with(S, env)
         a = S.csr_from_arrays(c, ip, ix, vals, (n, n))
@@ -192,14 +192,19 @@ def test_kernel_choice_names(S, ctx):
     n = len(ip) - 1
     a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
     a32 = a64.astype(np.float32)
-    # default (SX_DIA=1): the diagonal layout for FP64, the CSR pipeline for FP32
-    assert S.spmv_kernel(a32) == "spmv_pipe_kernel<ITEMS=8>"
+    # default (SX_DIA=1): the diagonal layout for FP64 and FP32 (7 diagonals)
+    assert S.spmv_kernel(a32) == "spmv_dia_kernel<ND=8>"
     assert S.spmv_kernel(a64, exact=False) == "spmv_dia_kernel<ND=8>"
     assert S.spmv_kernel(a64, exact=True) == "spmv_dia_kernel<ND=8>"
-    c2 = _ctx_with(S, {"SX_DIA": "2"})
-    d32 = S.csr_from_arrays(c2, ip, ix, v.astype(np.float32), (n, n))
+    # five diagonals (the 2D 5-point stencil): the six-slot kernel, one batch
+    ip5, ix5, v5 = S.generate("poisson2d", 40, 40)
+    f32 = S.csr_from_arrays(ctx, ip5, ix5, v5.astype(np.float32), (1600, 1600))
+    assert S.spmv_kernel(f32) == "spmv_dia_kernel<ND=6>"
+    c2 = _ctx_with(S, {"SX_DIA_ND6": "0"})
+    d32 = S.csr_from_arrays(c2, ip5, ix5, v5.astype(np.float32), (1600, 1600))
     assert S.spmv_kernel(d32) == "spmv_dia_kernel<ND=8>"
     d32.close()
+    f32.close()
     c2.close()
     c = _ctx_with(S, {"SX_DIA": "0"})
     b64 = S.csr_from_arrays(c, ip, ix, v, (n, n))
@@ -250,10 +255,11 @@ def _diag_cases(rng):
     yield "seventeen_diagonals", ip, cols.astype(np.int32), rng.uniform(-1, 1, len(cols)), False
 
 
+@pytest.mark.parametrize("env", [{}, {"SX_DIA_ND6": "0"}])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-def test_diagonal_layout_bit_exact(S, dtype):
+def test_diagonal_layout_bit_exact(S, dtype, env):
     rng = np.random.default_rng(12)
-    ctx = _ctx_with(S, {"SX_DIA": "2"})  # the layout for FP32 too
+    ctx = _ctx_with(S, env)
     for name, ip, ix, v, expect in _diag_cases(rng):
         n = len(ip) - 1
         vals = v.astype(dtype)

@@ -144,7 +144,7 @@ def _lower_of(ip, ix, dv):
     return lip, ix[keep].astype(np.uint64), dv[keep]
 
 
-@pytest.mark.parametrize("env", [{}, {"SX_DIA": "2"}, {"SX_DIA": "0"}, {"SX_DIA": "0", "SX_WIN": "2"}, {"SX_DIA": "0", "SX_SHORT": "2"},
+@pytest.mark.parametrize("env", [{}, {"SX_DIA_ND6": "0"}, {"SX_DIA": "0"}, {"SX_DIA": "0", "SX_WIN": "2"}, {"SX_DIA": "0", "SX_SHORT": "2"},
                                  {"SX_DIA": "0", "SX_WIN": "0", "SX_SHORT": "0"}])
 @pytest.mark.parametrize("kind", ["laplace3d", "powerlaw"])
 def test_kernel_choices_bit_exact(S, env, kind):
