@@ -13,6 +13,7 @@
 // CsrMatrix::transpose (csr.rs:289-326).
 
 #include <algorithm>
+#include <limits>
 #include <atomic>
 #include <climits>
 #include <cstdio>
@@ -182,6 +183,18 @@ __global__ void k_count(const int32_t* __restrict__ key, int64_t n, int32_t* cnt
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
     atomicAdd(cnt + key[k], 1);
+}
+// *out = max(cnt[0 .. m)), *out zero on entry
+__global__ void k_max_count(const int32_t* __restrict__ cnt, int64_t m, int32_t* out) {
+  int32_t v = 0;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += stride) v = max(v, cnt[k]);
+  v = max(v, __shfl_xor_sync(0xffffffffu, v, 16));
+  v = max(v, __shfl_xor_sync(0xffffffffu, v, 8));
+  v = max(v, __shfl_xor_sync(0xffffffffu, v, 4));
+  v = max(v, __shfl_xor_sync(0xffffffffu, v, 2));
+  v = max(v, __shfl_xor_sync(0xffffffffu, v, 1));
+  if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, v);
 }
 
 // Exclusive scan, three phases: block sums, scan of the sums (recursive),
@@ -418,6 +431,32 @@ __global__ void k_merge_pass(const unsigned long long* __restrict__ in, unsigned
 }  // namespace
 
 // Sort each segment [ptr[r], ptr[r+1]) of keys ascending.
+// Host copy of the segment pointers, taken only when some segment is
+// longer than the in-register sorts handle (cnt[m] is free scratch: the
+// counts use cnt[0 .. m)); empty otherwise.  Synchronises the stream.
+static int long_segment_ptr(sx_ctx ctx, int32_t* cnt, int64_t m, const int32_t* d_ptr,
+                            std::vector<int32_t>& h_ptr) {
+  h_ptr.clear();
+  int32_t maxc = 0;
+  cudaMemsetAsync(cnt + m, 0, 4, ctx->stream);
+  if (m > 0) {
+    k_max_count<<<vec_grid(ctx, m), kBlock, 0, ctx->stream>>>(cnt, m, cnt + m);
+    ctx->launches++;
+  }
+  cudaMemcpyAsync(&maxc, cnt + m, 4, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "segment lengths", __FILE__, __LINE__);
+  if (maxc > 2048) {
+    h_ptr.resize(m + 1);
+    cudaMemcpyAsync(h_ptr.data(), d_ptr, (m + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "segment pointers", __FILE__, __LINE__);
+  }
+  return SX_OK;
+}
+
+// h_ptr: the host segment pointers when a segment is longer than 2,048,
+// else empty
 static int segmented_sort(sx_ctx ctx, const int32_t* d_ptr, int64_t m, unsigned long long* keys,
                           const std::vector<int32_t>& h_ptr) {
   if (m <= 0) return SX_OK;
@@ -433,7 +472,7 @@ static int segmented_sort(sx_ctx ctx, const int32_t* d_ptr, int64_t m, unsigned 
   int rc = SX_OK;
   // long segments are rare: handle them one by one from the host copy
   unsigned long long* tmp = nullptr;
-  for (int64_t r = 0; r < m && rc == SX_OK; ++r) {
+  for (int64_t r = 0; r < (int64_t)h_ptr.size() - 1 && rc == SX_OK; ++r) {
     int32_t L = h_ptr[r + 1] - h_ptr[r];
     if (L <= 2048) continue;
     if (!tmp) {
@@ -1131,10 +1170,8 @@ int sx_csr_from_triplets(sx_ctx ctx, sx_dtype dtype, sx_csr_api api, const uint6
       k_scatter_rows<<<vec_grid(ctx, n), kBlock, 0, ctx->stream>>>(rows32, cols32, n, c.indptr,
                                                                       cursor, keys);
       ctx->launches++;
-      std::vector<int32_t> hptr(nrows + 1);
-      cudaMemcpyAsync(hptr.data(), c.indptr, (nrows + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream);
-      e = cudaStreamSynchronize(ctx->stream);
-      if (e != cudaSuccess) { rc = cuda_fail(e, "scatter", __FILE__, __LINE__); break; }
+      std::vector<int32_t> hptr;
+      if ((rc = long_segment_ptr(ctx, cnt, (int64_t)nrows, c.indptr, hptr))) break;
       if ((rc = segmented_sort(ctx, c.indptr, (int64_t)nrows, keys, hptr))) break;
       if (dtype == SX_F64)
         k_gather_sorted<double><<<vec_grid(ctx, n), kBlock, 0, ctx->stream>>>(
@@ -1322,7 +1359,9 @@ int sx_csr_from_raw_i32(sx_ctx ctx, sx_dtype dtype, const int64_t* indptr, const
 }  // extern "C"
 
 // ------------------------------------------------------------- transpose
-static int csr_transpose_dev(sx_ctx ctx, const DevCsr& a, int dtype, DevCsr& t) {
+// stats = false: the arrays only (no row statistics, tiles or diagonal
+// layout), for transposes used as index maps
+static int csr_transpose_dev(sx_ctx ctx, const DevCsr& a, int dtype, DevCsr& t, bool stats = true) {
   if (!a.monotone)
     return err_incons("transpose needs non-decreasing row pointers");
   const int64_t n = a.nnz;
@@ -1354,10 +1393,8 @@ static int csr_transpose_dev(sx_ctx ctx, const DevCsr& a, int dtype, DevCsr& t) 
           a.indptr, a.indices, a.nrows, t.indptr, cursor, keys);
       ctx->launches++;
     }
-    std::vector<int32_t> hptr(m + 1);
-    cudaMemcpyAsync(hptr.data(), t.indptr, (m + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream);
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) { rc = cuda_fail(e, "transpose scatter", __FILE__, __LINE__); break; }
+    std::vector<int32_t> hptr;
+    if ((rc = long_segment_ptr(ctx, cnt, m, t.indptr, hptr))) break;
     if ((rc = segmented_sort(ctx, t.indptr, m, keys, hptr))) break;
     if (n > 0) {
       if (dtype == SX_F64)
@@ -1368,7 +1405,15 @@ static int csr_transpose_dev(sx_ctx ctx, const DevCsr& a, int dtype, DevCsr& t) 
             keys, n, (const float*)a.vals, t.indices, (float*)t.vals);
       ctx->launches++;
     }
-    rc = csr_finalize_stats(ctx, t, (int)elt_size(dtype));
+    if (stats) {
+      rc = csr_finalize_stats(ctx, t, (int)elt_size(dtype));
+    } else {
+      t.monotone = true;
+      t.has_sorted_indices = true;
+      t.max_chunk_nnz = std::numeric_limits<int32_t>::max();  // no register-pipeline SpMV
+      const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) rc = cuda_fail(e, "transpose", __FILE__, __LINE__);
+    }
   } while (0);
   dev_free(cnt);
   dev_free(cursor);
@@ -1378,13 +1423,19 @@ static int csr_transpose_dev(sx_ctx ctx, const DevCsr& a, int dtype, DevCsr& t) 
 }
 
 namespace sx {
-int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out) {
+int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out, bool stats) {
   DevCsr t;
-  SX_CHECK(csr_transpose_dev(ctx, a->csr, a->dtype, t));
+  SX_CHECK(csr_transpose_dev(ctx, a->csr, a->dtype, t, stats));
   sx_op op = new_op(ctx, SX_OP_CSR, a->dtype, a->ncols, a->nrows);
   op->csr = t;
   *out = op;
   return SX_OK;
+}
+sx_op csr_op_adopt(sx_ctx ctx, int dtype, DevCsr& c) {
+  sx_op op = new_op(ctx, SX_OP_CSR, dtype, c.nrows, c.ncols);
+  op->csr = c;
+  c = DevCsr();
+  return op;
 }
 int ensure_transpose(sx_ctx ctx, sx_op a) {
   if (a->transpose) return SX_OK;

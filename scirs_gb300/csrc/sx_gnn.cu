@@ -600,10 +600,6 @@ __global__ void k_scale_g(const int32_t* __restrict__ gp, const float* __restric
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     for (int32_t e = gp[i]; e < gp[i + 1]; ++e) out[e] = (T)((double)g[e] * (double)dis[i]);
 }
-__global__ void k_i32_to_i64(const int32_t* __restrict__ in, int64_t n, int64_t* out) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = in[i];
-}
 
 // ============================================================ host side
 int prep_graph(sx_ctx ctx, sx_gnn net, sx_op a, Graph** out) {
@@ -676,7 +672,7 @@ int prep_graph(sx_ctx ctx, sx_gnn net, sx_op a, Graph** out) {
     s->csr.indices = g.gi;
     s->csr.vals = gidx;
     sx_op t = nullptr;
-    rc = csr_transpose_internal(ctx, s, &t);
+    rc = csr_transpose_internal(ctx, s, &t, false);
     s->csr.indptr = nullptr; s->csr.indices = nullptr; s->csr.vals = nullptr;
     delete s;
     if (rc) break;
@@ -1058,22 +1054,33 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out) {
   const int64_t n = g->n;
   const size_t w = elt_size(a->dtype);
   void* gv = nullptr;
-  int64_t* p64 = nullptr;
-  sx_op G = nullptr;
   int rc = SX_OK;
   do {
+    // G = D^-1/2 G^ on the network's pattern (rows sorted: the strictly
+    // lower entries by column, then the diagonal), adopted as a CSR
+    // operator without a round trip through the validating constructors
     if ((rc = dev_alloc(&gv, std::max<int64_t>(g->ng, 1) * w))) break;
-    if ((rc = dev_alloc((void**)&p64, (n + 1) * 8))) break;
     const int gr = vec_grid(ctx, n);
     if (a->dtype == SX_F64) k_scale_g<double><<<gr, kBlock, 0, ctx->stream>>>(g->gp, net->acts.g, g->dis, n, (double*)gv);
     else k_scale_g<float><<<gr, kBlock, 0, ctx->stream>>>(g->gp, net->acts.g, g->dis, n, (float*)gv);
-    k_i32_to_i64<<<vec_grid(ctx, n + 1), kBlock, 0, ctx->stream>>>(g->gp, n + 1, p64);
-    ctx->launches += 2;
-    if ((rc = sx_csr_from_raw_i32(ctx, (sx_dtype)a->dtype, p64, g->gi, gv, (uint64_t)n, (uint64_t)n,
-                                  (uint64_t)g->ng, SX_MEM_DEVICE, &G)))
+    ctx->launches++;
+    DevCsr c;
+    c.nrows = c.ncols = n;
+    c.nnz = g->ng;
+    c.vals = gv;
+    gv = nullptr;
+    if ((rc = dev_alloc((void**)&c.indptr, (n + 1) * 4)) == SX_OK &&
+        (rc = dev_alloc((void**)&c.indices, std::max<int64_t>(g->ng, 1) * 4)) == SX_OK) {
+      cudaMemcpyAsync(c.indptr, g->gp, (n + 1) * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+      if (g->ng > 0) cudaMemcpyAsync(c.indices, g->gi, g->ng * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+      rc = csr_finalize_stats(ctx, c, (int)w);
+    }
+    if (rc != SX_OK) {
+      sx_op tmp = csr_op_adopt(ctx, a->dtype, c);  // frees the arrays
+      destroy_op_internal(tmp);
       break;
-    rc = fsai_adopt(ctx, G, out);
-    G = nullptr;
+    }
+    rc = fsai_adopt(ctx, csr_op_adopt(ctx, a->dtype, c), out);
     // the factor's values in FP16 for the solvers (the network's output is
     // already limited by its BF16 weights); FP32 stays for exact applies
     if (rc == SX_OK && a->dtype == SX_F32) {
@@ -1085,8 +1092,6 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out) {
     }
   } while (0);
   dev_free(gv);
-  dev_free(p64);
-  if (G) destroy_op_internal(G);
   drop_fresh();
   return rc == SX_OK ? clear_error() : rc;
 }

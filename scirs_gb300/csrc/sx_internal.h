@@ -212,8 +212,9 @@ int ic0_health(sx_ctx ctx, sx_op op);
 
 // Cached transpose of a CSR operator (rmatvec, FSAI's G^T).
 int ensure_transpose(sx_ctx ctx, sx_op a);
-int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out);
+int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out, bool stats = true);
 int fsai_adopt(sx_ctx ctx, sx_op g, sx_op* out);  // takes g
+sx_op csr_op_adopt(sx_ctx ctx, int dtype, DevCsr& c);  // takes c
 int sym_half_spmv(sx_ctx ctx, sx_op a, const void* x, void* y);  // sx_sym.cu
 // rows in dependency-level order (forward: on the rows j < i of the pattern;
 // backward: on j > i), on the device (sx_ic0.cu)
