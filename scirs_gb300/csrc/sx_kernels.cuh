@@ -444,6 +444,14 @@ __global__ void __launch_bounds__(kBlock) vec_kernel(int64_t n, T* partials,
 
 namespace sx {
 
+// FP32 epilogues may provide out_acc4(row0, w[4], out[4], acc): out() and
+// acc() of four consecutive rows in row order, same arithmetic, with their
+// vector loads issued together; y must then be 16-byte aligned.
+template <class E, class = void>
+struct EpiRows4 : std::false_type {};
+template <class E>
+struct EpiRows4<E, std::void_t<decltype(&E::out_acc4)>> : std::true_type {};
+
 // Diagonal-layout SpMV.  The entries of row r sit at vals[d * ld + r] on the
 // diagonals d whose bit is set in mask[r]; no column indices are read.  A
 // thread owns VEC consecutive rows (4 in FP32, 2 in FP64): for every
@@ -572,6 +580,17 @@ __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ 
             }
           }
         }
+      }
+    }
+    if constexpr (EpiRows4<Epi>::value && VEC == 4) {
+      if (r0 + 4 <= n) {
+        // the epilogue's four rows with vector loads issued together (the
+        // row-by-row form waits on each row's loads after the previous
+        // row's stores, which may alias them)
+        T o[4];
+        epi.out_acc4(r0, acc, o, a);
+        *reinterpret_cast<float4*>(y + r0) = make_float4(o[0], o[1], o[2], o[3]);
+        continue;
       }
     }
 #pragma unroll

@@ -401,6 +401,19 @@ struct EpiMx1 {
     return add_rn(w, mul_rn(b, q[i]));  // stored to q[i]
   }
   __device__ void acc(int64_t i, float qi, Acc3<float>& a) const { a.a += p[i] * qi; }
+  __device__ void out_acc4(int64_t i, const float (&w)[4], float (&o)[4], Acc3<float>& a) const {
+    const float b = st->beta;
+    const Vec4<float> z4 = ldv4(z + i), p4 = ldv4(p + i), q4 = ldv4(q + i);
+    Vec4<float> pn;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      pn.v[j] = add_rn(z4.v[j], mul_rn(b, p4.v[j]));
+      o[j] = add_rn(w[j], mul_rn(b, q4.v[j]));
+    }
+    stv4(p + i, pn);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) a.a += pn.v[j] * o[j];
+  }
   __device__ void finish(const Acc3<float>& t) const {
     st->pap = t.a;
     if (t.a <= 0.0f) {
@@ -503,6 +516,21 @@ struct EpiMx2 {
     rn[i] = ri;
     a.a += ri * ri;
   }
+  __device__ void out_acc4(int64_t i, const float (&t)[4], float (&o)[4], Acc3<float>& a) const {
+    const float al = ms->cg.alpha;
+    const Vec4<float> x4 = ldv4(x + i), p4 = ldv4(p + i), r4 = ldv4(r + i), q4 = ldv4(q + i);
+    Vec4<float> xn, rv;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      o[j] = t[j];
+      xn.v[j] = add_rn(x4.v[j], mul_rn(al, p4.v[j]));
+      rv.v[j] = sub_rn(r4.v[j], mul_rn(al, q4.v[j]));
+    }
+    stv4(x + i, xn);
+    stv4(rn + i, rv);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) a.a += rv.v[j] * rv.v[j];
+  }
   __device__ void finish(const Acc3<float>& t) const {
     ms->rsel ^= 1;
     mx_converged(&ms->cg, sqrtf(t.a));
@@ -522,6 +550,14 @@ struct EpiMx3 {
   }
   __device__ float out(int64_t, float z) const { return z; }
   __device__ void acc(int64_t i, float z, Acc3<float>& a) const { a.a += rn[i] * z; }
+  __device__ void out_acc4(int64_t i, const float (&z)[4], float (&o)[4], Acc3<float>& a) const {
+    const Vec4<float> r4 = ldv4(rn + i);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      o[j] = z[j];
+      a.a += r4.v[j] * z[j];
+    }
+  }
   __device__ void finish(const Acc3<float>& t) const {
     st->beta = t.a / st->rz_old;
     st->rz_old = t.a;
