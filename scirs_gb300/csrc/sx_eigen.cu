@@ -94,7 +94,7 @@ struct EgAxpyNorm {
   __device__ void finish(const Acc3<T>& t) const { *out = t.a; }
 };
 
-// dst = src / s (host scalar), or dst = src when s is 1 and copy is set
+// dst = src / s (host scalar)
 template <typename T>
 struct EgScale {
   const T* src;
@@ -112,17 +112,6 @@ struct EgCopy {
   static constexpr bool kReduce = false;
   __device__ bool skip() const { return false; }
   __device__ void elem(int64_t i, Acc3<T>&) const { dst[i] = src[i]; }
-  __device__ void finish(const Acc3<T>&) const {}
-};
-// w -= a v (host scalar)
-template <typename T>
-struct EgAxpy {
-  T* w;
-  const T* v;
-  T s;
-  static constexpr bool kReduce = false;
-  __device__ bool skip() const { return false; }
-  __device__ void elem(int64_t i, Acc3<T>&) const { w[i] = sub_rn(w[i], mul_rn(s, v[i])); }
   __device__ void finish(const Acc3<T>&) const {}
 };
 // out = sum (ax - lambda x)^2
