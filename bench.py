@@ -472,7 +472,8 @@ def run_ours(args):
                      "achieved": b_a32 / t_a32 / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": b_a32 / t_a32 / 1e9 / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": b_a32, "format": fmt_a32,
-                     "csr_equivalent_bytes": spmv_bytes(n, nnz, 4), "traffic": traffic},
+                     "csr_equivalent_bytes": spmv_bytes(n, nnz, 4),
+                     "csr_equivalent_frac": spmv_bytes(n, nnz, 4) / t_a32 / 1e9 / peak, "traffic": traffic},
         "spmv_sweep": sweep,
         "workloads": workloads,
         "gpu_launches": int(launches),
@@ -638,7 +639,7 @@ def run_profile(args):
     ctx.close()
 
 
-# ------------------------------------------- learned SAI vs Jacobi (configs[4])
+# ---------------- learned SAI vs Jacobi (2D anisotropic Q1, held-out seeds)
 WEIGHTS = os.path.join(REPO, "scirs_gb300", "weights", "aniso_q1.npz")
 
 
@@ -723,7 +724,7 @@ def run_learned(args):
         t0 = time.perf_counter()
         net, train_log = LR.train(ctx, args.train_gnn, seed=args.train_seed, log_every=100)
         t_train = time.perf_counter() - t0
-        out = os.path.join(REPO, "gpurun_out", "aniso_q1.npz")
+        out = os.path.abspath(args.weights_out)
         os.makedirs(os.path.dirname(out), exist_ok=True)
         LR.save_weights(out, net, {"steps": args.train_gnn, "seed": args.train_seed, "train_s": t_train})
         log(json.dumps({"trained_steps": args.train_gnn, "train_s": t_train, "log": train_log[-5:]}))
@@ -760,6 +761,8 @@ def main():
                     help="run a few launches of one SpMV for an ncu capture and exit")
     ap.add_argument("--workload", default="laplace3d", choices=["laplace3d", "learned"])
     ap.add_argument("--train-gnn", type=int, default=0, help="train the network for N steps first")
+    ap.add_argument("--weights-out", default=os.path.join(REPO, "trained", "aniso_q1.npz"),
+                    help="where --train-gnn writes the trained weights")
     ap.add_argument("--train-seed", type=int, default=0)
     ap.add_argument("--eval-side", type=int, default=1024)
     ap.add_argument("--eval-seeds", default="1000001,1000002,1000003,1000004")
