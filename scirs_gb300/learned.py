@@ -71,3 +71,45 @@ def load_weights(ctx: S.Context, path: str) -> S.LearnedSAI:
     if int(d["version"]) != WEIGHTS_VERSION:
         raise ValueError(f"weights version {int(d['version'])} != {WEIGHTS_VERSION}")
     return S.LearnedSAI(ctx, params=d["params"])
+
+
+@dataclass
+class SolveResult:
+    """Outcome of `solve`: method is "learned-mixed" when the learned mixed
+    loop reached tol, "learned-mixed+jacobi-pcg" when the fallback ran."""
+    x: np.ndarray
+    converged: bool
+    method: str
+    outer_iterations: int
+    inner_iterations: int
+    fallback_iterations: int
+    rel_residual: float
+
+
+def solve(net: S.LearnedSAI, a64: S.Operator, b, tol: float = 1e-8, max_inner: int = 200000,
+          max_outer: int = 30, fallback_max_iter: int = 200000) -> SolveResult:
+    """A x = b to an FP64 relative residual of tol: the learned factor G of
+    the FP32 copy of A, FP32 PCG with M = G G^T inside the FP64
+    residual-replacement loop, and, when that loop stops short of tol
+    (stagnation, an FP32 p.Ap <= 0 or the outer limit), plain FP64
+    Jacobi-PCG from its last iterate (converged by its own FP64 test,
+    ||r|| <= tol ||b||; rel_residual is then the FP64 true residual)."""
+    a32 = a64.astype(np.float32)
+    g32 = None
+    try:
+        g32 = net.preconditioner(a32)
+        r = S.cg_mixed(a64, b, tol=tol, max_inner=max_inner, max_outer=max_outer, preconditioner=g32, a32=a32)
+    finally:
+        if g32 is not None:
+            g32.close()
+        a32.close()
+    if r.converged:
+        return SolveResult(r.x, True, "learned-mixed", r.outer_iterations, r.inner_iterations, 0, r.rel_residual)
+    m = S.jacobi(a64.ctx, a64)
+    try:
+        f = S.cg(a64, b, x0=r.x, max_iter=fallback_max_iter, rtol=tol, atol=0.0, preconditioner=m)
+    finally:
+        m.close()
+    rel = float(S.true_rel_residual(a64, b, f.x))
+    return SolveResult(f.x, bool(f.converged), "learned-mixed+jacobi-pcg", r.outer_iterations,
+                       r.inner_iterations, f.iterations, rel)
