@@ -478,6 +478,15 @@ void sx_lanczos_options_default(sx_lanczos_options* o);
  * the device (subspace x n values; max_subspace_size <= 4096). */
 int sx_lanczos(sx_ctx ctx, sx_op a, const sx_lanczos_options* opt, const void* v0, uint64_t v0_len, sx_mem mem,
                void* eigenvalues, void* eigenvectors, void* residuals, sx_eigen_result* result);
+/* The host tridiagonal eigensolver sx_lanczos runs between its steps
+ * (solve_tridiagonal_eigenproblem, eigen.rs:512-952: QL sweeps above three
+ * rows, closed forms below), FP64, no device work.  alpha has m entries,
+ * beta beta_len (m - 1, else DimensionMismatch).  Room: max(1, min(num, m))
+ * values and as many eigenvectors of m entries (vector k at vectors[k m]);
+ * count receives the number written.  IterativeSolverFailure when the QL
+ * sweep gives up, ValueError for m = 0, as the reference. */
+int sx_tridiag_eig(const double* alpha, const double* beta, uint64_t m, uint64_t beta_len, uint64_t num,
+                   double* values, double* vectors, uint64_t* count);
 
 /* ------------------------------------------- mixed precision (no reference
  * counterpart; nearest dense analogue scirs2-linalg mixed_precision) */

@@ -287,6 +287,7 @@ _SIGS = {
     "sx_power_iteration": (c_int, [ctx_t, op_t, P(PowerOptions), c_vp, c_u64, c_int, c_vp, c_vp, c_vp,
                                    P(EigenResult)]),
     "sx_lanczos_options_default": (None, [P(LanczosOptions)]),
+    "sx_tridiag_eig": (c_int, [c_vp, c_vp, c_u64, c_u64, c_u64, c_vp, c_vp, P(c_u64)]),
     "sx_lanczos": (c_int, [ctx_t, op_t, P(LanczosOptions), c_vp, c_u64, c_int, c_vp, c_vp, c_vp, P(EigenResult)]),
     "sx_iter_message": (c_int, [P(IterResult), c_int, C.c_char_p, c_u64]),
     "sx_ir_options_default": (None, [P(IROptions)]),

@@ -626,6 +626,20 @@ int sx_power_iteration(sx_ctx ctx, sx_op a, const sx_power_options* opt, const v
   return clear_error();
 }
 
+int sx_tridiag_eig(const double* alpha, const double* beta, uint64_t m, uint64_t beta_len, uint64_t num,
+                   double* values, double* vectors, uint64_t* count) {
+  if ((m > 0 && !alpha) || (beta_len > 0 && !beta) || !values || !vectors || !count)
+    return err_arg("null argument");
+  TriEig<double> te;
+  SX_CHECK(tri_eig<double>(std::vector<double>(alpha, alpha + m), std::vector<double>(beta, beta + beta_len),
+                           (size_t)num, te));
+  *count = te.vals.size();
+  for (size_t k = 0; k < te.vals.size(); ++k) values[k] = te.vals[k];
+  for (size_t k = 0; k < te.vecs.size(); ++k)
+    for (size_t i = 0; i < te.vecs[k].size(); ++i) vectors[k * m + i] = te.vecs[k][i];
+  return clear_error();
+}
+
 int sx_lanczos(sx_ctx ctx, sx_op a, const sx_lanczos_options* opt, const void* v0, uint64_t v0_len, sx_mem mem,
                void* eigenvalues, void* eigenvectors, void* residuals, sx_eigen_result* result) {
   if (!ctx || !eigenvalues || !residuals || !result) return err_arg("null argument");
