@@ -5,8 +5,8 @@
  * transpose, CSR SpMV, the LinearOperator slot (operators and
  * preconditioners), and the cg / bicgstab / gmres solvers.  Every entry point
  * names the reference item it replaces (paths relative to the reference
- * workspace).  A Rust shim implementing the crate's traits on top of these
- * calls is shown in INTEGRATION.md.
+ * workspace).  A Rust shim can implement the crate's traits on top of these
+ * calls.
  *
  * Conventions
  *  - Plain pointers and sizes only.  Indices cross the boundary as uint64_t
@@ -602,12 +602,15 @@ int sx_true_rel_residual(sx_ctx ctx, sx_op a64, const double* b, const double* x
  * they run (a framework that owns all GPU memory through its own pool, a
  * real-time loop that must not stall on an allocation).  No counterpart in
  * the reference.  b and x are device pointers; nothing is allocated: the
- * reduction scratch is a 1 MiB file-scope device array that every GPU which
- * loads the library holds until exit.  At most 16,777,216 rows
+ * reduction scratch is a file-scope device array of 1,572,912 bytes (about
+ * 1.5 MiB) that every GPU which loads the library holds until exit.  At most 16,777,216 rows
  * (SX_ERR_VALUE beyond).  Calls share that array, so calls that overlap on
  * the GPU race and must be serialised by the caller.  The first call on a
  * device looks the array up (cudaGetSymbolAddress); make it before any
- * stream capture.  The result is bit-identical to sx_true_rel_residual. */
+ * stream capture.  The residual entries b - A x are bit-identical to those
+ * of sx_true_rel_residual; the two norms are summed in a different order, so
+ * the returned ratio agrees with it to the rounding of that order (within
+ * 1e-14 relative in the tests), not bit for bit. */
 int sx_true_rel_residual_noalloc(sx_ctx ctx, sx_op a64, const double* b_dev, const double* x_dev,
                                  double* out);
 

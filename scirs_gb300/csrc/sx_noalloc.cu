@@ -18,7 +18,8 @@
 // Limits and sharing:
 //  - at most kNoAllocMaxRows rows (the scratch holds one partial pair per
 //    256-row block); larger matrices are rejected with SX_ERR_VALUE;
-//  - every GPU that loads this library holds the 1 MiB array until exit;
+//  - every GPU that loads this library holds the array (3 * 65,536 + 6
+//    doubles = 1,572,912 bytes, about 1.5 MiB) until exit;
 //  - the array is shared by every call: calls that overlap on the GPU (two
 //    streams, two host threads) race on it and must be serialised by the
 //    caller.  Each call clears the ticket counter it relies on.

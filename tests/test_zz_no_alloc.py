@@ -36,7 +36,8 @@ def test_noalloc_residual_matches_allocating_entry_point():
             out = C.c_double()
             S.sparse._check(L.lib.sx_true_rel_residual_noalloc(
                 ctx.handle, a.handle, C.c_void_p(bd.data_ptr()), C.c_void_p(xd.data_ptr()), C.byref(out)))
-            assert abs(out.value - ref) <= 1e-12 * ref, (out.value, ref)
+            # residual entries are bit-identical; the norms' summation order differs
+            assert abs(out.value - ref) <= 1e-14 * ref, (out.value, ref)
         # a second matrix of another size right after: the counter was cleared
         ip2, ix2, v2 = S.generate("poisson2d", 300, 200)
         n2 = len(ip2) - 1
@@ -49,7 +50,7 @@ def test_noalloc_residual_matches_allocating_entry_point():
         out = C.c_double()
         S.sparse._check(L.lib.sx_true_rel_residual_noalloc(
             ctx.handle, a2.handle, C.c_void_p(bd2.data_ptr()), C.c_void_p(xd2.data_ptr()), C.byref(out)))
-        assert abs(out.value - ref2) <= 1e-12 * ref2
+        assert abs(out.value - ref2) <= 1e-14 * ref2
         a.close()
         a2.close()
     finally:
