@@ -17,15 +17,18 @@ method) on the same problem and device, `speedup_vs_jacobi_fp64` is their
 ratio; IC(0)-PCG (the reference's quirky factorisation and the textbook
 one) is reported beside them.
 
-`roofline` times the dominant kernel of the step, the FP32 CSR SpMV of A,
+`roofline` times the dominant kernel of the step, the FP32 SpMV of A,
 alone with CUDA events on the library stream; `spmv_sweep` adds the 3D
 7-point 128^3 Laplacian and the 4M-row power-law matrix in FP32 and FP64.
 `workloads` reports the other configurations once each: 2D Poisson 256^2
 FP64 Jacobi-PCG, the 128^3 Laplacian and the 160^3 variable-coefficient
-problem with mixed precision, and 4096 batched 2D systems.
-`cpu_baseline` times the CPU oracle (a restatement of the reference's cg
-with Jacobi, single-threaded like the reference) on a bounded sample of the
-headline solve.
+problem with mixed precision and in FP64, and 4096 batched 2D systems.
+`cpu_baseline` is one complete solve of the headline problem by the CPU
+oracle (a restatement of the reference's cg with Jacobi; row-parallel SpMV
+and elementwise loops on the host cores, bit-identical to one thread,
+reductions serial like the reference's); `cpu_rows` times the other
+configurations the same way.  `--impl reference` times complete oracle
+solves of the headline problem, built by the oracle's own generators.
 
   python bench.py [--steps K] [--warmup W] [--impl reference]
 """
@@ -49,9 +52,6 @@ METRIC = "Time to 1e-8 FP64 residual: learned vs Jacobi PCG on GB300; SpMV HBM G
 TOL = 1e-8
 SIDE = 1024            # headline grid side
 PROBLEM_SEED = 1000001  # held-out seed of the training distribution
-# FP64 Jacobi-PCG iterations to 1e-8 on the headline problem, counted by a
-# full run of the CPU oracle (the reference arm scales its bounded sample by it)
-JACOBI_ITERS = 5396
 GRID = 128             # 3D Laplacian of the SpMV sweep
 SEED = 0
 
@@ -79,6 +79,7 @@ def kernel_bytes(S, op, ip, ix, w, exact=True):
 
 
 def headline_problem():
+    """The headline problem from the library's own generators (device arm)."""
     import scirs_gb300 as S
     from scirs_gb300 import learned as LR
 
@@ -86,13 +87,50 @@ def headline_problem():
     ip, ix, v = S.generate("aniso_q1", SIDE, SIDE, param0=prob.eps, param1=prob.theta)
     n = len(ip) - 1
     b = S.rhs_normal(PROBLEM_SEED, n)
-    return prob, ip, ix, v, n, b
+    return prob.eps, prob.theta, ip, ix, v, n, b
 
 
-def workload_desc(prob, n, nnz):
-    return (f"2D anisotropic Q1 diffusion {SIDE}x{SIDE} (n={n:,}, nnz={nnz:,}), eps={prob.eps:.2f}, "
-            f"theta={prob.theta:.4f} (held-out seed {PROBLEM_SEED}), b~N(0,1) from the seed, x0=0, "
+def oracle_headline_problem():
+    """The same problem from the oracle's restatement of the generators
+    (bit-identical arrays), so that the reference arm never loads the device
+    library."""
+    from oracle import oracle_ffi as O
+
+    _, eps, theta = O.sample_problem(PROBLEM_SEED)
+    ip, ix, v = O.generate("aniso_q1", SIDE, SIDE, param0=eps, param1=theta)
+    n = len(ip) - 1
+    b = O.rhs_normal(PROBLEM_SEED, n)
+    return eps, theta, ip, ix, v, n, b
+
+
+def workload_desc(eps, theta, n, nnz):
+    return (f"2D anisotropic Q1 diffusion {SIDE}x{SIDE} (n={n:,}, nnz={nnz:,}), eps={eps:.2f}, "
+            f"theta={theta:.4f} (held-out seed {PROBLEM_SEED}), b~N(0,1) from the seed, x0=0, "
             f"stop at FP64 true relative residual {TOL:g}")
+
+
+def host_info():
+    """CPU model, logical CPUs and the CPUs this process may use."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if model is None:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    usable = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return {"cpu_model": model, "nproc": os.cpu_count(), "usable_cpus": usable,
+            "machine": os.uname().machine}
 
 
 def load_peaks():
@@ -163,10 +201,18 @@ def build_problem():
 
 
 # ------------------------------------------------------------ reference arm
-def cpu_reference_solve(ip, ix, v, n, b, max_iter):
-    """The oracle's restatement of the reference cg + Jacobi (FP64), timed."""
+def oracle_threads() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def cpu_reference_solve(ip, ix, v, n, b, max_iter, threads):
+    """The oracle's restatement of the reference cg + Jacobi (FP64), timed.
+    Row-parallel SpMV and elementwise loops on `threads` host threads
+    (bit-identical to one thread); every reduction is the reference's serial
+    left fold."""
     from oracle import oracle_ffi as O
 
+    O.set_threads(threads)
     a = O.op_csr_i32(ip, ix, v, (n, n))
     m = O.op_jacobi(a)
     t0 = time.perf_counter()
@@ -176,32 +222,42 @@ def cpu_reference_solve(ip, ix, v, n, b, max_iter):
 
 
 def run_reference(args):
-    """The reference's method (cg + Jacobi, FP64, one thread) on the headline
-    problem: each step times a bounded sample of the iterations and scales it
-    to the full count."""
+    """The reference's method -- cg with a Jacobi preconditioner in FP64
+    (iterative.rs:40-162, preconditioners.rs:14-92) -- as the oracle restates
+    it, on the host cores, on the headline problem.  Every timed step is one
+    complete solve from x0 = 0 to the FP64 target; the warm-up steps are
+    short solves.  Inputs come from the oracle's generators: the device
+    library is never loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    prob, ip, ix, v, n, b = headline_problem()
+    from oracle import oracle_ffi as O
+
+    eps, theta, ip, ix, v, n, b = oracle_headline_problem()
     nnz = len(v)
-    sample_iters = min(args.cpu_sample_iters, JACOBI_ITERS)
+    threads = oracle_threads()
     for _ in range(args.warmup):
-        cpu_reference_solve(ip, ix, v, n, b, max(10, sample_iters // 10))
-    times = []
+        cpu_reference_solve(ip, ix, v, n, b, 20, threads)
+    times, iters, r = [], [], None
     for _ in range(args.steps):
-        _, dt = cpu_reference_solve(ip, ix, v, n, b, sample_iters)
-        times.append(dt * JACOBI_ITERS / sample_iters)
+        r, dt = cpu_reference_solve(ip, ix, v, n, b, 200000, threads)
+        times.append(dt)
+        iters.append(int(r["iterations"]))
     value = statistics.mean(times)
-    sample = (f"oracle cg+Jacobi FP64 (restatement of iterative.rs:40-162), first {sample_iters} of "
-              f"{JACOBI_ITERS} iterations per step, scaled to {JACOBI_ITERS}; single thread like the reference")
+    true_res = O.true_rel_residual(ip, ix, v, b, r["x"]) if r is not None else None
+    sample = (f"complete solves: oracle cg+Jacobi FP64 (restatement of iterative.rs:40-162) from x0=0 to "
+              f"the FP64 target, {iters[-1] if iters else 0} iterations each; SpMV and elementwise loops on "
+              f"{threads} host threads (bit-identical to one thread), dot products and norms serial left "
+              f"folds as in the reference")
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": workload_desc(prob, n, nnz), "method": "Jacobi-PCG FP64 (reference cg)",
-                   "iterations": JACOBI_ITERS},
-        "cpu_baseline": {"value": value, "unit": "s", "cores": 1, "kind": "port", "sample": sample},
+        "config": {"workload": workload_desc(eps, theta, n, nnz), "method": "Jacobi-PCG FP64 (reference cg)",
+                   "iterations": iters[-1] if iters else None, "converged": bool(r["converged"]) if r else None,
+                   "fp64_true_rel_residual": true_res, "step_s": times, "host": host_info()},
+        "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -227,7 +283,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    prob, ip, ix, v, n, b = headline_problem()
+    eps, theta, ip, ix, v, n, b = headline_problem()
     nnz = len(v)
     ctx = S.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
@@ -432,14 +488,17 @@ def run_ours(args):
             if line.startswith("traffic_bytes_per_launch:"):
                 traffic = float(line.split(":")[1])
 
-    # CPU baseline: the oracle on a bounded sample, scaled to the full Jacobi-PCG count
-    cpu = None
+    # CPU baseline: one complete oracle solve of the headline problem (the
+    # reference arm's step), then the other configurations' CPU rows
+    cpu, cpu_rows = None, None
     if rank == 0 and not args.no_cpu_baseline:
-        sample_iters = min(JACOBI_ITERS, args.cpu_sample_iters)
-        _, dt = cpu_reference_solve(ip, ix, v, n, b, sample_iters)
-        cpu = {"value": dt * JACOBI_ITERS / sample_iters, "unit": "s", "cores": 1, "kind": "port",
-               "sample": f"oracle cg+Jacobi FP64 on the headline problem, first {sample_iters} of "
-                         f"{JACOBI_ITERS} iterations, scaled"}
+        threads = oracle_threads()
+        rc_, dt = cpu_reference_solve(ip, ix, v, n, b, 200000, threads)
+        cpu = {"value": dt, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"one complete oracle cg+Jacobi FP64 solve of the headline problem "
+                         f"({int(rc_['iterations'])} iterations); SpMV and elementwise loops on {threads} host "
+                         f"threads (bit-identical to one thread), reductions serial as in the reference"}
+        cpu_rows = run_cpu_rows(threads, workloads or {})
 
     value = statistics.mean(t_dev)
     if dist:
@@ -447,12 +506,20 @@ def run_ours(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         value = float(tt.item())
     jac = statistics.mean(t_jac)
+    # FP64 Jacobi-PCG per iteration on the diagonal layout: A (9 FP64 values
+    # + the 2-byte mask per row), p read and Ap written by the SpMV; the
+    # update reads x, p, r, Ap, 1/diag and writes x, r; the p step reads r,
+    # 1/diag, p and writes p
+    jac_iter_s = jac / max(int(r_jac.iterations), 1)
+    jac_bytes = dia_bytes(n, 9, 8) + 7 * n * 8 + 4 * n * 8
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 residual and solution",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 Krylov vectors and A copy / f16 values of the learned factor G (widened to f32) / "
+                 "f64 residual, outer inner products and solution",
         "data": "synthetic",
-        "config": {"workload": workload_desc(prob, n, nnz),
+        "config": {"workload": workload_desc(eps, theta, n, nnz),
                    "method": "learned factorised SAI (GNN weights scirs_gb300/weights/aniso_q1.npz) + FP32 PCG "
                              "with FP64 residual replacement; step includes the FP32 copy and the network setup",
                    "outer_iterations": int(res.outer_iterations), "inner_iterations": int(res.inner_iterations),
@@ -460,25 +527,29 @@ def run_ours(args):
                    "setup_s": t_setup, "solve_s": t_lm_solve,
                    "l2": "working set > L2 (129 MB) and a 512 MB L2 flush between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "jacobi_pcg_fp64": {"value": jac, "unit": "s", "iterations": int(r_jac.iterations),
-                            "fp64_true_rel_residual": true_res_jac},
         "speedup_vs_jacobi_fp64": jac / value,
+        "learned_vs_jacobi_mixed": t_jm / value,
+        "jacobi_pcg_fp64": {"value": jac, "unit": "s", "iterations": int(r_jac.iterations),
+                            "us_per_iteration": jac_iter_s * 1e6, "bytes_per_iteration": jac_bytes,
+                            "GB/s": jac_bytes / jac_iter_s / 1e9, "frac": jac_bytes / jac_iter_s / 1e9 / peak,
+                            "fp64_true_rel_residual": true_res_jac},
         "jacobi_pcg_mixed": {"value": t_jm, "unit": "s", "outer_iterations": r_jm.outer_iterations,
                              "inner_iterations": r_jm.inner_iterations, "fp64_true_rel_residual": r_jm.rel_residual},
-        "ic0_pcg_fp64": ic0,
         "e2e": {"value": statistics.mean(t_e2e), "unit": "s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8},
         "roofline": {"bound": "hbm", "kernel": f"FP32 SpMV of A (aniso Q1 {SIDE}^2), {kname}",
                      "achieved": b_a32 / t_a32 / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": b_a32 / t_a32 / 1e9 / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": b_a32, "format": fmt_a32,
-                     "csr_equivalent_bytes": spmv_bytes(n, nnz, 4),
-                     "csr_equivalent_frac": spmv_bytes(n, nnz, 4) / t_a32 / 1e9 / peak, "traffic": traffic},
-        "spmv_sweep": sweep,
-        "workloads": workloads,
+                     "csr_equivalent_bytes": spmv_bytes(n, nnz, 4), "traffic": traffic},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "host": host_info(),
+        "ic0_pcg_fp64": ic0,
+        "spmv_sweep": sweep,
+        "workloads": workloads,
+        "cpu_rows": cpu_rows,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -487,6 +558,115 @@ def run_ours(args):
     ctx.close()
     if dist:
         dist.destroy_process_group()
+
+
+def run_cpu_rows(threads, dev):
+    """The other configurations on the host cores through the oracle (the
+    reference's algorithms restated; SpMV and elementwise loops on `threads`
+    threads, bit-identical to one).  Solves that take minutes on the CPU are
+    sampled and scaled, and say so."""
+    from oracle import oracle_ffi as O
+
+    O.set_threads(threads)
+    rows = {"threads": threads}
+
+    def med(fn, reps):
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    # 2D Poisson 256^2, FP64 Jacobi-PCG, complete solve
+    ip, ix, v = O.generate("poisson2d", 256, 256)
+    n = len(ip) - 1
+    b = O.rhs_normal(0, n)
+    a = O.op_csr_i32(ip, ix, v, (n, n))
+    t0 = time.perf_counter()
+    r = O.cg(a, b, max_iter=5000, rtol=TOL, atol=0.0, preconditioner=O.op_jacobi(a))
+    t = time.perf_counter() - t0
+    row = {"s": t, "iterations": int(r["iterations"]), "converged": bool(r["converged"])}
+    g = dev.get("poisson2d_256_jacobi_fp64")
+    if g:
+        row["gpu_s"] = g["s"]
+        row["gpu_iterations"] = g["iterations"]
+    rows["poisson2d_256_jacobi_fp64"] = row
+    # SpMV: 3D 7-point 128^3 and the 4M-row power-law matrix, FP64 and FP32
+    for name, gen in ((f"laplace3d_{GRID}", lambda: O.generate("laplace3d", GRID, GRID, GRID)),
+                      ("powerlaw_4M", lambda: O.generate("powerlaw", 4194304, seed=1, param0=16.0, param1=4096.0))):
+        ip, ix, v = gen()
+        n = len(ip) - 1
+        x = O.rhs_normal(3, n)
+        for dt in (np.float64, np.float32):
+            vv, xx = v.astype(dt), x.astype(dt)
+            w = 8 if dt == np.float64 else 4
+            tm = med(lambda: O.spmv_i32(ip, ix, vv, xx), 3)
+            rows[f"spmv_{name}_{'fp64' if w == 8 else 'fp32'}"] = {
+                "ms": tm * 1e3, "GB/s": spmv_bytes(n, len(ix), w) / tm / 1e9}
+        del ip, ix, v
+    # 3D variable-coefficient 160^3, FP64 cg + Jacobi to 1e-10: the first
+    # iterations, scaled to the device's FP64 count
+    ip, ix, v = O.generate("varcoef3d", 160, 160, 160, seed=SEED, param0=1.5)
+    n = len(ip) - 1
+    b = O.rhs_normal(SEED, n)
+    a = O.op_csr_i32(ip, ix, v, (n, n))
+    m = O.op_jacobi(a)
+    k = 100
+    t0 = time.perf_counter()
+    O.cg(a, b, max_iter=k, rtol=1e-10, atol=0.0, preconditioner=m)
+    t = time.perf_counter() - t0
+    g = dev.get("varcoef3d_160_fp64_1e-10")
+    full = g["iterations"] if g else None
+    rows["varcoef3d_160_cg_fp64_1e-10"] = {
+        "s_per_iteration": t / k, "s": t / k * full if full else None, "iterations": full,
+        "sample": f"first {k} iterations timed, scaled to the device FP64 Jacobi-PCG iteration count"}
+    del a, m, ip, ix, v
+    # batched: the reference runs one cg per system; complete solves of the
+    # first systems, scaled to the 4096 by the sum of side^3 (rows x iterations)
+    sides = O.batch_sides(4096, 32, 256, SEED)
+    ns, t = 8, 0.0
+    its = []
+    offs = np.concatenate([[0], np.cumsum(sides[:ns] ** 2)])
+    b_all = O.rhs_normal(SEED, int(offs[-1]))  # the batch's b restricted to these systems
+    for sidx in range(ns):
+        ip, ix, v = O.batch_system(sidx, int(sides[sidx]), SEED, 1.0)
+        n = len(ip) - 1
+        b = b_all[offs[sidx]:offs[sidx + 1]]
+        a = O.op_csr_i32(ip, ix, v, (n, n))
+        t0 = time.perf_counter()
+        r = O.cg(a, b, max_iter=20000, rtol=TOL, atol=0.0, preconditioner=O.op_jacobi(a))
+        t += time.perf_counter() - t0
+        its.append(int(r["iterations"]))
+    cube = sides.astype(np.float64) ** 3
+    rows["batched_4096_cg_fp64"] = {"s_sample": t, "systems_sampled": ns, "iterations": its,
+                                    "s": t * cube.sum() / cube[:ns].sum(),
+                                    "sample": f"complete FP64 Jacobi-PCG solves of the first {ns} systems, "
+                                              f"scaled to 4096 by the sum of side^3"}
+    # the reference IC(0) apply (ic.rs:163-214: the backward solve scans every
+    # row for each unknown, O(n^2)) on 2D Q1 problems, extrapolated to 1024^2
+    pts = []
+    for side in (48, 64, 96):
+        ip, ix, v = O.generate("aniso_q1", side, side, param0=845.08, param1=0.9632)
+        n = len(ip) - 1
+        a = O.op_csr_i32(ip, ix, v, (n, n))
+        try:
+            mi = O.op_ic0(a, fast=False)
+        except Exception as e:  # the quirky factorisation may break down
+            rows["ic0_reference_apply"] = {"error": str(e)}
+            pts = []
+            break
+        x = O.rhs_normal(5, n)
+        pts.append((n, med(lambda: mi.matvec(x), 2)))
+    if pts:
+        ex = float(np.polyfit(np.log([q[0] for q in pts]), np.log([q[1] for q in pts]), 1)[0])
+        n_big = SIDE * SIDE
+        t_big = pts[-1][1] * (n_big / pts[-1][0]) ** ex
+        rows["ic0_reference_apply"] = {"points": [{"n": q[0], "s": q[1]} for q in pts], "exponent": ex,
+                                       "s_per_apply_at_1024^2": t_big,
+                                       "sample": "apply times on 48^2, 64^2, 96^2 Q1 grids, power-law fit, "
+                                                 "extrapolated to n = 1,048,576"}
+    return rows
 
 
 def run_workloads(ctx, S, once, args):
@@ -533,6 +713,13 @@ def run_workloads(ctx, S, once, args):
     out["varcoef3d_160_mixed_1e-10"] = {"s": t, "inner_iterations": r.inner_iterations,
                                         "outer_iterations": r.outer_iterations, "converged": r.converged,
                                         "fp64_true_rel_residual": r.rel_residual}
+    # the same problem in plain FP64 Jacobi-PCG (the reference's method)
+    m64 = S.jacobi(ctx, a)
+    S.cg(a, b, max_iter=100000, rtol=1e-10, atol=0.0, preconditioner=m64)
+    r, t = once(lambda: S.cg(a, b, max_iter=100000, rtol=1e-10, atol=0.0, preconditioner=m64))
+    out["varcoef3d_160_fp64_1e-10"] = {"s": t, "iterations": r.iterations, "converged": r.converged,
+                                       "fp64_true_rel_residual": S.true_rel_residual(a, b, r.x)}
+    m64.close()
     m32.close()
     a32.close()
     a.close()
@@ -579,7 +766,7 @@ def run_profile(args):
     if args.profile == "learned":
         from scirs_gb300 import learned as LR
 
-        prob, ip, ix, v, n, b = headline_problem()
+        _, _, ip, ix, v, n, b = headline_problem()
         a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
         net = LR.load_weights(ctx, WEIGHTS)
         for _ in range(args.steps):
@@ -595,7 +782,7 @@ def run_profile(args):
         ctx.close()
         return
     if args.profile in ("jacobi64", "jacobi32mixed"):
-        prob, ip, ix, v, n, b = headline_problem()
+        _, _, ip, ix, v, n, b = headline_problem()
         a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
         a32 = a64.astype(np.float32)
         m = S.jacobi(ctx, a64 if args.profile == "jacobi64" else a32)
@@ -614,7 +801,7 @@ def run_profile(args):
     if args.profile in ("spmv32", "spmv64") or args.profile.startswith("sym"):
         ip, ix, v = S.generate("laplace3d", GRID, GRID, GRID)
     elif args.profile == "aniso32":
-        _, ip, ix, v, _, _ = headline_problem()
+        _, _, ip, ix, v, _, _ = headline_problem()
     else:
         ip, ix, v = S.generate("powerlaw", 4194304, seed=1, param0=16.0, param1=4096.0)
     n = len(ip) - 1
@@ -752,7 +939,6 @@ def main():
     ap.add_argument("--no-workloads", dest="workloads", action="store_false")
     ap.add_argument("--no-batched", dest="batched", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-iters", type=int, default=300)
     ap.add_argument("--ic0", action="store_true", help="also time IC(0)-PCG with the reference's factorisation")
     ap.add_argument("--ic0-max-iter", type=int, default=3000)
     ap.add_argument("--profile", default=None,

@@ -122,6 +122,13 @@ def lib():
                                     C.POINTER(EigInfo), E]),
             "or_tridiag_eig_f64": (ip, [vp, vp, u64, u64, u64, vp, vp, vp, E]),
             "or_solve_cubic_f64": (u64, [dbl, dbl, dbl, vp]),
+            "or_set_threads": (None, [ip]),
+            "or_get_threads": (ip, []),
+            "or_gen_matrix": (ip, [ip, i64, i64, i64, u64, dbl, dbl, C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_int64), vp, vp, vp]),
+            "or_gen_batch_sides": (None, [u64, i64, i64, u64, vp]),
+            "or_gen_batch_system_seed": (u64, [u64, u64]),
+            "or_gen_rhs_normal": (None, [u64, i64, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -541,3 +548,64 @@ def solve_cubic(p_, q, r):
     roots = np.zeros(3)
     k = lib().or_solve_cubic_f64(p_, q, r, p(roots))
     return roots[:k].copy()
+
+
+# ------------------------------------------------------------- host threads
+def set_threads(n: int) -> None:
+    """Host threads of the row-parallel SpMV and elementwise loops (results
+    are bit-identical for any count; reductions stay serial)."""
+    lib().or_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(lib().or_get_threads())
+
+
+# ----------------------------------------------------- workload generators
+GEN_KINDS = {"poisson2d": 0, "laplace3d": 1, "varcoef3d": 2, "varcoef2d": 3, "aniso_q1": 4, "powerlaw": 5}
+
+
+def generate(kind: str, nx: int, ny: int = 1, nz: int = 1, seed: int = 0, param0: float = 0.0,
+             param1: float = 0.0):
+    """The library's seeded generators, restated on the CPU: (indptr int64,
+    indices int32, values float64), bit-identical to scirs_gb300.generate."""
+    n, nnz = C.c_int64(), C.c_int64()
+    k = GEN_KINDS[kind]
+    rc = lib().or_gen_matrix(k, nx, ny, nz, seed, param0, param1, C.byref(n), C.byref(nnz), None, None, None)
+    if rc:
+        raise ValueError(f"generator {kind} rejected its arguments ({rc})")
+    indptr = np.empty(n.value + 1, dtype=np.int64)
+    indices = np.empty(nnz.value, dtype=np.int32)
+    vals = np.empty(nnz.value, dtype=np.float64)
+    rc = lib().or_gen_matrix(k, nx, ny, nz, seed, param0, param1, C.byref(n), C.byref(nnz), p(indptr),
+                             p(indices), p(vals))
+    if rc:
+        raise ValueError(f"generator {kind} failed ({rc})")
+    return indptr, indices, vals
+
+
+def rhs_normal(seed: int, n: int) -> np.ndarray:
+    b = np.empty(n, dtype=np.float64)
+    lib().or_gen_rhs_normal(seed, n, p(b))
+    return b
+
+
+def batch_sides(nsys: int, side_min: int, side_max: int, seed: int) -> np.ndarray:
+    out = np.empty(nsys, dtype=np.int64)
+    lib().or_gen_batch_sides(nsys, side_min, side_max, seed, p(out))
+    return out
+
+
+def batch_system(s: int, side: int, seed: int, sigma: float = 1.0):
+    """System s of the batched workload, numbered from 0 (its own CSR)."""
+    return generate("varcoef2d", side, side, 1, seed=int(lib().or_gen_batch_system_seed(seed, s)), param0=sigma)
+
+
+def sample_problem(seed: int, sides=(64, 512)):
+    """(side, eps, theta) of the anisotropic training distribution for a seed:
+    side uniform in `sides`, eps = 10^U(0, 3), theta ~ U[0, pi)."""
+    rng = np.random.default_rng(seed)
+    side = int(rng.integers(sides[0], sides[1] + 1))
+    eps = float(10.0 ** rng.uniform(0.0, 3.0))
+    theta = float(rng.uniform(0.0, np.pi))
+    return side, eps, theta

@@ -17,16 +17,113 @@
 #include "sx_oracle.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
+
+// ------------------------------------------------------------- worker pool
+// Row-parallel SpMV and elementwise vector loops may run on several host
+// threads (or_set_threads; one by default, like the reference).  Each row's
+// sum and each element's update keep their own arithmetic, so the results
+// are bit-identical to the single-threaded loops.  Reductions (dot, norm2)
+// always stay strict left folds on the calling thread.
+class Pool {
+ public:
+  ~Pool() { resize(1); }
+  int size() const { return nthreads_; }
+  void resize(int nt) {
+    if (nt < 1) nt = 1;
+    if (nt == nthreads_) return;
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+    workers_.clear();
+    stop_ = false;
+    nthreads_ = nt;
+    // a worker starts from the generation current now, so a job dispatched
+    // before it first takes the lock is still seen as new
+    const uint64_t g0 = gen_;
+    for (int w = 1; w < nt; ++w) workers_.emplace_back([this, w, g0]() { loop(w, g0); });
+  }
+  // fn(lo, hi) over [0, n) in nthreads contiguous pieces
+  void run(int64_t n, const std::function<void(int64_t, int64_t)>& fn) {
+    if (nthreads_ == 1 || n < 4096) {
+      fn(0, n);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> g(m_);
+      job_ = &fn;
+      n_ = n;
+      pending_ = nthreads_ - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    piece(0, fn);
+    std::unique_lock<std::mutex> g(m_);
+    done_.wait(g, [this]() { return pending_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  void piece(int w, const std::function<void(int64_t, int64_t)>& fn) {
+    const int64_t chunk = (n_ + nthreads_ - 1) / nthreads_;
+    const int64_t lo = std::min<int64_t>(n_, w * chunk), hi = std::min<int64_t>(n_, lo + chunk);
+    if (lo < hi) fn(lo, hi);
+  }
+  void loop(int w, uint64_t seen) {
+    for (;;) {
+      const std::function<void(int64_t, int64_t)>* job;
+      {
+        std::unique_lock<std::mutex> g(m_);
+        cv_.wait(g, [&]() { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+        job = job_;
+      }
+      piece(w, *job);
+      {
+        std::lock_guard<std::mutex> g(m_);
+        if (--pending_ == 0) done_.notify_one();
+      }
+    }
+  }
+  int nthreads_ = 1;
+  std::vector<std::thread> workers_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+  const std::function<void(int64_t, int64_t)>* job_ = nullptr;
+  int64_t n_ = 0;
+  int pending_ = 0;
+};
+
+Pool& pool() {
+  static Pool p;
+  return p;
+}
+
+template <class Fn>
+void par_for(int64_t n, Fn fn) {
+  pool().run(n, std::function<void(int64_t, int64_t)>(fn));
+}
 
 enum ErrCode {
   E_OK = 0,
@@ -264,11 +361,13 @@ T csr_get(const uint64_t* indptr, const uint64_t* indices, const T* data, uint64
 // end precedes its start (possible through CsrArray::new) is empty.
 template <class T, class IP, class IX>
 void spmv(const IP* indptr, const IX* indices, const T* data, uint64_t nrows, const T* x, T* y) {
-  for (uint64_t i = 0; i < nrows; ++i) {
-    T sum = T(0);
-    for (IP k = indptr[i]; k < indptr[i + 1]; ++k) sum = sum + data[k] * x[indices[k]];
-    y[i] = sum;
-  }
+  par_for((int64_t)nrows, [=](int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i) {
+      T sum = T(0);
+      for (IP k = indptr[i]; k < indptr[i + 1]; ++k) sum = sum + data[k] * x[indices[k]];
+      y[i] = sum;
+    }
+  });
 }
 
 // iterative.rs:827-834: `.sum()` of f32/f64 folds from -0.0 in current Rust
@@ -389,10 +488,16 @@ struct DiagOp : or_op {
   std::vector<double> d64;
   std::vector<float> d32;
   void mv64(const double* x, double* y) const override {
-    for (uint64_t i = 0; i < nrows; ++i) y[i] = x[i] * d64[i];
+    const double* d = d64.data();
+    par_for((int64_t)nrows, [=](int64_t lo, int64_t hi) {
+      for (int64_t i = lo; i < hi; ++i) y[i] = x[i] * d[i];
+    });
   }
   void mv32(const float* x, float* y) const override {
-    for (uint64_t i = 0; i < nrows; ++i) y[i] = x[i] * d32[i];
+    const float* d = d32.data();
+    par_for((int64_t)nrows, [=](int64_t lo, int64_t hi) {
+      for (int64_t i = lo; i < hi; ++i) y[i] = x[i] * d[i];
+    });
   }
 };
 
@@ -705,8 +810,14 @@ SolveOut<F> cg(const or_op* a, const std::vector<F>& b, uint64_t max_iter, F rto
       return o;
     }
     F alpha = rz_old / pap;
-    for (uint64_t i = 0; i < n; ++i) x[i] += alpha * p[i];
-    for (uint64_t i = 0; i < n; ++i) r[i] -= alpha * ap[i];
+    {
+      F *xp = x.data(), *rp = r.data();
+      const F *pp = p.data(), *app = ap.data();
+      par_for((int64_t)n, [=](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) xp[i] += alpha * pp[i];
+        for (int64_t i = lo; i < hi; ++i) rp[i] -= alpha * app[i];
+      });
+    }
     F rnorm = norm2(r);
     if (rnorm <= tol) {
       o.x = x; o.iterations = it + 1; o.residual_norm = rnorm; o.converged = true;
@@ -716,7 +827,13 @@ SolveOut<F> cg(const or_op* a, const std::vector<F>& b, uint64_t max_iter, F rto
     z = m ? op_apply(m, r) : r;
     F rz_new = dot(r, z);
     F beta = rz_new / rz_old;
-    for (uint64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    {
+      F* pp = p.data();
+      const F* zp = z.data();
+      par_for((int64_t)n, [=](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) pp[i] = zp[i] + beta * pp[i];
+      });
+    }
     rz_old = rz_new;
     ++it;
   }
@@ -1242,6 +1359,10 @@ int check_square_and_len(const or_op* a, const char* solver, or_err* err) {
 }  // namespace
 
 extern "C" {
+
+// Host threads for the row-parallel SpMV and elementwise loops (>= 1).
+void or_set_threads(int n) { pool().resize(n); }
+int or_get_threads(void) { return pool().size(); }
 
 int or_csr_matrix_new_f64(const double* data, const uint64_t* rows, const uint64_t* cols,
                           uint64_t nnz, uint64_t nrows, uint64_t ncols, uint64_t* indptr_out,

@@ -237,6 +237,22 @@ int or_tridiag_eig_f64(const double* alpha, const double* beta, uint64_t m, uint
 /* solve_cubic (eigen.rs:890-952): returns the number of roots written. */
 uint64_t or_solve_cubic_f64(double p, double q, double r, double* roots);
 
+/* ---- host threads ----
+ * Row-parallel SpMV and elementwise vector loops may use several host
+ * threads; every row sum and element update keeps its arithmetic, so results
+ * are bit-identical to one thread (the default).  Reductions stay serial. */
+void or_set_threads(int n);
+int or_get_threads(void);
+
+/* ---- workload generators (sx_gen_oracle.cpp) ----
+ * Restatement of the library's seeded generators (kind numbering of
+ * sx_gen_kind), bit-identical to them. */
+int or_gen_matrix(int kind, int64_t nx, int64_t ny, int64_t nz, uint64_t seed, double p0, double p1,
+                  int64_t* n_out, int64_t* nnz_out, int64_t* indptr, int32_t* indices, double* vals);
+void or_gen_batch_sides(uint64_t nsys, int64_t side_min, int64_t side_max, uint64_t seed, int64_t* sides);
+uint64_t or_gen_batch_system_seed(uint64_t seed, uint64_t s);
+void or_gen_rhs_normal(uint64_t seed, int64_t n, double* b);
+
 #ifdef __cplusplus
 }
 #endif

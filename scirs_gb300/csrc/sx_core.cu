@@ -76,6 +76,15 @@ static int err_cast(uint64_t v) {
                        " cannot be represented in the target type i32",
                    v);
 }
+// index_dtype.rs:109-170 reports the first value, in array order, that does
+// not fit the target type.  Called only when a dimension exceeds i32, on
+// host index arrays: returns the first entry above i32::MAX, or 0.
+static uint64_t first_cast_overflow(const uint64_t* a, uint64_t n) {
+  for (uint64_t k = 0; k < n; ++k)
+    if (a[k] > (uint64_t)INT32_MAX) return a[k];
+  return 0;
+}
+
 static int err_arg(const char* what) {
   return set_error(SX_ERR_INVALID_ARGUMENT, std::string("Invalid argument: ") + what);
 }
@@ -1147,8 +1156,14 @@ int sx_csr_from_triplets(sx_ctx ctx, sx_dtype dtype, sx_csr_api api, const uint6
         break;
       }
     }
-    if (nrows > kI32Max - 1) { rc = err_cast(nrows); break; }
-    if (ncols > kI32Max) { rc = err_cast(ncols); break; }
+    if (nrows > kI32Max - 1 || ncols > kI32Max) {
+      // the first row index, then the first column index, that does not fit;
+      // else the dimension itself
+      uint64_t v = first_cast_overflow(rows, nnz);
+      if (!v) v = first_cast_overflow(cols, nnz);
+      rc = err_cast(v ? v : (nrows > kI32Max - 1 ? nrows : ncols));
+      break;
+    }
     c.nrows = (int64_t)nrows;
     c.ncols = (int64_t)ncols;
     c.nnz = n;
@@ -1276,7 +1291,11 @@ int sx_csr_from_raw(sx_ctx ctx, sx_dtype dtype, sx_csr_api api, const uint64_t* 
       }
     }
     if (hm[1] > kI32Max) { rc = err_cast(hm[1]); break; }
-    if (ncols > kI32Max) { rc = err_cast(ncols); break; }
+    if (ncols > kI32Max) {
+      const uint64_t v = first_cast_overflow(indices, nnz);
+      rc = err_cast(v ? v : ncols);
+      break;
+    }
     c.nrows = (int64_t)nrows;
     c.ncols = (int64_t)ncols;
     c.nnz = n;
