@@ -231,5 +231,5 @@ def test_index_cast_overflow(S, ctx):
     assert e.value.variant == "IndexCastOverflow" and e.value.payload[0] == 3_000_000_000
     # the largest values that fit are accepted
     a = S.csr_array_from_triplets(ctx, [2], [2**31 - 2], [1.0], (3, 2**31 - 1))
-    assert a.nnz() == 1
+    assert a.nnz == 1
     a.close()
