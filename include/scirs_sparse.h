@@ -88,6 +88,22 @@ int sx_ctx_create_on_stream(int device, void* stream, sx_ctx* out);
 int sx_ctx_destroy(sx_ctx ctx);
 void* sx_ctx_stream(sx_ctx ctx);
 int sx_ctx_synchronize(sx_ctx ctx);
+
+/* Time limit of one dependency wait inside the triangular factorisations
+ * and sweeps (IC(0), ILU(0), SSOR) of this context, in nanoseconds; 0
+ * restores the default of 2 s.  A wait that runs longer gives up, every
+ * other wait of that launch ends at once, and the call reports
+ * SX_ERR_DEVICE_TIMEOUT; the context and its other handles stay usable.  A
+ * limit applies to launches made after it is set (solver graphs captured
+ * earlier keep the limit they were captured with).  No reference
+ * counterpart: the reference's triangular solves are sequential host loops. */
+int sx_ctx_set_wait_limit(sx_ctx ctx, uint64_t ns);
+
+/* One bounded device wait on a flag that nothing sets, with this context's
+ * limit: returns SX_ERR_DEVICE_TIMEOUT when the wait gives up (the expected
+ * outcome) and the wait's length in *waited_ns.  Checks the give-up path of
+ * the dependency waits without touching any operator. */
+int sx_wait_selftest(sx_ctx ctx, uint64_t* waited_ns);
 /* Number of kernels this library launched on the context (graph-launched
  * kernels included), for launch accounting. */
 uint64_t sx_ctx_kernel_launches(sx_ctx ctx);

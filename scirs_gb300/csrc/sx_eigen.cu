@@ -143,11 +143,12 @@ struct EgColumn {
 // Ritz vectors: out[i * cols + k] = sum_j coef[j * cols + k] V[j][i] for
 // j < nj, summed in j order from zero (eigen.rs:453-465)
 template <typename T>
-__global__ void k_ritz(const T* __restrict__ V, int64_t n, int nj, const T* __restrict__ coef, int cols, T* out) {
+__global__ void k_ritz(const T* __restrict__ V, int64_t n, int64_t ldv, int nj, const T* __restrict__ coef,
+                       int cols, T* out) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     for (int k = 0; k < cols; ++k) {
       T s = T(0);
-      for (int j = 0; j < nj; ++j) s = add_rn(s, mul_rn(coef[j * cols + k], V[(int64_t)j * n + i]));
+      for (int j = 0; j < nj; ++j) s = add_rn(s, mul_rn(coef[j * cols + k], V[(int64_t)j * ldv + i]));
       out[i * cols + k] = s;
     }
 }
@@ -486,7 +487,10 @@ int lanczos_impl(sx_ctx ctx, sx_op a, const sx_lanczos_options& o, const void* v
   EgWork<T> W{ctx};
   T *V = nullptr, *w = nullptr;
   SX_CHECK(dev_alloc((void**)&W.sc, (sub + 8) * sizeof(T)));
-  SX_CHECK(W.alloc(&V, (int64_t)sub * n));
+  // basis vectors one padded stride apart (a multiple of 32 elements), so
+  // that every vector starts 256-byte aligned like the other work vectors
+  const int64_t ldv = (n + 31) / 32 * 32;
+  SX_CHECK(W.alloc(&V, (int64_t)sub * ldv));
   SX_CHECK(W.alloc(&w, n));
   SX_CHECK(upload_start<T>(ctx, v0, n, mem, V));
   T h[2];
@@ -511,15 +515,15 @@ int lanczos_impl(sx_ctx ctx, sx_op a, const sx_lanczos_options& o, const void* v
   while (it < o.max_iter && alpha.size() < sub) {
     if (beta1 == T(0)) break;
     beta.push_back(beta1);
-    T* vn = V + (int64_t)nv * n;
+    T* vn = V + (int64_t)nv * ldv;
     SX_CHECK(launch_vec<T>(ctx, n, EgScale<T>{w, vn, beta1}));
     ++nv;
     SX_CHECK(apply<T>(ctx, a, vn, w));
     // Gram-Schmidt against every stored vector in order (modified: each
     // projection uses w after the previous subtraction); sc[j] = proj_j
     for (uint64_t j = 0; j < nv; ++j) {
-      const T* vp = j ? V + (int64_t)(j - 1) * n : nullptr;
-      SX_CHECK(launch_vec<T>(ctx, n, EgMgs<T>{w, vp, j ? W.sc + (j - 1) : nullptr, V + (int64_t)j * n, W.sc + j}));
+      const T* vp = j ? V + (int64_t)(j - 1) * ldv : nullptr;
+      SX_CHECK(launch_vec<T>(ctx, n, EgMgs<T>{w, vp, j ? W.sc + (j - 1) : nullptr, V + (int64_t)j * ldv, W.sc + j}));
     }
     // the last subtraction, then alpha = vn . w  (sc[nv])
     SX_CHECK(launch_vec<T>(ctx, n, EgMgs<T>{w, vn, W.sc + (nv - 1), vn, W.sc + nv}));
@@ -556,7 +560,7 @@ int lanczos_impl(sx_ctx ctx, sx_op a, const sx_lanczos_options& o, const void* v
     SX_CHECK(W.alloc(&e, n));
     SX_CUDA(cudaMemcpyAsync(dcoef, coef.data(), coef.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
     if (n > 0 && cols > 0) {
-      k_ritz<T><<<vec_grid(ctx, n), kBlock, 0, ctx->stream>>>(V, n, nj, dcoef, (int)cols, ritz);
+      k_ritz<T><<<vec_grid(ctx, n), kBlock, 0, ctx->stream>>>(V, n, ldv, nj, dcoef, (int)cols, ritz);
       ctx->launches++;
       SX_CUDA(cudaGetLastError());
     }

@@ -70,7 +70,7 @@ enum : int { E_NONE = 0, E_MISSING_DIAG = 1, E_NOT_PD = 2 };
 template <typename T>
 __global__ void k_ic0_factor_ref(const int32_t* __restrict__ lp, const int32_t* __restrict__ li,
                                  T* ld, int64_t n, int* ready, int* ctl, int* err_row,
-                                 int* err_code, const int32_t* __restrict__ order) {
+                                 int* err_code, const int32_t* __restrict__ order, unsigned long long wait_ns) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t i = 0;
@@ -90,7 +90,7 @@ __global__ void k_ic0_factor_ref(const int32_t* __restrict__ lp, const int32_t* 
         T dv = ldv(ld + di);
         for (int32_t k = rs; k < di; ++k) {
           const int32_t j = li[k];
-          if (!wait_flag(ready + j, ctl + 2)) break;
+          if (!wait_flag(ready + j, ctl + 2, wait_ns)) break;
           T ljj = T(0);
           for (int32_t q = lp[j]; q < lp[j + 1]; ++q)
             if (li[q] == j) { ljj = ldv(ld + q); break; }
@@ -107,7 +107,7 @@ __global__ void k_ic0_factor_ref(const int32_t* __restrict__ lp, const int32_t* 
         // duplicated input): ic.rs:107-128
         for (int32_t k = di + 1; k < re; ++k) {
           const int32_t j = li[k];
-          if (j < (int32_t)i && !wait_flag(ready + j, ctl + 2)) break;
+          if (j < (int32_t)i && !wait_flag(ready + j, ctl + 2, wait_ns)) break;
           T sum = T(0);
           for (int32_t p = rs; p < di; ++p) {
             const int32_t cp = li[p];
@@ -128,7 +128,8 @@ __global__ void k_ic0_factor_ref(const int32_t* __restrict__ lp, const int32_t* 
 template <typename T>
 __global__ void k_ic0_factor_textbook(const int32_t* __restrict__ lp, const int32_t* __restrict__ li,
                                       T* ld, int64_t n, int* ready, int* ctl, int* err_row,
-                                      int* err_code, const int32_t* __restrict__ order) {
+                                      int* err_code, const int32_t* __restrict__ order,
+                                      unsigned long long wait_ns) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t i = 0;
@@ -146,7 +147,7 @@ __global__ void k_ic0_factor_textbook(const int32_t* __restrict__ lp, const int3
         T dsum = T(0);
         for (int32_t k = rs; k < di; ++k) {
           const int32_t j = li[k];
-          if (!wait_flag(ready + j, ctl + 2)) break;
+          if (!wait_flag(ready + j, ctl + 2, wait_ns)) break;
           T s = ldv(ld + k);
           int32_t p = rs, q = lp[j];
           const int32_t qe = lp[j + 1] - 1;  // row j without its diagonal
@@ -229,7 +230,7 @@ template <typename T>
 __global__ void k_ic0_forward(const int32_t* __restrict__ lp, const int32_t* __restrict__ li,
                               const T* __restrict__ ld, const T* __restrict__ dlast, int64_t n,
                               const T* __restrict__ x, T* z, int* ready, int* ctl,
-                              const int32_t* __restrict__ order) {
+                              const int32_t* __restrict__ order, unsigned long long wait_ns) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t i = 0;
@@ -246,7 +247,7 @@ __global__ void k_ic0_forward(const int32_t* __restrict__ lp, const int32_t* __r
       if (k < re) {
         const int32_t j = li[k];
         if (j < (int32_t)i) {
-          wait_flag(ready + j, ctl + 2);
+          wait_flag(ready + j, ctl + 2, wait_ns);
           prod = mul_rn(ld[k], ldv(z + j));
           sub = true;
         }
@@ -272,7 +273,7 @@ template <typename T>
 __global__ void k_ic0_backward(const int32_t* __restrict__ tp, const int32_t* __restrict__ ti,
                                const T* __restrict__ tv, const T* __restrict__ dfirst, int64_t n,
                                const T* __restrict__ z, T* y, int* ready, int* ctl,
-                               const int32_t* __restrict__ order) {
+                               const int32_t* __restrict__ order, unsigned long long wait_ns) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t q = 0;
@@ -288,7 +289,7 @@ __global__ void k_ic0_backward(const int32_t* __restrict__ tp, const int32_t* __
       const bool act = k < re;
       if (act) {
         const int32_t j = ti[k];  // j > i
-        wait_flag(ready + j, ctl + 2);
+        wait_flag(ready + j, ctl + 2, wait_ns);
         prod = mul_rn(tv[k], ldv(y + j));
       }
       const unsigned m = __ballot_sync(0xffffffffu, act);
@@ -321,23 +322,65 @@ int ic0_apply(sx_ctx ctx, sx_op op, const void* x, void* y) {
   if (op->dtype == SX_F64) {
     k_ic0_forward<double><<<g, kBlock, 0, ctx->stream>>>(L.indptr, L.indices, (const double*)L.vals,
                                                          (const double*)d->dlast, n, (const double*)x,
-                                                         (double*)d->z, d->ready, d->ctl, d->fwd_order);
+                                                         (double*)d->z, d->ready, d->ctl, d->fwd_order, ctx->wait_ns);
     k_ic0_backward<double><<<g, kBlock, 0, ctx->stream>>>(T.indptr, T.indices, (const double*)T.vals,
                                                           (const double*)d->dfirst, n,
                                                           (const double*)d->z, (double*)y,
-                                                          d->ready + n, d->ctl, d->bwd_order);
+                                                          d->ready + n, d->ctl, d->bwd_order, ctx->wait_ns);
   } else {
     k_ic0_forward<float><<<g, kBlock, 0, ctx->stream>>>(L.indptr, L.indices, (const float*)L.vals,
                                                         (const float*)d->dlast, n, (const float*)x,
-                                                        (float*)d->z, d->ready, d->ctl, d->fwd_order);
+                                                        (float*)d->z, d->ready, d->ctl, d->fwd_order, ctx->wait_ns);
     k_ic0_backward<float><<<g, kBlock, 0, ctx->stream>>>(T.indptr, T.indices, (const float*)T.vals,
                                                          (const float*)d->dfirst, n,
                                                          (const float*)d->z, (float*)y,
-                                                         d->ready + n, d->ctl, d->bwd_order);
+                                                         d->ready + n, d->ctl, d->bwd_order, ctx->wait_ns);
   }
   ctx->launches += 2;
   SX_CUDA(cudaGetLastError());
   return SX_OK;
+}
+
+// a wait on a flag that nothing sets: ends only by its limit
+__global__ void k_wait_selftest(int* flags, unsigned long long wait_ns, unsigned long long* waited) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const unsigned long long t0 = globaltimer();
+  const bool ok = wait_flag(flags + 0, flags + 1, wait_ns);
+  waited[0] = globaltimer() - t0;
+  flags[2] = ok ? 1 : 0;
+}
+
+int ctx_set_wait_limit(sx_ctx ctx, uint64_t ns) {
+  ctx->wait_ns = ns ? (unsigned long long)ns : 2000000000ull;
+  return SX_OK;
+}
+
+int wait_selftest(sx_ctx ctx, uint64_t* waited_ns) {
+  int* flags = nullptr;
+  SX_CHECK(dev_alloc((void**)&flags, 4 * sizeof(int) + 8));
+  unsigned long long* waited = (unsigned long long*)(flags + 4);
+  int rc = SX_OK;
+  do {
+    if (cudaMemsetAsync(flags, 0, 4 * sizeof(int) + 8, ctx->stream) != cudaSuccess) {
+      rc = cuda_fail(cudaGetLastError(), "selftest memset", __FILE__, __LINE__);
+      break;
+    }
+    k_wait_selftest<<<1, 32, 0, ctx->stream>>>(flags, ctx->wait_ns, waited);
+    ctx->launches++;
+    int h[3] = {0, 0, 0};
+    unsigned long long w = 0;
+    cudaMemcpyAsync(h, flags, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaMemcpyAsync(&w, waited, 8, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "wait selftest", __FILE__, __LINE__);
+      break;
+    }
+    if (waited_ns) *waited_ns = w;
+    if (!h[2]) rc = set_error(SX_ERR_DEVICE_TIMEOUT, "Device timeout: the self-test wait gave up at its limit");
+  } while (0);
+  dev_free(flags);
+  return rc;
 }
 
 // abort flag of an IC(0) operator: a wait that gave up
@@ -351,6 +394,8 @@ int ic0_health(sx_ctx ctx, sx_op op) {
   int h[4] = {0, 0, 0, 0};
   SX_CUDA(cudaMemcpyAsync(h, ctl, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  // read and clear: the next call on this operator starts without the abort
+  if (h[2]) SX_CUDA(cudaMemsetAsync((void*)(ctl + 2), 0, sizeof(int), ctx->stream));
   if (h[2])
     return set_error(SX_ERR_DEVICE_TIMEOUT,
                      op->kind == SX_OP_IC0
@@ -396,6 +441,18 @@ int level_order(sx_ctx ctx, const DevCsr& c, bool forward, int32_t** out) {
 }  // namespace sx
 
 using namespace sx;
+
+extern "C" int sx_ctx_set_wait_limit(sx_ctx ctx, uint64_t ns) {
+  if (!ctx) return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: null ctx");
+  return ctx_set_wait_limit(ctx, ns) == SX_OK ? clear_error() : SX_ERR_INVALID_ARGUMENT;
+}
+
+extern "C" int sx_wait_selftest(sx_ctx ctx, uint64_t* waited_ns) {
+  if (!ctx) return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: null ctx");
+  SX_CUDA(cudaSetDevice(ctx->device));
+  const int rc = wait_selftest(ctx, waited_ns);
+  return rc == SX_OK ? clear_error() : rc;
+}
 
 extern "C" int sx_precond_ic0(sx_ctx ctx, sx_op a, int variant, sx_op* out) {
   if (!ctx || !a || !out) return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: null");
@@ -463,14 +520,14 @@ extern "C" int sx_precond_ic0(sx_ctx ctx, sx_op a, int variant, sx_op* out) {
       const int sg = solve_grid(ctx);
       if (a->dtype == SX_F64) {
         if (variant == SX_IC0_REFERENCE)
-          k_ic0_factor_ref<double><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (double*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order);
+          k_ic0_factor_ref<double><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (double*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order, ctx->wait_ns);
         else
-          k_ic0_factor_textbook<double><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (double*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order);
+          k_ic0_factor_textbook<double><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (double*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order, ctx->wait_ns);
       } else {
         if (variant == SX_IC0_REFERENCE)
-          k_ic0_factor_ref<float><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (float*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order);
+          k_ic0_factor_ref<float><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (float*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order, ctx->wait_ns);
         else
-          k_ic0_factor_textbook<float><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (float*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order);
+          k_ic0_factor_textbook<float><<<sg, kBlock, 0, ctx->stream>>>(d->L.indptr, d->L.indices, (float*)d->L.vals, n, d->ready, d->ctl, err, codes, d->fwd_order, ctx->wait_ns);
       }
       ctx->launches++;
     }

@@ -67,7 +67,7 @@ enum : int { E_NONE = 0, E_MISSING_DIAG = 1, E_ZERO_PIVOT = 2 };
 template <typename T>
 __global__ void k_ilu0_factor(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, T* val,
                               int64_t n, int* ready, int* ctl, int* err_row, int* err_code,
-                              const int32_t* __restrict__ order) {
+                              const int32_t* __restrict__ order, unsigned long long wait_ns) {
   const int lane = threadIdx.x & 31;
   const T eps = sizeof(T) == 8 ? (T)2.220446049250313e-16 : (T)1.1920928955078125e-07f;
   while (true) {
@@ -84,7 +84,7 @@ __global__ void k_ilu0_factor(const int32_t* __restrict__ ptr, const int32_t* __
         const bool found = k > run_max;  // the reference's scan for column k reaches p
         run_max = max(run_max, k);
         if (!found || k >= (int32_t)i) continue;
-        if (!wait_flag(ready + k, ctl + 2)) break;
+        if (!wait_flag(ready + k, ctl + 2, wait_ns)) break;
         // pivot: the first diagonal entry of row k (find_diagonal_index)
         int32_t kd = -1;
         for (int32_t q = ptr[k]; q < ptr[k + 1]; ++q)
@@ -155,7 +155,8 @@ template <typename T, bool LOWER>
 __global__ void k_tri_sweep(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                             const T* __restrict__ val, int64_t n, const T* __restrict__ in,
                             const T* __restrict__ pre, const T* __restrict__ div, int use_omega, T omega, T* out,
-                            int* ready, int* ctl, int counter, const int32_t* __restrict__ order) {
+                            int* ready, int* ctl, int counter, const int32_t* __restrict__ order,
+                            unsigned long long wait_ns) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int64_t t = 0;
@@ -173,7 +174,7 @@ __global__ void k_tri_sweep(const int32_t* __restrict__ ptr, const int32_t* __re
       if (k < re) {
         const int32_t j = idx[k];
         if (LOWER ? j < (int32_t)i : j > (int32_t)i) {
-          wait_flag(ready + j, ctl + 2);
+          wait_flag(ready + j, ctl + 2, wait_ns);
           const T c = use_omega ? mul_rn(omega, val[k]) : val[k];
           prod = mul_rn(c, ldv(out + j));
           act = true;
@@ -212,11 +213,11 @@ int tri_apply_t(sx_ctx ctx, sx_op op, const T* x, T* y) {
   // w = (D + wU)^-1 (y * D) (preconditioners.rs:148-187).
   k_tri_sweep<T, true><<<g, kBlock, 0, ctx->stream>>>(m.indptr, m.indices, (const T*)m.vals, n, x, nullptr,
                                                       ssor ? div : nullptr, ssor ? 1 : 0, om, (T*)d->tmp,
-                                                      d->ready, d->ctl, 0, d->fwd_order);
+                                                      d->ready, d->ctl, 0, d->fwd_order, ctx->wait_ns);
   k_tri_sweep<T, false><<<g, kBlock, 0, ctx->stream>>>(m.indptr, m.indices, (const T*)m.vals, n,
                                                        (const T*)d->tmp, ssor ? div : nullptr, div,
                                                        ssor ? 1 : 0, om, y, d->ready + n, d->ctl, 1,
-                                                       d->bwd_order);
+                                                       d->bwd_order, ctx->wait_ns);
   ctx->launches += 2;
   SX_CUDA(cudaGetLastError());
   return SX_OK;
@@ -304,10 +305,10 @@ int sx_precond_ilu0(sx_ctx ctx, sx_op a, sx_op* out) {
     if (n > 0) {
       if (a->dtype == SX_F64)
         k_ilu0_factor<double><<<sweep_grid(ctx), kBlock, 0, ctx->stream>>>(
-            d->m.indptr, d->m.indices, (double*)d->m.vals, n, d->ready, d->ctl, err, err + 1, d->fwd_order);
+            d->m.indptr, d->m.indices, (double*)d->m.vals, n, d->ready, d->ctl, err, err + 1, d->fwd_order, ctx->wait_ns);
       else
         k_ilu0_factor<float><<<sweep_grid(ctx), kBlock, 0, ctx->stream>>>(
-            d->m.indptr, d->m.indices, (float*)d->m.vals, n, d->ready, d->ctl, err, err + 1, d->fwd_order);
+            d->m.indptr, d->m.indices, (float*)d->m.vals, n, d->ready, d->ctl, err, err + 1, d->fwd_order, ctx->wait_ns);
       ctx->launches++;
     }
     int h[4] = {0, 0, 0, 0};

@@ -162,6 +162,14 @@ struct sx_ctx_s {
   // every matrix that has it
   int dia = 1;
   bool dia_nd6 = true;  // SX_DIA_ND6=0: five or six diagonals take the 8-slot kernel
+  // SX_DIA_TILE=1: the diagonal layout runs the tiled kernel (x windows in
+  // shared memory) instead of the register-batched kernel
+  bool dia_tile = false;
+  int smem_per_sm = 0;  // shared memory per SM (bytes)
+  // limit of one dependency wait of the triangular factorisations and
+  // sweeps (IC(0), ILU(0), SSOR), in nanoseconds: a wait that runs longer
+  // gives up and the call reports SX_ERR_DEVICE_TIMEOUT
+  unsigned long long wait_ns = 2000000000ull;
   int win_shape = 0;
 };
 
@@ -209,6 +217,8 @@ int exclusive_scan_i32(sx_ctx ctx, const int32_t* in, int64_t m, int32_t* out);
 
 // Abort flag of an IC(0) operator's bounded waits -> SX_ERR_DEVICE_TIMEOUT.
 int ic0_health(sx_ctx ctx, sx_op op);
+int ctx_set_wait_limit(sx_ctx ctx, uint64_t ns);
+int wait_selftest(sx_ctx ctx, uint64_t* waited_ns);
 
 // Cached transpose of a CSR operator (rmatvec, FSAI's G^T).
 int ensure_transpose(sx_ctx ctx, sx_op a);

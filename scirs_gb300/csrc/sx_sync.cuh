@@ -10,7 +10,6 @@
 namespace sx {
 namespace {
 
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
@@ -27,16 +26,17 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 }
 
 // Waits until *flag != 0; false if the wait was abandoned (abort raised or
-// the 2-s limit passed).  Spins without sleeping first: the wait sits on
-// the critical path of the triangular solves, one wait per dependency level.
-__device__ bool wait_flag(const int* flag, int* abort) {
+// the context's limit of `limit_ns` per wait passed; 2 s by default).  Spins
+// without sleeping first: the wait sits on the critical path of the
+// triangular solves, one wait per dependency level.
+__device__ bool wait_flag(const int* flag, int* abort, unsigned long long limit_ns) {
   if (ld_acquire(flag)) return true;
   const unsigned long long t0 = globaltimer();
   for (unsigned it = 1;; ++it) {
     if (ld_acquire(flag)) return true;
     if ((it & 63u) == 0) {
       if (ld_flag(abort)) return false;
-      if (globaltimer() - t0 > kWaitNs) {
+      if (globaltimer() - t0 > limit_ns) {
         atomicExch(abort, 1);
         return false;
       }

@@ -104,6 +104,20 @@ class Context:
     def synchronize(self) -> None:
         _check(L.lib.sx_ctx_synchronize(self.handle))
 
+    def set_wait_limit(self, ns: int) -> None:
+        """Limit of one dependency wait of the triangular factorisations and
+        sweeps, in nanoseconds (0: the default of 2 s)."""
+        _check(L.lib.sx_ctx_set_wait_limit(self.handle, int(ns)))
+
+    def wait_selftest(self):
+        """One bounded device wait on a flag nothing sets: (gave_up, waited_ns).
+        gave_up is True when the wait ran out at this context's limit."""
+        w = C.c_uint64()
+        rc = L.lib.sx_wait_selftest(self.handle, C.byref(w))
+        if rc not in (0, 101):
+            _check(rc)
+        return rc == 101, int(w.value)
+
     def close(self) -> None:
         if self.handle:
             L.lib.sx_ctx_destroy(self.handle)

@@ -143,3 +143,37 @@ def test_large_power_iteration(S, ctx):
     assert abs(d.eigenvalues[0] - top) < 1e-3 * top
     x = d.eigenvectors[:, 0]
     assert abs(np.linalg.norm(x) - 1.0) < 1e-9
+
+
+@pytest.mark.parametrize("tile", ["0", "1"])
+def test_lanczos_odd_sizes_on_the_diagonal_layout(S, tile):
+    # odd n: the basis vectors sit one padded stride apart, so every SpMV
+    # operand is aligned for the diagonal layout's vector loads
+    import os
+
+    old = os.environ.get("SX_DIA_TILE")
+    os.environ["SX_DIA_TILE"] = tile
+    try:
+        ctx = S.Context(0)
+    finally:
+        if old is None:
+            del os.environ["SX_DIA_TILE"]
+        else:
+            os.environ["SX_DIA_TILE"] = old
+    rng = np.random.default_rng(5)
+    ip, ix, v = S.generate("poisson2d", 21, 19)
+    cases = [(_lower(ip, ix, v), rng.standard_normal(399)),
+             ((np.array([0, 1, 3, 5, 7, 9], dtype=np.uint64), np.array([0, 0, 1, 1, 2, 2, 3, 3, 4], dtype=np.uint64),
+               np.array([4.0, -1, 4, -1, 4, -1, 4, -1, 4])), None)]
+    for (lip, lix, lv), v0 in cases:
+        a = _sym(S, ctx, lip, lix, lv)
+        assert S.spmv_kernel(a).startswith("spmv_dia")
+        kw = dict(max_iter=100, max_subspace_size=3, tol=1e-10, num_eigenvalues=2, compute_eigenvectors=True,
+                  initial_guess=v0)
+        d = S.lanczos(a, **kw)
+        o = O.lanczos(lip, lix, lv, **kw)
+        assert (d.iterations, d.converged) == (o["iterations"], o["converged"])
+        _close(d.eigenvalues, o["eigenvalues"], 1e-8, 1e-10)
+        _close(d.eigenvectors, o["eigenvectors"], 1e-7, 1e-9)
+        a.close()
+    ctx.close()

@@ -255,7 +255,7 @@ def _diag_cases(rng):
     yield "seventeen_diagonals", ip, cols.astype(np.int32), rng.uniform(-1, 1, len(cols)), False
 
 
-@pytest.mark.parametrize("env", [{}, {"SX_DIA_ND6": "0"}])
+@pytest.mark.parametrize("env", [{}, {"SX_DIA_ND6": "0"}, {"SX_DIA_TILE": "1"}])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_diagonal_layout_bit_exact(S, dtype, env):
     rng = np.random.default_rng(12)
@@ -264,7 +264,7 @@ def test_diagonal_layout_bit_exact(S, dtype, env):
         n = len(ip) - 1
         vals = v.astype(dtype)
         a = S.csr_from_arrays(ctx, ip, ix, vals, (n, n))
-        assert S.spmv_kernel(a).startswith("spmv_dia_kernel") == expect, name
+        assert S.spmv_kernel(a).startswith("spmv_dia") == expect, name
         x = rng.standard_normal(n).astype(dtype)
         # one infinite x: the rows that store its column give +-inf; a padded
         # (absent) entry multiplied into it would give NaN
@@ -272,4 +272,39 @@ def test_diagonal_layout_bit_exact(S, dtype, env):
         y = a.matvec(x)
         assert np.array_equal(y.view(np.uint8), O.spmv_i32(ip, ix, vals, x).view(np.uint8)), name
         a.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("tile", ["0", "1"])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_diagonal_layout_unaligned_vectors(S, dtype, tile):
+    # device vectors that do not start on 16 bytes (an odd element offset)
+    # take the CSR kernels: the same bits, no misaligned vector access
+    import torch
+
+    from scirs_gb300 import _lib as L
+
+    ctx = _ctx_with(S, {"SX_DIA_TILE": tile})
+    ip, ix, v = S.generate("poisson2d", 33, 31)
+    n = len(ip) - 1
+    vals = v.astype(dtype)
+    a = S.csr_from_arrays(ctx, ip, ix, vals, (n, n))
+    assert S.spmv_kernel(a).startswith("spmv_dia")
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    x = np.random.default_rng(3).standard_normal(n).astype(dtype)
+    xb = torch.zeros(n + 1, dtype=tdt, device="cuda")
+    yb = torch.zeros(n + 1, dtype=tdt, device="cuda")
+    xb[1:] = torch.from_numpy(x).cuda()
+    torch.cuda.synchronize()
+    for flags in (1, 0) if dtype == np.float64 else (1,):
+        S.sparse._check(L.lib.sx_spmv_ex(ctx.handle, a.handle, C.c_void_p(xb.data_ptr() + xb.element_size()),
+                                         C.c_void_p(yb.data_ptr() + yb.element_size()), flags))
+        ctx.synchronize()
+        y = yb[1:].cpu().numpy()
+        yr = O.spmv_i32(ip, ix, vals, x)
+        if flags == 1:
+            assert np.array_equal(y.view(np.uint8), yr.view(np.uint8))
+        else:
+            assert np.allclose(y, yr, rtol=1e-14, atol=1e-14)
+    a.close()
     ctx.close()
