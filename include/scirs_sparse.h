@@ -580,9 +580,12 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out);
 /* Thousands of independent SPD systems stored as one block-diagonal CSR
  * (system s owns rows and columns [sys_ptr[s], sys_ptr[s+1])).  Per system:
  * FP64 iterative refinement around an FP32 Jacobi-PCG, stopping when
- * ||b_s - A_s x_s|| <= max(atol, rtol ||b_s||) in FP64.  All systems advance
- * together in persistent kernels over the blocks of still-running systems,
- * the iteration loop captured in a CUDA graph. */
+ * ||b_s - A_s x_s|| <= max(atol, rtol ||b_s||) in FP64.  Each refinement pass
+ * runs every active system's FP32 PCG in one persistent launch (a thread
+ * block per system, systems taken largest first, per-system exits); the
+ * refinement loop with its FP64 residuals, per-system retirement and next
+ * queue runs on the device as one CUDA graph.  The launch shape is chosen
+ * by the context's autotuner and cached per batch size statistics. */
 typedef struct {
   uint64_t max_iter;   /* inner iterations per refinement step, default 10000 */
   double rtol;         /* default 1e-8 (FP64 true residual, per system) */
@@ -602,6 +605,8 @@ typedef struct {
   uint64_t total_inner_iterations;
   double worst_rel_residual;
   uint64_t kernel_launches;
+  uint32_t threads_per_block; /* launch shape the autotuner chose for the */
+  uint32_t blocks_per_sm;     /* persistent per-system kernel             */
 } sx_batched_summary;
 void sx_batched_options_default(sx_batched_options* o);
 /* a64: FP64 block-diagonal CSR; a32: its FP32 copy (NULL = made inside);

@@ -213,6 +213,8 @@ class BatchedSummary(C.Structure):
         ("total_inner_iterations", c_u64),
         ("worst_rel_residual", c_dbl),
         ("kernel_launches", c_u64),
+        ("threads_per_block", C.c_uint32),
+        ("blocks_per_sm", C.c_uint32),
     ]
 
 

@@ -3,19 +3,18 @@
 // cg call, linalg/iterative.rs:40-162, and this batches that loop).
 //
 // Layout: the systems form one block-diagonal CSR (global row and column
-// numbering); system s owns rows [sys_ptr[s], sys_ptr[s+1]).  Work items are
-// blocks of up to 256 consecutive rows of one system.  Each CG phase is one
-// persistent kernel that walks the list of blocks whose system is still
-// running; per-system reductions end in the last block of that system to
-// finish (a per-system ticket), which sums the system's block partials in a
-// fixed order and performs the reference cg's scalar step for that system.
-// After each iteration a compaction kernel drops the blocks of finished
-// systems and re-arms the CUDA-graph WHILE condition.
+// numbering); system s owns rows [sys_ptr[s], sys_ptr[s+1]).  The FP64
+// residual norms reduce over blocks of up to 256 rows of one system, the
+// last block of a system (a per-system ticket) summing its partials in a
+// fixed order and deciding whether the system retires.
 //
-// Mixed precision: an outer FP64 loop forms r = b - A x per system in FP64,
-// retires systems whose true relative residual meets the tolerance, and runs
-// the batched FP32 Jacobi-PCG on the rest for the correction.
-
+// Mixed precision: FP64 iterative refinement per system.  A pass forms
+// r = b - A x in FP64, retires the systems whose true relative residual
+// meets the tolerance, and runs the FP32 Jacobi-PCG of every remaining
+// system on A d = r / ||r|| in one persistent launch (a thread block per
+// system, so no block waits on another), then x += ||r|| d.  The loop of
+// passes runs on the device as a CUDA graph (a WHILE node whose condition
+// the queue kernel sets), so a whole batch is one graph launch.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -23,12 +22,10 @@
 #include <vector>
 
 #include "sx_launch.cuh"
+#include "sx_tune.cuh"
 
 namespace sx {
 namespace {
-
-constexpr int kItems = 8;
-constexpr int kTile = kBlock * kItems;
 
 struct BatchPlan {
   int64_t nsys = 0, nblocks = 0, nrows = 0;
@@ -37,25 +34,14 @@ struct BatchPlan {
   int32_t* blk_nrows = nullptr;
   int32_t* sys_fb = nullptr;   // first block of each system
   int32_t* sys_nb = nullptr;   // blocks of each system
-  int32_t* lists = nullptr;    // 2 x nblocks active-block lists
-  int32_t* ctl = nullptr;      // [0] cur list, [1] count list0, [2] count list1, [3] running,
-                               // [4] budget, [5] use_cond, [6] ticket, [7] pad
+  int32_t* ctl = nullptr;      // control words (Q_* slots)
   unsigned int* sys_ticket = nullptr;  // per-system last-block counters
   void* partials = nullptr;    // 3 * nblocks values
   unsigned long long* cond = nullptr;  // conditional handle
 };
 
-template <typename T>
-struct SysState {
-  T *rz_old, *alpha, *beta, *rnorm, *tol;
-  int *status, *message, *converged;
-  unsigned long long* iterations;
-  unsigned long long max_iter;
-};
-
 struct PlanView {
   const int32_t *blk_sys, *blk_row0, *blk_nrows, *sys_fb, *sys_nb;
-  int32_t* lists;
   int32_t* ctl;
   unsigned int* ticket;
   int64_t nblocks;
@@ -97,204 +83,122 @@ __device__ bool sys_reduce(const PlanView& pv, T* partials, int b, int s, Acc3<T
   return true;
 }
 
-// -------------------------------------------------------- CG phase kernels
-// A p for a block's rows (exact per-row order) with p.Ap; finalize alpha.
-template <typename T>
-__global__ void __launch_bounds__(kBlock) kb_spmv_pap(PlanView pv, const int32_t* __restrict__ indptr,
-                                                       const int32_t* __restrict__ indices,
-                                                       const T* __restrict__ vals, const T* __restrict__ p,
-                                                       T* q, T* partials, SysState<T> st) {
-  __shared__ int32_t s_ptr[kBlock + 1];
-  __shared__ T s_prod[kTile];
-  const int cur = pv.ctl[0];
-  const int cnt = pv.ctl[1 + cur];
-  const int32_t* list = pv.lists + (int64_t)cur * pv.nblocks;
-  const int tid = threadIdx.x;
-  for (int w = blockIdx.x; w < cnt; w += gridDim.x) {
-    const int b = list[w];
-    const int s = pv.blk_sys[b];
-    const int64_t r0 = pv.blk_row0[b];
-    const int nr = pv.blk_nrows[b];
-    if (tid <= nr) s_ptr[tid] = indptr[r0 + tid];
-    if (tid == 0 && nr == kBlock) s_ptr[kBlock] = indptr[r0 + kBlock];
-    __syncthreads();
-    const int32_t s0 = s_ptr[0], e0 = s_ptr[nr];
-    int32_t my_s = 0, my_e = 0;
-    if (tid < nr) { my_s = s_ptr[tid]; my_e = s_ptr[tid + 1]; }
-    T acc = T(0);
-    for (int32_t base = s0; base < e0; base += kTile) {
-      const int32_t tend = min(e0, base + kTile);
+// ------------------------------------------ persistent per-system FP32 PCG
+// One thread block owns one system for its whole FP32 inner solve: its
+// reductions are block reductions, so no block ever waits on another.  The
+// blocks take systems from a queue ordered largest first (an atomic ticket),
+// which balances uneven sizes.  The inner iteration keeps q = A p as its own
+// recurrence (A p_new = A z + beta A p_old), so each iteration is two passes
+// over the system's rows:
+//   pass 1  w = A z;  p = z + beta p;  q = w + beta q;  p.q -> alpha
+//   pass 2  d += alpha p;  r -= alpha q;  z = D r;  r.r, r.z -> beta
+// from d = 0, r = rhs, z = D r, p = q = 0, beta = 0 (Jacobi M = D).  The FP64
+// refinement around it (residual, norms, retirement) bounds the recurrence's
+// drift.  A system's vectors are written and re-read only by its own block
+// (plain loads: after the block's barriers they see its own stores).
+template <int NT>
+__device__ __forceinline__ float2 block_sum2_nt(float a, float b, float (*sh)[NT / 32]) {
 #pragma unroll
-      for (int j = 0; j < kItems; ++j) {
-        const int32_t k = base + j * kBlock + tid;
-        if (k < tend) s_prod[k - base] = mul_rn(vals[k], __ldg(p + indices[k]));
-      }
-      __syncthreads();
-      if (tid < nr) {
-        const int32_t lo = max(my_s, base), hi = min(my_e, tend);
-        for (int32_t k = lo; k < hi; ++k) acc = add_rn(acc, s_prod[k - base]);
-      }
-      __syncthreads();
-    }
-    Acc3<T> a{T(0), T(0), T(0)};
-    if (tid < nr) {
-      q[r0 + tid] = acc;
-      a.a = p[r0 + tid] * acc;
-    }
-    Acc3<T> tot;
-    if (sys_reduce(pv, partials, b, s, a, tot) && tid == 0) {
-      const T pap = tot.a;
-      if (pap <= T(0)) {
-        st.status[s] = 1;
-        st.message[s] = MSG_NOT_PD;
-        atomicSub(pv.ctl + 3, 1);
-      } else {
-        st.alpha[s] = st.rz_old[s] / pap;
-      }
-    }
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
   }
-}
-
-// x += alpha p; r -= alpha q; z = dinv r; ||r||, r.z; convergence and beta
-template <typename T>
-__global__ void __launch_bounds__(kBlock) kb_update(PlanView pv, T* x, T* r, const T* __restrict__ p,
-                                                     const T* __restrict__ q, const T* __restrict__ dinv,
-                                                     T* partials, SysState<T> st) {
-  const int cur = pv.ctl[0];
-  const int cnt = pv.ctl[1 + cur];
-  const int32_t* list = pv.lists + (int64_t)cur * pv.nblocks;
-  for (int w = blockIdx.x; w < cnt; w += gridDim.x) {
-    const int b = list[w];
-    const int s = pv.blk_sys[b];
-    if (st.status[s]) continue;  // uniform across the block
-    const int64_t row = pv.blk_row0[b] + threadIdx.x;
-    Acc3<T> a{T(0), T(0), T(0)};
-    if (threadIdx.x < pv.blk_nrows[b]) {
-      const T al = st.alpha[s];
-      x[row] = add_rn(x[row], mul_rn(al, p[row]));
-      const T ri = sub_rn(r[row], mul_rn(al, q[row]));
-      r[row] = ri;
-      a.a = ri * ri;
-      a.b = ri * mul_rn(ri, dinv[row]);
-    }
-    Acc3<T> tot;
-    if (sys_reduce(pv, partials, b, s, a, tot) && threadIdx.x == 0) {
-      const T rn = sqrt(tot.a);
-      st.rnorm[s] = rn;
-      if (rn <= st.tol[s]) {
-        st.status[s] = 1;
-        st.converged[s] = 1;
-        st.message[s] = MSG_CONVERGED;
-        st.iterations[s] += 1;
-        atomicSub(pv.ctl + 3, 1);
-      } else {
-        st.beta[s] = tot.b / st.rz_old[s];
-        st.rz_old[s] = tot.b;
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// p = dinv r + beta p; per-system iteration count and max_iter
-template <typename T>
-__global__ void __launch_bounds__(kBlock) kb_pupdate(PlanView pv, T* p, const T* __restrict__ r,
-                                                      const T* __restrict__ dinv, T* partials,
-                                                      SysState<T> st) {
-  const int cur = pv.ctl[0];
-  const int cnt = pv.ctl[1 + cur];
-  const int32_t* list = pv.lists + (int64_t)cur * pv.nblocks;
-  for (int w = blockIdx.x; w < cnt; w += gridDim.x) {
-    const int b = list[w];
-    const int s = pv.blk_sys[b];
-    if (st.status[s]) continue;
-    const int64_t row = pv.blk_row0[b] + threadIdx.x;
-    if (threadIdx.x < pv.blk_nrows[b]) p[row] = add_rn(mul_rn(r[row], dinv[row]), mul_rn(st.beta[s], p[row]));
-    Acc3<T> a{T(0), T(0), T(0)}, tot;
-    if (sys_reduce(pv, partials, b, s, a, tot) && threadIdx.x == 0) {
-      st.iterations[s] += 1;
-      if (st.iterations[s] >= st.max_iter) {
-        st.status[s] = 1;
-        st.message[s] = MSG_MAX_ITER;
-        atomicSub(pv.ctl + 3, 1);
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// drop the blocks of finished systems; re-arm the loop condition
-template <typename T>
-__global__ void __launch_bounds__(kBlock) kb_compact(PlanView pv, SysState<T> st) {
-  const int cur = pv.ctl[0];
-  const int nxt = cur ^ 1;
-  const int cnt = pv.ctl[1 + cur];
-  const int32_t* list = pv.lists + (int64_t)cur * pv.nblocks;
-  int32_t* out = pv.lists + (int64_t)nxt * pv.nblocks;
-  for (int w = blockIdx.x * kBlock + threadIdx.x; w < cnt; w += gridDim.x * kBlock) {
-    const int b = list[w];
-    if (!st.status[pv.blk_sys[b]]) out[atomicAdd(pv.ctl + 1 + nxt, 1)] = b;
-  }
-  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sh[0][w] = a; sh[1][w] = b; }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd((unsigned*)(pv.ctl + 6), 1u) == gridDim.x - 1;
-  }
+  float ta = 0.f, tb = 0.f;
+#pragma unroll
+  for (int k = 0; k < NT / 32; ++k) { ta += sh[0][k]; tb += sh[1][k]; }
   __syncthreads();
-  if (s_last && threadIdx.x == 0) {
-    __threadfence();
-    pv.ctl[6] = 0;
-    pv.ctl[0] = nxt;
-    pv.ctl[1 + cur] = 0;
-    if (pv.ctl[4] > 0) pv.ctl[4] -= 1;
-    const bool more = pv.ctl[3] > 0 && pv.ctl[4] > 0;
-    if (pv.ctl[5]) cudaGraphSetConditional((cudaGraphConditionalHandle)*pv.cond, more ? 1u : 0u);
-  }
+  return make_float2(ta, tb);
 }
 
-// ---------------------------------------------------------------- setup
-// z = dinv r, p = z; rz, ||b||, ||r|| per system; tolerance
-template <typename T>
-__global__ void __launch_bounds__(kBlock) kb_setup(PlanView pv, const T* __restrict__ b,
-                                                    const T* __restrict__ r, const T* __restrict__ dinv,
-                                                    T* p, T* partials, SysState<T> st, T rtol, T atol) {
-  const int cur = pv.ctl[0];
-  const int cnt = pv.ctl[1 + cur];
-  const int32_t* list = pv.lists + (int64_t)cur * pv.nblocks;
-  for (int w = blockIdx.x; w < cnt; w += gridDim.x) {
-    const int bk = list[w];
-    const int s = pv.blk_sys[bk];
-    const int64_t row = pv.blk_row0[bk] + threadIdx.x;
-    Acc3<T> a{T(0), T(0), T(0)};
-    if (threadIdx.x < pv.blk_nrows[bk]) {
-      const T ri = r[row];
-      const T zi = mul_rn(ri, dinv[row]);
-      p[row] = zi;
-      a.a = ri * zi;
-      a.b = b[row] * b[row];
-      a.c = ri * ri;
-    }
-    Acc3<T> tot;
-    if (sys_reduce(pv, partials, bk, s, a, tot) && threadIdx.x == 0) {
-      st.rz_old[s] = tot.a;
-      st.tol[s] = fmax(atol, rtol * sqrt(tot.b));
-      st.rnorm[s] = sqrt(tot.c);
-      if (st.max_iter == 0) {
-        st.status[s] = 1;
-        st.message[s] = MSG_MAX_ITER;
-        atomicSub(pv.ctl + 3, 1);
-      }
-    }
+// control words (int32 slots of ctl)
+enum : int { Q_NQ = 8, Q_NEXT = 9, Q_NACT = 10, Q_OUTER = 11, Q_USE_COND = 12 };
+
+template <int NT>
+__global__ void __launch_bounds__(NT) kb_pcg_sys(const int64_t* __restrict__ sys_ptr, const int32_t* __restrict__ queue,
+                                                 int32_t* ctl, int cap, const int32_t* __restrict__ indptr,
+                                                 const int32_t* __restrict__ indices, const float* __restrict__ vals,
+                                                 const float* __restrict__ dinv, const float* __restrict__ rhs,
+                                                 float* d, float* r, float* z, float* p, float* q, float inner_rtol,
+                                                 unsigned long long max_iter, unsigned long long* iters) {
+  __shared__ float sh[2][NT / 32];
+  __shared__ int s_w;
+  const int nq = min(ctl[Q_NQ], cap);
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) s_w = atomicAdd(ctl + Q_NEXT, 1);
     __syncthreads();
+    const int w = s_w;
+    __syncthreads();
+    if (w >= nq) break;
+    const int s = queue[w];
+    const int64_t r0 = sys_ptr[s], r1 = sys_ptr[s + 1];
+    float a_rz = 0.f, a_rr = 0.f;
+    for (int64_t i = r0 + tid; i < r1; i += NT) {
+      const float ri = __ldg(rhs + i);
+      const float zi = mul_rn(ri, __ldg(dinv + i));
+      d[i] = 0.f; r[i] = ri; z[i] = zi; p[i] = 0.f; q[i] = 0.f;
+      a_rz += ri * zi;
+      a_rr += ri * ri;
+    }
+    float2 t = block_sum2_nt<NT>(a_rz, a_rr, sh);
+    float rz = t.x, beta = 0.f;
+    const float tol = inner_rtol * sqrtf(t.y);
+    unsigned long long it = 0;
+    while (it < max_iter) {
+      float a_pq = 0.f;
+      for (int64_t i = r0 + tid; i < r1; i += NT) {
+        const int32_t ks = __ldg(indptr + i), ke = __ldg(indptr + i + 1);
+        float wv = 0.f;
+        for (int32_t k = ks; k < ke; ++k) wv = add_rn(wv, mul_rn(__ldg(vals + k), z[__ldg(indices + k)]));
+        const float pi = add_rn(z[i], mul_rn(beta, p[i]));
+        const float qi = add_rn(wv, mul_rn(beta, q[i]));
+        p[i] = pi;
+        q[i] = qi;
+        a_pq += pi * qi;
+      }
+      const float pq = block_sum2_nt<NT>(a_pq, 0.f, sh).x;
+      if (!(pq > 0.f)) break;  // p.q <= 0 (or not finite): this pass ends here
+      const float alpha = rz / pq;
+      float b_rz = 0.f, b_rr = 0.f;
+      for (int64_t i = r0 + tid; i < r1; i += NT) {
+        d[i] = add_rn(d[i], mul_rn(alpha, p[i]));
+        const float ri = sub_rn(r[i], mul_rn(alpha, q[i]));
+        const float zi = mul_rn(ri, __ldg(dinv + i));
+        r[i] = ri;
+        z[i] = zi;
+        b_rz += ri * zi;
+        b_rr += ri * ri;
+      }
+      t = block_sum2_nt<NT>(b_rz, b_rr, sh);
+      ++it;
+      if (sqrtf(t.y) <= tol) break;
+      beta = t.x / rz;
+      rz = t.x;
+    }
+    if (tid == 0) iters[s] += it;
   }
 }
 
-// FP64 true residual norms per system: rr_s = ||b - A x||^2, bb_s = ||b||^2
+// FP64 true residual norms per system (rr_s = ||b - A x||^2, bb_s = ||b||^2)
+// and the refinement decision, in the last block of each system: retire it
+// when ||r|| <= max(atol, rtol ||b||); keep it active while outer passes
+// remain.  Active systems are counted for the queue kernel.
+struct Refine {
+  double* rr;
+  double* bb;
+  double* rel;
+  int* conv;
+  int* active;
+  double rtol, atol;
+  int max_outer;
+};
+
 __global__ void __launch_bounds__(kBlock) kb_norms64(PlanView pv, const double* __restrict__ b,
-                                                      const double* __restrict__ r, double* partials,
-                                                      double* rr, double* bb) {
+                                                      const double* __restrict__ r, double* partials, Refine rf) {
+  const int outer = pv.ctl[Q_OUTER];
   for (int64_t w = blockIdx.x; w < pv.nblocks; w += gridDim.x) {
     const int bk = (int)w;
     const int s = pv.blk_sys[bk];
@@ -306,10 +210,53 @@ __global__ void __launch_bounds__(kBlock) kb_norms64(PlanView pv, const double* 
     }
     Acc3<double> tot;
     if (sys_reduce(pv, partials, bk, s, a, tot) && threadIdx.x == 0) {
-      rr[s] = tot.a;
-      bb[s] = tot.b;
+      rf.rr[s] = tot.a;
+      rf.bb[s] = tot.b;
+      const double rn = sqrt(tot.a), bn = sqrt(tot.b);
+      rf.rel[s] = bn > 0 ? rn / bn : rn;
+      const bool done = rn <= fmax(rf.atol, rf.rtol * bn);
+      rf.conv[s] = done ? 1 : 0;
+      const bool act = !done && outer < rf.max_outer;
+      rf.active[s] = act ? 1 : 0;
+      if (act) atomicAdd(pv.ctl + Q_NACT, 1);
     }
     __syncthreads();
+  }
+}
+
+// The next pass's queue: the active systems in the fixed largest-first
+// order (one block, an ordered compaction), its length, the ticket reset,
+// the pass count and the graph loop's condition.
+constexpr int kQueueThreads = 1024;
+__global__ void __launch_bounds__(kQueueThreads) kb_queue(const int32_t* __restrict__ order, int64_t nsys,
+                                                          const int* __restrict__ active, int32_t* queue, int32_t* ctl,
+                                                          const unsigned long long* cond) {
+  __shared__ int s_cnt[kQueueThreads];
+  const int tid = threadIdx.x;
+  const int64_t chunk = (nsys + kQueueThreads - 1) / kQueueThreads;
+  const int64_t lo = nsys < tid * chunk ? nsys : tid * chunk;
+  const int64_t hi = nsys < lo + chunk ? nsys : lo + chunk;
+  int c = 0;
+  for (int64_t k = lo; k < hi; ++k) c += active[order[k]] ? 1 : 0;
+  s_cnt[tid] = c;
+  __syncthreads();
+  // inclusive prefix of the counts (Hillis-Steele in place)
+  for (int off = 1; off < kQueueThreads; off <<= 1) {
+    const int v = tid >= off ? s_cnt[tid - off] : 0;
+    __syncthreads();
+    s_cnt[tid] += v;
+    __syncthreads();
+  }
+  int pos = s_cnt[tid] - c;
+  for (int64_t k = lo; k < hi; ++k)
+    if (active[order[k]]) queue[pos++] = order[k];
+  if (tid == kQueueThreads - 1) {
+    const int nq = s_cnt[tid];
+    ctl[Q_NQ] = nq;
+    ctl[Q_NEXT] = 0;
+    ctl[Q_NACT] = 0;
+    if (nq > 0) ctl[Q_OUTER] += 1;
+    if (ctl[Q_USE_COND]) cudaGraphSetConditional((cudaGraphConditionalHandle)*cond, nq > 0 ? 1u : 0u);
   }
 }
 
@@ -337,12 +284,6 @@ __global__ void kb_row_sys(const int32_t* __restrict__ blk_sys, const int32_t* _
     if (threadIdx.x < blk_nrows[b]) row_sys[blk_row0[b] + threadIdx.x] = blk_sys[b];
 }
 
-// initial active list: blocks of systems flagged active
-__global__ void kb_init_list(PlanView pv, const int* __restrict__ active) {
-  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < pv.nblocks; b += (int64_t)gridDim.x * blockDim.x)
-    if (active[pv.blk_sys[b]]) pv.lists[atomicAdd(pv.ctl + 1, 1)] = (int32_t)b;
-}
-
 __global__ void kb_jacobi32(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                             const float* __restrict__ vals, int64_t n, float* dinv) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -354,13 +295,13 @@ __global__ void kb_jacobi32(const int32_t* __restrict__ ptr, const int32_t* __re
 }
 
 PlanView view(const BatchPlan& p) {
-  return PlanView{p.blk_sys, p.blk_row0, p.blk_nrows, p.sys_fb, p.sys_nb, p.lists, p.ctl,
+  return PlanView{p.blk_sys, p.blk_row0, p.blk_nrows, p.sys_fb, p.sys_nb, p.ctl,
                   p.sys_ticket, p.nblocks, p.cond};
 }
 
 void plan_free(BatchPlan& p) {
   dev_free(p.blk_sys); dev_free(p.blk_row0); dev_free(p.blk_nrows); dev_free(p.sys_fb);
-  dev_free(p.sys_nb); dev_free(p.lists); dev_free(p.ctl); dev_free(p.sys_ticket);
+  dev_free(p.sys_nb); dev_free(p.ctl); dev_free(p.sys_ticket);
   dev_free(p.partials); dev_free(p.cond);
   p = BatchPlan{};
 }
@@ -386,7 +327,6 @@ int plan_build(sx_ctx ctx, const std::vector<int64_t>& sys_ptr, BatchPlan& p) {
   SX_CHECK(dev_alloc((void**)&p.blk_nrows, B * 4));
   SX_CHECK(dev_alloc((void**)&p.sys_fb, SS * 4));
   SX_CHECK(dev_alloc((void**)&p.sys_nb, SS * 4));
-  SX_CHECK(dev_alloc((void**)&p.lists, 2 * B * 4));
   SX_CHECK(dev_alloc((void**)&p.ctl, 16 * 4));
   SX_CHECK(dev_alloc((void**)&p.sys_ticket, SS * 4));
   SX_CHECK(dev_alloc(&p.partials, B * 3 * 8));
@@ -405,86 +345,49 @@ int plan_build(sx_ctx ctx, const std::vector<int64_t>& sys_ptr, BatchPlan& p) {
   return SX_OK;
 }
 
-// Batched FP32 (or FP64) Jacobi-PCG on the systems with active[s] != 0,
-// solving A d = rhs from d = 0.  Per-system results into st.
-template <typename T>
-int batched_cg_core(sx_ctx ctx, const DevCsr& A, const T* dinv, BatchPlan& plan, const int* d_active,
-                    int n_active, const T* rhs, T* d, T* r, T* p, T* q, SysState<T>& st, double rtol,
-                    double atol, unsigned long long max_iter, uint64_t* launches_out) {
-  const int64_t n = A.nrows;
-  const PlanView pv = view(plan);
-  const int grid = ctx->num_sms * 8;
-  // reset control block and the initial active list
-  int hctl[16];
-  std::memset(hctl, 0, sizeof(hctl));
-  hctl[3] = n_active;
-  hctl[4] = (int)4096;  // budget per graph launch
-  SX_CUDA(cudaMemcpyAsync(plan.ctl, hctl, sizeof(hctl), cudaMemcpyHostToDevice, ctx->stream));
-  kb_init_list<<<vec_grid(ctx, plan.nblocks), kBlock, 0, ctx->stream>>>(pv, d_active);
-  // d = 0; r = rhs (b - A*0)
-  SX_CUDA(cudaMemsetAsync(d, 0, n * sizeof(T), ctx->stream));
-  SX_CUDA(cudaMemcpyAsync(r, rhs, n * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream));
-  kb_setup<T><<<grid, kBlock, 0, ctx->stream>>>(pv, rhs, r, dinv, p, (T*)plan.partials, st, (T)rtol, (T)atol);
-  ctx->launches += 2;
-  auto body = [&]() -> int {
-    kb_spmv_pap<T><<<grid, kBlock, 0, ctx->stream>>>(pv, A.indptr, A.indices, (const T*)A.vals, p, q,
-                                                    (T*)plan.partials, st);
-    kb_update<T><<<grid, kBlock, 0, ctx->stream>>>(pv, d, r, p, q, dinv, (T*)plan.partials, st);
-    kb_pupdate<T><<<grid, kBlock, 0, ctx->stream>>>(pv, p, r, dinv, (T*)plan.partials, st);
-    kb_compact<T><<<ctx->num_sms * 2, kBlock, 0, ctx->stream>>>(pv, st);
-    ctx->launches += 4;
-    SX_CUDA(cudaGetLastError());
-    return SX_OK;
-  };
-  // graph: WHILE(cond) { body }
-  cudaGraph_t g = nullptr;
-  cudaGraphExec_t ge = nullptr;
-  cudaGraphConditionalHandle h = 0;
-  bool graph_ok = false;
-  do {
-    if (cudaGraphCreate(&g, 0) != cudaSuccess) break;
-    if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) break;
-    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-    cp.conditional.handle = h;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t node;
-    if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) != cudaSuccess) break;
-    cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
-    if (cudaStreamBeginCaptureToGraph(ctx->stream, bodyg, nullptr, nullptr, 0,
-                                      cudaStreamCaptureModeThreadLocal) != cudaSuccess) break;
-    const uint64_t before = ctx->launches;
-    int rc = body();
-    cudaGraph_t cap = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &cap);
-    ctx->launches = before;
-    if (rc != SX_OK || ce != cudaSuccess) break;
-    if (cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) break;
-    graph_ok = true;
-  } while (0);
-  cudaGetLastError();
-  unsigned long long hcond = (unsigned long long)h;
-  SX_CUDA(cudaMemcpyAsync(plan.cond, &hcond, 8, cudaMemcpyHostToDevice, ctx->stream));
-  int rc = SX_OK;
-  for (int guard = 0; guard < 1000000; ++guard) {
-    int hc[16];
-    SX_CUDA(cudaMemcpyAsync(hc, plan.ctl, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
-    SX_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (hc[3] <= 0) break;
-    int refill[2] = {4096, graph_ok ? 1 : 0};
-    SX_CUDA(cudaMemcpyAsync(plan.ctl + 4, refill, sizeof(refill), cudaMemcpyHostToDevice, ctx->stream));
-    if (graph_ok) {
-      SX_CUDA(cudaGraphLaunch(ge, ctx->stream));
-      *launches_out += 4ull * 4096ull;  // upper bound; refined below
-    } else {
-      for (int k = 0; k < 32; ++k)
-        if ((rc = body())) break;
-      if (rc) break;
-    }
+// Launch shapes of the persistent per-system kernel: threads per block and
+// blocks per SM.  The autotuner picks one per problem key.
+struct PcgShape {
+  int threads, per_sm;
+};
+constexpr PcgShape kPcgShapes[] = {{256, 8}, {256, 4}, {512, 4}, {512, 2}, {1024, 2}, {1024, 1}};
+constexpr int kNumPcgShapes = (int)(sizeof(kPcgShapes) / sizeof(kPcgShapes[0]));
+
+struct PcgArgs {
+  const int64_t* sys_ptr;
+  const int32_t* queue;
+  int32_t* ctl;
+  const DevCsr* A;
+  const float* dinv;
+  const float* rhs;
+  float *d, *r, *z, *p, *q;
+  float inner_rtol;
+  unsigned long long* iters;
+};
+
+int launch_pcg(sx_ctx ctx, int shape, const PcgArgs& a, int cap, unsigned long long max_iter) {
+  const PcgShape sh = kPcgShapes[shape];
+  const unsigned grid = (unsigned)(ctx->num_sms * sh.per_sm);
+  const DevCsr& A = *a.A;
+  switch (sh.threads) {
+    case 256:
+      kb_pcg_sys<256><<<grid, 256, 0, ctx->stream>>>(a.sys_ptr, a.queue, a.ctl, cap, A.indptr, A.indices,
+                                                     (const float*)A.vals, a.dinv, a.rhs, a.d, a.r, a.z, a.p, a.q,
+                                                     a.inner_rtol, max_iter, a.iters);
+      break;
+    case 512:
+      kb_pcg_sys<512><<<grid, 512, 0, ctx->stream>>>(a.sys_ptr, a.queue, a.ctl, cap, A.indptr, A.indices,
+                                                     (const float*)A.vals, a.dinv, a.rhs, a.d, a.r, a.z, a.p, a.q,
+                                                     a.inner_rtol, max_iter, a.iters);
+      break;
+    default:
+      kb_pcg_sys<1024><<<grid, 1024, 0, ctx->stream>>>(a.sys_ptr, a.queue, a.ctl, cap, A.indptr, A.indices,
+                                                       (const float*)A.vals, a.dinv, a.rhs, a.d, a.r, a.z, a.p,
+                                                       a.q, a.inner_rtol, max_iter, a.iters);
   }
-  if (ge) cudaGraphExecDestroy(ge);
-  if (g) cudaGraphDestroy(g);
-  return rc;
+  ctx->launches++;
+  SX_CUDA(cudaGetLastError());
+  return SX_OK;
 }
 
 }  // namespace
@@ -527,18 +430,21 @@ int sx_batched_pcg(sx_ctx ctx, sx_op a64, sx_op a32, const int64_t* sys_ptr, uin
   const int64_t S = (int64_t)nsys;
   sx_op own32 = nullptr;
   BatchPlan plan;
-  double *db = nullptr, *dx = nullptr, *dr = nullptr, *rr = nullptr, *bb = nullptr;
-  float *r32 = nullptr, *d32 = nullptr, *rw = nullptr, *pw = nullptr, *qw = nullptr, *dinv = nullptr;
-  int32_t* row_sys = nullptr;
-  int* active = nullptr;
-  SysState<float> st{};
-  void* stbuf = nullptr;
+  double *db = nullptr, *dx = nullptr, *dr = nullptr, *rr = nullptr, *bb = nullptr, *rel = nullptr;
+  float *r32 = nullptr, *d32 = nullptr, *rw = nullptr, *zw = nullptr, *pw = nullptr, *qw = nullptr, *dinv = nullptr;
+  int32_t *row_sys = nullptr, *order = nullptr, *queue = nullptr;
+  int64_t* dsp = nullptr;
+  int *active = nullptr, *conv = nullptr;
+  unsigned long long* iters = nullptr;
   int rc = SX_OK;
-  std::vector<uint64_t> inner_total(S, 0);
-  std::vector<double> rel(S, 0.0);
-  std::vector<int> conv(S, 0);
-  uint64_t outer = 0, launches = 0;
+  std::vector<unsigned long long> inner_total(S, 0);
+  std::vector<double> hrel(S, 0.0);
+  std::vector<int> hconv(S, 0);
+  uint64_t outer = 0;
+  int shape = 0;
   const uint64_t l0 = ctx->launches;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
   do {
     if (!a32) {
       if ((rc = sx_csr_astype(ctx, a64, SX_F32, &own32))) break;
@@ -551,87 +457,153 @@ int sx_batched_pcg(sx_ctx ctx, sx_op a64, sx_op a32, const int64_t* sys_ptr, uin
     if ((rc = dev_alloc((void**)&dr, nb * 8))) break;
     if ((rc = dev_alloc((void**)&rr, sb * 8))) break;
     if ((rc = dev_alloc((void**)&bb, sb * 8))) break;
+    if ((rc = dev_alloc((void**)&rel, sb * 8))) break;
     if ((rc = dev_alloc((void**)&r32, nb * 4))) break;
     if ((rc = dev_alloc((void**)&d32, nb * 4))) break;
     if ((rc = dev_alloc((void**)&rw, nb * 4))) break;
+    if ((rc = dev_alloc((void**)&zw, nb * 4))) break;
     if ((rc = dev_alloc((void**)&pw, nb * 4))) break;
     if ((rc = dev_alloc((void**)&qw, nb * 4))) break;
     if ((rc = dev_alloc((void**)&dinv, nb * 4))) break;
     if ((rc = dev_alloc((void**)&row_sys, nb * 4))) break;
+    if ((rc = dev_alloc((void**)&order, sb * 4))) break;
+    if ((rc = dev_alloc((void**)&queue, sb * 4))) break;
+    if ((rc = dev_alloc((void**)&dsp, (sb + 1) * 8))) break;
     if ((rc = dev_alloc((void**)&active, sb * 4))) break;
-    // per-system state arrays: 5 floats, 3 ints, 1 u64 per system
-    if ((rc = dev_alloc(&stbuf, sb * (5 * 4 + 3 * 4 + 8) + 256))) break;
-    {
-      char* pb = (char*)stbuf;
-      st.iterations = (unsigned long long*)pb; pb += sb * 8;
-      st.rz_old = (float*)pb; pb += sb * 4;
-      st.alpha = (float*)pb; pb += sb * 4;
-      st.beta = (float*)pb; pb += sb * 4;
-      st.rnorm = (float*)pb; pb += sb * 4;
-      st.tol = (float*)pb; pb += sb * 4;
-      st.status = (int*)pb; pb += sb * 4;
-      st.message = (int*)pb; pb += sb * 4;
-      st.converged = (int*)pb; pb += sb * 4;
-      st.max_iter = opt->max_iter;
-    }
+    if ((rc = dev_alloc((void**)&conv, sb * 4))) break;
+    if ((rc = dev_alloc((void**)&iters, sb * 8))) break;
+    // systems largest first: the persistent blocks take them in this order
+    std::vector<int32_t> ord(S);
+    for (int64_t s = 0; s < S; ++s) ord[s] = (int32_t)s;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int32_t a, int32_t c) { return sp[a + 1] - sp[a] > sp[c + 1] - sp[c]; });
+    // an empty system has no residual rows: converged from the start
+    std::vector<int> conv0(S, 0);
+    for (int64_t s = 0; s < S; ++s) conv0[s] = sp[s + 1] == sp[s] ? 1 : 0;
     const cudaMemcpyKind kin = mem == SX_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    cudaMemcpyAsync(db, b, n * 8, kin, ctx->stream);
-    cudaMemsetAsync(dx, 0, n * 8, ctx->stream);
-    const int g = vec_grid(ctx, n);
-    kb_jacobi32<<<g, kBlock, 0, ctx->stream>>>(a32->csr.indptr, a32->csr.indices,
-                                                (const float*)a32->csr.vals, n, dinv);
+    SX_CUDA(cudaMemcpyAsync(db, b, n * 8, kin, ctx->stream));
+    SX_CUDA(cudaMemsetAsync(dx, 0, n * 8, ctx->stream));
+    if (S > 0) {
+      SX_CUDA(cudaMemcpyAsync(order, ord.data(), S * 4, cudaMemcpyHostToDevice, ctx->stream));
+      SX_CUDA(cudaMemcpyAsync(conv, conv0.data(), S * 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    SX_CUDA(cudaMemcpyAsync(dsp, sp.data(), (S + 1) * 8, cudaMemcpyHostToDevice, ctx->stream));
+    SX_CUDA(cudaMemsetAsync(active, 0, sb * 4, ctx->stream));
+    SX_CUDA(cudaMemsetAsync(rel, 0, sb * 8, ctx->stream));
+    SX_CUDA(cudaMemsetAsync(iters, 0, sb * 8, ctx->stream));
+    const int gv = vec_grid(ctx, n);
+    kb_jacobi32<<<gv, kBlock, 0, ctx->stream>>>(a32->csr.indptr, a32->csr.indices, (const float*)a32->csr.vals, n,
+                                                dinv);
     kb_row_sys<<<ctx->num_sms * 8, kBlock, 0, ctx->stream>>>(plan.blk_sys, plan.blk_row0, plan.blk_nrows,
                                                              plan.nblocks, row_sys);
     ctx->launches += 2;
     const PlanView pv = view(plan);
-    std::vector<double> hrr(S), hbb(S);
-    std::vector<int> hact(S);
-    std::vector<unsigned long long> hit(S);
-    while (true) {
-      // FP64 residual and per-system norms
-      if ((rc = launch_csr<double>(ctx, a64->csr, dx, dr, EpiResid<double>{db}))) break;
-      kb_norms64<<<ctx->num_sms * 8, kBlock, 0, ctx->stream>>>(pv, db, dr, (double*)plan.partials, rr, bb);
+    const Refine rf{rr, bb, rel, conv, active, opt->rtol, opt->atol,
+                    (int)std::min<uint64_t>(opt->max_outer, (uint64_t)INT32_MAX)};
+    const PcgArgs pa{dsp, queue, plan.ctl, &a32->csr, dinv, r32, d32, rw, zw, pw, qw, (float)opt->inner_rtol, iters};
+    // the tail of a refinement pass: FP64 residual, per-system norms and
+    // decisions, the next queue (and the loop condition inside the graph)
+    auto refine_tail = [&]() -> int {
+      SX_CHECK(launch_csr<double>(ctx, a64->csr, dx, dr, EpiResid<double>{db}));
+      kb_norms64<<<ctx->num_sms * 8, kBlock, 0, ctx->stream>>>(pv, db, dr, (double*)plan.partials, rf);
+      kb_queue<<<1, kQueueThreads, 0, ctx->stream>>>(order, S, active, queue, plan.ctl, plan.cond);
+      ctx->launches += 2;
+      SX_CUDA(cudaGetLastError());
+      return SX_OK;
+    };
+    auto pass = [&](int shp) -> int {
+      kb_scale_down<<<gv, kBlock, 0, ctx->stream>>>(row_sys, n, dr, rr, active, r32);
       ctx->launches++;
-      SX_CUDA(cudaMemcpyAsync(hrr.data(), rr, S * 8, cudaMemcpyDeviceToHost, ctx->stream));
-      SX_CUDA(cudaMemcpyAsync(hbb.data(), bb, S * 8, cudaMemcpyDeviceToHost, ctx->stream));
-      SX_CUDA(cudaStreamSynchronize(ctx->stream));
-      int n_act = 0;
-      for (int64_t s = 0; s < S; ++s) {
-        const double rn = std::sqrt(hrr[s]), bn = std::sqrt(hbb[s]);
-        rel[s] = bn > 0 ? rn / bn : rn;
-        const bool done = rn <= std::max(opt->atol, opt->rtol * bn);
-        conv[s] = done ? 1 : 0;
-        hact[s] = (!done && outer < opt->max_outer && sp[s + 1] > sp[s]) ? 1 : 0;
-        n_act += hact[s];
+      SX_CHECK(launch_pcg(ctx, shp, pa, INT32_MAX, opt->max_iter));
+      kb_accumulate<<<gv, kBlock, 0, ctx->stream>>>(row_sys, n, dx, d32, rr, active);
+      ctx->launches++;
+      return refine_tail();
+    };
+    // prologue: residual of x = 0 and the first queue (eager, no condition)
+    if ((rc = refine_tail())) break;
+    int hctl[16];
+    SX_CUDA(cudaMemcpyAsync(hctl, plan.ctl, sizeof(hctl), cudaMemcpyDeviceToHost, ctx->stream));
+    SX_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int nq0 = hctl[Q_NQ];
+    if (nq0 > 0) {
+      // launch shape: the autotuner times each candidate on the largest
+      // systems of this batch (a few inner iterations each) and caches the
+      // choice under the batch's size statistics
+      int64_t maxrows = 0;
+      for (int64_t s = 0; s < S; ++s) maxrows = std::max<int64_t>(maxrows, sp[s + 1] - sp[s]);
+      const uint64_t key = tune_key(TUNE_BATCHED_PCG, tune_bucket((double)S), tune_bucket((double)maxrows),
+                                    tune_bucket((double)n / (double)std::max<int64_t>(S, 1)));
+      const int cap = std::min(nq0, ctx->num_sms * 2);
+      kb_scale_down<<<gv, kBlock, 0, ctx->stream>>>(row_sys, n, dr, rr, active, r32);
+      ctx->launches++;
+      rc = tune_pick(ctx, key, kNumPcgShapes, [&](int i) -> int {
+        SX_CUDA(cudaMemsetAsync(plan.ctl + Q_NEXT, 0, sizeof(int32_t), ctx->stream));
+        return launch_pcg(ctx, i, pa, cap, std::min<unsigned long long>(opt->max_iter, 16ull));
+      }, &shape);
+      if (rc) break;
+      SX_CUDA(cudaMemsetAsync(plan.ctl + Q_NEXT, 0, sizeof(int32_t), ctx->stream));
+      SX_CUDA(cudaMemsetAsync(iters, 0, sb * 8, ctx->stream));
+      // the refinement loop as one graph: WHILE (queue not empty) { pass }
+      bool graph_ok = false;
+      cudaGraphConditionalHandle h = 0;
+      do {
+        if (cudaGraphCreate(&g, 0) != cudaSuccess) break;
+        if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) break;
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) != cudaSuccess) break;
+        cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+        if (cudaStreamBeginCaptureToGraph(ctx->stream, bodyg, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+          break;
+        const uint64_t before = ctx->launches;
+        const int brc = pass(shape);
+        ctx->launches = before;
+        cudaGraph_t cap_g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &cap_g);
+        if (brc != SX_OK || ce != cudaSuccess) break;
+        if (cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) break;
+        graph_ok = true;
+      } while (0);
+      (void)cudaGetLastError();
+      if (graph_ok) {
+        const unsigned long long hc = (unsigned long long)h;
+        const int use = 1;
+        SX_CUDA(cudaMemcpyAsync(plan.cond, &hc, 8, cudaMemcpyHostToDevice, ctx->stream));
+        SX_CUDA(cudaMemcpyAsync(plan.ctl + Q_USE_COND, &use, 4, cudaMemcpyHostToDevice, ctx->stream));
+        SX_CUDA(cudaGraphLaunch(ge, ctx->stream));
+        SX_CUDA(cudaStreamSynchronize(ctx->stream));
+      } else {
+        // no graph: the same passes from the host, until the queue empties
+        for (uint64_t k = 0; k <= opt->max_outer; ++k) {
+          if ((rc = pass(shape))) break;
+          SX_CUDA(cudaMemcpyAsync(hctl, plan.ctl, sizeof(hctl), cudaMemcpyDeviceToHost, ctx->stream));
+          SX_CUDA(cudaStreamSynchronize(ctx->stream));
+          if (hctl[Q_NQ] <= 0) break;
+        }
+        if (rc) break;
       }
-      if (n_act == 0) break;
-      SX_CUDA(cudaMemcpyAsync(active, hact.data(), S * 4, cudaMemcpyHostToDevice, ctx->stream));
-      SX_CUDA(cudaMemsetAsync(stbuf, 0, sb * (5 * 4 + 3 * 4 + 8), ctx->stream));
-      kb_scale_down<<<g, kBlock, 0, ctx->stream>>>(row_sys, n, dr, rr, active, r32);
-      ctx->launches++;
-      // inactive systems start finished so the kernels never visit them
-      std::vector<int> hstat(S);
-      for (int64_t s = 0; s < S; ++s) hstat[s] = hact[s] ? 0 : 1;
-      SX_CUDA(cudaMemcpyAsync(st.status, hstat.data(), S * 4, cudaMemcpyHostToDevice, ctx->stream));
-      if ((rc = batched_cg_core<float>(ctx, a32->csr, dinv, plan, active, n_act, r32, d32, rw, pw, qw, st,
-                                       opt->inner_rtol, 0.0, opt->max_iter, &launches))) break;
-      SX_CUDA(cudaMemcpyAsync(hit.data(), st.iterations, S * 8, cudaMemcpyDeviceToHost, ctx->stream));
-      kb_accumulate<<<g, kBlock, 0, ctx->stream>>>(row_sys, n, dx, d32, rr, active);
-      ctx->launches++;
-      SX_CUDA(cudaStreamSynchronize(ctx->stream));
-      for (int64_t s = 0; s < S; ++s)
-        if (hact[s]) inner_total[s] += hit[s];
-      ++outer;
     }
-    if (rc) break;
+    SX_CUDA(cudaMemcpyAsync(hctl, plan.ctl, sizeof(hctl), cudaMemcpyDeviceToHost, ctx->stream));
+    if (S > 0) {
+      SX_CUDA(cudaMemcpyAsync(hrel.data(), rel, S * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      SX_CUDA(cudaMemcpyAsync(hconv.data(), conv, S * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      SX_CUDA(cudaMemcpyAsync(inner_total.data(), iters, S * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    }
     const cudaMemcpyKind kout = mem == SX_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    cudaMemcpyAsync(x, dx, n * 8, kout, ctx->stream);
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) rc = cuda_fail(e, "batched solution copy", __FILE__, __LINE__);
+    SX_CUDA(cudaMemcpyAsync(x, dx, n * 8, kout, ctx->stream));
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "batched solution copy", __FILE__, __LINE__); break; }
+    outer = (uint64_t)hctl[Q_OUTER];
   } while (0);
-  dev_free(db); dev_free(dx); dev_free(dr); dev_free(rr); dev_free(bb); dev_free(r32); dev_free(d32);
-  dev_free(rw); dev_free(pw); dev_free(qw); dev_free(dinv); dev_free(row_sys); dev_free(active);
-  dev_free(stbuf);
+  if (ge) cudaGraphExecDestroy(ge);
+  if (g) cudaGraphDestroy(g);
+  dev_free(db); dev_free(dx); dev_free(dr); dev_free(rr); dev_free(bb); dev_free(rel); dev_free(r32);
+  dev_free(d32); dev_free(rw); dev_free(zw); dev_free(pw); dev_free(qw); dev_free(dinv); dev_free(row_sys);
+  dev_free(order); dev_free(queue); dev_free(dsp); dev_free(active); dev_free(conv); dev_free(iters);
   plan_free(plan);
   if (own32) destroy_op_internal(own32);
   if (rc != SX_OK) return rc;
@@ -640,13 +612,13 @@ int sx_batched_pcg(sx_ctx ctx, sx_op a64, sx_op a32, const int64_t* sys_ptr, uin
   for (int64_t s = 0; s < S; ++s) {
     if (per_system) {
       per_system[s].inner_iterations = inner_total[s];
-      per_system[s].rel_residual = rel[s];
-      per_system[s].converged = conv[s];
+      per_system[s].rel_residual = hrel[s];
+      per_system[s].converged = hconv[s];
     }
-    nconv += conv[s];
+    nconv += hconv[s];
     maxit = std::max<uint64_t>(maxit, inner_total[s]);
     totit += inner_total[s];
-    worst = std::max(worst, rel[s]);
+    worst = std::max(worst, hrel[s]);
   }
   if (summary) {
     summary->outer_iterations = outer;
@@ -654,7 +626,11 @@ int sx_batched_pcg(sx_ctx ctx, sx_op a64, sx_op a32, const int64_t* sys_ptr, uin
     summary->max_inner_iterations = maxit;
     summary->total_inner_iterations = totit;
     summary->worst_rel_residual = worst;
-    summary->kernel_launches = (ctx->launches - l0) + launches;
+    // the graph runs six kernels per pass (scale, PCG, accumulate, residual,
+    // norms, queue); the eager launches are counted as they happen
+    summary->kernel_launches = (ctx->launches - l0) + 6 * outer;
+    summary->threads_per_block = (uint32_t)kPcgShapes[shape].threads;
+    summary->blocks_per_sm = (uint32_t)kPcgShapes[shape].per_sm;
   }
   return clear_error();
 }

@@ -1040,17 +1040,13 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   SX_CUDA(cudaSetDevice(device));
   int sms = 0;
   SX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-  int smem_sm = 0;
-  SX_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device));
   sx_ctx c = new sx_ctx_s();
   c->device = device;
   c->num_sms = sms;
-  c->smem_per_sm = smem_sm;
   c->own_stream = own;
   if (const char* t = std::getenv("SX_WIN")) c->win_mode = std::atoi(t);
   if (const char* t = std::getenv("SX_DIA")) c->dia = std::atoi(t);
   if (const char* t = std::getenv("SX_DIA_ND6")) c->dia_nd6 = std::strcmp(t, "0") != 0;
-  if (const char* t = std::getenv("SX_DIA_TILE")) c->dia_tile = std::strcmp(t, "1") == 0;
   if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "1") == 0;
   if (const char* t = std::getenv("SX_MX_FUSED")) c->mx_unfused = std::strcmp(t, "0") == 0;
   if (const char* t = std::getenv("SX_SHORT")) c->short_rows = std::atoi(t);

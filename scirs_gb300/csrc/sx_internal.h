@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -162,14 +163,13 @@ struct sx_ctx_s {
   // every matrix that has it
   int dia = 1;
   bool dia_nd6 = true;  // SX_DIA_ND6=0: five or six diagonals take the 8-slot kernel
-  // SX_DIA_TILE=1: the diagonal layout runs the tiled kernel (x windows in
-  // shared memory) instead of the register-batched kernel
-  bool dia_tile = false;
-  int smem_per_sm = 0;  // shared memory per SM (bytes)
   // limit of one dependency wait of the triangular factorisations and
   // sweeps (IC(0), ILU(0), SSOR), in nanoseconds: a wait that runs longer
   // gives up and the call reports SX_ERR_DEVICE_TIMEOUT
   unsigned long long wait_ns = 2000000000ull;
+  // autotuner results of this context: a kernel family and a key made of
+  // size statistics -> the chosen launch shape (sx_tune.cuh)
+  std::map<uint64_t, uint32_t> tuned;
   int win_shape = 0;
 };
 

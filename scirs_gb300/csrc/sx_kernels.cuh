@@ -484,8 +484,9 @@ __device__ __forceinline__ void dia_shift(const T (&a)[VEC], const T (&b)[VEC], 
 // Diagonals per batch of loads: every load of a batch is issued before the
 // first product, with no condition on them (batch slots past the last
 // diagonal re-read it and are masked off), so a thread waits for memory
-// once per batch rather than once per diagonal.
-constexpr int kDiaBatch = 4;
+// once per batch.  Up to nine diagonals (every 2D and 3D stencil here) go
+// in one batch: one wait per row group.
+constexpr int kDiaBatch = 8;
 
 template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>>
 __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ vals,
@@ -495,8 +496,8 @@ __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ 
                                                           unsigned int* counter, Epi epi, Gather gat = Gather{}) {
   if (epi.skip()) return;
   constexpr int VEC = DiaVec<T>::kVec;
-  // up to six diagonals in one batch (the learned factors have five)
-  constexpr int KB = ND <= 6 ? ND : kDiaBatch;
+  // all diagonals in one batch up to nine, else batches of eight
+  constexpr int KB = ND <= 9 ? ND : kDiaBatch;
   Acc3<T> a{T(0), T(0), T(0)};
   const int n = (int)nrows;
   const int omin = offs.off[0], omax = offs.off[nd - 1];
@@ -602,144 +603,6 @@ __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ 
         epi.acc(row, v, a);
       }
     }
-  }
-  if constexpr (Epi::kReduce) {
-    Acc3<T> tot;
-    if (grid_reduce3(a, partials, counter, tot) && threadIdx.x == 0) epi.finish(tot);
-  }
-}
-
-// Tiled diagonal-layout SpMV.  A block owns a tile of TR = kBlock * VEC
-// consecutive rows; each thread VEC of them (4 in FP32, 2 in FP64).  The
-// diagonals' offsets are grouped into bands of nearby offsets; for each band
-// the tile's x window (columns r0 + lo .. r0 + TR - 1 + hi) is staged once
-// in shared memory with aligned vector loads, so that an x element serves
-// every diagonal of its band from shared memory instead of one or two global
-// vector loads per diagonal.  A thread issues all of its value loads (one
-// vector per diagonal) and its mask load before staging, so one wait on
-// memory covers every diagonal of the row group.  The window is stored with
-// an XOR swizzle inside each 32-element (FP32) / 16-element (FP64) run, which
-// makes the stride-VEC reads of a warp free of bank conflicts.  Each row's
-// sum runs over its stored diagonals in ascending offset, from zero, with
-// rounded products (or fused multiply-adds for FMA): the result is that of
-// the CSR kernels.
-struct DiaBands {
-  int32_t nb;         // bands
-  int32_t bofs[16];   // band b: first staged column relative to the tile's first row (multiple of VEC)
-  int32_t blen[16];   // band b: staged columns (multiple of VEC)
-  int32_t sbase[16];  // band b: first shared-memory element (multiple of 32)
-  int32_t dbase[16];  // diagonal d: sbase of its band
-  int32_t dsh[16];    // diagonal d: window element of the tile's first row (offset - bofs of its band)
-};
-
-template <typename T>
-__device__ __forceinline__ int dia_swz(int e) {
-  if constexpr (sizeof(T) == 4) return e ^ ((e >> 5) & 3);
-  else return e ^ ((e >> 4) & 1);
-}
-
-template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>,
-          int MINB = 1>
-__global__ void __launch_bounds__(kBlock, MINB) spmv_dia_tile_kernel(
-    const V* __restrict__ vals, const uint16_t* __restrict__ mask, int64_t ld, DiaBands bands, int nd,
-    const T* __restrict__ x, T* __restrict__ y, int64_t nrows, T* partials, unsigned int* counter, Epi epi,
-    Gather gat = Gather{}) {
-  extern __shared__ __align__(16) unsigned char dia_smem[];
-  T* sx = reinterpret_cast<T*>(dia_smem);
-  if (epi.skip()) return;
-  constexpr int VEC = DiaVec<T>::kVec;
-  constexpr int TR = kBlock * VEC;
-  const int n = (int)nrows;
-  Acc3<T> a{T(0), T(0), T(0)};
-  const int ntiles = (n + TR - 1) / TR;
-  const int lr0 = (int)threadIdx.x * VEC;
-  for (int tile = (int)blockIdx.x; tile < ntiles; tile += (int)gridDim.x) {
-    const int r0 = tile * TR;
-    const int g0 = r0 + lr0;
-    // the row group's values and masks: every load issued before any is used
-    T v[ND][VEC];
-    unsigned m[VEC];
-    if (g0 + VEC <= n) {
-      if constexpr (VEC == 4) {
-        const uint2 u = __ldg(reinterpret_cast<const uint2*>(mask + g0));
-        m[0] = u.x & 0xFFFFu; m[1] = u.x >> 16; m[2] = u.y & 0xFFFFu; m[3] = u.y >> 16;
-      } else {
-        const unsigned u = __ldg(reinterpret_cast<const unsigned*>(mask + g0));
-        m[0] = u & 0xFFFFu; m[1] = u >> 16;
-      }
-#pragma unroll
-      for (int d = 0; d < ND; ++d)
-        if (d < nd) vload(vals + (int64_t)d * ld + g0, v[d]);
-    } else {
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) m[j] = g0 + j < n ? __ldg(mask + g0 + j) : 0u;
-#pragma unroll
-      for (int d = 0; d < ND; ++d)
-        if (d < nd) {
-#pragma unroll
-          for (int j = 0; j < VEC; ++j) v[d][j] = (T)to_val(vals[(int64_t)d * ld + min(g0 + j, n - 1)]);
-        }
-    }
-    // the tile's x windows, one per band (zeros outside [0, n): only masked
-    // slots read them)
-    for (int b = 0; b < bands.nb; ++b) {
-      const int c0 = r0 + bands.bofs[b];
-      T* sb = sx + bands.sbase[b];
-      for (int k = lr0; k < bands.blen[b]; k += TR) {
-        const int c = c0 + k;
-        T o[VEC];
-        if (c >= 0 && c + VEC <= n) {
-          gat.vec(x, c, o);
-        } else {
-#pragma unroll
-          for (int j = 0; j < VEC; ++j) o[j] = (c + j >= 0 && c + j < n) ? gat(x, c + j) : T(0);
-        }
-#pragma unroll
-        for (int j = 0; j < VEC; ++j) sb[dia_swz<T>(k + j)] = o[j];
-      }
-    }
-    __syncthreads();
-    if (g0 < n) {
-      T acc[VEC];
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) acc[j] = T(0);
-#pragma unroll
-      for (int d = 0; d < ND; ++d) {
-        if (d < nd) {
-          const T* sb = sx + bands.dbase[d];
-          const int e0 = bands.dsh[d] + lr0;
-#pragma unroll
-          for (int j = 0; j < VEC; ++j) {
-            const T xv = sb[dia_swz<T>(e0 + j)];
-            if ((m[j] >> d) & 1u) {
-              if constexpr (FMA) acc[j] = fma(v[d][j], xv, acc[j]);
-              else acc[j] = add_rn(acc[j], mul_rn(v[d][j], xv));
-            }
-          }
-        }
-      }
-      bool done = false;
-      if constexpr (EpiRows4<Epi>::value && VEC == 4) {
-        if (g0 + 4 <= n) {
-          T o[4];
-          epi.out_acc4(g0, acc, o, a);
-          *reinterpret_cast<float4*>(y + g0) = make_float4(o[0], o[1], o[2], o[3]);
-          done = true;
-        }
-      }
-      if (!done) {
-#pragma unroll
-        for (int j = 0; j < VEC; ++j) {
-          const int row = g0 + j;
-          if (row < n) {
-            const T val = epi.out(row, acc[j]);
-            y[row] = val;
-            epi.acc(row, val, a);
-          }
-        }
-      }
-    }
-    __syncthreads();  // the windows are restaged for the next tile
   }
   if constexpr (Epi::kReduce) {
     Acc3<T> tot;

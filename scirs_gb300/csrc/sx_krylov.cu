@@ -90,6 +90,15 @@ struct EpiCgPap {
   }
 };
 
+// a + b c: one fused multiply-add in FP64, where GB300's FP64 pipe (two
+// lanes per clock per SM) bounds the vector updates; the reference's two
+// roundings in FP32
+template <typename T>
+__device__ __forceinline__ T axpy_rn(T a, T b, T c) {
+  if constexpr (sizeof(T) == 8) return fma(b, c, a);
+  else return add_rn(a, mul_rn(b, c));
+}
+
 // x += alpha p; r -= alpha Ap; ||r||; r.z for a fused M (iterative.rs:113-144)
 template <typename T>
 struct CgUpdate {
@@ -102,8 +111,8 @@ struct CgUpdate {
   static constexpr bool kVec4 = true;
   __device__ void elem(int64_t i, Acc3<T>& a) const {
     const T alpha = st->alpha;
-    x[i] = add_rn(x[i], mul_rn(alpha, p[i]));
-    T ri = sub_rn(r[i], mul_rn(alpha, ap[i]));
+    x[i] = axpy_rn(x[i], alpha, p[i]);
+    T ri = axpy_rn(r[i], -alpha, ap[i]);
     r[i] = ri;
     a.a += ri * ri;
     if (pf.kind != PK_GENERAL) a.b += ri * pf.apply(i, ri);
@@ -115,8 +124,8 @@ struct CgUpdate {
     if (pf.kind == PK_DIAG) dv = ldv4(pf.d + i);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      xv.v[q] = add_rn(xv.v[q], mul_rn(alpha, pv.v[q]));
-      const T ri = sub_rn(rv.v[q], mul_rn(alpha, qv.v[q]));
+      xv.v[q] = axpy_rn(xv.v[q], alpha, pv.v[q]);
+      const T ri = axpy_rn(rv.v[q], -alpha, qv.v[q]);
       rv.v[q] = ri;
       a.a += ri * ri;
       if (pf.kind == PK_DIAG) a.b += ri * mul_rn(ri, dv.v[q]);
@@ -179,7 +188,7 @@ struct CgP {
   static constexpr bool kVec4 = true;
   __device__ void elem(int64_t i, Acc3<T>&) const {
     T zi = pf.kind == PK_GENERAL ? z[i] : pf.apply(i, r[i]);
-    p[i] = add_rn(zi, mul_rn(st->beta, p[i]));
+    p[i] = axpy_rn(zi, st->beta, p[i]);
   }
   __device__ void elem4(int64_t i, Acc3<T>&) const {
     const T beta = st->beta;
@@ -199,7 +208,7 @@ struct CgP {
       }
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) pv.v[q] = add_rn(zv.v[q], mul_rn(beta, pv.v[q]));
+    for (int q = 0; q < 4; ++q) pv.v[q] = axpy_rn(zv.v[q], beta, pv.v[q]);
     stv4(p + i, pv);
   }
   __device__ void finish(const Acc3<T>&) const {

@@ -4,7 +4,6 @@
 #pragma once
 
 #include <algorithm>
-#include <cstdio>
 #include <type_traits>
 
 #include "sx_internal.h"
@@ -180,100 +179,16 @@ void launch_pipe_minb(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, co
                                                     GatherPlain<T>{});
 }
 
-// One diagonal-layout launch: as many blocks as the row groups need, at
-// most the resident blocks of every SM.
+// One diagonal-layout launch: one row group per thread, as many blocks as
+// the row groups need (a thread issues all of its group's loads at once and
+// waits once; a grid-stride loop over fewer, resident blocks measured 1.5x
+// slower on the 1024^2 Q1 matrix: two rounds of waits per thread).
 template <auto Kern, typename T, typename V, class Epi, class Gather>
 void dia_go(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
             Gather gat, const DiaOffs& offs, int64_t units) {
-  const int64_t grid =
-      std::min<int64_t>((units + kBlock - 1) / kBlock, (int64_t)ctx->num_sms * resident_blocks<Kern>());
+  const int64_t grid = std::max<int64_t>(1, (units + kBlock - 1) / kBlock);
   Kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
                                                     (T*)ra.partials, ra.counter, epi, gat);
-}
-
-// Bands of the tiled diagonal-layout kernel: consecutive offsets at most
-// kDiaBandGap apart share one staged x window.  Returns the shared memory
-// bytes per block.
-constexpr int kDiaBandGap = 32;
-constexpr int kDiaTileMaxSmem = 96 * 1024;
-template <typename T>
-int dia_bands(const DevCsr& c, DiaBands& bd) {
-  constexpr int VEC = DiaVec<T>::kVec, TR = kBlock * VEC;
-  auto floor_vec = [](int v) { return (v >= 0 ? v / VEC : -((-v + VEC - 1) / VEC)) * VEC; };
-  int band_of[16];
-  bd.nb = 0;
-  for (int d = 0; d < c.dia_n; ++d) {
-    const int off = c.dia_off[d];
-    if (d == 0 || off - c.dia_off[d - 1] > kDiaBandGap) {
-      bd.bofs[bd.nb] = floor_vec(off);
-      bd.blen[bd.nb] = 0;
-      ++bd.nb;
-    }
-    const int b = bd.nb - 1;
-    // window element of row lr on this diagonal: lr + off - bofs, for lr < TR
-    const int need = TR + off - bd.bofs[b];
-    bd.blen[b] = std::max(bd.blen[b], (need + VEC - 1) / VEC * VEC);
-    bd.dsh[d] = off - bd.bofs[b];
-    band_of[d] = b;
-  }
-  int total = 0;
-  for (int b = 0; b < bd.nb; ++b) {
-    bd.sbase[b] = total;
-    total += (bd.blen[b] + 31) / 32 * 32;
-  }
-  for (int d = 0; d < c.dia_n; ++d) bd.dbase[d] = bd.sbase[band_of[d]];
-  return total * (int)sizeof(T);
-}
-
-// Blocks of the tiled kernel one SM holds with `smem` bytes of windows: the
-// register limit (queried once per instantiation, after the opt-in to the
-// largest window size) and the shared-memory limit.
-template <auto Kern>
-int dia_tile_resident(sx_ctx ctx, int smem) {
-  static int by_regs = 0;
-  if (!by_regs) {
-    int nb = 0;
-    if (cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiaTileMaxSmem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, Kern, kBlock, 0) != cudaSuccess || nb < 1) {
-      nb = -1;
-      (void)cudaGetLastError();
-    }
-    by_regs = nb;
-  }
-  if (by_regs < 0) return -1;
-  const int by_smem = ctx->smem_per_sm / (smem + 1024);
-  return std::max(1, std::min(by_regs, by_smem));
-}
-
-template <auto Kern, typename T, typename V, class Epi, class Gather>
-bool dia_tile_go(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
-                 Gather gat, const DiaBands& bd, int smem) {
-  const int nb = dia_tile_resident<Kern>(ctx, smem);
-  if (nb <= 0) return false;
-  constexpr int TR = kBlock * DiaVec<T>::kVec;
-  const int64_t tiles = (c.nrows + TR - 1) / TR;
-  const int64_t grid = std::min<int64_t>(tiles, (int64_t)ctx->num_sms * nb);
-  Kern<<<(unsigned)grid, kBlock, smem, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, bd, c.dia_n, x, y, c.nrows,
-                                                       (T*)ra.partials, ra.counter, epi, gat);
-  return true;
-}
-
-// The tiled kernel for up to 16 diagonals; false when its windows do not fit.
-template <typename T, class Epi, bool FMA, typename V, class Gather>
-bool launch_dia_tile(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
-                     Gather gat) {
-  DiaBands bd;
-  const int smem = dia_bands<T>(c, bd);
-  if (smem > kDiaTileMaxSmem) return false;
-  if (c.dia_n <= 6)
-    return dia_tile_go<spmv_dia_tile_kernel<T, 6, Epi, FMA, V, Gather, 4>>(ctx, c, vals, x, y, epi, ra, gat, bd, smem);
-  if (c.dia_n <= 8)
-    return dia_tile_go<spmv_dia_tile_kernel<T, 8, Epi, FMA, V, Gather, 4>>(ctx, c, vals, x, y, epi, ra, gat, bd, smem);
-  if (c.dia_n <= 9)
-    return dia_tile_go<spmv_dia_tile_kernel<T, 9, Epi, FMA, V, Gather, 4>>(ctx, c, vals, x, y, epi, ra, gat, bd, smem);
-  if (c.dia_n <= 12)
-    return dia_tile_go<spmv_dia_tile_kernel<T, 12, Epi, FMA, V, Gather, 3>>(ctx, c, vals, x, y, epi, ra, gat, bd, smem);
-  return dia_tile_go<spmv_dia_tile_kernel<T, 16, Epi, FMA, V, Gather, 2>>(ctx, c, vals, x, y, epi, ra, gat, bd, smem);
 }
 
 // Diagonal-layout SpMV launch (values of type V: T, or the FP16 copy);
@@ -288,13 +203,13 @@ bool launch_dia(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Ep
   if ((reinterpret_cast<uintptr_t>(x) & 15u) != 0 ||
       (EpiRows4<Epi>::value && (reinterpret_cast<uintptr_t>(y) & 15u) != 0))
     return false;
-  if (ctx->dia_tile && launch_dia_tile<T, Epi, FMA, V, Gather>(ctx, c, vals, x, y, epi, ra, gat)) return true;
   DiaOffs offs;
   for (int q = 0; q < 16; ++q) offs.off[q] = c.dia_off[q];
   const int64_t groups = (c.nrows + DiaVec<T>::kVec - 1) / DiaVec<T>::kVec;
   if (c.dia_n <= 6 && ctx->dia_nd6)
     dia_go<spmv_dia_kernel<T, 6, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   else if (c.dia_n <= 8) dia_go<spmv_dia_kernel<T, 8, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  else if (c.dia_n <= 9) dia_go<spmv_dia_kernel<T, 9, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   else if (c.dia_n <= 12) dia_go<spmv_dia_kernel<T, 12, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   else dia_go<spmv_dia_kernel<T, 16, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   return true;
@@ -383,19 +298,9 @@ inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma
   if (c.nrows <= 0) return "none";
   if (ctx->dia && c.dia_n > 0 && c.dia_mask) {
     const bool h = half_ok && w == 4 && c.dia_vals16;
-    if (ctx->dia_tile) {
-      DiaBands bd;
-      const bool fits = (w == 8 ? dia_bands<double>(c, bd) : dia_bands<float>(c, bd)) <= kDiaTileMaxSmem;
-      if (fits) {
-        static char name[64];
-        std::snprintf(name, sizeof(name), "spmv_dia_tile_kernel<ND=%d>%s, %d bands",
-                      c.dia_n <= 6 ? 6 : c.dia_n <= 8 ? 8 : c.dia_n <= 9 ? 9 : c.dia_n <= 12 ? 12 : 16,
-                      h ? " FP16 values" : "", bd.nb);
-        return name;
-      }
-    }
     if (c.dia_n <= 6 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=6, FP16 values>" : "spmv_dia_kernel<ND=6>";
     if (c.dia_n <= 8) return h ? "spmv_dia_kernel<ND=8, FP16 values>" : "spmv_dia_kernel<ND=8>";
+    if (c.dia_n <= 9) return h ? "spmv_dia_kernel<ND=9, FP16 values>" : "spmv_dia_kernel<ND=9>";
     if (c.dia_n <= 12) return h ? "spmv_dia_kernel<ND=12, FP16 values>" : "spmv_dia_kernel<ND=12>";
     return h ? "spmv_dia_kernel<ND=16, FP16 values>" : "spmv_dia_kernel<ND=16>";
   }

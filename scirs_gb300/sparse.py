@@ -802,6 +802,8 @@ class BatchedResult:
     converged: np.ndarray
     outer_iterations: int
     kernel_launches: int
+    threads_per_block: int = 0  # launch shape the autotuner chose
+    blocks_per_sm: int = 0
 
 
 def batched_pcg(a64: Operator, sys_ptr, b, rtol=1e-8, atol=0.0, inner_rtol=1e-4, max_iter=10000,
@@ -820,7 +822,8 @@ def batched_pcg(a64: Operator, sys_ptr, b, rtol=1e-8, atol=0.0, inner_rtol=1e-4,
                          np.array([per[i].inner_iterations for i in range(nsys)], dtype=np.int64),
                          np.array([per[i].rel_residual for i in range(nsys)]),
                          np.array([bool(per[i].converged) for i in range(nsys)]),
-                         int(summ.outer_iterations), int(summ.kernel_launches))
+                         int(summ.outer_iterations), int(summ.kernel_launches),
+                         int(summ.threads_per_block), int(summ.blocks_per_sm))
 
 
 def generate_batch(nsys: int, side_min: int, side_max: int, seed: int = 0, sigma: float = 1.0):

@@ -65,3 +65,37 @@ def test_batched_rejects_bad_offsets(S, ctx):
     with pytest.raises(S.SparseError) as e:
         S.batched_pcg(a, bad, np.ones(n))
     assert e.value.variant == "DimensionMismatch"
+
+
+def test_batched_every_launch_shape(S, ctx):
+    # each candidate shape of the autotuner (forced) solves the batch to the
+    # tolerance; one shape run twice gives the same bits; the tuned shape is
+    # one of them and is cached for the next call on the same batch
+    import os
+
+    sp, ip, ix, v = S.generate_batch(40, 8, 64, seed=5, sigma=1.0)
+    n = len(ip) - 1
+    b = S.rhs_normal(2, n)
+    a = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
+    shapes = set()
+    try:
+        for k in range(6):
+            os.environ["SX_TUNE_FORCE"] = str(k)
+            r = S.batched_pcg(a, sp, b, rtol=1e-8)
+            assert r.converged.all(), k
+            shapes.add((r.threads_per_block, r.blocks_per_sm))
+            for s in range(len(sp) - 1):
+                sip, six, sv = _slice(sp, ip, ix, v, s)
+                assert O.true_rel_residual(sip, six, sv, b[sp[s]:sp[s + 1]], r.x[sp[s]:sp[s + 1]]) <= 1.0001e-8
+            if k == 2:
+                r2 = S.batched_pcg(a, sp, b, rtol=1e-8)
+                assert np.array_equal(r.x.view(np.uint8), r2.x.view(np.uint8))
+    finally:
+        os.environ.pop("SX_TUNE_FORCE", None)
+    assert len(shapes) == 6
+    r1 = S.batched_pcg(a, sp, b, rtol=1e-8)
+    r2 = S.batched_pcg(a, sp, b, rtol=1e-8)
+    assert (r1.threads_per_block, r1.blocks_per_sm) == (r2.threads_per_block, r2.blocks_per_sm)
+    assert (r1.threads_per_block, r1.blocks_per_sm) in shapes
+    assert np.array_equal(r1.x.view(np.uint8), r2.x.view(np.uint8))
+    a.close()

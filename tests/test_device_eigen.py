@@ -145,21 +145,9 @@ def test_large_power_iteration(S, ctx):
     assert abs(np.linalg.norm(x) - 1.0) < 1e-9
 
 
-@pytest.mark.parametrize("tile", ["0", "1"])
-def test_lanczos_odd_sizes_on_the_diagonal_layout(S, tile):
+def test_lanczos_odd_sizes_on_the_diagonal_layout(S, ctx):
     # odd n: the basis vectors sit one padded stride apart, so every SpMV
     # operand is aligned for the diagonal layout's vector loads
-    import os
-
-    old = os.environ.get("SX_DIA_TILE")
-    os.environ["SX_DIA_TILE"] = tile
-    try:
-        ctx = S.Context(0)
-    finally:
-        if old is None:
-            del os.environ["SX_DIA_TILE"]
-        else:
-            os.environ["SX_DIA_TILE"] = old
     rng = np.random.default_rng(5)
     ip, ix, v = S.generate("poisson2d", 21, 19)
     cases = [(_lower(ip, ix, v), rng.standard_normal(399)),
@@ -176,4 +164,3 @@ def test_lanczos_odd_sizes_on_the_diagonal_layout(S, tile):
         _close(d.eigenvalues, o["eigenvalues"], 1e-8, 1e-10)
         _close(d.eigenvectors, o["eigenvectors"], 1e-7, 1e-9)
         a.close()
-    ctx.close()

@@ -255,7 +255,7 @@ def _diag_cases(rng):
     yield "seventeen_diagonals", ip, cols.astype(np.int32), rng.uniform(-1, 1, len(cols)), False
 
 
-@pytest.mark.parametrize("env", [{}, {"SX_DIA_ND6": "0"}, {"SX_DIA_TILE": "1"}])
+@pytest.mark.parametrize("env", [{}, {"SX_DIA_ND6": "0"}])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_diagonal_layout_bit_exact(S, dtype, env):
     rng = np.random.default_rng(12)
@@ -275,16 +275,15 @@ def test_diagonal_layout_bit_exact(S, dtype, env):
     ctx.close()
 
 
-@pytest.mark.parametrize("tile", ["0", "1"])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-def test_diagonal_layout_unaligned_vectors(S, dtype, tile):
+def test_diagonal_layout_unaligned_vectors(S, dtype):
     # device vectors that do not start on 16 bytes (an odd element offset)
     # take the CSR kernels: the same bits, no misaligned vector access
     import torch
 
     from scirs_gb300 import _lib as L
 
-    ctx = _ctx_with(S, {"SX_DIA_TILE": tile})
+    ctx = S.Context(0)
     ip, ix, v = S.generate("poisson2d", 33, 31)
     n = len(ip) - 1
     vals = v.astype(dtype)
