@@ -738,13 +738,42 @@ int csr_make_half(sx_ctx ctx, DevCsr& c) {
   return SX_OK;
 }
 
+// Rows by length, longest first: a stable counting sort on the host over
+// min(length, 4096), and the counts the binned SpMV splits its work by.
+static int csr_prepare_bins(sx_ctx ctx, DevCsr& c) {
+  const int64_t n = c.nrows;
+  std::vector<int32_t> ptr(n + 1);
+  SX_CUDA(cudaMemcpyAsync(ptr.data(), c.indptr, (n + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<int64_t> start(kBinBuckets + 2, 0);
+  auto key = [&](int64_t r) { return (int)std::min<int64_t>(ptr[r + 1] - ptr[r], kBinBuckets); };
+  for (int64_t r = 0; r < n; ++r) start[kBinBuckets - key(r) + 1] += 1;  // bucket 0 = longest
+  for (int b = 0; b <= kBinBuckets; ++b) start[b + 1] += start[b];
+  std::vector<int32_t> perm(std::max<int64_t>(n, 1));
+  int64_t long_rows = 0;
+  for (int64_t r = 0; r < n; ++r) {
+    const int k = key(r);
+    perm[start[kBinBuckets - k]++] = (int32_t)r;
+    if (ptr[r + 1] - ptr[r] > kBinLong) ++long_rows;
+  }
+  SX_CHECK(dev_alloc((void**)&c.bin_perm, std::max<int64_t>(n, 1) * 4));
+  SX_CUDA(cudaMemcpyAsync(c.bin_perm, perm.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  SX_CUDA(cudaStreamSynchronize(ctx->stream));
+  c.bin_long_rows = long_rows;
+  c.bin_long_groups = (long_rows + 31) / 32;
+  return SX_OK;
+}
+
 int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
   dev_free(c.tile_row);
   dev_free(c.col16);
   dev_free(c.chunk_base);
+  dev_free(c.bin_perm);
   c.tile_row = nullptr;
   c.col16 = nullptr;
   c.chunk_base = nullptr;
+  c.bin_perm = nullptr;
+  c.bin_long_groups = c.bin_long_rows = 0;
   c.units = 0;
   if (!c.monotone || c.nnz <= 0 || c.nrows <= 0) return SX_OK;
   // only what this context's kernel choice can use: the 16-bit columns when
@@ -767,6 +796,7 @@ int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
     return cuda_fail(e, "tile rows", __FILE__, __LINE__);
   }
   c.units = units;
+  if (ctx->bin && c.max_row_len > kBinLong) SX_CHECK(csr_prepare_bins(ctx, c));
   return SX_OK;
 }
 
@@ -943,6 +973,8 @@ static void free_csr(DevCsr& c) {
   dev_free(c.indices);
   dev_free(c.vals);
   dev_free(c.tile_row);
+  dev_free(c.bin_perm);
+  c.bin_perm = nullptr;
   dev_free(c.col16);
   dev_free(c.chunk_base);
   dev_free(c.vals16);
@@ -1047,6 +1079,7 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   if (const char* t = std::getenv("SX_WIN")) c->win_mode = std::atoi(t);
   if (const char* t = std::getenv("SX_DIA")) c->dia = std::atoi(t);
   if (const char* t = std::getenv("SX_DIA_ND6")) c->dia_nd6 = std::strcmp(t, "0") != 0;
+  if (const char* t = std::getenv("SX_BIN")) c->bin = std::strcmp(t, "0") != 0;
   if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "1") == 0;
   if (const char* t = std::getenv("SX_MX_FUSED")) c->mx_unfused = std::strcmp(t, "0") == 0;
   if (const char* t = std::getenv("SX_SHORT")) c->short_rows = std::atoi(t);
@@ -1478,6 +1511,7 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
   SX_CUDA(cudaSetDevice(ctx->device));
   DevCsr c = a->csr;
   c.indptr = nullptr; c.indices = nullptr; c.vals = nullptr; c.tile_row = nullptr; c.units = 0;
+  c.bin_perm = nullptr;
   c.col16 = nullptr; c.chunk_base = nullptr; c.vals16 = nullptr;
   c.dia_vals = nullptr; c.dia_vals16 = nullptr; c.dia_mask = nullptr;
   const int64_t n = a->csr.nnz;

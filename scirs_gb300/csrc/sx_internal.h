@@ -72,6 +72,12 @@ struct DevCsr {
   // set for monotone matrices with indptr[0] == 0 and nnz > 0
   int32_t* tile_row = nullptr;
   int64_t units = 0;
+  // rows ordered by length, longest first (a stable counting sort on
+  // min(length, 4096)), for the length-binned SpMV of long-row matrices;
+  // bin_long_groups: groups of 32 that hold a row longer than 32 entries,
+  // bin_long_rows: rows longer than 32 entries
+  int32_t* bin_perm = nullptr;
+  int64_t bin_long_groups = 0, bin_long_rows = 0;
   // compressed columns for the register-pipelined SpMV: col = chunk_base[r / 256]
   // + col16[k]; set when every 256-row chunk spans fewer than 65,536 columns
   uint16_t* col16 = nullptr;
@@ -163,6 +169,9 @@ struct sx_ctx_s {
   // every matrix that has it
   int dia = 1;
   bool dia_nd6 = true;  // SX_DIA_ND6=0: five or six diagonals take the 8-slot kernel
+  // SX_BIN=0: long-row matrices take the windowed SpMV instead of the
+  // length-binned one
+  bool bin = true;
   // limit of one dependency wait of the triangular factorisations and
   // sweeps (IC(0), ILU(0), SSOR), in nanoseconds: a wait that runs longer
   // gives up and the call reports SX_ERR_DEVICE_TIMEOUT
@@ -197,6 +206,8 @@ uint64_t next_op_serial();
 // buffer that captured graphs reference is reallocated
 void solver_graphs_drop(sx_ctx ctx);
 constexpr int kUnit = 256;  // nonzeros per tile_row entry
+constexpr int kBinLong = 32;       // rows longer than this are long (binned SpMV)
+constexpr int kBinBuckets = 4096;  // the length order's key is min(length, kBinBuckets)
 // builds what the context's SpMV choice can use: c.tile_row for the
 // windowed SpMV, and (SX_COL16=1, where the column spans allow) c.col16 /
 // c.chunk_base for the register pipeline (allocates and synchronises)

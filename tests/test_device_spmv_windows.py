@@ -80,6 +80,27 @@ def test_window_boundaries_bit_exact(S, dtype, shape):
     c.close()
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_length_binned_bit_exact(S, ctx, dtype):
+    # the default for long-row matrices: rows ordered by length, long groups
+    # summed by one lane each after the block staged their products; rows
+    # longer than the sort's 4096 cap, empty rows, one-entry rows
+    rng = np.random.default_rng(23)
+    seen = 0
+    for name, lengths in _cases(rng):
+        ncols = 8000
+        ip, ix, v = _from_lengths(rng, lengths, ncols)
+        n = len(ip) - 1
+        vals = v.astype(dtype)
+        a = S.csr_from_arrays(ctx, ip, ix, vals, (n, ncols))
+        seen += S.spmv_kernel(a) == "spmv_bin_kernel"
+        x = rng.standard_normal(ncols).astype(dtype)
+        y = a.matvec(x)
+        assert np.array_equal(y.view(np.uint8), O.spmv_i32(ip, ix, vals, x).view(np.uint8)), name
+        a.close()
+    assert seen >= 3
+
+
 def test_windowed_kernel_matches_row_kernel(S):
     # the same products and sums with and without the windowed kernel
     rng = np.random.default_rng(3)
@@ -96,7 +117,8 @@ def test_windowed_kernel_matches_row_kernel(S):
     assert np.array_equal(out["0"].view(np.uint8), out["2"].view(np.uint8))
 
 
-@pytest.mark.parametrize("env", [{"SX_WIN": "0", "SX_DIA": "0"}, {"SX_WIN": "2", "SX_DIA": "0"}, {}])
+@pytest.mark.parametrize("env", [{"SX_WIN": "0", "SX_DIA": "0"}, {"SX_WIN": "2", "SX_DIA": "0"}, {},
+                                 {"SX_BIN": "0"}])
 @pytest.mark.parametrize("kind,dims", [("laplace3d", (64, 64, 64)), ("powerlaw", (300000, 1, 1))])
 def test_fp64_fma_mode_within_ulps(S, kind, dims, env):
     # the CSR kernels (row-wise, windowed) and, for the stencil, the diagonal layout
@@ -215,10 +237,15 @@ def test_kernel_choice_names(S, ctx):
     ip, ix, v = S.generate("powerlaw", 50000, 1, 1, seed=2, param0=16.0, param1=4096.0)
     n = len(ip) - 1
     p = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
-    assert S.spmv_kernel(p) == "spmv_win_kernel"
-    for op in (a32, a64, b32, b64, p):
+    assert S.spmv_kernel(p) == "spmv_bin_kernel"
+    assert S.spmv_kernel(p, exact=False) == "spmv_bin_kernel<FMA>"
+    cw = _ctx_with(S, {"SX_BIN": "0"})
+    pw = S.csr_from_arrays(cw, ip, ix, v, (n, n))
+    assert S.spmv_kernel(pw) == "spmv_win_kernel"
+    for op in (a32, a64, b32, b64, p, pw):
         op.close()
     c.close()
+    cw.close()
 
 
 def _diag_cases(rng):
