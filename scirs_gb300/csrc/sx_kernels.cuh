@@ -484,20 +484,22 @@ __device__ __forceinline__ void dia_shift(const T (&a)[VEC], const T (&b)[VEC], 
 // Diagonals per batch of loads: every load of a batch is issued before the
 // first product, with no condition on them (batch slots past the last
 // diagonal re-read it and are masked off), so a thread waits for memory
-// once per batch.  Up to nine diagonals (every 2D and 3D stencil here) go
-// in one batch: one wait per row group.
-constexpr int kDiaBatch = 8;
+// once per batch rather than once per diagonal.  (All nine diagonals of a
+// 2D stencil in one batch measured no faster on the 1024^2 Q1 matrix and
+// slower on the 3D ones: 104-206 registers per thread in the fused solver
+// kernels instead of 64-80.)
+constexpr int kDiaBatch = 4;
 
 template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>>
-__global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ vals,
+__global__ void __launch_bounds__(kBlock, 2) spmv_dia_kernel(const V* __restrict__ vals,
                                                           const uint16_t* __restrict__ mask, int64_t ld,
                                                           DiaOffs offs, int nd, const T* __restrict__ x,
                                                           T* __restrict__ y, int64_t nrows, T* partials,
                                                           unsigned int* counter, Epi epi, Gather gat = Gather{}) {
   if (epi.skip()) return;
   constexpr int VEC = DiaVec<T>::kVec;
-  // all diagonals in one batch up to nine, else batches of eight
-  constexpr int KB = ND <= 9 ? ND : kDiaBatch;
+  // up to six diagonals in one batch (the learned factors have five)
+  constexpr int KB = ND <= 6 ? ND : kDiaBatch;
   Acc3<T> a{T(0), T(0), T(0)};
   const int n = (int)nrows;
   const int omin = offs.off[0], omax = offs.off[nd - 1];
@@ -520,29 +522,29 @@ __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ 
         const unsigned u = __ldg(reinterpret_cast<const unsigned*>(mask + r0));
         m[0] = u & 0xFFFFu; m[1] = u >> 16;
       }
+      // every diagonal's values of the group first (one vector each, the
+      // loads that go to HBM); then, diagonal by diagonal, the two aligned
+      // x vectors (mostly L1/L2 hits) and the products.  Batching the x
+      // loads with the values as well measured 1.45x slower on the 1024^2
+      // Q1 matrix: they hold registers the value loads need.
+      T v[ND][VEC];
 #pragma unroll
-      for (int d0 = 0; d0 < ND; d0 += KB) {
-        if (d0 < nd) {
-          T v[KB][VEC], xa[KB][VEC], xb[KB][VEC];
+      for (int d = 0; d < ND; ++d)
+        if (d < nd) vload(vals + (int64_t)d * ld + r0, v[d]);
 #pragma unroll
-          for (int t = 0; t < KB; ++t) {
-            const int d = min(d0 + t, nd - 1);
-            vload(vals + (int64_t)d * ld + r0, v[t]);
-            const int c = r0 + offs.off[d] - (offs.off[d] & (VEC - 1));
-            gat.vec(x, c, xa[t]);
-            gat.vec(x, c + VEC, xb[t]);
-          }
+      for (int d = 0; d < ND; ++d) {
+        if (d < nd) {
+          const int off = offs.off[d];
+          const int c = r0 + off - (off & (VEC - 1));
+          T xa[VEC], xb[VEC], xv[VEC];
+          gat.vec(x, c, xa);
+          gat.vec(x, c + VEC, xb);
+          dia_shift<T, VEC>(xa, xb, off & (VEC - 1), xv);
 #pragma unroll
-          for (int t = 0; t < KB; ++t) {
-            const int d = d0 + t;
-            T xv[VEC];
-            dia_shift<T, VEC>(xa[t], xb[t], offs.off[min(d, nd - 1)] & (VEC - 1), xv);
-#pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-              if (d < nd && ((m[j] >> d) & 1u)) {
-                if constexpr (FMA) acc[j] = fma(v[t][j], xv[j], acc[j]);
-                else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[j]));
-              }
+          for (int j = 0; j < VEC; ++j) {
+            if ((m[j] >> d) & 1u) {
+              if constexpr (FMA) acc[j] = fma(v[d][j], xv[j], acc[j]);
+              else acc[j] = add_rn(acc[j], mul_rn(v[d][j], xv[j]));
             }
           }
         }
@@ -583,16 +585,28 @@ __global__ void __launch_bounds__(kBlock) spmv_dia_kernel(const V* __restrict__ 
         }
       }
     }
-    if constexpr (EpiRows4<Epi>::value && VEC == 4) {
-      if (r0 + 4 <= n) {
-        // the epilogue's four rows with vector loads issued together (the
-        // row-by-row form waits on each row's loads after the previous
-        // row's stores, which may alias them)
-        T o[4];
+    if (r0 + VEC <= n) {
+      // the group's VEC results with one 16-byte store; epilogues with a
+      // four-row form issue their vector loads together (the row-by-row form
+      // waits on each row's loads after the previous row's stores, which
+      // may alias them)
+      T o[VEC];
+      bool done = false;
+      if constexpr (EpiRows4<Epi>::value && VEC == 4) {
         epi.out_acc4(r0, acc, o, a);
-        *reinterpret_cast<float4*>(y + r0) = make_float4(o[0], o[1], o[2], o[3]);
-        continue;
+        done = true;
       }
+      if (!done) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) o[j] = epi.out(r0 + j, acc[j]);
+      }
+      if constexpr (VEC == 4) *reinterpret_cast<float4*>(y + r0) = make_float4(o[0], o[1], o[2], o[3]);
+      else *reinterpret_cast<double2*>(y + r0) = make_double2(o[0], o[1]);
+      if (!done) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) epi.acc(r0 + j, o[j], a);
+      }
+      continue;
     }
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {

@@ -201,14 +201,13 @@ void launch_pipe_minb(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, co
                                                     GatherPlain<T>{});
 }
 
-// One diagonal-layout launch: one row group per thread, as many blocks as
-// the row groups need (a thread issues all of its group's loads at once and
-// waits once; a grid-stride loop over fewer, resident blocks measured 1.5x
-// slower on the 1024^2 Q1 matrix: two rounds of waits per thread).
+// One diagonal-layout launch: as many blocks as the row groups need, at
+// most the resident blocks of every SM.
 template <auto Kern, typename T, typename V, class Epi, class Gather>
 void dia_go(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
             Gather gat, const DiaOffs& offs, int64_t units) {
-  const int64_t grid = std::max<int64_t>(1, (units + kBlock - 1) / kBlock);
+  const int64_t grid =
+      std::min<int64_t>((units + kBlock - 1) / kBlock, (int64_t)ctx->num_sms * resident_blocks<Kern>());
   Kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
                                                     (T*)ra.partials, ra.counter, epi, gat);
 }
@@ -219,12 +218,10 @@ template <typename T, class Epi, bool FMA, typename V = T, class Gather = Gather
 bool launch_dia(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
                 int64_t /*blocks*/, Gather gat = Gather{}) {
   if (!ctx->dia || !vals || c.dia_n <= 0 || !c.dia_mask) return false;
-  // the layout's kernels read x, and store y for the four-row epilogues, with
-  // 16-byte vectors: a caller's vector at another alignment (a basis vector
-  // at an odd offset, say) takes the CSR kernels instead
-  if ((reinterpret_cast<uintptr_t>(x) & 15u) != 0 ||
-      (EpiRows4<Epi>::value && (reinterpret_cast<uintptr_t>(y) & 15u) != 0))
-    return false;
+  // the layout's kernels read x and store y with 16-byte vectors: a caller's
+  // vector at another alignment (a basis vector at an odd offset, say) takes
+  // the CSR kernels instead
+  if ((reinterpret_cast<uintptr_t>(x) & 15u) != 0 || (reinterpret_cast<uintptr_t>(y) & 15u) != 0) return false;
   DiaOffs offs;
   for (int q = 0; q < 16; ++q) offs.off[q] = c.dia_off[q];
   const int64_t groups = (c.nrows + DiaVec<T>::kVec - 1) / DiaVec<T>::kVec;

@@ -10,12 +10,13 @@
 //
 // Exact mode (the reference's order: sum = 0, then sum = sum + a*x in
 // storage order, products rounded, csr.rs:479-497):
-//  - long groups (the first bin_nlong_groups groups, rows up to thousands
-//    of entries): one thread block per group.  Its 8 warps load eight
-//    32-entry chunks of every row of the group with coalesced loads, form
-//    the rounded products and stage them in shared memory; then lane r of
-//    warp 0 adds row r's products in storage order.  A row's entries are
-//    thus loaded by 8 warps in parallel while its sum stays sequential.
+//  - long groups (the first bin_long_groups groups, rows up to thousands
+//    of entries): one thread block per group.  Round by round, its 256
+//    threads load 256 consecutive entries of every row of the group with
+//    coalesced loads, form the rounded products and stage them in shared
+//    memory; then lane r of warp 0 adds row r's products in storage order.
+//    A row's entries are thus loaded by the whole block while its sum stays
+//    sequential.
 //  - short groups (rows of at most 32 entries): one warp per group, lane r
 //    walks row r in storage order.
 // FMA mode (solver-internal FP64, a few ulp per row): long rows get one
@@ -30,7 +31,8 @@ namespace sx {
 
 template <typename T>
 struct BinSmem {
-  T prod[kWarps][32][33];  // [chunk][row of the group][entry of the chunk]
+  T prod[32][kBlock + 1];  // [row of the group][entry of the round], padded
+  int32_t start[32], len[32];
 };
 
 template <typename T, class Epi, bool FMA>
@@ -46,40 +48,50 @@ __global__ void __launch_bounds__(kBlock) spmv_bin_kernel(
   for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
     if (it < nlong) {
       if constexpr (!FMA) {
-        // ---- exact: one long group of 32 rows per block
-        const int64_t pidx = it * 32 + lane;
-        const int32_t row = pidx < nrows ? __ldg(perm + pidx) : -1;
-        const int32_t s = row >= 0 ? __ldg(indptr + row) : 0;
-        const int32_t len = row >= 0 ? __ldg(indptr + row + 1) - s : 0;
-        int32_t lmax = len;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-        T acc = T(0);
-        for (int32_t c0 = 0; c0 < lmax; c0 += kWarps * 32) {
-          const int32_t cb = c0 + w * 32;
-          if (cb < lmax) {
+        // ---- exact: one long group of 32 rows per block.  A round covers
+        // 256 consecutive entries of every row: thread t forms the product
+        // at position c0 + t of each row (loads coalesced across threads,
+        // 16 rows' loads in flight), staged in shared memory; lane r of
+        // warp 0 then adds row r's products of the round in storage order.
+        int32_t row = -1;
+        if (w == 0) {
+          const int64_t pidx = it * 32 + lane;
+          row = pidx < nrows ? __ldg(perm + pidx) : -1;
+          const int32_t s0 = row >= 0 ? __ldg(indptr + row) : 0;
+          sm.start[lane] = s0;
+          sm.len[lane] = row >= 0 ? __ldg(indptr + row + 1) - s0 : 0;
+        }
+        __syncthreads();
+        int32_t lmax = 0;
 #pragma unroll 8
-            for (int r = 0; r < 32; ++r) {
-              const int32_t lr = __shfl_sync(0xffffffffu, len, r);
-              const int32_t sr = __shfl_sync(0xffffffffu, s, r);
-              if (cb < lr) {
-                const int32_t j = cb + lane;
-                T p = T(0);
-                if (j < lr) {
-                  const int32_t k = sr + j;
-                  p = mul_rn(__ldg(vals + k), __ldg(x + __ldg(indices + k)));
-                }
-                sm.prod[w][r][lane] = p;
-              }
+        for (int r = 0; r < 32; ++r) lmax = max(lmax, sm.len[r]);
+        T acc = T(0);
+        for (int32_t c0 = 0; c0 < lmax; c0 += kBlock) {
+          const int32_t j = c0 + (int32_t)threadIdx.x;
+#pragma unroll
+          for (int h = 0; h < 32; h += 16) {
+            int32_t col[16];
+            T v[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const bool in = j < sm.len[h + q];
+              const int32_t k = sm.start[h + q] + j;
+              col[q] = in ? __ldg(indices + k) : -1;
+              v[q] = in ? __ldg(vals + k) : T(0);
             }
+#pragma unroll
+            for (int q = 0; q < 16; ++q) sm.prod[h + q][threadIdx.x] = col[q] >= 0 ? mul_rn(v[q], __ldg(x + col[q])) : T(0);
           }
           __syncthreads();
           if (w == 0) {
-            // lane r: row r's products of this round, chunk by chunk in order
-            for (int cw = 0; cw < kWarps; ++cw) {
-              const int32_t cnt = min(32, len - (c0 + cw * 32));
-              for (int32_t j = 0; j < cnt; ++j) acc = add_rn(acc, sm.prod[cw][lane][j]);
+            const int32_t cnt = min(kBlock, sm.len[lane] - c0);
+            const T* pr = sm.prod[lane];
+            int32_t q = 0;
+            for (; q + 8 <= cnt; q += 8) {
+#pragma unroll
+              for (int u = 0; u < 8; ++u) acc = add_rn(acc, pr[q + u]);
             }
+            for (; q < cnt; ++q) acc = add_rn(acc, pr[q]);
           }
           __syncthreads();
         }
@@ -88,6 +100,7 @@ __global__ void __launch_bounds__(kBlock) spmv_bin_kernel(
           y[row] = v;
           epi.acc(row, v, a);
         }
+        __syncthreads();  // start/len are rewritten by the next group
       } else {
         // ---- FMA: one long row per warp, lane-strided, then a shuffle tree
         const int64_t pidx = it * kWarps + w;
