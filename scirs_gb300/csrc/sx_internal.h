@@ -168,7 +168,9 @@ struct sx_ctx_s {
   // diagonal layout (SX_DIA): 0 never built or used; 1 (default) used for
   // every matrix that has it
   int dia = 1;
-  bool dia_nd6 = true;  // SX_DIA_ND6=0: five or six diagonals take the 8-slot kernel
+  // SX_DIA_ND6=0: every diagonal count takes the generic (runtime-count)
+  // diagonal kernel instead of the exact-count ones
+  bool dia_nd6 = true;
   // SX_BIN=0: long-row matrices take the windowed SpMV instead of the
   // length-binned one
   bool bin = true;

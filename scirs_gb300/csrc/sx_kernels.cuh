@@ -489,6 +489,9 @@ __device__ __forceinline__ void dia_shift(const T (&a)[VEC], const T (&b)[VEC], 
 // slower on the 3D ones: 104-206 registers per thread in the fused solver
 // kernels instead of 64-80.)
 constexpr int kDiaBatch = 4;
+// the diagonal kernel for any count up to 16 (runtime count); smaller ND
+// instantiations are for exactly ND diagonals
+constexpr int kDiaGeneric = 16;
 
 template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>>
 __global__ void __launch_bounds__(kBlock, 2) spmv_dia_kernel(const V* __restrict__ vals,
@@ -498,11 +501,16 @@ __global__ void __launch_bounds__(kBlock, 2) spmv_dia_kernel(const V* __restrict
                                                           unsigned int* counter, Epi epi, Gather gat = Gather{}) {
   if (epi.skip()) return;
   constexpr int VEC = DiaVec<T>::kVec;
-  // up to six diagonals in one batch (the learned factors have five)
-  constexpr int KB = ND <= 6 ? ND : kDiaBatch;
+  // ND < kDiaGeneric: exactly ND diagonals, every loop straight-line code
+  // (runtime bounds there split the unrolled loops into branches, and the
+  // compiler then no longer issues later diagonals' x loads early: 1.45x
+  // slower on the 1024^2 Q1 matrix); ND == kDiaGeneric: nd <= ND at runtime
+  constexpr bool kExact = ND < kDiaGeneric;
+  const int ndr = kExact ? ND : nd;
+  constexpr int KB = kExact ? ND : kDiaBatch;
   Acc3<T> a{T(0), T(0), T(0)};
   const int n = (int)nrows;
-  const int omin = offs.off[0], omax = offs.off[nd - 1];
+  const int omin = offs.off[0], omax = offs.off[ndr - 1];
   const int groups = (n + VEC - 1) / VEC;
   const int stride = (int)gridDim.x * kBlock;
   for (int g = (int)blockIdx.x * kBlock + (int)threadIdx.x; g < groups; g += stride) {
@@ -522,29 +530,60 @@ __global__ void __launch_bounds__(kBlock, 2) spmv_dia_kernel(const V* __restrict
         const unsigned u = __ldg(reinterpret_cast<const unsigned*>(mask + r0));
         m[0] = u & 0xFFFFu; m[1] = u >> 16;
       }
-      // every diagonal's values of the group first (one vector each, the
-      // loads that go to HBM); then, diagonal by diagonal, the two aligned
-      // x vectors (mostly L1/L2 hits) and the products.  Batching the x
-      // loads with the values as well measured 1.45x slower on the 1024^2
-      // Q1 matrix: they hold registers the value loads need.
-      T v[ND][VEC];
+      if constexpr (kExact) {
+        // every diagonal's values of the group first (one vector each, the
+        // loads that go to HBM); then, diagonal by diagonal, the two aligned
+        // x vectors (mostly L1/L2 hits) and the products.  Batching the x
+        // loads with the values as well measured 1.45x slower on the 1024^2
+        // Q1 matrix: they hold registers the value loads need.
+        T v[ND][VEC];
 #pragma unroll
-      for (int d = 0; d < ND; ++d)
-        if (d < nd) vload(vals + (int64_t)d * ld + r0, v[d]);
+        for (int d = 0; d < ND; ++d)
+          if (d < ndr) vload(vals + (int64_t)d * ld + r0, v[d]);
 #pragma unroll
-      for (int d = 0; d < ND; ++d) {
-        if (d < nd) {
-          const int off = offs.off[d];
-          const int c = r0 + off - (off & (VEC - 1));
-          T xa[VEC], xb[VEC], xv[VEC];
-          gat.vec(x, c, xa);
-          gat.vec(x, c + VEC, xb);
-          dia_shift<T, VEC>(xa, xb, off & (VEC - 1), xv);
+        for (int d = 0; d < ND; ++d) {
+          if (d < ndr) {
+            const int off = offs.off[d];
+            const int c = r0 + off - (off & (VEC - 1));
+            T xa[VEC], xb[VEC], xv[VEC];
+            gat.vec(x, c, xa);
+            gat.vec(x, c + VEC, xb);
+            dia_shift<T, VEC>(xa, xb, off & (VEC - 1), xv);
 #pragma unroll
-          for (int j = 0; j < VEC; ++j) {
-            if ((m[j] >> d) & 1u) {
-              if constexpr (FMA) acc[j] = fma(v[d][j], xv[j], acc[j]);
-              else acc[j] = add_rn(acc[j], mul_rn(v[d][j], xv[j]));
+            for (int j = 0; j < VEC; ++j) {
+              if ((m[j] >> d) & 1u) {
+                if constexpr (FMA) acc[j] = fma(v[d][j], xv[j], acc[j]);
+                else acc[j] = add_rn(acc[j], mul_rn(v[d][j], xv[j]));
+              }
+            }
+          }
+        }
+      } else {
+        // any count: batches of KB diagonals' value and x loads
+#pragma unroll
+        for (int d0 = 0; d0 < ND; d0 += KB) {
+          if (d0 < ndr) {
+            T v[KB][VEC], xa[KB][VEC], xb[KB][VEC];
+#pragma unroll
+            for (int t = 0; t < KB; ++t) {
+              const int d = min(d0 + t, ndr - 1);
+              vload(vals + (int64_t)d * ld + r0, v[t]);
+              const int c = r0 + offs.off[d] - (offs.off[d] & (VEC - 1));
+              gat.vec(x, c, xa[t]);
+              gat.vec(x, c + VEC, xb[t]);
+            }
+#pragma unroll
+            for (int t = 0; t < KB; ++t) {
+              const int d = d0 + t;
+              T xv[VEC];
+              dia_shift<T, VEC>(xa[t], xb[t], offs.off[min(d, ndr - 1)] & (VEC - 1), xv);
+#pragma unroll
+              for (int j = 0; j < VEC; ++j) {
+                if (d < ndr && ((m[j] >> d) & 1u)) {
+                  if constexpr (FMA) acc[j] = fma(v[t][j], xv[j], acc[j]);
+                  else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[j]));
+                }
+              }
             }
           }
         }
@@ -559,11 +598,11 @@ __global__ void __launch_bounds__(kBlock, 2) spmv_dia_kernel(const V* __restrict
       for (int j = 0; j < VEC; ++j) m[j] = r0 + j < n ? __ldg(mask + r0 + j) : 0u;
 #pragma unroll
       for (int d0 = 0; d0 < ND; d0 += KB) {
-        if (d0 < nd) {
+        if (d0 < ndr) {
           T v[KB][VEC], xv[KB][VEC];
 #pragma unroll
           for (int t = 0; t < KB; ++t) {
-            const int d = min(d0 + t, nd - 1);
+            const int d = min(d0 + t, ndr - 1);
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
               const int row = min(r0 + j, n - 1);
@@ -576,7 +615,7 @@ __global__ void __launch_bounds__(kBlock, 2) spmv_dia_kernel(const V* __restrict
             const int d = d0 + t;
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
-              if (d < nd && ((m[j] >> d) & 1u)) {
+              if (d < ndr && ((m[j] >> d) & 1u)) {
                 if constexpr (FMA) acc[j] = fma(v[t][j], xv[t][j], acc[j]);
                 else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[t][j]));
               }

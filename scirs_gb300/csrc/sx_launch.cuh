@@ -225,12 +225,13 @@ bool launch_dia(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Ep
   DiaOffs offs;
   for (int q = 0; q < 16; ++q) offs.off[q] = c.dia_off[q];
   const int64_t groups = (c.nrows + DiaVec<T>::kVec - 1) / DiaVec<T>::kVec;
-  if (c.dia_n <= 6 && ctx->dia_nd6)
-    dia_go<spmv_dia_kernel<T, 6, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
-  else if (c.dia_n <= 8) dia_go<spmv_dia_kernel<T, 8, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
-  else if (c.dia_n <= 9) dia_go<spmv_dia_kernel<T, 9, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
-  else if (c.dia_n <= 12) dia_go<spmv_dia_kernel<T, 12, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
-  else dia_go<spmv_dia_kernel<T, 16, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  // exact-count kernels for the stencils here (5: 2D 5-point and the learned
+  // factors, 7: 3D 7-point, 9: 2D Q1), the generic one for any other count
+  // (and for every count with SX_DIA_ND6=0)
+  if (c.dia_n == 5 && ctx->dia_nd6) dia_go<spmv_dia_kernel<T, 5, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  else if (c.dia_n == 7 && ctx->dia_nd6) dia_go<spmv_dia_kernel<T, 7, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  else if (c.dia_n == 9 && ctx->dia_nd6) dia_go<spmv_dia_kernel<T, 9, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+  else dia_go<spmv_dia_kernel<T, kDiaGeneric, Epi, FMA, V, Gather>>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
   return true;
 }
 
@@ -317,10 +318,9 @@ inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma
   if (c.nrows <= 0) return "none";
   if (ctx->dia && c.dia_n > 0 && c.dia_mask) {
     const bool h = half_ok && w == 4 && c.dia_vals16;
-    if (c.dia_n <= 6 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=6, FP16 values>" : "spmv_dia_kernel<ND=6>";
-    if (c.dia_n <= 8) return h ? "spmv_dia_kernel<ND=8, FP16 values>" : "spmv_dia_kernel<ND=8>";
-    if (c.dia_n <= 9) return h ? "spmv_dia_kernel<ND=9, FP16 values>" : "spmv_dia_kernel<ND=9>";
-    if (c.dia_n <= 12) return h ? "spmv_dia_kernel<ND=12, FP16 values>" : "spmv_dia_kernel<ND=12>";
+    if (c.dia_n == 5 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=5, FP16 values>" : "spmv_dia_kernel<ND=5>";
+    if (c.dia_n == 7 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=7, FP16 values>" : "spmv_dia_kernel<ND=7>";
+    if (c.dia_n == 9 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=9, FP16 values>" : "spmv_dia_kernel<ND=9>";
     return h ? "spmv_dia_kernel<ND=16, FP16 values>" : "spmv_dia_kernel<ND=16>";
   }
   if (c.tile_row && ctx->win_mode == 1 && !pipe_fits && ctx->bin && c.bin_perm)

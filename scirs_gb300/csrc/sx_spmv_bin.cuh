@@ -72,15 +72,18 @@ __global__ void __launch_bounds__(kBlock) spmv_bin_kernel(
           for (int h = 0; h < 32; h += 16) {
             int32_t col[16];
             T v[16];
+            // unconditional loads at clamped, always valid positions (so
+            // the 16 rows' loads issue back to back); positions past a
+            // row's end are masked when summed, not here
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
-              const bool in = j < sm.len[h + q];
-              const int32_t k = sm.start[h + q] + j;
-              col[q] = in ? __ldg(indices + k) : -1;
-              v[q] = in ? __ldg(vals + k) : T(0);
+              const int32_t lq = sm.len[h + q];
+              const int32_t k = lq > 0 ? sm.start[h + q] + min(j, lq - 1) : 0;
+              col[q] = __ldg(indices + k);
+              v[q] = __ldg(vals + k);
             }
 #pragma unroll
-            for (int q = 0; q < 16; ++q) sm.prod[h + q][threadIdx.x] = col[q] >= 0 ? mul_rn(v[q], __ldg(x + col[q])) : T(0);
+            for (int q = 0; q < 16; ++q) sm.prod[h + q][threadIdx.x] = mul_rn(v[q], __ldg(x + col[q]));
           }
           __syncthreads();
           if (w == 0) {

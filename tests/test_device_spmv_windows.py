@@ -215,16 +215,17 @@ def test_kernel_choice_names(S, ctx):
     a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
     a32 = a64.astype(np.float32)
     # default (SX_DIA=1): the diagonal layout for FP64 and FP32 (7 diagonals)
-    assert S.spmv_kernel(a32) == "spmv_dia_kernel<ND=8>"
-    assert S.spmv_kernel(a64, exact=False) == "spmv_dia_kernel<ND=8>"
-    assert S.spmv_kernel(a64, exact=True) == "spmv_dia_kernel<ND=8>"
-    # five diagonals (the 2D 5-point stencil): the six-slot kernel, one batch
+    assert S.spmv_kernel(a32) == "spmv_dia_kernel<ND=7>"
+    assert S.spmv_kernel(a64, exact=False) == "spmv_dia_kernel<ND=7>"
+    assert S.spmv_kernel(a64, exact=True) == "spmv_dia_kernel<ND=7>"
+    # five diagonals (the 2D 5-point stencil): the exact-count kernel; the
+    # generic one with SX_DIA_ND6=0
     ip5, ix5, v5 = S.generate("poisson2d", 40, 40)
     f32 = S.csr_from_arrays(ctx, ip5, ix5, v5.astype(np.float32), (1600, 1600))
-    assert S.spmv_kernel(f32) == "spmv_dia_kernel<ND=6>"
+    assert S.spmv_kernel(f32) == "spmv_dia_kernel<ND=5>"
     c2 = _ctx_with(S, {"SX_DIA_ND6": "0"})
     d32 = S.csr_from_arrays(c2, ip5, ix5, v5.astype(np.float32), (1600, 1600))
-    assert S.spmv_kernel(d32) == "spmv_dia_kernel<ND=8>"
+    assert S.spmv_kernel(d32) == "spmv_dia_kernel<ND=16>"
     d32.close()
     f32.close()
     c2.close()
