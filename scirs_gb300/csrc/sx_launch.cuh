@@ -323,7 +323,7 @@ inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma
     if (c.dia_n == 9 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=9, FP16 values>" : "spmv_dia_kernel<ND=9>";
     return h ? "spmv_dia_kernel<ND=16, FP16 values>" : "spmv_dia_kernel<ND=16>";
   }
-  if (c.tile_row && ctx->win_mode == 1 && !pipe_fits && ctx->bin && c.bin_perm)
+  if (w == 8 && c.tile_row && ctx->win_mode == 1 && !pipe_fits && ctx->bin && c.bin_perm)
     return fma ? "spmv_bin_kernel<FMA>" : "spmv_bin_kernel";
   if (c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) return "spmv_win_kernel";
   if (ctx->short_rows && (fma || (w == 4 && ctx->short_rows == 2)) && c.monotone && c.max_row_len <= 16)
@@ -352,7 +352,11 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
     if (c.dia_vals16) done = launch_dia<T, Epi, FMA, __half>(ctx, c, (const __half*)c.dia_vals16, x, y, epi, ra, blocks);
   }
   if (!done) done = launch_dia<T, Epi, FMA>(ctx, c, (const T*)c.dia_vals, x, y, epi, ra, blocks);
-  if (!done && c.tile_row && ctx->win_mode == 1 && !pipe_fits) done = launch_bin<T, Epi, FMA>(ctx, c, x, y, epi, ra, blocks);
+  // long rows: the length-binned kernel in FP64 (all lanes busy on the thin
+  // FP64 pipe); FP32 keeps the windowed kernel, faster there (424 vs 502 us
+  // on the 4M-row power-law matrix)
+  if (!done && sizeof(T) == 8 && c.tile_row && ctx->win_mode == 1 && !pipe_fits)
+    done = launch_bin<T, Epi, FMA>(ctx, c, x, y, epi, ra, blocks);
   if (!done && c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) {
     switch (ctx->win_shape) {
       case 1: done = launch_win<T, 1, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;

@@ -80,8 +80,7 @@ def test_window_boundaries_bit_exact(S, dtype, shape):
     c.close()
 
 
-@pytest.mark.parametrize("dtype", [np.float64, np.float32])
-def test_length_binned_bit_exact(S, ctx, dtype):
+def test_length_binned_bit_exact(S, ctx):
     # the default for long-row matrices: rows ordered by length, long groups
     # summed by one lane each after the block staged their products; rows
     # longer than the sort's 4096 cap, empty rows, one-entry rows
@@ -91,10 +90,10 @@ def test_length_binned_bit_exact(S, ctx, dtype):
         ncols = 8000
         ip, ix, v = _from_lengths(rng, lengths, ncols)
         n = len(ip) - 1
-        vals = v.astype(dtype)
+        vals = v.astype(np.float64)
         a = S.csr_from_arrays(ctx, ip, ix, vals, (n, ncols))
         seen += S.spmv_kernel(a) == "spmv_bin_kernel"
-        x = rng.standard_normal(ncols).astype(dtype)
+        x = rng.standard_normal(ncols)
         y = a.matvec(x)
         assert np.array_equal(y.view(np.uint8), O.spmv_i32(ip, ix, vals, x).view(np.uint8)), name
         a.close()
@@ -240,6 +239,9 @@ def test_kernel_choice_names(S, ctx):
     p = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
     assert S.spmv_kernel(p) == "spmv_bin_kernel"
     assert S.spmv_kernel(p, exact=False) == "spmv_bin_kernel<FMA>"
+    p32 = p.astype(np.float32)
+    assert S.spmv_kernel(p32) == "spmv_win_kernel"
+    p32.close()
     cw = _ctx_with(S, {"SX_BIN": "0"})
     pw = S.csr_from_arrays(cw, ip, ix, v, (n, n))
     assert S.spmv_kernel(pw) == "spmv_win_kernel"
