@@ -738,9 +738,52 @@ int csr_make_half(sx_ctx ctx, DevCsr& c) {
   return SX_OK;
 }
 
-// Rows by length, longest first: a stable counting sort on the host over
-// min(length, 4096), and the counts the binned SpMV splits its work by.
-static int csr_prepare_bins(sx_ctx ctx, DevCsr& c) {
+// Sliced layout fill: one warp per slice, lane q copies row q of the slice
+// (rows in bin_perm order) to positions sl_base[s] + 32 j + q, zero past the
+// row's end (column 0: a valid index, never summed).
+template <typename T>
+__global__ void k_sliced_fill(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                              const T* __restrict__ val, const int32_t* __restrict__ perm,
+                              const int64_t* __restrict__ base, int64_t nrows, int64_t nslices, int32_t* scols,
+                              T* svals) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x / 32);
+  for (int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; s < nslices; s += nwarps) {
+    const int64_t B = base[s];
+    const int32_t Lg = (int32_t)((base[s + 1] - B) / 32);
+    const int64_t p = s * 32 + lane;
+    int32_t st = 0, len = 0;
+    if (p < nrows) {
+      const int32_t r = perm[p];
+      st = ptr[r];
+      len = ptr[r + 1] - st;
+    }
+    for (int32_t j = 0; j < Lg; ++j) {
+      const bool in = j < len;
+      scols[B + (int64_t)j * 32 + lane] = in ? idx[st + j] : 0;
+      svals[B + (int64_t)j * 32 + lane] = in ? val[st + j] : T(0);
+    }
+  }
+}
+
+void free_sliced(DevCsr& c) {
+  dev_free(c.bin_perm);
+  dev_free(c.sl_cols);
+  dev_free(c.sl_vals);
+  dev_free(c.sl_base);
+  dev_free(c.sl_len);
+  c.bin_perm = nullptr;
+  c.sl_cols = nullptr;
+  c.sl_vals = nullptr;
+  c.sl_base = nullptr;
+  c.sl_len = nullptr;
+  c.sl_slices = c.sl_big = c.sl_short = 0;
+}
+
+// Rows by length, longest first (a stable counting sort on the host over
+// min(length, 4096)), and the sliced layout over that order: slice bases
+// and row lengths on the host, the columns and values by k_sliced_fill.
+static int csr_prepare_sliced(sx_ctx ctx, DevCsr& c, int w) {
   const int64_t n = c.nrows;
   std::vector<int32_t> ptr(n + 1);
   SX_CUDA(cudaMemcpyAsync(ptr.data(), c.indptr, (n + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -750,30 +793,63 @@ static int csr_prepare_bins(sx_ctx ctx, DevCsr& c) {
   for (int64_t r = 0; r < n; ++r) start[kBinBuckets - key(r) + 1] += 1;  // bucket 0 = longest
   for (int b = 0; b <= kBinBuckets; ++b) start[b + 1] += start[b];
   std::vector<int32_t> perm(std::max<int64_t>(n, 1));
-  int64_t long_rows = 0;
-  for (int64_t r = 0; r < n; ++r) {
-    const int k = key(r);
-    perm[start[kBinBuckets - k]++] = (int32_t)r;
-    if (ptr[r + 1] - ptr[r] > kBinLong) ++long_rows;
+  for (int64_t r = 0; r < n; ++r) perm[start[kBinBuckets - key(r)]++] = (int32_t)r;
+  const int64_t ns = (n + 31) / 32;
+  std::vector<int32_t> len(ns * 32, 0);
+  std::vector<int64_t> base(ns + 1, 0);
+  int64_t big = 0, shrt = 0;
+  for (int64_t s = 0; s < ns; ++s) {
+    int32_t lmax = 0;
+    for (int q = 0; q < 32 && s * 32 + q < n; ++q) {
+      const int32_t r = perm[s * 32 + q];
+      len[s * 32 + q] = ptr[r + 1] - ptr[r];
+      lmax = std::max(lmax, len[s * 32 + q]);
+    }
+    base[s + 1] = base[s] + 32 * (int64_t)lmax;
+    // the length order makes both sets prefixes of the slices
+    if (lmax > kSlBig) big = s + 1;
+    if (lmax > kSlShort) shrt = s + 1;
   }
-  SX_CHECK(dev_alloc((void**)&c.bin_perm, std::max<int64_t>(n, 1) * 4));
-  SX_CUDA(cudaMemcpyAsync(c.bin_perm, perm.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream));
-  SX_CUDA(cudaStreamSynchronize(ctx->stream));
-  c.bin_long_rows = long_rows;
-  c.bin_long_groups = (long_rows + 31) / 32;
+  const int64_t m = std::max<int64_t>(base[ns], 1);
+  int rc = SX_OK;
+  do {
+    if ((rc = dev_alloc((void**)&c.bin_perm, std::max<int64_t>(n, 1) * 4))) break;
+    if ((rc = dev_alloc((void**)&c.sl_base, (ns + 1) * 8))) break;
+    if ((rc = dev_alloc((void**)&c.sl_len, std::max<int64_t>(ns * 32, 1) * 4))) break;
+    if ((rc = dev_alloc((void**)&c.sl_cols, m * 4))) break;
+    if ((rc = dev_alloc(&c.sl_vals, m * w))) break;
+    cudaMemcpyAsync(c.bin_perm, perm.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(c.sl_base, base.data(), (ns + 1) * 8, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(c.sl_len, len.data(), ns * 32 * 4, cudaMemcpyHostToDevice, ctx->stream);
+    const int g = (int)std::min<int64_t>((ns + kWarps - 1) / kWarps, (int64_t)ctx->num_sms * 8);
+    if (w == 8)
+      k_sliced_fill<double><<<g, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const double*)c.vals, c.bin_perm,
+                                                           c.sl_base, n, ns, c.sl_cols, (double*)c.sl_vals);
+    else
+      k_sliced_fill<float><<<g, kBlock, 0, ctx->stream>>>(c.indptr, c.indices, (const float*)c.vals, c.bin_perm,
+                                                          c.sl_base, n, ns, c.sl_cols, (float*)c.sl_vals);
+    ctx->launches++;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "sliced layout", __FILE__, __LINE__);
+  } while (0);
+  if (rc != SX_OK) {
+    free_sliced(c);
+    return rc;
+  }
+  c.sl_slices = ns;
+  c.sl_big = big;
+  c.sl_short = shrt;
   return SX_OK;
 }
 
-int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
+int csr_prepare_tiles(sx_ctx ctx, DevCsr& c, int w) {
   dev_free(c.tile_row);
   dev_free(c.col16);
   dev_free(c.chunk_base);
-  dev_free(c.bin_perm);
+  free_sliced(c);
   c.tile_row = nullptr;
   c.col16 = nullptr;
   c.chunk_base = nullptr;
-  c.bin_perm = nullptr;
-  c.bin_long_groups = c.bin_long_rows = 0;
   c.units = 0;
   if (!c.monotone || c.nnz <= 0 || c.nrows <= 0) return SX_OK;
   // only what this context's kernel choice can use: the 16-bit columns when
@@ -796,7 +872,7 @@ int csr_prepare_tiles(sx_ctx ctx, DevCsr& c) {
     return cuda_fail(e, "tile rows", __FILE__, __LINE__);
   }
   c.units = units;
-  if (ctx->bin && c.max_row_len > kBinLong) SX_CHECK(csr_prepare_bins(ctx, c));
+  if (ctx->bin && c.max_row_len > kBinLong && (w == 4 || w == 8)) SX_CHECK(csr_prepare_sliced(ctx, c, w));
   return SX_OK;
 }
 
@@ -945,7 +1021,7 @@ int csr_finalize_stats(sx_ctx ctx, DevCsr& c, int w) {
   c.has_sorted_indices = h[2] == 0;
   c.max_chunk_nnz = h[3];
   c.mean_row_len = c.nrows > 0 ? (double)c.nnz / (double)c.nrows : 0.0;
-  SX_CHECK(csr_prepare_tiles(ctx, c));
+  SX_CHECK(csr_prepare_tiles(ctx, c, w));
   return csr_prepare_dia(ctx, c, w);
 }
 
@@ -973,8 +1049,7 @@ static void free_csr(DevCsr& c) {
   dev_free(c.indices);
   dev_free(c.vals);
   dev_free(c.tile_row);
-  dev_free(c.bin_perm);
-  c.bin_perm = nullptr;
+  free_sliced(c);
   dev_free(c.col16);
   dev_free(c.chunk_base);
   dev_free(c.vals16);
@@ -1511,7 +1586,8 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
   SX_CUDA(cudaSetDevice(ctx->device));
   DevCsr c = a->csr;
   c.indptr = nullptr; c.indices = nullptr; c.vals = nullptr; c.tile_row = nullptr; c.units = 0;
-  c.bin_perm = nullptr;
+  c.bin_perm = nullptr; c.sl_cols = nullptr; c.sl_vals = nullptr; c.sl_base = nullptr; c.sl_len = nullptr;
+  c.sl_slices = c.sl_big = c.sl_short = 0;
   c.col16 = nullptr; c.chunk_base = nullptr; c.vals16 = nullptr;
   c.dia_vals = nullptr; c.dia_vals16 = nullptr; c.dia_mask = nullptr;
   const int64_t n = a->csr.nnz;
@@ -1556,7 +1632,7 @@ int sx_csr_astype(sx_ctx ctx, sx_op a, sx_dtype dtype, sx_op* out) {
     }
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) { rc = cuda_fail(e, "astype", __FILE__, __LINE__); break; }
-    rc = csr_prepare_tiles(ctx, c);
+    rc = csr_prepare_tiles(ctx, c, (int)elt_size(dtype));
   } while (0);
   if (rc != SX_OK) { free_csr(c); return rc; }
   sx_op op = new_op(ctx, SX_OP_CSR, dtype, a->nrows, a->ncols);

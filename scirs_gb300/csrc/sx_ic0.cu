@@ -47,7 +47,7 @@ void ic0_destroy(IC0Dev* p) {
   dev_free(p->L.indices);
   dev_free(p->L.vals);
   dev_free(p->L.tile_row);
-  dev_free(p->L.bin_perm);
+  free_sliced(p->L);
   dev_free(p->L.col16);
   dev_free(p->L.chunk_base);
   dev_free(p->L.vals16);

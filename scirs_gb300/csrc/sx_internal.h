@@ -73,11 +73,19 @@ struct DevCsr {
   int32_t* tile_row = nullptr;
   int64_t units = 0;
   // rows ordered by length, longest first (a stable counting sort on
-  // min(length, 4096)), for the length-binned SpMV of long-row matrices;
-  // bin_long_groups: groups of 32 that hold a row longer than 32 entries,
-  // bin_long_rows: rows longer than 32 entries
+  // min(length, 4096)), for the sliced SpMV of long-row matrices
   int32_t* bin_perm = nullptr;
-  int64_t bin_long_groups = 0, bin_long_rows = 0;
+  // sliced layout: the rows in bin_perm order, in slices of 32 rows; slice s
+  // stores position j of its row q at sl_base[s] + 32 j + q (columns and
+  // values of the handle dtype), zero-padded to its longest row;
+  // sl_len[32 s + q] = the length of that row (0 past the last row).
+  // Slices [0, sl_big) hold a row longer than kSlBig entries, slices
+  // [sl_short, sl_slices) only rows of at most kSlShort entries.
+  int32_t* sl_cols = nullptr;
+  void* sl_vals = nullptr;
+  int64_t* sl_base = nullptr;  // sl_slices + 1
+  int32_t* sl_len = nullptr;   // 32 * sl_slices
+  int64_t sl_slices = 0, sl_big = 0, sl_short = 0;
   // compressed columns for the register-pipelined SpMV: col = chunk_base[r / 256]
   // + col16[k]; set when every 256-row chunk spans fewer than 65,536 columns
   uint16_t* col16 = nullptr;
@@ -208,12 +216,18 @@ uint64_t next_op_serial();
 // buffer that captured graphs reference is reallocated
 void solver_graphs_drop(sx_ctx ctx);
 constexpr int kUnit = 256;  // nonzeros per tile_row entry
-constexpr int kBinLong = 32;       // rows longer than this are long (binned SpMV)
+constexpr int kBinLong = 32;       // a row longer than this makes a long-row matrix (sliced SpMV)
 constexpr int kBinBuckets = 4096;  // the length order's key is min(length, kBinBuckets)
+constexpr int kSlBig = 256;        // sliced layout: big slices hold a row longer than this
+constexpr int kSlShort = 4;        // sliced layout: short slices hold rows of at most this
 // builds what the context's SpMV choice can use: c.tile_row for the
-// windowed SpMV, and (SX_COL16=1, where the column spans allow) c.col16 /
-// c.chunk_base for the register pipeline (allocates and synchronises)
-int csr_prepare_tiles(sx_ctx ctx, DevCsr& c);
+// windowed SpMV, the row order and sliced layout for long-row matrices (w =
+// value bytes, 4 or 8; none for w = 0), and (SX_COL16=1, where the column
+// spans allow) c.col16 / c.chunk_base for the register pipeline (allocates
+// and synchronises)
+int csr_prepare_tiles(sx_ctx ctx, DevCsr& c, int w);
+// frees the row order and the sliced layout
+void free_sliced(DevCsr& c);
 
 
 // ------------------------------------------------------------ kernels API

@@ -8,7 +8,7 @@
 
 #include "sx_internal.h"
 #include "sx_kernels.cuh"
-#include "sx_spmv_bin.cuh"
+#include "sx_spmv_sliced.cuh"
 #include "sx_spmv_win.cuh"
 
 namespace sx {
@@ -169,24 +169,22 @@ bool launch_win(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const Re
   return true;
 }
 
-// Length-binned SpMV launch: long groups (exact) or long rows (FMA) first,
-// then the short groups, eight per block; false when the matrix has no
-// length order or the kernel cannot be resident.
+// Sliced SpMV launch (long-row matrices): big slices (exact) or their rows
+// (FMA) first, then the mid and short slices; false when the matrix has no
+// sliced layout or the kernel cannot be resident.
 template <typename T, class Epi, bool FMA>
-bool launch_bin(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const ReduceArea& ra, int64_t blocks) {
-  if (!ctx->bin || !c.bin_perm) return false;
-  constexpr auto kern = spmv_bin_kernel<T, Epi, FMA>;
-  constexpr int smem = FMA ? 0 : (int)sizeof(BinSmem<T>);
+bool launch_sliced(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, const ReduceArea& ra, int64_t blocks) {
+  if (!ctx->bin || !c.sl_vals) return false;
+  constexpr auto kern = spmv_sliced_kernel<T, Epi, FMA>;
+  constexpr int smem = FMA ? 0 : (int)sizeof(SlSmem<T>);
   const int nb = resident_blocks_smem<kern>(smem);
   if (nb <= 0) return false;
-  const int64_t nlong = FMA ? (c.bin_long_rows + kWarps - 1) / kWarps : c.bin_long_groups;
-  const int64_t sbeg = std::min<int64_t>(c.nrows, FMA ? c.bin_long_rows : c.bin_long_groups * 32);
-  const int64_t nshort = (c.nrows - sbeg + 32 * kWarps - 1) / (32 * kWarps);
-  const int64_t nitems = nlong + nshort;
-  int64_t grid = std::min<int64_t>((int64_t)ctx->num_sms * nb, nitems);
+  const SlItems items(c.sl_slices, c.sl_big, c.sl_short, FMA);
+  int64_t grid = std::min<int64_t>((int64_t)ctx->num_sms * nb, items.total);
   grid = std::max<int64_t>(1, std::min<int64_t>(grid, blocks));
-  kern<<<(unsigned)grid, kBlock, smem, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, c.bin_perm, c.nrows,
-                                                       nlong, sbeg, nitems, x, y, (T*)ra.partials, ra.counter, epi);
+  kern<<<(unsigned)grid, kBlock, smem, ctx->stream>>>(c.indptr, c.indices, (const T*)c.vals, c.bin_perm, c.sl_cols,
+                                                       (const T*)c.sl_vals, c.sl_base, c.sl_len, c.nrows, c.sl_slices,
+                                                       c.sl_big, c.sl_short, x, y, (T*)ra.partials, ra.counter, epi);
   return true;
 }
 
@@ -323,8 +321,8 @@ inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma
     if (c.dia_n == 9 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=9, FP16 values>" : "spmv_dia_kernel<ND=9>";
     return h ? "spmv_dia_kernel<ND=16, FP16 values>" : "spmv_dia_kernel<ND=16>";
   }
-  if (w == 8 && c.tile_row && ctx->win_mode == 1 && !pipe_fits && ctx->bin && c.bin_perm)
-    return fma ? "spmv_bin_kernel<FMA>" : "spmv_bin_kernel";
+  if (c.tile_row && ctx->win_mode == 1 && !pipe_fits && ctx->bin && c.sl_vals)
+    return fma ? "spmv_sliced_kernel<FMA>" : "spmv_sliced_kernel";
   if (c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) return "spmv_win_kernel";
   if (ctx->short_rows && (fma || (w == 4 && ctx->short_rows == 2)) && c.monotone && c.max_row_len <= 16)
     return c.max_row_len <= 8 ? "spmv_short_kernel<K=8>"
@@ -352,11 +350,10 @@ int launch_csr(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi) {
     if (c.dia_vals16) done = launch_dia<T, Epi, FMA, __half>(ctx, c, (const __half*)c.dia_vals16, x, y, epi, ra, blocks);
   }
   if (!done) done = launch_dia<T, Epi, FMA>(ctx, c, (const T*)c.dia_vals, x, y, epi, ra, blocks);
-  // long rows: the length-binned kernel in FP64 (all lanes busy on the thin
-  // FP64 pipe); FP32 keeps the windowed kernel, faster there (424 vs 502 us
-  // on the 4M-row power-law matrix)
-  if (!done && sizeof(T) == 8 && c.tile_row && ctx->win_mode == 1 && !pipe_fits)
-    done = launch_bin<T, Epi, FMA>(ctx, c, x, y, epi, ra, blocks);
+  // long rows: the sliced layout (coalesced loads whatever the row lengths,
+  // all lanes busy on the thin FP64 pipe)
+  if (!done && c.tile_row && ctx->win_mode == 1 && !pipe_fits)
+    done = launch_sliced<T, Epi, FMA>(ctx, c, x, y, epi, ra, blocks);
   if (!done && c.tile_row && (ctx->win_mode == 2 || (ctx->win_mode == 1 && !pipe_fits))) {
     switch (ctx->win_shape) {
       case 1: done = launch_win<T, 1, Epi, FMA>(ctx, c, x, y, epi, ra, blocks); break;

@@ -80,9 +80,11 @@ def test_window_boundaries_bit_exact(S, dtype, shape):
     c.close()
 
 
-def test_length_binned_bit_exact(S, ctx):
-    # the default for long-row matrices: rows ordered by length, long groups
-    # summed by one lane each after the block staged their products; rows
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_sliced_bit_exact(S, ctx, dtype):
+    # the default for long-row matrices: rows ordered by length in slices of
+    # 32 (big slices summed by one lane each from products staged by the
+    # block, mid slices in registers, short slices four per warp); rows
     # longer than the sort's 4096 cap, empty rows, one-entry rows
     rng = np.random.default_rng(23)
     seen = 0
@@ -90,12 +92,22 @@ def test_length_binned_bit_exact(S, ctx):
         ncols = 8000
         ip, ix, v = _from_lengths(rng, lengths, ncols)
         n = len(ip) - 1
-        vals = v.astype(np.float64)
+        vals = v.astype(dtype)
         a = S.csr_from_arrays(ctx, ip, ix, vals, (n, ncols))
-        seen += S.spmv_kernel(a) == "spmv_bin_kernel"
-        x = rng.standard_normal(ncols)
+        seen += S.spmv_kernel(a) == "spmv_sliced_kernel"
+        x = rng.standard_normal(ncols).astype(dtype)
         y = a.matvec(x)
         assert np.array_equal(y.view(np.uint8), O.spmv_i32(ip, ix, vals, x).view(np.uint8)), name
+        # x[0] = inf: rows holding column 0 become +-inf (NaN where column 0
+        # repeats with both signs) like the reference's; the padding (column
+        # 0, value 0) must never enter a sum.  A NaN's sign bit is the
+        # platform's choice (IEEE 754 leaves it open), so NaNs compare by place.
+        x[0] = np.inf
+        y = a.matvec(x)
+        yr = O.spmv_i32(ip, ix, vals, x)
+        nan = np.isnan(yr)
+        assert np.array_equal(np.isnan(y), nan), name
+        assert np.array_equal(y[~nan].view(np.uint8), yr[~nan].view(np.uint8)), name
         a.close()
     assert seen >= 3
 
@@ -237,10 +249,10 @@ def test_kernel_choice_names(S, ctx):
     ip, ix, v = S.generate("powerlaw", 50000, 1, 1, seed=2, param0=16.0, param1=4096.0)
     n = len(ip) - 1
     p = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
-    assert S.spmv_kernel(p) == "spmv_bin_kernel"
-    assert S.spmv_kernel(p, exact=False) == "spmv_bin_kernel<FMA>"
+    assert S.spmv_kernel(p) == "spmv_sliced_kernel"
+    assert S.spmv_kernel(p, exact=False) == "spmv_sliced_kernel<FMA>"
     p32 = p.astype(np.float32)
-    assert S.spmv_kernel(p32) == "spmv_win_kernel"
+    assert S.spmv_kernel(p32) == "spmv_sliced_kernel"
     p32.close()
     cw = _ctx_with(S, {"SX_BIN": "0"})
     pw = S.csr_from_arrays(cw, ip, ix, v, (n, n))
