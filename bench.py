@@ -522,6 +522,19 @@ def run_ours(args):
                                                     spmv_time(p64, pn, np.float64, flags=0, reps=10))
         p32.close()
         p64.close()
+        # the matrix's columns are uniform random: every nonzero gathers x at
+        # an unpredictable address, so the bound is this GPU's random-gather
+        # rate (measured live: pnnz gathers from an L2-resident x of pn
+        # elements), not HBM
+        rates = {}
+        for dt in (0, 1):
+            rate = C.c_double(0.0)
+            S.sparse._check(L.lib.sx_probe_gather_rate(ctx.handle, dt, pn, pnnz, C.byref(rate)))
+            rates[dt] = rate.value
+        for key, dt in (("powerlaw_4M_fp32", 0), ("powerlaw_4M_fp64", 1), ("powerlaw_4M_fp64_fma", 1)):
+            bound_us = pnnz / rates[dt] * 1e6
+            sweep[key]["gather_bound"] = {"Ggathers_per_s": rates[dt] / 1e9, "bound_us": bound_us,
+                                          "frac": bound_us / sweep[key]["us"]}
 
     workloads = run_workloads(ctx, S, once, args) if args.workloads else None
 

@@ -104,6 +104,13 @@ int sx_ctx_set_wait_limit(sx_ctx ctx, uint64_t ns);
  * outcome) and the wait's length in *waited_ns.  Checks the give-up path of
  * the dependency waits without touching any operator. */
 int sx_wait_selftest(sx_ctx ctx, uint64_t* waited_ns);
+/* Roofline probe: the rate (gathers per second) at which this GPU reads
+ * elements of an L2-resident vector of n elements (dtype SX_F32 or SX_F64)
+ * at m uniform random positions, the positions streamed with coalesced
+ * loads.  SpMV on matrices with scattered columns (power-law graphs) is
+ * bound by this rate rather than by HBM.  Allocates (n elements, m + a few
+ * MB) and synchronises.  No reference counterpart. */
+int sx_probe_gather_rate(sx_ctx ctx, sx_dtype dtype, uint64_t n, uint64_t m, double* gathers_per_s);
 /* Number of kernels this library launched on the context (graph-launched
  * kernels included), for launch accounting. */
 uint64_t sx_ctx_kernel_launches(sx_ctx ctx);

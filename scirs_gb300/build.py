@@ -33,6 +33,7 @@ SOURCES = [
     "sx_ilu.cu",
     "sx_io.cu",
     "sx_eigen.cu",
+    "sx_probe.cu",
     "sx_gen.cpp",
 ]
 
