@@ -99,7 +99,9 @@ __device__ __forceinline__ bool grid_reduce3(Acc3<T> v, T* partials, unsigned in
 // Epilogue interface (all __device__):
 //   bool skip() const                        -> whole launch is a no-op
 //   T out(int64_t row, T ax) const           -> value stored to y[row]
-//   void acc(int64_t row, T y, Acc3<T>& a)   -> per-row reduction terms
+//   void acc(int64_t row, T y, Acc3<T>& a)   -> per-row reduction terms (from
+//                                               the value y, never from memory
+//                                               at y[row])
 //   static constexpr bool kReduce            -> run the grid reduction
 //   void finish(const Acc3<T>& tot)          -> thread 0 of the last block
 template <typename T>
@@ -461,8 +463,8 @@ struct EpiRows4<E, std::void_t<decltype(&E::out_acc4)>> : std::true_type {};
 // diagonals ascend in offset, which is the storage order of the sorted CSR
 // row, and each row's sum runs over its stored diagonals in that order
 // (from zero, rounded products, or fused multiply-adds for FMA), so the
-// result is that of the CSR kernels.  Groups near the ends of the matrix,
-// where a vector load could leave [0, n), read element by element.
+// result is that of the CSR kernels.  Rows near the ends of the matrix,
+// where a vector load could leave [0, n), take a row-per-thread pass.
 struct DiaOffs {
   int32_t off[16];
 };
@@ -493,8 +495,16 @@ constexpr int kDiaBatch = 4;
 // instantiations are for exactly ND diagonals
 constexpr int kDiaGeneric = 16;
 
+// Resident blocks asked of the compiler: three for the exact-count FP32
+// kernels (at most 80 registers, every load of the vector path still in
+// flight), two otherwise (the generic and FP64 kernels would spill).
+template <typename T, int ND>
+constexpr int dia_min_blocks() {
+  return sizeof(T) == 4 && ND < 16 ? 3 : 2;
+}
+
 template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>>
-__global__ void __launch_bounds__(kBlock, 2) spmv_dia_kernel(const V* __restrict__ vals,
+__global__ void __launch_bounds__(kBlock, dia_min_blocks<T, ND>()) spmv_dia_kernel(const V* __restrict__ vals,
                                                           const uint16_t* __restrict__ mask, int64_t ld,
                                                           DiaOffs offs, int nd, const T* __restrict__ x,
                                                           T* __restrict__ y, int64_t nrows, T* partials,
@@ -513,149 +523,140 @@ __global__ void __launch_bounds__(kBlock, 2) spmv_dia_kernel(const V* __restrict
   const int omin = offs.off[0], omax = offs.off[ndr - 1];
   const int groups = (n + VEC - 1) / VEC;
   const int stride = (int)gridDim.x * kBlock;
-  for (int g = (int)blockIdx.x * kBlock + (int)threadIdx.x; g < groups; g += stride) {
+  const int tid = (int)blockIdx.x * kBlock + (int)threadIdx.x;
+  // inner groups [glo, ghi): VEC whole rows whose aligned x vectors all lie
+  // inside [0, n).  They take the vector path below; the few rows outside
+  // (near both ends) take the row path after it, so that its code does not
+  // raise the vector path's register count (a group-level branch between the
+  // two cost 40 registers per thread and a third of the resident warps).
+  const int need = VEC - omin;
+  int glo = need <= 0 ? 0 : (need + VEC - 1) / VEC;
+  const int lim = min(n - omax - 2 * VEC, n - VEC);
+  int ghi = lim < 0 ? 0 : lim / VEC + 1;
+  glo = min(glo, groups);
+  ghi = max(min(ghi, groups), glo);
+  for (int g = glo + tid; g < ghi; g += stride) {
     const int r0 = g * VEC;
     T acc[VEC];
 #pragma unroll
     for (int j = 0; j < VEC; ++j) acc[j] = T(0);
-    // every aligned x vector of the group stays inside [0, n)
-    const bool inner = r0 + omin - VEC >= 0 && r0 + omax + 2 * VEC <= n && r0 + VEC <= n;
-    if (inner) {
-      unsigned m[VEC];  // one 8- or 4-byte load (r0 is a multiple of VEC)
-      if constexpr (VEC == 4) {
-        const uint2 u = __ldg(reinterpret_cast<const uint2*>(mask + r0));
-        m[0] = u.x & 0xFFFFu; m[1] = u.x >> 16; m[2] = u.y & 0xFFFFu; m[3] = u.y >> 16;
-      } else {
-        static_assert(VEC == 2, "DIA groups are 2 or 4 rows");
-        const unsigned u = __ldg(reinterpret_cast<const unsigned*>(mask + r0));
-        m[0] = u & 0xFFFFu; m[1] = u >> 16;
-      }
-      if constexpr (kExact) {
-        // every diagonal's values of the group first (one vector each, the
-        // loads that go to HBM); then, diagonal by diagonal, the two aligned
-        // x vectors (mostly L1/L2 hits) and the products.  Batching the x
-        // loads with the values as well measured 1.45x slower on the 1024^2
-        // Q1 matrix: they hold registers the value loads need.
-        T v[ND][VEC];
+    unsigned m[VEC];  // one 8- or 4-byte load (r0 is a multiple of VEC)
+    if constexpr (VEC == 4) {
+      const uint2 u = __ldg(reinterpret_cast<const uint2*>(mask + r0));
+      m[0] = u.x & 0xFFFFu; m[1] = u.x >> 16; m[2] = u.y & 0xFFFFu; m[3] = u.y >> 16;
+    } else {
+      static_assert(VEC == 2, "DIA groups are 2 or 4 rows");
+      const unsigned u = __ldg(reinterpret_cast<const unsigned*>(mask + r0));
+      m[0] = u & 0xFFFFu; m[1] = u >> 16;
+    }
+    if constexpr (kExact) {
+      // every diagonal's values of the group first (one vector each, the
+      // loads that go to HBM); then, diagonal by diagonal, the two aligned
+      // x vectors (mostly L1/L2 hits) and the products.  Batching the x
+      // loads with the values as well measured 1.45x slower on the 1024^2
+      // Q1 matrix: they hold registers the value loads need.
+      T v[ND][VEC];
 #pragma unroll
-        for (int d = 0; d < ND; ++d)
-          if (d < ndr) vload(vals + (int64_t)d * ld + r0, v[d]);
+      for (int d = 0; d < ND; ++d) vload(vals + (int64_t)d * ld + r0, v[d]);
 #pragma unroll
-        for (int d = 0; d < ND; ++d) {
-          if (d < ndr) {
-            const int off = offs.off[d];
-            const int c = r0 + off - (off & (VEC - 1));
-            T xa[VEC], xb[VEC], xv[VEC];
-            gat.vec(x, c, xa);
-            gat.vec(x, c + VEC, xb);
-            dia_shift<T, VEC>(xa, xb, off & (VEC - 1), xv);
+      for (int d = 0; d < ND; ++d) {
+        const int off = offs.off[d];
+        const int c = r0 + off - (off & (VEC - 1));
+        T xa[VEC], xb[VEC], xv[VEC];
+        gat.vec(x, c, xa);
+        gat.vec(x, c + VEC, xb);
+        dia_shift<T, VEC>(xa, xb, off & (VEC - 1), xv);
 #pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-              if ((m[j] >> d) & 1u) {
-                if constexpr (FMA) acc[j] = fma(v[d][j], xv[j], acc[j]);
-                else acc[j] = add_rn(acc[j], mul_rn(v[d][j], xv[j]));
-              }
-            }
-          }
-        }
-      } else {
-        // any count: batches of KB diagonals' value and x loads
-#pragma unroll
-        for (int d0 = 0; d0 < ND; d0 += KB) {
-          if (d0 < ndr) {
-            T v[KB][VEC], xa[KB][VEC], xb[KB][VEC];
-#pragma unroll
-            for (int t = 0; t < KB; ++t) {
-              const int d = min(d0 + t, ndr - 1);
-              vload(vals + (int64_t)d * ld + r0, v[t]);
-              const int c = r0 + offs.off[d] - (offs.off[d] & (VEC - 1));
-              gat.vec(x, c, xa[t]);
-              gat.vec(x, c + VEC, xb[t]);
-            }
-#pragma unroll
-            for (int t = 0; t < KB; ++t) {
-              const int d = d0 + t;
-              T xv[VEC];
-              dia_shift<T, VEC>(xa[t], xb[t], offs.off[min(d, ndr - 1)] & (VEC - 1), xv);
-#pragma unroll
-              for (int j = 0; j < VEC; ++j) {
-                if (d < ndr && ((m[j] >> d) & 1u)) {
-                  if constexpr (FMA) acc[j] = fma(v[t][j], xv[j], acc[j]);
-                  else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[j]));
-                }
-              }
-            }
+        for (int j = 0; j < VEC; ++j) {
+          if ((m[j] >> d) & 1u) {
+            if constexpr (FMA) acc[j] = fma(v[d][j], xv[j], acc[j]);
+            else acc[j] = add_rn(acc[j], mul_rn(v[d][j], xv[j]));
           }
         }
       }
     } else {
-      // groups near the ends: element loads at clamped rows and columns
-      // (in bounds for every slot; the slots of absent entries are masked
-      // off), batched like the vector path so that they too are in flight
-      // together
-      unsigned m[VEC];
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) m[j] = r0 + j < n ? __ldg(mask + r0 + j) : 0u;
+      // any count: batches of KB diagonals' value and x loads
 #pragma unroll
       for (int d0 = 0; d0 < ND; d0 += KB) {
         if (d0 < ndr) {
-          T v[KB][VEC], xv[KB][VEC];
+          T v[KB][VEC], xa[KB][VEC], xb[KB][VEC];
 #pragma unroll
           for (int t = 0; t < KB; ++t) {
             const int d = min(d0 + t, ndr - 1);
-#pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-              const int row = min(r0 + j, n - 1);
-              v[t][j] = (T)to_val(vals[(int64_t)d * ld + row]);
-              xv[t][j] = gat(x, min(max(row + offs.off[d], 0), n - 1));
-            }
+            vload(vals + (int64_t)d * ld + r0, v[t]);
+            const int c = r0 + offs.off[d] - (offs.off[d] & (VEC - 1));
+            gat.vec(x, c, xa[t]);
+            gat.vec(x, c + VEC, xb[t]);
           }
 #pragma unroll
           for (int t = 0; t < KB; ++t) {
             const int d = d0 + t;
+            T xv[VEC];
+            dia_shift<T, VEC>(xa[t], xb[t], offs.off[min(d, ndr - 1)] & (VEC - 1), xv);
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
               if (d < ndr && ((m[j] >> d) & 1u)) {
-                if constexpr (FMA) acc[j] = fma(v[t][j], xv[t][j], acc[j]);
-                else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[t][j]));
+                if constexpr (FMA) acc[j] = fma(v[t][j], xv[j], acc[j]);
+                else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[j]));
               }
             }
           }
         }
       }
     }
-    if (r0 + VEC <= n) {
-      // the group's VEC results with one 16-byte store; epilogues with a
-      // four-row form issue their vector loads together (the row-by-row form
-      // waits on each row's loads after the previous row's stores, which
-      // may alias them)
-      T o[VEC];
-      bool done = false;
-      if constexpr (EpiRows4<Epi>::value && VEC == 4) {
-        epi.out_acc4(r0, acc, o, a);
-        done = true;
-      }
-      if (!done) {
+    // the group's VEC results with one 16-byte store, after the epilogue's
+    // own loads and reduction terms (acc() takes the stored value as an
+    // argument, never from y): loads placed after the store would wait
+    // for it, as they may alias y (1.5x slower FP64 CG on the 1024^2 Q1
+    // matrix).  Epilogues with a four-row form issue their vector loads
+    // together.
+    T o[VEC];
+    if constexpr (EpiRows4<Epi>::value && VEC == 4) {
+      epi.out_acc4(r0, acc, o, a);
+    } else {
 #pragma unroll
-        for (int j = 0; j < VEC; ++j) o[j] = epi.out(r0 + j, acc[j]);
-      }
-      if constexpr (VEC == 4) *reinterpret_cast<float4*>(y + r0) = make_float4(o[0], o[1], o[2], o[3]);
-      else *reinterpret_cast<double2*>(y + r0) = make_double2(o[0], o[1]);
-      if (!done) {
+      for (int j = 0; j < VEC; ++j) o[j] = epi.out(r0 + j, acc[j]);
 #pragma unroll
-        for (int j = 0; j < VEC; ++j) epi.acc(r0 + j, o[j], a);
-      }
-      continue;
+      for (int j = 0; j < VEC; ++j) epi.acc(r0 + j, o[j], a);
     }
+    if constexpr (VEC == 4) *reinterpret_cast<float4*>(y + r0) = make_float4(o[0], o[1], o[2], o[3]);
+    else *reinterpret_cast<double2*>(y + r0) = make_double2(o[0], o[1]);
+  }
+  // rows outside the inner groups, one per thread: every value and x element
+  // of the row loaded first (x at clamped, always valid columns; absent
+  // entries are masked off), then the storage-order sum.  They go to the
+  // threads counted from the end of the grid, which the grid-stride loop
+  // above gave the fewest groups.
+  const int head = min(glo * VEC, n);
+  const int nb = head + max(n - ghi * VEC, 0);
+  for (int t = stride - 1 - tid; t < nb; t += stride) {
+    const int row = t < head ? t : ghi * VEC + (t - head);
+    const unsigned mr = __ldg(mask + row);
+    constexpr int RB = kExact ? ND : 8;  // diagonals per batch of loads
+    T acc = T(0);
 #pragma unroll
-    for (int j = 0; j < VEC; ++j) {
-      const int row = r0 + j;
-      if (row < n) {
-        const T v = epi.out(row, acc[j]);
-        y[row] = v;
-        epi.acc(row, v, a);
+    for (int d0 = 0; d0 < ND; d0 += RB) {
+      if (d0 < ndr) {
+        T v[RB], xv[RB];
+#pragma unroll
+        for (int t = 0; t < RB; ++t) {
+          const int dd = min(d0 + t, ndr - 1);
+          v[t] = (T)to_val(vals[(int64_t)dd * ld + row]);
+          xv[t] = gat(x, min(max(row + offs.off[dd], 0), n - 1));
+        }
+#pragma unroll
+        for (int t = 0; t < RB; ++t) {
+          const int d = d0 + t;
+          if (d < ndr && ((mr >> d) & 1u)) {
+            if constexpr (FMA) acc = fma(v[t], xv[t], acc);
+            else acc = add_rn(acc, mul_rn(v[t], xv[t]));
+          }
+        }
       }
     }
+    const T val = epi.out(row, acc);
+    epi.acc(row, val, a);
+    y[row] = val;
   }
   if constexpr (Epi::kReduce) {
     Acc3<T> tot;
