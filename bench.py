@@ -449,8 +449,11 @@ def run_ours(args):
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            # the device waits (about 40 us per launch at 2 GHz) until the host
+            # has queued every launch, so the timed run measures the kernels
+            # back to back, not the host's issue rate
             with torch.cuda.stream(stream):
-                torch.cuda._sleep(200000)
+                torch.cuda._sleep(80000 * launches)
             e0.record(stream)
             for j in range(launches):
                 k = j % len(ops)

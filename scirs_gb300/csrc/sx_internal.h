@@ -179,8 +179,11 @@ struct sx_ctx_s {
   // SX_DIA_ND6=0: every diagonal count takes the generic (runtime-count)
   // diagonal kernel instead of the exact-count ones
   bool dia_nd6 = true;
+  // SX_DIA_BAND=0: the exact-count kernels read x per diagonal, never per
+  // band of adjacent diagonals
+  bool dia_band = true;
   // SX_BIN=0: long-row matrices take the windowed SpMV instead of the
-  // length-binned one
+  // sliced one
   bool bin = true;
   // limit of one dependency wait of the triangular factorisations and
   // sweeps (IC(0), ILU(0), SSOR), in nanoseconds: a wait that runs longer

@@ -483,6 +483,98 @@ __device__ __forceinline__ void dia_shift(const T (&a)[VEC], const T (&b)[VEC], 
     }
 }
 
+// Bands: runs of diagonals with consecutive offsets (at most three long;
+// a 2D 9-point stencil is three bands of three).  A band's x operands lie in
+// one window of three aligned vectors read once, instead of two vectors per
+// diagonal.  Bit d of a band mask is set when diagonal d starts a band.
+struct DiaBands {
+  int count;
+  int start[16];
+  int len[16];
+};
+__host__ __device__ constexpr DiaBands dia_bands(unsigned bands, int nd) {
+  DiaBands t{0, {0}, {0}};
+  for (int d = 0; d < nd; ++d) {
+    if (d == 0 || ((bands >> d) & 1u)) {
+      t.start[t.count] = d;
+      t.len[t.count] = 1;
+      ++t.count;
+    } else {
+      ++t.len[t.count - 1];
+    }
+  }
+  return t;
+}
+// the band mask of sorted offsets (runs capped at three diagonals)
+inline unsigned dia_band_mask(const int32_t* off, int nd) {
+  unsigned m = 0;
+  int run = 0;
+  for (int d = 0; d < nd; ++d) {
+    if (d == 0 || off[d] != off[d - 1] + 1 || run == 3) {
+      m |= 1u << d;
+      run = 1;
+    } else {
+      ++run;
+    }
+  }
+  return m;
+}
+// x operands of VEC rows at window position q (the window: w[0], w[1], w[2]
+// back to back), 0 <= q <= VEC + 1.  For four FP32 rows the window goes
+// through three float4 values first: this exact form compiled to a much
+// faster schedule than the same selection written over the arrays (10.6 vs
+// 12.3 us back to back on the 1024^2 Q1 matrix).
+__device__ __forceinline__ void win_shift4(const float4& a, const float4& b, const float4& c, int q, float (&o)[4]) {
+  const float t[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+  for (int sh = 0; sh < 6; ++sh)
+    if (q == sh) {
+      o[0] = t[sh];
+      o[1] = t[sh + 1];
+      o[2] = t[sh + 2];
+      o[3] = t[sh + 3];
+    }
+}
+template <typename T, int VEC>
+__device__ __forceinline__ void win_shift(const T (&w)[3][VEC], int q, T (&o)[VEC]) {
+  if constexpr (VEC == 4 && std::is_same<T, float>::value) {
+    win_shift4(make_float4(w[0][0], w[0][1], w[0][2], w[0][3]), make_float4(w[1][0], w[1][1], w[1][2], w[1][3]),
+               make_float4(w[2][0], w[2][1], w[2][2], w[2][3]), q, o);
+  } else {
+    T t[3 * VEC];
+#pragma unroll
+    for (int i = 0; i < 3 * VEC; ++i) t[i] = w[i / VEC][i % VEC];
+#pragma unroll
+    for (int sh = 0; sh <= VEC + 1; ++sh)
+      if (q == sh) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) o[j] = t[sh + j];
+      }
+  }
+}
+// Inner row groups [glo, ghi) of the diagonal layout (VEC whole rows whose
+// aligned x vectors, two per diagonal or a three-vector window per band of
+// up to three, all lie inside [0, n)) and the count of the other rows
+__host__ __device__ inline void dia_ranges(int n, int omin, int omax, int vec, int& glo, int& ghi, int& nb) {
+  const int groups = (n + vec - 1) / vec;
+  const int need = vec - omin;
+  glo = need <= 0 ? 0 : (need + vec - 1) / vec;
+  const int lim = (n - omax - 2 * vec - 2) < (n - vec) ? (n - omax - 2 * vec - 2) : (n - vec);
+  ghi = lim < 0 ? 0 : lim / vec + 1;
+  glo = glo < groups ? glo : groups;
+  ghi = ghi < groups ? ghi : groups;
+  ghi = ghi > glo ? ghi : glo;
+  const int head = glo * vec < n ? glo * vec : n;
+  nb = head + (n - ghi * vec > 0 ? n - ghi * vec : 0);
+}
+// Epilogues that declare kBanded get the band kernels (the plain product and
+// the solvers' hot epilogues); the others keep one window per diagonal,
+// which bounds the number of kernel instantiations
+template <class E, class = void>
+struct EpiBanded : std::false_type {};
+template <class E>
+struct EpiBanded<E, std::void_t<decltype(E::kBanded)>> : std::integral_constant<bool, E::kBanded> {};
+
 // Diagonals per batch of loads: every load of a batch is issued before the
 // first product, with no condition on them (batch slots past the last
 // diagonal re-read it and are masked off), so a thread waits for memory
@@ -498,16 +590,170 @@ constexpr int kDiaGeneric = 16;
 // Resident blocks asked of the compiler: three for the exact-count FP32
 // kernels (at most 80 registers, every load of the vector path still in
 // flight), two otherwise (the generic and FP64 kernels would spill).
-template <typename T, int ND>
+// With bands (a third of the x registers) the FP32 kernels fit four blocks.
+template <typename T, int ND, unsigned BANDS>
 constexpr int dia_min_blocks() {
-  return sizeof(T) == 4 && ND < 16 ? 3 : 2;
+  return sizeof(T) == 4 && ND < 16 ? (BANDS != 0 && BANDS != (1u << ND) - 1 ? 4 : 3) : 2;
 }
 
-template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>>
-__global__ void __launch_bounds__(kBlock, dia_min_blocks<T, ND>()) spmv_dia_kernel(const V* __restrict__ vals,
+// One inner row group of the diagonal-layout SpMV (the kernel below).
+template <typename T, int ND, class Epi, bool FMA, typename V, class Gather, unsigned BANDS>
+__device__ __forceinline__ void dia_group(int g, const V* __restrict__ vals, const uint16_t* __restrict__ mask,
+                                          int64_t ld, DiaOffs offs, int ndr, const T* __restrict__ x,
+                                          T* __restrict__ y, Epi epi, Gather gat, Acc3<T>& a) {
+  constexpr int VEC = DiaVec<T>::kVec;
+  constexpr bool kExact = ND < kDiaGeneric;
+  constexpr int KB = kExact ? ND : kDiaBatch;
+  const int r0 = g * VEC;
+  T acc[VEC];
+#pragma unroll
+  for (int j = 0; j < VEC; ++j) acc[j] = T(0);
+  unsigned m[VEC];  // one 8- or 4-byte load (r0 is a multiple of VEC)
+  if constexpr (VEC == 4) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(mask + r0));
+    m[0] = u.x & 0xFFFFu; m[1] = u.x >> 16; m[2] = u.y & 0xFFFFu; m[3] = u.y >> 16;
+  } else {
+    static_assert(VEC == 2, "DIA groups are 2 or 4 rows");
+    const unsigned u = __ldg(reinterpret_cast<const unsigned*>(mask + r0));
+    m[0] = u & 0xFFFFu; m[1] = u >> 16;
+  }
+  if constexpr (kExact) {
+    // every diagonal's values of the group first (one vector each, the
+    // loads that go to HBM); then band by band the x window (mostly L1/L2
+    // hits) and the products in diagonal order
+    constexpr unsigned kB = (BANDS != 0 && kExact) ? BANDS : (1u << (kExact ? ND : 1)) - 1;
+    constexpr DiaBands kT = dia_bands(kB, kExact ? ND : 1);
+    T v[ND][VEC];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) vload(vals + (int64_t)d * ld + r0, v[d]);
+#pragma unroll
+    for (int b = 0; b < kT.count; ++b) {
+      // the band's x window: the vectors its last diagonal reaches, up to
+      // window element (VEC - 1) + (L - 1) + (VEC - 1)
+      const int d0 = kT.start[b], L = kT.len[b];
+      const int nv = (L + 2 * VEC - 3) / VEC + 1;
+      const int off = offs.off[d0];
+      const int s = off & (VEC - 1);
+      const int c = r0 + off - s;
+      T w[3][VEC];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        if (i < nv) gat.vec(x, c + i * VEC, w[i]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (k < L) {
+          const int d = d0 + k;
+          T xv[VEC];
+          win_shift<T, VEC>(w, s + k, xv);
+#pragma unroll
+          for (int j = 0; j < VEC; ++j) {
+            if ((m[j] >> d) & 1u) {
+              if constexpr (FMA) acc[j] = fma(v[d][j], xv[j], acc[j]);
+              else acc[j] = add_rn(acc[j], mul_rn(v[d][j], xv[j]));
+            }
+          }
+        }
+      }
+    }
+  } else {
+    // any count: batches of KB diagonals' value and x loads
+#pragma unroll
+    for (int d0 = 0; d0 < ND; d0 += KB) {
+      if (d0 < ndr) {
+        T v[KB][VEC], xa[KB][VEC], xb[KB][VEC];
+#pragma unroll
+        for (int t = 0; t < KB; ++t) {
+          const int d = min(d0 + t, ndr - 1);
+          vload(vals + (int64_t)d * ld + r0, v[t]);
+          const int c = r0 + offs.off[d] - (offs.off[d] & (VEC - 1));
+          gat.vec(x, c, xa[t]);
+          gat.vec(x, c + VEC, xb[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < KB; ++t) {
+          const int d = d0 + t;
+          T xv[VEC];
+          dia_shift<T, VEC>(xa[t], xb[t], offs.off[min(d, ndr - 1)] & (VEC - 1), xv);
+#pragma unroll
+          for (int j = 0; j < VEC; ++j) {
+            if (d < ndr && ((m[j] >> d) & 1u)) {
+              if constexpr (FMA) acc[j] = fma(v[t][j], xv[j], acc[j]);
+              else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[j]));
+            }
+          }
+        }
+      }
+    }
+  }
+  // the group's VEC results with one 16-byte store, after the epilogue's
+  // own loads and reduction terms (acc() takes the stored value as an
+  // argument, never from y): loads placed after the store would wait
+  // for it, as they may alias y (1.5x slower FP64 CG on the 1024^2 Q1
+  // matrix).  Epilogues with a four-row form issue their vector loads
+  // together.
+  T o[VEC];
+  if constexpr (EpiRows4<Epi>::value && VEC == 4) {
+    epi.out_acc4(r0, acc, o, a);
+  } else {
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) o[j] = epi.out(r0 + j, acc[j]);
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) epi.acc(r0 + j, o[j], a);
+  }
+  if constexpr (VEC == 4) *reinterpret_cast<float4*>(y + r0) = make_float4(o[0], o[1], o[2], o[3]);
+  else *reinterpret_cast<double2*>(y + r0) = make_double2(o[0], o[1]);
+}
+
+// One row outside the inner groups: every value and x element of the row
+// loaded first (x at clamped, always valid columns; absent entries are
+// masked off), then the storage-order sum.
+template <typename T, int ND, class Epi, bool FMA, typename V, class Gather>
+__device__ __forceinline__ void dia_row(int row, int n, const V* __restrict__ vals, const uint16_t* __restrict__ mask,
+                                        int64_t ld, DiaOffs offs, int ndr, const T* __restrict__ x,
+                                        T* __restrict__ y, Epi epi, Gather gat, Acc3<T>& a) {
+  constexpr bool kExact = ND < kDiaGeneric;
+  const unsigned mr = __ldg(mask + row);
+  constexpr int RB = kExact ? ND : 8;  // diagonals per batch of loads
+  T acc = T(0);
+#pragma unroll
+  for (int d0 = 0; d0 < ND; d0 += RB) {
+    if (d0 < ndr) {
+      T v[RB], xv[RB];
+#pragma unroll
+      for (int t2 = 0; t2 < RB; ++t2) {
+        const int dd = min(d0 + t2, ndr - 1);
+        v[t2] = (T)to_val(vals[(int64_t)dd * ld + row]);
+        xv[t2] = gat(x, min(max(row + offs.off[dd], 0), n - 1));
+      }
+#pragma unroll
+      for (int t2 = 0; t2 < RB; ++t2) {
+        const int d = d0 + t2;
+        if (d < ndr && ((mr >> d) & 1u)) {
+          if constexpr (FMA) acc = fma(v[t2], xv[t2], acc);
+          else acc = add_rn(acc, mul_rn(v[t2], xv[t2]));
+        }
+      }
+    }
+  }
+  const T val = epi.out(row, acc);
+  epi.acc(row, val, a);
+  y[row] = val;
+}
+
+// BANDS: the band mask of an exact-count kernel (0: one band per diagonal).
+// FULL: the grid has a thread for every inner group and every other row
+// (each thread does one of them, straight-line code); else a grid-stride
+// loop over the inner groups, then over the other rows.
+template <typename T, int ND, class Epi, bool FMA = false, typename V = T, class Gather = GatherPlain<T>,
+          unsigned BANDS = 0, bool FULL = false>
+//
+// (nd follows nrows: placed between offs and x, it measured 12.3 instead of
+// 10.7 us back to back on the 1024^2 Q1 matrix with identical code, the
+// parameters' offsets being the only difference)
+__global__ void __launch_bounds__(kBlock, dia_min_blocks<T, ND, BANDS>()) spmv_dia_kernel(const V* __restrict__ vals,
                                                           const uint16_t* __restrict__ mask, int64_t ld,
-                                                          DiaOffs offs, int nd, const T* __restrict__ x,
-                                                          T* __restrict__ y, int64_t nrows, T* partials,
+                                                          DiaOffs offs, const T* __restrict__ x,
+                                                          T* __restrict__ y, int64_t nrows, int nd, T* partials,
                                                           unsigned int* counter, Epi epi, Gather gat = Gather{}) {
   if (epi.skip()) return;
   constexpr int VEC = DiaVec<T>::kVec;
@@ -517,146 +763,35 @@ __global__ void __launch_bounds__(kBlock, dia_min_blocks<T, ND>()) spmv_dia_kern
   // slower on the 1024^2 Q1 matrix); ND == kDiaGeneric: nd <= ND at runtime
   constexpr bool kExact = ND < kDiaGeneric;
   const int ndr = kExact ? ND : nd;
-  constexpr int KB = kExact ? ND : kDiaBatch;
   Acc3<T> a{T(0), T(0), T(0)};
   const int n = (int)nrows;
-  const int omin = offs.off[0], omax = offs.off[ndr - 1];
-  const int groups = (n + VEC - 1) / VEC;
   const int stride = (int)gridDim.x * kBlock;
   const int tid = (int)blockIdx.x * kBlock + (int)threadIdx.x;
-  // inner groups [glo, ghi): VEC whole rows whose aligned x vectors all lie
-  // inside [0, n).  They take the vector path below; the few rows outside
-  // (near both ends) take the row path after it, so that its code does not
-  // raise the vector path's register count (a group-level branch between the
-  // two cost 40 registers per thread and a third of the resident warps).
-  const int need = VEC - omin;
-  int glo = need <= 0 ? 0 : (need + VEC - 1) / VEC;
-  const int lim = min(n - omax - 2 * VEC, n - VEC);
-  int ghi = lim < 0 ? 0 : lim / VEC + 1;
-  glo = min(glo, groups);
-  ghi = max(min(ghi, groups), glo);
-  for (int g = glo + tid; g < ghi; g += stride) {
-    const int r0 = g * VEC;
-    T acc[VEC];
-#pragma unroll
-    for (int j = 0; j < VEC; ++j) acc[j] = T(0);
-    unsigned m[VEC];  // one 8- or 4-byte load (r0 is a multiple of VEC)
-    if constexpr (VEC == 4) {
-      const uint2 u = __ldg(reinterpret_cast<const uint2*>(mask + r0));
-      m[0] = u.x & 0xFFFFu; m[1] = u.x >> 16; m[2] = u.y & 0xFFFFu; m[3] = u.y >> 16;
-    } else {
-      static_assert(VEC == 2, "DIA groups are 2 or 4 rows");
-      const unsigned u = __ldg(reinterpret_cast<const unsigned*>(mask + r0));
-      m[0] = u & 0xFFFFu; m[1] = u >> 16;
-    }
-    if constexpr (kExact) {
-      // every diagonal's values of the group first (one vector each, the
-      // loads that go to HBM); then, diagonal by diagonal, the two aligned
-      // x vectors (mostly L1/L2 hits) and the products.  Batching the x
-      // loads with the values as well measured 1.45x slower on the 1024^2
-      // Q1 matrix: they hold registers the value loads need.
-      T v[ND][VEC];
-#pragma unroll
-      for (int d = 0; d < ND; ++d) vload(vals + (int64_t)d * ld + r0, v[d]);
-#pragma unroll
-      for (int d = 0; d < ND; ++d) {
-        const int off = offs.off[d];
-        const int c = r0 + off - (off & (VEC - 1));
-        T xa[VEC], xb[VEC], xv[VEC];
-        gat.vec(x, c, xa);
-        gat.vec(x, c + VEC, xb);
-        dia_shift<T, VEC>(xa, xb, off & (VEC - 1), xv);
-#pragma unroll
-        for (int j = 0; j < VEC; ++j) {
-          if ((m[j] >> d) & 1u) {
-            if constexpr (FMA) acc[j] = fma(v[d][j], xv[j], acc[j]);
-            else acc[j] = add_rn(acc[j], mul_rn(v[d][j], xv[j]));
-          }
-        }
-      }
-    } else {
-      // any count: batches of KB diagonals' value and x loads
-#pragma unroll
-      for (int d0 = 0; d0 < ND; d0 += KB) {
-        if (d0 < ndr) {
-          T v[KB][VEC], xa[KB][VEC], xb[KB][VEC];
-#pragma unroll
-          for (int t = 0; t < KB; ++t) {
-            const int d = min(d0 + t, ndr - 1);
-            vload(vals + (int64_t)d * ld + r0, v[t]);
-            const int c = r0 + offs.off[d] - (offs.off[d] & (VEC - 1));
-            gat.vec(x, c, xa[t]);
-            gat.vec(x, c + VEC, xb[t]);
-          }
-#pragma unroll
-          for (int t = 0; t < KB; ++t) {
-            const int d = d0 + t;
-            T xv[VEC];
-            dia_shift<T, VEC>(xa[t], xb[t], offs.off[min(d, ndr - 1)] & (VEC - 1), xv);
-#pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-              if (d < ndr && ((m[j] >> d) & 1u)) {
-                if constexpr (FMA) acc[j] = fma(v[t][j], xv[j], acc[j]);
-                else acc[j] = add_rn(acc[j], mul_rn(v[t][j], xv[j]));
-              }
-            }
-          }
-        }
-      }
-    }
-    // the group's VEC results with one 16-byte store, after the epilogue's
-    // own loads and reduction terms (acc() takes the stored value as an
-    // argument, never from y): loads placed after the store would wait
-    // for it, as they may alias y (1.5x slower FP64 CG on the 1024^2 Q1
-    // matrix).  Epilogues with a four-row form issue their vector loads
-    // together.
-    T o[VEC];
-    if constexpr (EpiRows4<Epi>::value && VEC == 4) {
-      epi.out_acc4(r0, acc, o, a);
-    } else {
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) o[j] = epi.out(r0 + j, acc[j]);
-#pragma unroll
-      for (int j = 0; j < VEC; ++j) epi.acc(r0 + j, o[j], a);
-    }
-    if constexpr (VEC == 4) *reinterpret_cast<float4*>(y + r0) = make_float4(o[0], o[1], o[2], o[3]);
-    else *reinterpret_cast<double2*>(y + r0) = make_double2(o[0], o[1]);
-  }
-  // rows outside the inner groups, one per thread: every value and x element
-  // of the row loaded first (x at clamped, always valid columns; absent
-  // entries are masked off), then the storage-order sum.  They go to the
-  // threads counted from the end of the grid, which the grid-stride loop
-  // above gave the fewest groups.
+  // inner groups take the vector path; the few rows outside them (near both
+  // ends) take the row path, kept apart so that its code does not raise the
+  // vector path's register count (a group-level branch between the two cost
+  // 40 registers per thread and a third of the resident warps)
+  int glo, ghi, nb;
+  dia_ranges(n, offs.off[0], offs.off[ndr - 1], VEC, glo, ghi, nb);
   const int head = min(glo * VEC, n);
-  const int nb = head + max(n - ghi * VEC, 0);
-  for (int t = stride - 1 - tid; t < nb; t += stride) {
-    const int row = t < head ? t : ghi * VEC + (t - head);
-    const unsigned mr = __ldg(mask + row);
-    constexpr int RB = kExact ? ND : 8;  // diagonals per batch of loads
-    T acc = T(0);
-#pragma unroll
-    for (int d0 = 0; d0 < ND; d0 += RB) {
-      if (d0 < ndr) {
-        T v[RB], xv[RB];
-#pragma unroll
-        for (int t = 0; t < RB; ++t) {
-          const int dd = min(d0 + t, ndr - 1);
-          v[t] = (T)to_val(vals[(int64_t)dd * ld + row]);
-          xv[t] = gat(x, min(max(row + offs.off[dd], 0), n - 1));
-        }
-#pragma unroll
-        for (int t = 0; t < RB; ++t) {
-          const int d = d0 + t;
-          if (d < ndr && ((mr >> d) & 1u)) {
-            if constexpr (FMA) acc = fma(v[t], xv[t], acc);
-            else acc = add_rn(acc, mul_rn(v[t], xv[t]));
-          }
-        }
-      }
+  const int span = ghi - glo;
+  if constexpr (FULL) {
+    // the other rows first: their blocks are scheduled first and overlap
+    // the inner groups, instead of lengthening the kernel's tail
+    if (tid < nb) {
+      dia_row<T, ND, Epi, FMA, V, Gather>(tid < head ? tid : ghi * VEC + (tid - head), n, vals, mask, ld, offs, ndr,
+                                          x, y, epi, gat, a);
+    } else if (tid - nb < span) {
+      dia_group<T, ND, Epi, FMA, V, Gather, BANDS>(glo + tid - nb, vals, mask, ld, offs, ndr, x, y, epi, gat, a);
     }
-    const T val = epi.out(row, acc);
-    epi.acc(row, val, a);
-    y[row] = val;
+  } else {
+    for (int g = glo + tid; g < ghi; g += stride)
+      dia_group<T, ND, Epi, FMA, V, Gather, BANDS>(g, vals, mask, ld, offs, ndr, x, y, epi, gat, a);
+    // the other rows go to the threads counted from the end of the grid,
+    // which the grid-stride loop gave the fewest groups
+    for (int t = stride - 1 - tid; t < nb; t += stride)
+      dia_row<T, ND, Epi, FMA, V, Gather>(t < head ? t : ghi * VEC + (t - head), n, vals, mask, ld, offs, ndr, x, y,
+                                          epi, gat, a);
   }
   if constexpr (Epi::kReduce) {
     Acc3<T> tot;

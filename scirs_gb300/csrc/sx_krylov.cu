@@ -71,6 +71,7 @@ struct CgSetup {
 // Ap with pAp fused (iterative.rs:98-111)
 template <typename T>
 struct EpiCgPap {
+  static constexpr bool kBanded = true;
   CgState<T>* st;
   const T* p;
   static constexpr bool kReduce = true;
@@ -158,6 +159,7 @@ struct CgUpdate {
 // once the solve has ended
 template <typename T>
 struct EpiCgRz {
+  static constexpr bool kBanded = true;
   CgState<T>* st;
   const T* r;
   static constexpr bool kReduce = true;
@@ -399,6 +401,7 @@ struct MxState {
 };
 
 struct EpiMx1 {
+  static constexpr bool kBanded = true;
   CgState<float>* st;
   const float* z;
   float *p, *q;
@@ -511,6 +514,7 @@ struct GatherMxResid {
   }
 };
 struct EpiMx2 {
+  static constexpr bool kBanded = true;
   MxState* ms;
   float* x;
   const float *p, *q, *r;
@@ -547,6 +551,7 @@ struct EpiMx2 {
 };
 // K3 for G G^T: z = G t with r'.z, beta, end of the iteration
 struct EpiMx3 {
+  static constexpr bool kBanded = true;
   CgState<float>* st;
   const float* rn;
   static constexpr bool kReduce = true;

@@ -16,6 +16,7 @@ namespace sx {
 // Epilogue that only stores A x.
 template <typename T>
 struct EpiPlain {
+  static constexpr bool kBanded = true;
   static constexpr bool kReduce = false;
   __device__ bool skip() const { return false; }
   __device__ T out(int64_t, T ax) const { return ax; }
@@ -200,13 +201,19 @@ void launch_pipe_minb(sx_ctx ctx, const DevCsr& c, const T* x, T* y, Epi epi, co
 }
 
 // One diagonal-layout launch: as many blocks as the row groups need, at
-// most the resident blocks of every SM.
-template <auto Kern, typename T, typename V, class Epi, class Gather>
+// most the resident blocks of every SM (FULL: every group its own thread,
+// the hardware handing out blocks as others finish).
+template <auto Kern, bool FULL = false, typename T, typename V, class Epi, class Gather>
 void dia_go(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi epi, const ReduceArea& ra,
             Gather gat, const DiaOffs& offs, int64_t units) {
-  const int64_t grid =
-      std::min<int64_t>((units + kBlock - 1) / kBlock, (int64_t)ctx->num_sms * resident_blocks<Kern>());
-  Kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, c.dia_n, x, y, c.nrows,
+  int64_t grid = std::min<int64_t>((units + kBlock - 1) / kBlock, (int64_t)ctx->num_sms * resident_blocks<Kern>());
+  if constexpr (FULL) {
+    // a thread per inner group and per other row
+    int glo = 0, ghi = 0, nb = 0;
+    dia_ranges((int)c.nrows, c.dia_off[0], c.dia_off[c.dia_n - 1], DiaVec<T>::kVec, glo, ghi, nb);
+    grid = std::max<int64_t>(1, ((int64_t)(ghi - glo) + nb + kBlock - 1) / kBlock);
+  }
+  Kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, x, y, c.nrows, c.dia_n,
                                                     (T*)ra.partials, ra.counter, epi, gat);
 }
 
@@ -223,6 +230,31 @@ bool launch_dia(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Ep
   DiaOffs offs;
   for (int q = 0; q < 16; ++q) offs.off[q] = c.dia_off[q];
   const int64_t groups = (c.nrows + DiaVec<T>::kVec - 1) / DiaVec<T>::kVec;
+  // band kernels for the stencil shapes here (2D Q1: three bands of three;
+  // 3D 7-point: 1,1,3,1,1; 2D 5-point: 1,3,1; the learned factors of Q1: 3,2
+  // and 2,3), for the plain product and the solvers' hot epilogues; FP32
+  // ones on a full grid (four resident blocks: measured 10.4 vs 12.3 us
+  // back to back on the 1024^2 Q1 matrix against a persistent grid)
+  if constexpr (EpiBanded<Epi>::value) {
+    if (ctx->dia_nd6 && ctx->dia_band) {
+      constexpr bool kFull = sizeof(T) == 4;
+      const unsigned bm = dia_band_mask(c.dia_off, c.dia_n);
+      bool done = true;
+      if (c.dia_n == 9 && bm == 0x49u)
+        dia_go<spmv_dia_kernel<T, 9, Epi, FMA, V, Gather, 0x49u, kFull>, kFull>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+      else if (c.dia_n == 7 && bm == 0x67u)
+        dia_go<spmv_dia_kernel<T, 7, Epi, FMA, V, Gather, 0x67u, kFull>, kFull>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+      else if (c.dia_n == 5 && bm == 0x13u)
+        dia_go<spmv_dia_kernel<T, 5, Epi, FMA, V, Gather, 0x13u, kFull>, kFull>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+      else if (c.dia_n == 5 && bm == 0x09u)
+        dia_go<spmv_dia_kernel<T, 5, Epi, FMA, V, Gather, 0x09u, kFull>, kFull>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+      else if (c.dia_n == 5 && bm == 0x05u)
+        dia_go<spmv_dia_kernel<T, 5, Epi, FMA, V, Gather, 0x05u, kFull>, kFull>(ctx, c, vals, x, y, epi, ra, gat, offs, groups);
+      else
+        done = false;
+      if (done) return true;
+    }
+  }
   // exact-count kernels for the stencils here (5: 2D 5-point and the learned
   // factors, 7: 3D 7-point, 9: 2D Q1), the generic one for any other count
   // (and for every count with SX_DIA_ND6=0)
@@ -316,6 +348,14 @@ inline const char* spmv_kernel_name(sx_ctx ctx, const DevCsr& c, int w, bool fma
   if (c.nrows <= 0) return "none";
   if (ctx->dia && c.dia_n > 0 && c.dia_mask) {
     const bool h = half_ok && w == 4 && c.dia_vals16;
+    if (ctx->dia_nd6 && ctx->dia_band) {
+      const unsigned bm = dia_band_mask(c.dia_off, c.dia_n);
+      if (c.dia_n == 9 && bm == 0x49u) return h ? "spmv_dia_kernel<ND=9, bands 3+3+3, FP16 values>" : "spmv_dia_kernel<ND=9, bands 3+3+3>";
+      if (c.dia_n == 7 && bm == 0x67u) return h ? "spmv_dia_kernel<ND=7, bands 1+1+3+1+1, FP16 values>" : "spmv_dia_kernel<ND=7, bands 1+1+3+1+1>";
+      if (c.dia_n == 5 && bm == 0x13u) return h ? "spmv_dia_kernel<ND=5, bands 1+3+1, FP16 values>" : "spmv_dia_kernel<ND=5, bands 1+3+1>";
+      if (c.dia_n == 5 && bm == 0x09u) return h ? "spmv_dia_kernel<ND=5, bands 3+2, FP16 values>" : "spmv_dia_kernel<ND=5, bands 3+2>";
+      if (c.dia_n == 5 && bm == 0x05u) return h ? "spmv_dia_kernel<ND=5, bands 2+3, FP16 values>" : "spmv_dia_kernel<ND=5, bands 2+3>";
+    }
     if (c.dia_n == 5 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=5, FP16 values>" : "spmv_dia_kernel<ND=5>";
     if (c.dia_n == 7 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=7, FP16 values>" : "spmv_dia_kernel<ND=7>";
     if (c.dia_n == 9 && ctx->dia_nd6) return h ? "spmv_dia_kernel<ND=9, FP16 values>" : "spmv_dia_kernel<ND=9>";

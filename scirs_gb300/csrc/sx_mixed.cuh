@@ -11,6 +11,7 @@ struct IrNorms {
 
 // y = b - A x in FP64 with ||y||^2 and ||b||^2 fused
 struct EpiIrResid {
+  static constexpr bool kBanded = true;
   const double* b;
   IrNorms* norms;
   static constexpr bool kReduce = true;

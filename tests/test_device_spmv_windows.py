@@ -225,15 +225,21 @@ def test_kernel_choice_names(S, ctx):
     n = len(ip) - 1
     a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
     a32 = a64.astype(np.float32)
-    # default (SX_DIA=1): the diagonal layout for FP64 and FP32 (7 diagonals)
-    assert S.spmv_kernel(a32) == "spmv_dia_kernel<ND=7>"
-    assert S.spmv_kernel(a64, exact=False) == "spmv_dia_kernel<ND=7>"
-    assert S.spmv_kernel(a64, exact=True) == "spmv_dia_kernel<ND=7>"
+    # default (SX_DIA=1): the diagonal layout for FP64 and FP32 (7 diagonals
+    # in bands 1+1+3+1+1: the three adjacent ones share one x window)
+    assert S.spmv_kernel(a32) == "spmv_dia_kernel<ND=7, bands 1+1+3+1+1>"
+    assert S.spmv_kernel(a64, exact=False) == "spmv_dia_kernel<ND=7, bands 1+1+3+1+1>"
+    assert S.spmv_kernel(a64, exact=True) == "spmv_dia_kernel<ND=7, bands 1+1+3+1+1>"
+    cb = _ctx_with(S, {"SX_DIA_BAND": "0"})
+    nb32 = S.csr_from_arrays(cb, ip, ix, v.astype(np.float32), (n, n))
+    assert S.spmv_kernel(nb32) == "spmv_dia_kernel<ND=7>"
+    nb32.close()
+    cb.close()
     # five diagonals (the 2D 5-point stencil): the exact-count kernel; the
     # generic one with SX_DIA_ND6=0
     ip5, ix5, v5 = S.generate("poisson2d", 40, 40)
     f32 = S.csr_from_arrays(ctx, ip5, ix5, v5.astype(np.float32), (1600, 1600))
-    assert S.spmv_kernel(f32) == "spmv_dia_kernel<ND=5>"
+    assert S.spmv_kernel(f32) == "spmv_dia_kernel<ND=5, bands 1+3+1>"
     c2 = _ctx_with(S, {"SX_DIA_ND6": "0"})
     d32 = S.csr_from_arrays(c2, ip5, ix5, v5.astype(np.float32), (1600, 1600))
     assert S.spmv_kernel(d32) == "spmv_dia_kernel<ND=16>"
@@ -349,3 +355,59 @@ def test_diagonal_layout_unaligned_vectors(S, dtype):
             assert np.allclose(y, yr, rtol=1e-14, atol=1e-14)
     a.close()
     ctx.close()
+
+
+def _tri(ip, ix, v, lower):
+    # the lower (or upper) triangle of a CSR matrix, diagonal included
+    rows = np.repeat(np.arange(len(ip) - 1), np.diff(ip))
+    keep = ix <= rows if lower else ix >= rows
+    cnt = np.bincount(rows[keep], minlength=len(ip) - 1)
+    ptr = np.zeros(len(ip), np.int64)
+    ptr[1:] = np.cumsum(cnt)
+    return ptr, ix[keep], v[keep]
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_band_kernels_bit_exact(S, ctx, dtype):
+    # every band shape the exact-count kernels specialise (Q1: 3+3+3; 3D
+    # 7-point: 1+1+3+1+1; 2D 5-point: 1+3+1; the learned factors' lower and
+    # upper Q1 triangles: 3+2 and 2+3) on grids small enough that many rows
+    # are boundary rows: the oracle's bits, with and without bands, and with
+    # an infinite x entry
+    cases = [
+        ("aniso_q1", (37, 29), dict(param0=30.0, param1=0.4), "bands 3+3+3", None),
+        ("laplace3d", (11, 9, 13), {}, "bands 1+1+3+1+1", None),
+        ("poisson2d", (33, 21), {}, "bands 1+3+1", None),
+        ("aniso_q1", (41, 23), dict(param0=8.0, param1=1.1), "bands 3+2", True),
+        ("aniso_q1", (26, 31), dict(param0=8.0, param1=1.1), "bands 2+3", False),
+        ("aniso_q1", (3, 2), dict(param0=2.0, param1=0.3), "bands 3+3+3", None),
+    ]
+    cb = _ctx_with(S, {"SX_DIA_BAND": "0"})
+    rng = np.random.default_rng(41)
+    try:
+        for kind, dims, kw, shape, lower in cases:
+            ip, ix, v = S.generate(kind, *dims, **kw)
+            if lower is not None:
+                ip, ix, v = _tri(ip, ix, v, lower)
+            n = len(ip) - 1
+            vals = v.astype(dtype)
+            a = S.csr_from_arrays(ctx, ip, ix, vals, (n, n))
+            b = S.csr_from_arrays(cb, ip, ix, vals, (n, n))
+            if n >= 64:
+                assert shape in S.spmv_kernel(a), (kind, dims, S.spmv_kernel(a))
+            for trial in range(2):
+                x = rng.standard_normal(n).astype(dtype)
+                if trial:
+                    x[n // 2] = np.inf
+                y = a.matvec(x)
+                yr = O.spmv_i32(ip, ix, vals, x)
+                nan = np.isnan(yr)
+                assert np.array_equal(np.isnan(y), nan), (kind, dims)
+                assert np.array_equal(y[~nan].view(np.uint8), yr[~nan].view(np.uint8)), (kind, dims)
+                yb = b.matvec(x)
+                assert np.array_equal(np.isnan(yb), nan), (kind, dims)
+                assert np.array_equal(yb[~nan].view(np.uint8), yr[~nan].view(np.uint8)), (kind, dims)
+            a.close()
+            b.close()
+    finally:
+        cb.close()
