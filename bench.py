@@ -14,7 +14,9 @@ and x resident on the device; `e2e` times the same step through the C ABI
 with b copied from pinned host memory and x copied back inside the timed
 region.  `jacobi_pcg_fp64` times plain FP64 Jacobi-PCG (the reference's
 method) on the same problem and device, `speedup_vs_jacobi_fp64` is their
-ratio; IC(0)-PCG (the reference's quirky factorisation and the textbook
+ratio; `jacobi_pcg_fp64_fused` and `speedup_vs_jacobi_fp64_fused` the same
+method in two kernels per iteration (A p by the recurrence q = A z + beta q);
+IC(0)-PCG (the reference's quirky factorisation and the textbook
 one) is reported beside them.
 
 `roofline` times the dominant kernel of the step, the FP32 SpMV of A,
@@ -372,6 +374,13 @@ def run_ours(args):
     # the reference's method on the same device
     t_jac, r_jac, _ = timed(lambda: jacobi_step(dev_b, dev_x, L.SX_MEM_DEVICE), max(2, args.steps // 2), 1)
     true_res_jac = S.true_rel_residual(a64, b, x_dev.cpu().numpy())
+    # the same method in two kernels per iteration (A p by the recurrence
+    # q = A z + beta q, the p-update in the SpMV's epilogue): the FP64 loop
+    # fused as far as the FP32 one
+    ctx.set_cg_recurrence(True)
+    t_jacf, r_jacf, _ = timed(lambda: jacobi_step(dev_b, dev_x, L.SX_MEM_DEVICE), max(2, args.steps // 2), 1)
+    ctx.set_cg_recurrence(False)
+    true_res_jacf = S.true_rel_residual(a64, b, x_dev.cpu().numpy())
 
     def once(fn):
         torch.cuda.synchronize()
@@ -566,6 +575,11 @@ def run_ours(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         value = float(tt.item())
     jac = statistics.mean(t_jac)
+    jacf = statistics.mean(t_jacf)
+    jacf_iter_s = jacf / max(int(r_jacf.iterations), 1)
+    # K1: A (layout), z gathered once, p read and written, q read (written as y);
+    # K2: x, r read and written, p, q, D read, z written
+    jacf_bytes = dia_bytes(n, 9, 8) + 11 * n * 8
     # FP64 Jacobi-PCG per iteration on the diagonal layout: A (9 FP64 values
     # + the 2-byte mask per row), p read and Ap written by the SpMV; the
     # update reads x, p, r, Ap, 1/diag and writes x, r; the p step reads r,
@@ -588,11 +602,17 @@ def run_ours(args):
                    "l2": "working set > L2 (129 MB) and a 512 MB L2 flush between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "speedup_vs_jacobi_fp64": jac / value,
+        "speedup_vs_jacobi_fp64_fused": jacf / value,
         "learned_vs_jacobi_mixed": t_jm / value,
         "jacobi_pcg_fp64": {"value": jac, "unit": "s", "iterations": int(r_jac.iterations),
                             "us_per_iteration": jac_iter_s * 1e6, "bytes_per_iteration": jac_bytes,
                             "GB/s": jac_bytes / jac_iter_s / 1e9, "frac": jac_bytes / jac_iter_s / 1e9 / peak,
                             "fp64_true_rel_residual": true_res_jac},
+        "jacobi_pcg_fp64_fused": {"value": jacf, "unit": "s", "iterations": int(r_jacf.iterations),
+                                  "us_per_iteration": jacf_iter_s * 1e6, "bytes_per_iteration": jacf_bytes,
+                                  "GB/s": jacf_bytes / jacf_iter_s / 1e9,
+                                  "frac": jacf_bytes / jacf_iter_s / 1e9 / peak,
+                                  "kernels_per_iteration": 2, "fp64_true_rel_residual": true_res_jacf},
         "jacobi_pcg_mixed": {"value": t_jm, "unit": "s", "outer_iterations": r_jm.outer_iterations,
                              "inner_iterations": r_jm.inner_iterations, "fp64_true_rel_residual": r_jm.rel_residual},
         "e2e": {"value": statistics.mean(t_e2e), "unit": "s", "h2d_bytes_per_step": n * 8,

@@ -104,6 +104,16 @@ int sx_ctx_set_wait_limit(sx_ctx ctx, uint64_t ns);
  * outcome) and the wait's length in *waited_ns.  Checks the give-up path of
  * the dependency waits without touching any operator. */
 int sx_wait_selftest(sx_ctx ctx, uint64_t* waited_ns);
+/* CG variant of this context (on != 0): with a Jacobi, diagonal, scaled or no
+ * preconditioner, sx_cg carries A p by the recurrence q = A z + beta q
+ * (z = M r), so that each iteration takes two device kernels instead of
+ * three (the p-update runs in the SpMV's epilogue, z = M r in the vector
+ * update).  Mathematically the reference's loop (linalg/iterative.rs:95-151)
+ * with the same roundings elsewhere; q differs from A p by the recurrence's
+ * rounding, so iterates and iteration counts can differ slightly from the
+ * reference's.  Off (0) by default; applies to solves started after it is
+ * set.  No reference counterpart. */
+int sx_ctx_set_cg_recurrence(sx_ctx ctx, int on);
 /* Roofline probe: the rate (gathers per second) at which this GPU reads
  * elements of an L2-resident vector of n elements (dtype SX_F32 or SX_F64)
  * at m uniform random positions, the positions streamed with coalesced

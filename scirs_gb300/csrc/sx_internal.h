@@ -189,6 +189,9 @@ struct sx_ctx_s {
   // sweeps (IC(0), ILU(0), SSOR), in nanoseconds: a wait that runs longer
   // gives up and the call reports SX_ERR_DEVICE_TIMEOUT
   unsigned long long wait_ns = 2000000000ull;
+  // sx_ctx_set_cg_recurrence: CG with a diagonal preconditioner carries A p
+  // by the recurrence q = A z + beta q (two kernels per iteration)
+  bool cg_recurrence = false;
   // autotuner results of this context: a kernel family and a key made of
   // size statistics -> the chosen launch shape (sx_tune.cuh)
   std::map<uint64_t, uint32_t> tuned;

@@ -226,6 +226,144 @@ struct CgP {
   }
 };
 
+// ---- CG in two kernels per iteration (opt-in, sx_ctx_set_cg_recurrence):
+// for diagonal preconditioners, A p is carried by the recurrence
+// q = A z + beta q instead of a product of A with p, so the p-update folds
+// into the SpMV's epilogue and z = D r into the vector update.  Every other
+// operation is the reference loop's (iterative.rs:95-151) with the same
+// roundings; q differs from A p by the recurrence's rounding.
+//   setup  z = D r, p = 0, q = 0, beta = 0, rz, ||b||, ||r||, tol
+//   K1     w = A z; p = z + beta p; q = w + beta q; p.q -> alpha
+//   K2     x += alpha p; r -= alpha q; ||r|| (convergence); z = D r; r.z -> beta;
+//          iteration count, max_iter, graph condition
+template <typename T>
+struct CgSetupQ {
+  CgState<T>* st;
+  const T *b, *r;
+  T *z, *p;
+  PrecFused<T> pf;
+  static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = false;
+  __device__ bool skip() const { return false; }
+  __device__ void elem(int64_t i, Acc3<T>& a) const {
+    const T ri = r[i];
+    const T zi = pf.apply(i, ri);
+    z[i] = zi;
+    p[i] = T(0);
+    a.a += ri * zi;
+    a.b += b[i] * b[i];
+    a.c += ri * ri;
+  }
+  __device__ void finish(const Acc3<T>& t) const {
+    st->rz_old = t.a;
+    st->beta = T(0);
+    T bnorm = sqrt(t.b);
+    st->tol = fmax(st->atol, st->rtol * bnorm);
+    st->rnorm = sqrt(t.c);
+    st->result_norm = st->rnorm;
+    if (st->c.max_iter == 0) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_MAX_ITER;
+    }
+  }
+};
+
+// K1's epilogue: y is q (updated in place), p is updated beside it
+template <typename T>
+struct EpiCgQ {
+  static constexpr bool kBanded = true;
+  CgState<T>* st;
+  const T* z;
+  T *p, *q;
+  static constexpr bool kReduce = true;
+  __device__ bool skip() const { return st->c.status != ST_RUNNING; }
+  __device__ T out(int64_t i, T w) const {
+    const T b = st->beta;
+    p[i] = axpy_rn(z[i], b, p[i]);
+    return axpy_rn(w, b, q[i]);  // stored to q[i]
+  }
+  __device__ void acc(int64_t i, T qi, Acc3<T>& a) const { a.a += p[i] * qi; }
+  __device__ void finish(const Acc3<T>& t) const {
+    const T pap = t.a;
+    st->pap = pap;
+    if (pap <= T(0)) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_NOT_PD;
+      st->result_norm = st->rnorm;
+      return;
+    }
+    st->alpha = st->rz_old / pap;
+  }
+};
+
+template <typename T>
+struct CgUpdateQ {
+  CgState<T>* st;
+  T *x, *r, *z;
+  const T *p, *q;
+  PrecFused<T> pf;
+  static constexpr bool kReduce = true;
+  static constexpr bool kVec4 = true;
+  __device__ bool skip() const {
+    if (st->c.status != ST_RUNNING) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(st->c.use_cond, st->c.cond, 0u);
+      return true;
+    }
+    return false;
+  }
+  __device__ void elem(int64_t i, Acc3<T>& a) const {
+    const T alpha = st->alpha;
+    x[i] = axpy_rn(x[i], alpha, p[i]);
+    const T ri = axpy_rn(r[i], -alpha, q[i]);
+    r[i] = ri;
+    const T zi = pf.apply(i, ri);
+    z[i] = zi;
+    a.a += ri * ri;
+    a.b += ri * zi;
+  }
+  __device__ void elem4(int64_t i, Acc3<T>& a) const {
+    const T alpha = st->alpha;
+    Vec4<T> xv = ldv4(x + i), pv = ldv4(p + i), rv = ldv4(r + i), qv = ldv4(q + i), zv;
+    Vec4<T> dv{{T(1), T(1), T(1), T(1)}};
+    if (pf.kind == PK_DIAG) dv = ldv4(pf.d + i);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      xv.v[k] = axpy_rn(xv.v[k], alpha, pv.v[k]);
+      const T ri = axpy_rn(rv.v[k], -alpha, qv.v[k]);
+      rv.v[k] = ri;
+      zv.v[k] = pf.kind == PK_DIAG ? mul_rn(ri, dv.v[k]) : pf.apply(i + k, ri);
+      a.a += ri * ri;
+      a.b += ri * zv.v[k];
+    }
+    stv4(x + i, xv);
+    stv4(r + i, rv);
+    stv4(z + i, zv);
+  }
+  __device__ void finish(const Acc3<T>& t) const {
+    const T rnorm = sqrt(t.a);
+    st->rnorm = rnorm;
+    if (rnorm <= st->tol) {
+      st->c.status = ST_DONE;
+      st->c.converged = 1;
+      st->c.message = MSG_CONVERGED;
+      st->c.iterations += 1;
+      st->result_norm = rnorm;
+      set_cond(st->c.use_cond, st->c.cond, 0u);
+      return;
+    }
+    st->beta = t.b / st->rz_old;
+    st->rz_old = t.b;
+    st->c.iterations += 1;
+    if (st->c.iterations >= st->c.max_iter) {
+      st->c.status = ST_DONE;
+      st->c.message = MSG_MAX_ITER;
+      st->result_norm = st->rnorm;
+    }
+    if (st->c.budget > 0) st->c.budget -= 1;
+    set_cond(st->c.use_cond, st->c.cond, (st->c.status == ST_RUNNING && st->c.budget > 0) ? 1u : 0u);
+  }
+};
+
 template <typename T>
 static int cg_run(sx_ctx ctx, sx_op a, const void* b, const sx_cg_options* opt, void* x_out,
                   sx_mem mem, sx_iter_result* res) {
@@ -262,8 +400,19 @@ static int cg_run(sx_ctx ctx, sx_op a, const void* b, const sx_cg_options* opt, 
   SX_CHECK(launch_apply<T>(ctx, a, X, R, EpiResid<T>{B}));
   if (pk == PK_GENERAL)
     SX_CHECK(launch_apply<T>(ctx, m, R, Z, EpiPlain<T>{}));
-  SX_CHECK(launch_vec<T>(ctx, n, CgSetup<T>{st, B, R, Z, P, pf}));
+  const bool recur = ctx->cg_recurrence && pk != PK_GENERAL;
+  if (recur) {
+    if (n > 0) SX_CUDA(cudaMemsetAsync(AP, 0, n * w, ctx->stream));
+    SX_CHECK(launch_vec<T>(ctx, n, CgSetupQ<T>{st, B, R, Z, P, pf}));
+  } else {
+    SX_CHECK(launch_vec<T>(ctx, n, CgSetup<T>{st, B, R, Z, P, pf}));
+  }
   auto body = [&]() -> int {
+    if (recur) {
+      SX_CHECK(launch_apply<T>(ctx, a, Z, AP, EpiCgQ<T>{st, Z, P, AP}));
+      SX_CHECK(launch_vec<T>(ctx, n, CgUpdateQ<T>{st, X, R, Z, P, AP, pf}));
+      return SX_OK;
+    }
     SX_CHECK(launch_apply<T>(ctx, a, P, AP, EpiCgPap<T>{st, P}));
     SX_CHECK(launch_vec<T>(ctx, n, CgUpdate<T>{st, X, R, P, AP, pf}));
     if (pk == PK_GENERAL) {
@@ -273,7 +422,7 @@ static int cg_run(sx_ctx ctx, sx_op a, const void* b, const sx_cg_options* opt, 
     return SX_OK;
   };
   const uint64_t key[8] = {1, (uint64_t)sizeof(T), a->serial, m ? m->serial : 0,
-                           (uint64_t)n, (uint64_t)(uintptr_t)ws, (uint64_t)pk, 0};
+                           (uint64_t)n, (uint64_t)(uintptr_t)ws, (uint64_t)pk, recur ? 1u : 0u};
   SX_CHECK(run_loop(ctx, st, key, op_graphable(a) && op_graphable(m), body));
   SX_CHECK(ic0_health(ctx, m));
   SX_CHECK(ic0_health(ctx, a));
@@ -1515,6 +1664,12 @@ void sx_gmres_options_default(sx_gmres_options* o) {
   o->atol = 1e-12;
   o->x0 = nullptr;
   o->preconditioner = nullptr;
+}
+
+int sx_ctx_set_cg_recurrence(sx_ctx ctx, int on) {
+  if (!ctx) return set_error(SX_ERR_INVALID_ARGUMENT, "Invalid argument: null ctx");
+  ctx->cg_recurrence = on != 0;
+  return clear_error();
 }
 
 int sx_cg(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_cg_options* opt,

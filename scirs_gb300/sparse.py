@@ -109,6 +109,12 @@ class Context:
         sweeps, in nanoseconds (0: the default of 2 s)."""
         _check(L.lib.sx_ctx_set_wait_limit(self.handle, int(ns)))
 
+    def set_cg_recurrence(self, on: bool) -> None:
+        """CG with a diagonal preconditioner in two kernels per iteration: A p
+        carried by the recurrence q = A z + beta q (rounding differs slightly
+        from the reference's loop).  Off by default."""
+        _check(L.lib.sx_ctx_set_cg_recurrence(self.handle, 1 if on else 0))
+
     def wait_selftest(self):
         """One bounded device wait on a flag nothing sets: (gave_up, waited_ns).
         gave_up is True when the wait ran out at this context's limit."""
