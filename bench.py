@@ -882,13 +882,14 @@ def run_profile(args):
         a64.close()
         ctx.close()
         return
-    if args.profile in ("jacobi64", "jacobi32mixed"):
+    if args.profile in ("jacobi64", "jacobi64fused", "jacobi32mixed"):
         _, _, ip, ix, v, n, b = headline_problem()
         a64 = S.csr_from_arrays(ctx, ip, ix, v, (n, n))
         a32 = a64.astype(np.float32)
-        m = S.jacobi(ctx, a64 if args.profile == "jacobi64" else a32)
+        m = S.jacobi(ctx, a64 if args.profile != "jacobi32mixed" else a32)
+        ctx.set_cg_recurrence(args.profile == "jacobi64fused")
         for _ in range(args.steps):
-            if args.profile == "jacobi64":
+            if args.profile != "jacobi32mixed":
                 r = S.cg(a64, b, max_iter=200000, rtol=TOL, atol=0.0, preconditioner=m)
                 its = r.iterations
             else:
@@ -1044,7 +1045,7 @@ def main():
     ap.add_argument("--ic0-max-iter", type=int, default=3000)
     ap.add_argument("--profile", default=None,
                     choices=["spmv32", "spmv64", "powerlaw32", "powerlaw64", "aniso32", "solve", "learned",
-                             "jacobi64", "jacobi32mixed", "sym64", "sym32", "symhalf64", "symhalf32"],
+                             "jacobi64", "jacobi64fused", "jacobi32mixed", "sym64", "sym32", "symhalf64", "symhalf32"],
                     help="run a few launches of one SpMV for an ncu capture and exit")
     ap.add_argument("--workload", default="laplace3d", choices=["laplace3d", "learned"])
     ap.add_argument("--train-gnn", type=int, default=0, help="train the network for N steps first")
