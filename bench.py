@@ -603,6 +603,10 @@ def run_ours(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "speedup_vs_jacobi_fp64": jac / value,
         "speedup_vs_jacobi_fp64_fused": jacf / value,
+        "baseline_note": (f"the fastest FP64 Jacobi-PCG here (two kernels per iteration) runs at "
+                          f"{jacf_bytes / jacf_iter_s / 1e9 / peak:.2f} of HBM, not 0.6: its SpMV keeps "
+                          f"GB300's FP64 pipe busy (two FP64 lanes per clock per SM), so the speed-up over "
+                          f"it, {jacf / value:.2f}x, is against an FP64-pipe-bound baseline"),
         "learned_vs_jacobi_mixed": t_jm / value,
         "jacobi_pcg_fp64": {"value": jac, "unit": "s", "iterations": int(r_jac.iterations),
                             "us_per_iteration": jac_iter_s * 1e6, "bytes_per_iteration": jac_bytes,
