@@ -872,7 +872,16 @@ int csr_prepare_tiles(sx_ctx ctx, DevCsr& c, int w) {
     return cuda_fail(e, "tile rows", __FILE__, __LINE__);
   }
   c.units = units;
-  if (ctx->bin && c.max_row_len > kBinLong && (w == 4 || w == 8)) SX_CHECK(csr_prepare_sliced(ctx, c, w));
+  if (ctx->bin && c.max_row_len > kBinLong && (w == 4 || w == 8)) {
+    // the sliced layout is a second copy of the matrix: without the memory
+    // for it the windowed kernel serves the matrix instead
+    const int rc = csr_prepare_sliced(ctx, c, w);
+    if (rc == SX_ERR_OUT_OF_MEMORY) {
+      (void)cudaGetLastError();
+      return clear_error();
+    }
+    SX_CHECK(rc);
+  }
   return SX_OK;
 }
 
