@@ -1164,6 +1164,7 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   if (const char* t = std::getenv("SX_DIA")) c->dia = std::atoi(t);
   if (const char* t = std::getenv("SX_DIA_ND6")) c->dia_nd6 = std::strcmp(t, "0") != 0;
   if (const char* t = std::getenv("SX_DIA_BAND")) c->dia_band = std::strcmp(t, "0") != 0;
+  if (const char* t = std::getenv("SX_PDL")) c->pdl = std::strcmp(t, "0") != 0;
   if (const char* t = std::getenv("SX_BIN")) c->bin = std::strcmp(t, "0") != 0;
   if (const char* t = std::getenv("SX_COL16")) c->col16 = std::strcmp(t, "1") == 0;
   if (const char* t = std::getenv("SX_MX_FUSED")) c->mx_unfused = std::strcmp(t, "0") == 0;

@@ -182,6 +182,9 @@ struct sx_ctx_s {
   // SX_DIA_BAND=0: the exact-count kernels read x per diagonal, never per
   // band of adjacent diagonals
   bool dia_band = true;
+  // SX_PDL=0: diagonal-layout SpMVs launched without programmatic dependent
+  // launch (each waits for the previous kernel to finish before starting)
+  bool pdl = true;
   // SX_BIN=0: long-row matrices take the windowed SpMV instead of the
   // sliced one
   bool bin = true;

@@ -596,9 +596,22 @@ constexpr int dia_min_blocks() {
   return sizeof(T) == 4 && ND < 16 ? (BANDS != 0 && BANDS != (1u << ND) - 1 ? 4 : 3) : 2;
 }
 
-// One inner row group of the diagonal-layout SpMV (the kernel below).
-template <typename T, int ND, class Epi, bool FMA, typename V, class Gather, unsigned BANDS>
-__device__ __forceinline__ void dia_group(int g, const V* __restrict__ vals, const uint16_t* __restrict__ mask,
+// Programmatic dependent launch: a kernel launched with it may start while
+// the previous kernel in the stream finishes.  It lets its own dependents
+// start at once (pdl_launch_dependents) and waits for the previous kernel's
+// completion and memory (pdl_wait) before reading anything that kernel, or
+// any before it, wrote.  Both are no-ops for a launch without it.
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// One inner row group of the diagonal-layout SpMV (the kernel below).  PRE:
+// the group's mask and values (never written by a kernel) are loaded before
+// the wait for the previous kernel, and the epilogue's skip test after it;
+// returns false when the launch is skipped.
+template <typename T, int ND, class Epi, bool FMA, typename V, class Gather, unsigned BANDS, bool PRE = false>
+__device__ __forceinline__ bool dia_group(int g, const V* __restrict__ vals, const uint16_t* __restrict__ mask,
                                           int64_t ld, DiaOffs offs, int ndr, const T* __restrict__ x,
                                           T* __restrict__ y, Epi epi, Gather gat, Acc3<T>& a) {
   constexpr int VEC = DiaVec<T>::kVec;
@@ -626,6 +639,10 @@ __device__ __forceinline__ void dia_group(int g, const V* __restrict__ vals, con
     T v[ND][VEC];
 #pragma unroll
     for (int d = 0; d < ND; ++d) vload(vals + (int64_t)d * ld + r0, v[d]);
+    if constexpr (PRE) {
+      pdl_wait();
+      if (epi.skip()) return false;
+    }
 #pragma unroll
     for (int b = 0; b < kT.count; ++b) {
       // the band's x window: the vectors its last diagonal reaches, up to
@@ -656,6 +673,10 @@ __device__ __forceinline__ void dia_group(int g, const V* __restrict__ vals, con
       }
     }
   } else {
+    if constexpr (PRE) {
+      pdl_wait();
+      if (epi.skip()) return false;
+    }
     // any count: batches of KB diagonals' value and x loads
 #pragma unroll
     for (int d0 = 0; d0 < ND; d0 += KB) {
@@ -702,6 +723,7 @@ __device__ __forceinline__ void dia_group(int g, const V* __restrict__ vals, con
   }
   if constexpr (VEC == 4) *reinterpret_cast<float4*>(y + r0) = make_float4(o[0], o[1], o[2], o[3]);
   else *reinterpret_cast<double2*>(y + r0) = make_double2(o[0], o[1]);
+  return true;
 }
 
 // One row outside the inner groups: every value and x element of the row
@@ -755,7 +777,7 @@ __global__ void __launch_bounds__(kBlock, dia_min_blocks<T, ND, BANDS>()) spmv_d
                                                           DiaOffs offs, const T* __restrict__ x,
                                                           T* __restrict__ y, int64_t nrows, int nd, T* partials,
                                                           unsigned int* counter, Epi epi, Gather gat = Gather{}) {
-  if (epi.skip()) return;
+  pdl_launch_dependents();
   constexpr int VEC = DiaVec<T>::kVec;
   // ND < kDiaGeneric: exactly ND diagonals, every loop straight-line code
   // (runtime bounds there split the unrolled loops into branches, and the
@@ -775,16 +797,26 @@ __global__ void __launch_bounds__(kBlock, dia_min_blocks<T, ND, BANDS>()) spmv_d
   dia_ranges(n, offs.off[0], offs.off[ndr - 1], VEC, glo, ghi, nb);
   const int head = min(glo * VEC, n);
   const int span = ghi - glo;
+  // every thread waits for the previous kernel (under a programmatic launch)
+  // and tests the epilogue's skip after the wait, all alike; the inner groups
+  // of a full grid load their values first
   if constexpr (FULL) {
     // the other rows first: their blocks are scheduled first and overlap
     // the inner groups, instead of lengthening the kernel's tail
-    if (tid < nb) {
-      dia_row<T, ND, Epi, FMA, V, Gather>(tid < head ? tid : ghi * VEC + (tid - head), n, vals, mask, ld, offs, ndr,
-                                          x, y, epi, gat, a);
-    } else if (tid - nb < span) {
-      dia_group<T, ND, Epi, FMA, V, Gather, BANDS>(glo + tid - nb, vals, mask, ld, offs, ndr, x, y, epi, gat, a);
+    if (tid >= nb && tid - nb < span) {
+      if (!dia_group<T, ND, Epi, FMA, V, Gather, BANDS, true>(glo + tid - nb, vals, mask, ld, offs, ndr, x, y, epi,
+                                                              gat, a))
+        return;
+    } else {
+      pdl_wait();
+      if (epi.skip()) return;
+      if (tid < nb)
+        dia_row<T, ND, Epi, FMA, V, Gather>(tid < head ? tid : ghi * VEC + (tid - head), n, vals, mask, ld, offs,
+                                            ndr, x, y, epi, gat, a);
     }
   } else {
+    pdl_wait();
+    if (epi.skip()) return;
     for (int g = glo + tid; g < ghi; g += stride)
       dia_group<T, ND, Epi, FMA, V, Gather, BANDS>(g, vals, mask, ld, offs, ndr, x, y, epi, gat, a);
     // the other rows go to the threads counted from the end of the grid,

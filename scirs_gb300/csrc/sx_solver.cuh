@@ -164,15 +164,20 @@ static int graph_build(sx_ctx ctx, const uint64_t key[8], Rec record, GraphEntry
   cudaError_t ce = cudaStreamEndCapture(ctx->stream, &captured);
   e.kernels_per_iter = (int)(ctx->launches - before);
   ctx->launches = before;
-  if (rc != SX_OK || ce != cudaSuccess) {
+  cudaError_t ie = cudaSuccess;
+  if (rc == SX_OK && ce == cudaSuccess) ie = cudaGraphInstantiate(&e.exec, e.graph, 0);
+  if (rc != SX_OK || ce != cudaSuccess || ie != cudaSuccess) {
     cudaGraphDestroy(e.graph);
     cudaGetLastError();
+    // a graph whose programmatic launches the driver will not capture or
+    // instantiate: once more with plain launches for this context
+    if (ctx->pdl && (ce != cudaSuccess || ie != cudaSuccess)) {
+      ctx->pdl = false;
+      clear_error();
+      return graph_build(ctx, key, record, out);
+    }
     if (rc != SX_OK) return rc;
-    return cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
-  }
-  cudaError_t ie = cudaGraphInstantiate(&e.exec, e.graph, 0);
-  if (ie != cudaSuccess) {
-    cudaGraphDestroy(e.graph);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
     return cuda_fail(ie, "cudaGraphInstantiate", __FILE__, __LINE__);
   }
   c->graphs.push_back(e);

@@ -411,3 +411,29 @@ def test_band_kernels_bit_exact(S, ctx, dtype):
             b.close()
     finally:
         cb.close()
+
+
+def test_programmatic_launch_same_bits(S):
+    # SpMVs launched with programmatic dependent launch (the default) and
+    # without (SX_PDL=0): the same products and solver runs, bit for bit
+    ip, ix, v = S.generate("aniso_q1", 96, 80, param0=40.0, param1=0.7)
+    n = len(ip) - 1
+    b = np.random.default_rng(5).standard_normal(n)
+    out = {}
+    for mode in ("1", "0"):
+        c = _ctx_with(S, {"SX_PDL": mode})
+        a = S.csr_from_arrays(c, ip, ix, v, (n, n))
+        a32 = a.astype(np.float32)
+        m = S.jacobi(c, a)
+        m32 = S.jacobi(c, a32)
+        r = S.cg(a, b, max_iter=5000, rtol=1e-10, atol=0.0, preconditioner=m)
+        rm = S.cg_mixed(a, b, tol=1e-9, preconditioner=m32, a32=a32)
+        out[mode] = (a32.matvec(b.astype(np.float32)), r.iterations, r.x, rm.inner_iterations, rm.x)
+        for op in (m, m32, a32, a):
+            op.close()
+        c.close()
+    y1, it1, x1, im1, xm1 = out["1"]
+    y0, it0, x0, im0, xm0 = out["0"]
+    assert np.array_equal(y1.view(np.uint8), y0.view(np.uint8))
+    assert it1 == it0 and np.array_equal(x1.view(np.uint8), x0.view(np.uint8))
+    assert im1 == im0 and np.array_equal(xm1.view(np.uint8), xm0.view(np.uint8))
