@@ -628,6 +628,8 @@ def run_ours(args):
                      "launch_us": t_a32_stream * 1e6,
                      "timing": "average launch duration over 60 back-to-back launches rotating over "
                                f"{len(copies)} copies of A, x, y (> 2x L2), L2 flushed before each run; "
+                               "each launch programmatic (it loads its values while the previous one "
+                               "finishes, and waits for it on the device before reading x); "
                                f"a single event-bracketed launch takes {t_a32 * 1e6:.2f} us "
                                f"({b_a32 / t_a32 / 1e9 / peak:.3f} of peak)",
                      "csr_equivalent_bytes": spmv_bytes(n, nnz, 4), "traffic": traffic},
