@@ -443,7 +443,7 @@ static int cg_run(sx_ctx ctx, sx_op a, const void* b, const sx_cg_options* opt, 
   };
   const uint64_t key[8] = {1, (uint64_t)sizeof(T), a->serial, m ? m->serial : 0,
                            (uint64_t)n, (uint64_t)(uintptr_t)ws, (uint64_t)pk, recur ? 1u : 0u};
-  SX_CHECK(run_loop(ctx, st, key, op_graphable(a) && op_graphable(m), body));
+  SX_CHECK(run_loop(ctx, st, key, op_graphable(a) && op_graphable(m) && loop_as_graph(ctx, n), body));
   SX_CHECK(ic0_health(ctx, m));
   SX_CHECK(ic0_health(ctx, a));
   SX_CHECK(read_ctl(ctx, st, &h, sizeof(h)));
@@ -868,7 +868,7 @@ static int cg_mixed_fused(sx_ctx ctx, sx_op a64, sx_op a32, sx_op m, const doubl
   double prev = rnorm;
   int stalls = 0;
   for (;;) {
-    SX_CHECK(run_loop(ctx, ms, key, true, body));
+    SX_CHECK(run_loop(ctx, ms, key, loop_as_graph(ctx, n), body));
     SX_CHECK(read_ctl(ctx, ms, &hs, sizeof(hs)));
     *inner += hs.cg.c.iterations;
     SX_CHECK(launch_vec<double>(ctx, n, IrFold{dx, X}));

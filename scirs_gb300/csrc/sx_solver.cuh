@@ -239,6 +239,14 @@ static int vec_out(sx_ctx ctx, void* dst, const void* src, size_t bytes, sx_mem 
   return SX_OK;
 }
 
+// Rows from which the CG loops run as stream launches rather than a captured
+// graph while SpMVs are programmatic: consecutive programmatic launches
+// overlap on a stream but not inside a graph's WHILE body (1024^2 Q1 learned
+// solve: 102.4 ms on the stream, 106.4 ms as a graph; small problems keep
+// the graph, whose launches cost the host nothing)
+constexpr int64_t kStreamLoopRows = int64_t(1) << 18;
+static bool loop_as_graph(sx_ctx ctx, int64_t n) { return !(ctx->pdl && n >= kStreamLoopRows); }
+
 // Runs iterations until the state reports the end.  With a graph, one launch
 // executes up to kBudget iterations of the captured body; otherwise the same
 // body is enqueued in chunks of 32 iterations.
