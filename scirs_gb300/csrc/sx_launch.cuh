@@ -228,9 +228,14 @@ void dia_go(sx_ctx ctx, const DevCsr& c, const V* vals, const T* x, T* y, Epi ep
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, Kern, vals, (const uint16_t*)c.dia_mask, (int64_t)c.dia_ld, offs, x, y,
-                       (int64_t)c.nrows, (int)c.dia_n, (T*)ra.partials, ra.counter, epi, gat);
-    return;
+    const cudaError_t le = cudaLaunchKernelEx(&cfg, Kern, vals, (const uint16_t*)c.dia_mask, (int64_t)c.dia_ld,
+                                              offs, x, y, (int64_t)c.nrows, (int)c.dia_n, (T*)ra.partials,
+                                              ra.counter, epi, gat);
+    if (le == cudaSuccess) return;
+    // a runtime that refuses the attribute: plain launches from here on (a
+    // launch error proper comes back from the plain launch below)
+    (void)cudaGetLastError();
+    ctx->pdl = false;
   }
   Kern<<<(unsigned)grid, kBlock, 0, ctx->stream>>>(vals, c.dia_mask, c.dia_ld, offs, x, y, c.nrows, c.dia_n,
                                                     (T*)ra.partials, ra.counter, epi, gat);

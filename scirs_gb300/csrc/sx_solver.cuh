@@ -169,7 +169,7 @@ static int graph_build(sx_ctx ctx, const uint64_t key[8], Rec record, GraphEntry
   if (rc != SX_OK || ce != cudaSuccess || ie != cudaSuccess) {
     cudaGraphDestroy(e.graph);
     cudaGetLastError();
-    // a graph whose programmatic launches the driver will not capture or
+    // a graph whose programmatic launches the CUDA driver will not capture or
     // instantiate: once more with plain launches for this context
     if (ctx->pdl && (ce != cudaSuccess || ie != cudaSuccess)) {
       ctx->pdl = false;
