@@ -125,6 +125,15 @@ int sx_probe_gather_rate(sx_ctx ctx, sx_dtype dtype, uint64_t n, uint64_t m, dou
  * kernels included), for launch accounting. */
 uint64_t sx_ctx_kernel_launches(sx_ctx ctx);
 
+/* Device memory the library freed is held for reuse (up to 4 GiB per GPU;
+ * a block is reused only after the work queued on every context stream of
+ * its GPU at the time of the free has completed; SX_MEM_CACHE=0 in the
+ * environment turns this off).  sx_mem_cache_trim returns every held block
+ * to the CUDA driver; sx_mem_cache_bytes reports how much is held.  No
+ * reference counterpart: the reference's arrays live in host memory. */
+int sx_mem_cache_trim(void);
+uint64_t sx_mem_cache_bytes(void);
+
 /* --------------------------------------------------------------- operators */
 /* One handle type for matrices, operators and preconditioners: the
  * reference's preconditioner slot is itself Box<dyn LinearOperator<F>>

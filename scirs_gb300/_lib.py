@@ -235,6 +235,8 @@ _SIGS = {
     "sx_wait_selftest": (c_int, [ctx_t, P(c_u64)]),
     "sx_probe_gather_rate": (c_int, [ctx_t, c_int, c_u64, c_u64, P(C.c_double)]),
     "sx_ctx_set_cg_recurrence": (c_int, [ctx_t, c_int]),
+    "sx_mem_cache_trim": (c_int, []),
+    "sx_mem_cache_bytes": (c_u64, []),
     "sx_csr_from_triplets": (c_int, [ctx_t, c_int, c_int, c_vp, c_vp, c_vp, c_u64, c_u64, c_u64, c_int, P(op_t)]),
     "sx_csr_from_raw": (c_int, [ctx_t, c_int, c_int, c_vp, c_u64, c_vp, c_vp, c_u64, c_u64, c_u64, P(op_t)]),
     "sx_csr_from_raw_i32": (c_int, [ctx_t, c_int, c_vp, c_vp, c_vp, c_u64, c_u64, c_u64, c_int, P(op_t)]),

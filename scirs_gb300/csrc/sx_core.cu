@@ -19,7 +19,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include <cuda_fp16.h>
@@ -89,22 +92,227 @@ static int err_arg(const char* what) {
   return set_error(SX_ERR_INVALID_ARGUMENT, std::string("Invalid argument: ") + what);
 }
 
+// ------------------------------------------------------------ block cache
+// Freed device blocks are kept for reuse rather than returned through
+// cudaFree (which waits for the whole device) and taken again from
+// cudaMalloc: one learned-preconditioner setup frees and allocates about
+// sixty blocks, 4 ms of a 100 ms solve when each goes to the driver.
+//
+// A block freed while work queued on the library's streams may still use it
+// carries one event per stream registered on its device (every context's
+// stream), recorded at the free; it is handed out again only once all of
+// them have completed (cudaEventQuery: the allocation never waits; a block
+// still in use is skipped and cudaMalloc serves the request).  At most
+// kCacheBytes per device are held (blocks above kCacheMaxBlock go straight
+// back to the driver); a failed cudaMalloc empties the device's cache and
+// tries once more.  Blocks freed while one of the device's streams is being
+// captured go back to cudaFree as before.  SX_MEM_CACHE=0 turns the cache
+// off; sx_mem_cache_trim() returns every held block to the driver.
+namespace {
+constexpr size_t kCacheBytes = (size_t)4 << 30;
+constexpr size_t kCacheMaxBlock = (size_t)1 << 30;
+
+struct CachedBlock {
+  void* p;
+  size_t bytes;
+  std::vector<cudaEvent_t> evs;
+};
+
+struct BlockCache {
+  std::mutex mu;
+  bool init = false, on = true;
+  std::unordered_map<void*, std::pair<size_t, int>> live;         // block -> (bytes, device)
+  std::multimap<std::pair<int, size_t>, CachedBlock> blocks;       // (device, bytes) -> block
+  std::map<int, size_t> held;                                      // device -> bytes held
+  std::vector<std::pair<int, cudaStream_t>> streams;               // registered context streams
+  std::map<int, std::vector<cudaEvent_t>> spare;                   // device -> unused events
+};
+
+// never destroyed: blocks may be freed from static destructors at exit
+BlockCache& block_cache() {
+  static BlockCache* c = new BlockCache();
+  return *c;
+}
+
+// sizes served: up to 1 MiB a power of two (at least 1 KiB), above that a
+// multiple of 2 MiB, so that repeated requests of one array size meet
+size_t cache_round(size_t bytes) {
+  if (bytes <= ((size_t)1 << 20)) {
+    size_t r = 1024;
+    while (r < bytes) r <<= 1;
+    return r;
+  }
+  return align_up(bytes, (size_t)2 << 20);
+}
+
+bool events_done(const CachedBlock& b) {
+  for (cudaEvent_t e : b.evs)
+    if (cudaEventQuery(e) != cudaSuccess) return false;
+  return true;
+}
+
+// caller holds mu; the block's events go back to the device's spare list
+void recycle_events(BlockCache& bc, int dev, CachedBlock& b) {
+  auto& sp = bc.spare[dev];
+  sp.insert(sp.end(), b.evs.begin(), b.evs.end());
+  b.evs.clear();
+}
+
+// returns the device's held blocks to the driver (cudaFree waits for the
+// device first); caller holds mu
+void cache_release_device(BlockCache& bc, int dev) {
+  for (auto it = bc.blocks.lower_bound({dev, 0}); it != bc.blocks.end() && it->first.first == dev;) {
+    recycle_events(bc, dev, it->second);
+    cudaFree(it->second.p);
+    it = bc.blocks.erase(it);
+  }
+  bc.held[dev] = 0;
+}
+
+void cache_init(BlockCache& bc) {
+  if (bc.init) return;
+  bc.init = true;
+  if (const char* t = std::getenv("SX_MEM_CACHE")) bc.on = std::strcmp(t, "0") != 0;
+}
+}  // namespace
+
+void mem_cache_register_stream(int device, cudaStream_t s) {
+  BlockCache& bc = block_cache();
+  std::lock_guard<std::mutex> lk(bc.mu);
+  bc.streams.emplace_back(device, s);
+}
+
+void mem_cache_unregister_stream(int device, cudaStream_t s) {
+  BlockCache& bc = block_cache();
+  std::lock_guard<std::mutex> lk(bc.mu);
+  for (auto it = bc.streams.begin(); it != bc.streams.end(); ++it)
+    if (it->first == device && it->second == s) {
+      bc.streams.erase(it);
+      return;
+    }
+}
+
 // Every device array carries 64 bytes of slack past its end: the windowed
 // SpMV's 16-byte copies may read up to 15 bytes past the last element.
 int dev_alloc(void** p, size_t bytes) {
   *p = nullptr;
-  SX_CUDA(cudaMalloc(p, align_up(bytes, 16) + 64));
+  const size_t want = cache_round(align_up(bytes, 16) + 64);
+  int dev = 0;
+  SX_CUDA(cudaGetDevice(&dev));
+  BlockCache& bc = block_cache();
+  {
+    std::lock_guard<std::mutex> lk(bc.mu);
+    cache_init(bc);
+    if (bc.on) {
+      // the smallest held block that fits, at most 1/8 larger, whose users
+      // have finished
+      const size_t most = want + want / 8;
+      for (auto it = bc.blocks.lower_bound({dev, want});
+           it != bc.blocks.end() && it->first.first == dev && it->first.second <= most; ++it) {
+        if (!events_done(it->second)) continue;
+        *p = it->second.p;
+        const size_t got = it->second.bytes;
+        recycle_events(bc, dev, it->second);
+        bc.blocks.erase(it);
+        bc.held[dev] -= got;
+        bc.live[*p] = {got, dev};
+        return SX_OK;
+      }
+    }
+  }
+  cudaError_t e = cudaMalloc(p, want);
+  if (e == cudaErrorMemoryAllocation) {
+    (void)cudaGetLastError();
+    {
+      std::lock_guard<std::mutex> lk(bc.mu);
+      cache_release_device(bc, dev);
+    }
+    e = cudaMalloc(p, want);
+  }
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+  }
+  std::lock_guard<std::mutex> lk(bc.mu);
+  bc.live[*p] = {want, dev};
   return SX_OK;
 }
+
 void dev_free(void* p) {
-  if (p) cudaFree(p);
+  if (!p) return;
+  BlockCache& bc = block_cache();
+  std::unique_lock<std::mutex> lk(bc.mu);
+  cache_init(bc);
+  auto it = bc.live.find(p);
+  if (it == bc.live.end()) {  // not from dev_alloc
+    lk.unlock();
+    cudaFree(p);
+    return;
+  }
+  const size_t bytes = it->second.first;
+  const int dev = it->second.second;
+  bc.live.erase(it);
+  bool keep = bc.on && bytes <= kCacheMaxBlock;
+  for (const auto& s : bc.streams) {
+    if (!keep) break;
+    if (s.first != dev) continue;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s.second, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) keep = false;
+  }
+  if (!keep) {
+    lk.unlock();
+    cudaFree(p);
+    return;
+  }
+  int cur = dev;
+  cudaGetDevice(&cur);
+  if (cur != dev) cudaSetDevice(dev);
+  CachedBlock b{p, bytes, {}};
+  auto& sp = bc.spare[dev];
+  for (const auto& s : bc.streams) {
+    if (s.first != dev) continue;
+    cudaEvent_t e = nullptr;
+    if (!sp.empty()) {
+      e = sp.back();
+      sp.pop_back();
+    } else if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      keep = false;
+      break;
+    }
+    b.evs.push_back(e);
+    if (cudaEventRecord(e, s.second) != cudaSuccess) {
+      keep = false;
+      break;
+    }
+  }
+  if (!keep) {
+    (void)cudaGetLastError();
+    recycle_events(bc, dev, b);
+    if (cur != dev) cudaSetDevice(cur);
+    lk.unlock();
+    cudaFree(p);
+    return;
+  }
+  bc.blocks.emplace(std::make_pair(dev, bytes), std::move(b));
+  bc.held[dev] += bytes;
+  // over the limit: the largest finished blocks go back to the driver
+  for (auto jt = bc.blocks.lower_bound({dev + 1, 0}); bc.held[dev] > kCacheBytes && jt != bc.blocks.begin();) {
+    --jt;
+    if (jt->first.first != dev) break;
+    if (!events_done(jt->second)) continue;
+    recycle_events(bc, dev, jt->second);
+    cudaFree(jt->second.p);
+    bc.held[dev] -= jt->first.second;
+    jt = bc.blocks.erase(jt);
+  }
+  if (cur != dev) cudaSetDevice(cur);
 }
 
 int ctx_scratch(sx_ctx ctx, size_t bytes, void** out) {
   if (bytes > ctx->scratch_bytes) {
     if (ctx->scratch) {
       SX_CUDA(cudaStreamSynchronize(ctx->stream));
-      cudaFree(ctx->scratch);
+      dev_free(ctx->scratch);
       ctx->scratch = nullptr;
       ctx->scratch_bytes = 0;
     }
@@ -152,7 +360,7 @@ int ctx_reduce_area(sx_ctx ctx, int64_t blocks, ReduceArea* out) {
       SX_CUDA(cudaStreamSynchronize(ctx->stream));
       // captured solver graphs hold the old address
       solver_graphs_drop(ctx);
-      cudaFree(ctx->red_partials);
+      dev_free(ctx->red_partials);
       ctx->red_partials = nullptr;
       ctx->red_bytes = 0;
     }
@@ -1179,6 +1387,7 @@ static int ctx_init(int device, cudaStream_t stream, bool own, sx_ctx* out) {
   } else {
     c->stream = stream;
   }
+  mem_cache_register_stream(device, c->stream);
   *out = c;
   return clear_error();
 }
@@ -1199,9 +1408,33 @@ int sx_ctx_destroy(sx_ctx ctx) {
   dev_free(ctx->red_counter);
   dev_free(ctx->scratch);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  mem_cache_unregister_stream(ctx->device, ctx->stream);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SX_OK;
+}
+
+int sx_mem_cache_trim(void) {
+  BlockCache& bc = block_cache();
+  std::lock_guard<std::mutex> lk(bc.mu);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  std::vector<int> devs;
+  for (const auto& h : bc.held) devs.push_back(h.first);
+  for (int d : devs) {
+    cudaSetDevice(d);
+    cache_release_device(bc, d);
+  }
+  cudaSetDevice(cur);
+  return SX_OK;
+}
+
+uint64_t sx_mem_cache_bytes(void) {
+  BlockCache& bc = block_cache();
+  std::lock_guard<std::mutex> lk(bc.mu);
+  uint64_t t = 0;
+  for (const auto& h : bc.held) t += h.second;
+  return t;
 }
 void* sx_ctx_stream(sx_ctx ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 int sx_ctx_synchronize(sx_ctx ctx) {

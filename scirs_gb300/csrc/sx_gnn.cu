@@ -601,6 +601,13 @@ __global__ void k_scale_g(const int32_t* __restrict__ gp, const float* __restric
     for (int32_t e = gp[i]; e < gp[i + 1]; ++e) out[e] = (T)((double)g[e] * (double)dis[i]);
 }
 
+// G^T values on the transposed pattern: entry k of G^T is entry perm[k] of G
+template <typename T>
+__global__ void k_gather_entries(const int32_t* __restrict__ perm, const T* __restrict__ src, int64_t m, T* out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = src[perm[k]];
+}
+
 // ============================================================ host side
 int prep_graph(sx_ctx ctx, sx_gnn net, sx_op a, Graph** out) {
   for (auto& g : net->graphs)
@@ -1075,12 +1082,35 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out) {
       if (g->ng > 0) cudaMemcpyAsync(c.indices, g->gi, g->ng * 4, cudaMemcpyDeviceToDevice, ctx->stream);
       rc = csr_finalize_stats(ctx, c, (int)w);
     }
+    // G^T on the transposed pattern the graph already holds: a gather of
+    // G's values instead of a second transpose (the same arrays: the
+    // graph's transpose is the counting sort of G's pattern)
+    DevCsr t;
+    t.nrows = t.ncols = n;
+    t.nnz = g->ng;
+    if (rc == SX_OK && (rc = dev_alloc((void**)&t.indptr, (n + 1) * 4)) == SX_OK &&
+        (rc = dev_alloc((void**)&t.indices, std::max<int64_t>(g->ng, 1) * 4)) == SX_OK &&
+        (rc = dev_alloc(&t.vals, std::max<int64_t>(g->ng, 1) * w)) == SX_OK) {
+      cudaMemcpyAsync(t.indptr, g->tp, (n + 1) * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+      if (g->ng > 0) {
+        cudaMemcpyAsync(t.indices, g->ti, g->ng * 4, cudaMemcpyDeviceToDevice, ctx->stream);
+        const int ge = vec_grid(ctx, g->ng);
+        if (a->dtype == SX_F64)
+          k_gather_entries<double><<<ge, kBlock, 0, ctx->stream>>>(g->tperm, (const double*)c.vals, g->ng,
+                                                                   (double*)t.vals);
+        else
+          k_gather_entries<float><<<ge, kBlock, 0, ctx->stream>>>(g->tperm, (const float*)c.vals, g->ng,
+                                                                  (float*)t.vals);
+        ctx->launches++;
+      }
+      rc = csr_finalize_stats(ctx, t, (int)w);
+    }
     if (rc != SX_OK) {
-      sx_op tmp = csr_op_adopt(ctx, a->dtype, c);  // frees the arrays
-      destroy_op_internal(tmp);
+      destroy_op_internal(csr_op_adopt(ctx, a->dtype, c));  // frees the arrays
+      destroy_op_internal(csr_op_adopt(ctx, a->dtype, t));
       break;
     }
-    rc = fsai_adopt(ctx, csr_op_adopt(ctx, a->dtype, c), out);
+    rc = fsai_adopt(ctx, csr_op_adopt(ctx, a->dtype, c), out, csr_op_adopt(ctx, a->dtype, t));
     // the factor's values in FP16 for the solvers (the network's output is
     // already limited by its BF16 weights); FP32 stays for exact applies
     if (rc == SX_OK && a->dtype == SX_F32) {

@@ -211,6 +211,9 @@ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 // Allocation helpers that record the CUDA error.
 int dev_alloc(void** p, size_t bytes);
 void dev_free(void* p);
+// the streams whose queued work a freed block waits for before its reuse
+void mem_cache_register_stream(int device, cudaStream_t s);
+void mem_cache_unregister_stream(int device, cudaStream_t s);
 
 // Upload host-side CSR arrays (already validated, int32) into a DevCsr and
 // compute row statistics.
@@ -259,7 +262,7 @@ int wait_selftest(sx_ctx ctx, uint64_t* waited_ns);
 // Cached transpose of a CSR operator (rmatvec, FSAI's G^T).
 int ensure_transpose(sx_ctx ctx, sx_op a);
 int csr_transpose_internal(sx_ctx ctx, sx_op a, sx_op* out, bool stats = true);
-int fsai_adopt(sx_ctx ctx, sx_op g, sx_op* out);  // takes g
+int fsai_adopt(sx_ctx ctx, sx_op g, sx_op* out, sx_op gt = nullptr);  // takes g (and gt: G^T, else computed)
 sx_op csr_op_adopt(sx_ctx ctx, int dtype, DevCsr& c);  // takes c
 int sym_half_spmv(sx_ctx ctx, sx_op a, const void* x, void* y);  // sx_sym.cu
 // rows in dependency-level order (forward: on the rows j < i of the pattern;

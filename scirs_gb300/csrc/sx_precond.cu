@@ -217,8 +217,9 @@ int sx_precond_jacobi_from_diagonal(sx_ctx ctx, sx_dtype dtype, const void* diag
 namespace sx {
 // FSAI operator that takes over the CSR arrays of g (a temporary the caller
 // no longer needs): one transpose for G^T instead of the public entry's
-// copy.  g's shell is destroyed whatever the outcome.
-int fsai_adopt(sx_ctx ctx, sx_op g, sx_op* out) {
+// copy, or none when the caller built G^T (gt, taken over as well).  g's and
+// gt's shells are destroyed whatever the outcome.
+int fsai_adopt(sx_ctx ctx, sx_op g, sx_op* out, sx_op gt) {
   *out = nullptr;
   sx_op op = new sx_op_s();
   op->kind = SX_OP_FSAI;
@@ -226,7 +227,9 @@ int fsai_adopt(sx_ctx ctx, sx_op g, sx_op* out) {
   op->device = ctx->device;
   op->nrows = op->ncols = g->nrows;
   op->serial = next_op_serial();
-  int rc = csr_transpose_internal(ctx, g, &op->transpose);
+  int rc = SX_OK;
+  if (gt) op->transpose = gt;
+  else rc = csr_transpose_internal(ctx, g, &op->transpose);
   if (rc == SX_OK) {
     op->csr = g->csr;
     g->csr = DevCsr();

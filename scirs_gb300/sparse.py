@@ -65,6 +65,16 @@ def message_string(code: int) -> str:
     return L.lib.sx_message_string(code).decode("utf-8")
 
 
+def mem_cache_trim() -> None:
+    """Return the device blocks the library holds for reuse to the driver."""
+    _check(L.lib.sx_mem_cache_trim())
+
+
+def mem_cache_bytes() -> int:
+    """Device bytes the library holds for reuse (freed blocks)."""
+    return int(L.lib.sx_mem_cache_bytes())
+
+
 _NP = {L.SX_F32: np.float32, L.SX_F64: np.float64}
 
 

@@ -105,6 +105,39 @@ def test_learned_preconditioner_is_spd_apply(S, ctx):
         assert x @ mx > 0
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_learned_factor_matches_dense_g(S, ctx, dtype):
+    # M^-1 x = G (G^T x) with G = D^-1/2 G^ on the network's pattern (each
+    # row's strict-lower columns, then the diagonal): G^T comes from the
+    # graph's transposed pattern, so a wrong entry permutation would break
+    # the product (and its symmetry), not just round it differently
+    ip, ix, v, a = _aniso(S, ctx, 20, 17, 30.0, 0.6, dtype)
+    net = S.LearnedSAI(ctx, seed=2)
+    m = net.preconditioner(a)
+    g = net.edge_values(a).astype(np.float64)
+    n = a.shape[0]
+    G = np.zeros((n, n))
+    pos = 0
+    for i in range(n):
+        row = ix[ip[i]:ip[i + 1]]
+        d = np.float64(v.astype(dtype)[ip[i]:ip[i + 1]][row == i][0])
+        dis = np.float64(np.float32(1.0 / np.sqrt(d)))
+        for c in list(row[row < i]) + [i]:
+            G[i, c] = np.float64(dtype(g[pos] * dis))
+            pos += 1
+    assert pos == len(g)
+    rng = np.random.default_rng(5)
+    for _ in range(2):
+        x = rng.standard_normal(n)
+        ref = G @ (G.T @ x.astype(dtype).astype(np.float64))
+        out = m.matvec(x.astype(dtype)).astype(np.float64)
+        tol = 1e-12 if dtype == np.float64 else 2e-5
+        assert np.abs(out - ref).max() <= tol * np.abs(ref).max()
+    m.close()
+    net.close()
+    a.close()
+
+
 def test_fp16_factor_matches_fp32_factor_iterations(S, ctx):
     # the learned preconditioner's solver applies read G in FP16; the same G
     # in FP32 (a user FSAI operator) needs about as many PCG iterations
