@@ -159,6 +159,65 @@ __global__ void k_count_off_lower(const int32_t* __restrict__ ptr, const int32_t
   }
 }
 
+// position of column c in row r (columns strictly increasing), or -1
+__device__ __forceinline__ int32_t row_find(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                            int32_t r, int32_t c) {
+  int32_t lo = ptr[r], hi = ptr[r + 1];
+  while (lo < hi) {
+    const int32_t mid = lo + (hi - lo) / 2;
+    if (idx[mid] < c) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < ptr[r + 1] && idx[lo] == c ? lo : -1;
+}
+
+// Structurally symmetric A (every row's columns strictly increasing, and
+// (j, i) stored for every stored (i, j)): the transpose of G's pattern (each
+// row's strict-lower columns, then the diagonal) has in row j the diagonal
+// and then row j's upper columns, in that order.  flag is set when A is not
+// such a matrix; t_cnt[j] = row j's upper entries + 1.
+__global__ void k_sym_pattern(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n,
+                              int32_t* t_cnt, int* flag) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t up = 0, prev = -1;
+    bool bad = false;
+    for (int32_t k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int32_t j = idx[k];
+      if (j <= prev || j < 0 || j >= n) {
+        bad = true;
+        break;
+      }
+      prev = j;
+      up += j > (int32_t)i;
+      if (row_find(ptr, idx, j, (int32_t)i) < 0) bad = true;
+    }
+    t_cnt[i] = up + 1;
+    if (bad) *flag = 1;
+  }
+}
+
+// G^T's pattern and entry map (G^T entry -> G entry) of a structurally
+// symmetric A: entry (j, j) is G's last entry of row j; entry (j, i), i > j,
+// is G's entry of column j in row i, whose strict-lower columns are row i's
+// first ones
+__global__ void k_gt_from_sym(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n,
+                              const int32_t* __restrict__ gp, const int32_t* __restrict__ tp, int32_t* ti,
+                              int32_t* tperm) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    int32_t t = tp[j];
+    ti[t] = (int32_t)j;
+    tperm[t] = gp[j + 1] - 1;
+    ++t;
+    for (int32_t k = ptr[j]; k < ptr[j + 1]; ++k) {
+      const int32_t i = idx[k];
+      if (i <= (int32_t)j) continue;
+      ti[t] = i;
+      tperm[t] = gp[i] + (row_find(ptr, idx, i, (int32_t)j) - ptr[i]);
+      ++t;
+    }
+  }
+}
+
 template <typename T>
 __global__ void k_fill_graph(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                              const T* __restrict__ val, int64_t n, const float* __restrict__ dis,
@@ -182,13 +241,13 @@ __global__ void k_fill_graph(const int32_t* __restrict__ ptr, const int32_t* __r
       if (j < (int32_t)i) {
         gi[g] = j;
         ga[g] = a;
-        gidx[g] = (double)g;
+        if (gidx) gidx[g] = (double)g;
         ++g;
       }
     }
     gi[g] = (int32_t)i;
     ga[g] = 0.f;
-    gidx[g] = (double)g;
+    if (gidx) gidx[g] = (double)g;
     bf16* xr = x0 + i * kK0;
     xr[0] = __float2bfloat16(1.f);
     xr[1] = __float2bfloat16(s_abs);
@@ -248,6 +307,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const bf16* __restrict__ A, c
 }
 
 // --- message passing: pre = S_self + sum_j a^_ij S_nb[j] + b; h = bf16(relu(pre))
+// (pre is stored for the backward pass only: null when the network predicts)
 __global__ void k_aggregate(const float* __restrict__ S, const int32_t* __restrict__ op,
                             const int32_t* __restrict__ oi, const float* __restrict__ ov,
                             const float* __restrict__ bias, int64_t n, float* pre, bf16* hout) {
@@ -264,7 +324,7 @@ __global__ void k_aggregate(const float* __restrict__ S, const int32_t* __restri
     }
     const float px = self.x + ax + bias[2 * lane];
     const float py = self.y + ay + bias[2 * lane + 1];
-    *reinterpret_cast<float2*>(pre + i * kH + 2 * lane) = make_float2(px, py);
+    if (pre) *reinterpret_cast<float2*>(pre + i * kH + 2 * lane) = make_float2(px, py);
     hout[i * kH + 2 * lane] = __float2bfloat16(fmaxf(px, 0.f));
     hout[i * kH + 2 * lane + 1] = __float2bfloat16(fmaxf(py, 0.f));
   }
@@ -625,7 +685,7 @@ int prep_graph(sx_ctx ctx, sx_gnn net, sx_op a, Graph** out) {
   g.n = a->nrows;
   const int64_t n = g.n;
   const int gr = vec_grid(ctx, n);
-  int32_t *ocnt = nullptr, *gcnt = nullptr;
+  int32_t *ocnt = nullptr, *gcnt = nullptr, *tcnt = nullptr;
   int* bad = nullptr;
   double* gidx = nullptr;
   int rc = SX_OK;
@@ -635,30 +695,36 @@ int prep_graph(sx_ctx ctx, sx_gnn net, sx_op a, Graph** out) {
     if ((rc = dev_alloc((void**)&bad, 16))) break;
     if ((rc = dev_alloc((void**)&ocnt, (nb + 1) * 4))) break;
     if ((rc = dev_alloc((void**)&gcnt, (nb + 1) * 4))) break;
+    if ((rc = dev_alloc((void**)&tcnt, (nb + 1) * 4))) break;
     if ((rc = dev_alloc((void**)&g.op, (nb + 1) * 4))) break;
     if ((rc = dev_alloc((void**)&g.gp, (nb + 1) * 4))) break;
+    if ((rc = dev_alloc((void**)&g.tp, (nb + 1) * 4))) break;
     SX_CUDA(cudaMemsetAsync(bad, 0, 16, ctx->stream));
     if (a->dtype == SX_F64)
       k_dis<double><<<gr, kBlock, 0, ctx->stream>>>(a->csr.indptr, a->csr.indices, (const double*)a->csr.vals, n, g.dis, bad);
     else
       k_dis<float><<<gr, kBlock, 0, ctx->stream>>>(a->csr.indptr, a->csr.indices, (const float*)a->csr.vals, n, g.dis, bad);
     k_count_off_lower<<<gr, kBlock, 0, ctx->stream>>>(a->csr.indptr, a->csr.indices, n, ocnt, gcnt);
-    ctx->launches += 2;
+    k_sym_pattern<<<gr, kBlock, 0, ctx->stream>>>(a->csr.indptr, a->csr.indices, n, tcnt, bad + 1);
+    ctx->launches += 3;
     if ((rc = exclusive_scan_i32(ctx, ocnt, n, g.op))) break;
     if ((rc = exclusive_scan_i32(ctx, gcnt, n, g.gp))) break;
-    int hb = 0;
+    if ((rc = exclusive_scan_i32(ctx, tcnt, n, g.tp))) break;
+    int hb[2] = {0, 0};
     int32_t noff = 0, ng = 0;
-    SX_CUDA(cudaMemcpy(&hb, bad, 4, cudaMemcpyDeviceToHost));
-    SX_CUDA(cudaMemcpy(&noff, g.op + n, 4, cudaMemcpyDeviceToHost));
-    SX_CUDA(cudaMemcpy(&ng, g.gp + n, 4, cudaMemcpyDeviceToHost));
-    if (hb) { rc = set_error(SX_ERR_VALUE, "Value error: the network needs a positive diagonal"); break; }
+    SX_CUDA(cudaMemcpyAsync(hb, bad, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    SX_CUDA(cudaMemcpyAsync(&noff, g.op + n, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SX_CUDA(cudaMemcpyAsync(&ng, g.gp + n, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hb[0]) { rc = set_error(SX_ERR_VALUE, "Value error: the network needs a positive diagonal"); break; }
+    const bool sym = hb[1] == 0;
     g.noff = noff;
     g.ng = ng;
     if ((rc = dev_alloc((void**)&g.oi, std::max(noff, 1) * 4))) break;
     if ((rc = dev_alloc((void**)&g.ov, std::max(noff, 1) * 4))) break;
     if ((rc = dev_alloc((void**)&g.gi, std::max(ng, 1) * 4))) break;
     if ((rc = dev_alloc((void**)&g.ga, std::max(ng, 1) * 4))) break;
-    if ((rc = dev_alloc((void**)&gidx, std::max(ng, 1) * 8))) break;
+    if (!sym && (rc = dev_alloc((void**)&gidx, std::max(ng, 1) * 8))) break;
     if ((rc = dev_alloc((void**)&g.x0, nb * kK0 * sizeof(bf16)))) break;
     if (a->dtype == SX_F64)
       k_fill_graph<double><<<gr, kBlock, 0, ctx->stream>>>(a->csr.indptr, a->csr.indices, (const double*)a->csr.vals, n,
@@ -667,7 +733,19 @@ int prep_graph(sx_ctx ctx, sx_gnn net, sx_op a, Graph** out) {
       k_fill_graph<float><<<gr, kBlock, 0, ctx->stream>>>(a->csr.indptr, a->csr.indices, (const float*)a->csr.vals, n,
                                                           g.dis, g.op, g.oi, g.ov, g.gp, g.gi, g.ga, g.x0, gidx);
     ctx->launches++;
-    // transposed pattern with the entry permutation (exact through FP64 values)
+    if (sym) {
+      // the transposed pattern read off A's upper triangle: no sort
+      if ((rc = dev_alloc((void**)&g.ti, std::max(ng, 1) * 4))) break;
+      if ((rc = dev_alloc((void**)&g.tperm, std::max(ng, 1) * 4))) break;
+      k_gt_from_sym<<<gr, kBlock, 0, ctx->stream>>>(a->csr.indptr, a->csr.indices, n, g.gp, g.tp, g.ti, g.tperm);
+      ctx->launches++;
+      SX_CUDA(cudaStreamSynchronize(ctx->stream));
+      break;
+    }
+    dev_free(g.tp);
+    g.tp = nullptr;
+    // any other pattern: the transpose with the entry permutation (exact
+    // through FP64 values)
     sx_op s = new sx_op_s();
     s->kind = SX_OP_CSR;
     s->dtype = SX_F64;
@@ -692,7 +770,7 @@ int prep_graph(sx_ctx ctx, sx_gnn net, sx_op a, Graph** out) {
     t->csr.indptr = nullptr; t->csr.indices = nullptr;
     destroy_op_internal(t);
   } while (0);
-  dev_free(ocnt); dev_free(gcnt); dev_free(bad); dev_free(gidx);
+  dev_free(ocnt); dev_free(gcnt); dev_free(tcnt); dev_free(bad); dev_free(gidx);
   if (rc != SX_OK) { graph_free(g); return rc; }
   net->graphs.push_back(g);
   *out = &net->graphs.back();
@@ -741,7 +819,8 @@ void refresh_weights(sx_ctx ctx, sx_gnn net) {
 
 constexpr int kWarpGrid = 4096;   // blocks of 256 threads for warp-per-row kernels (8 warps each)
 
-int forward(sx_ctx ctx, sx_gnn net, const Graph& g) {
+// keep_pre: store the pre-activations for a backward pass
+int forward(sx_ctx ctx, sx_gnn net, const Graph& g, bool keep_pre) {
   Acts& A = net->acts;
   const int64_t n = g.n;
   const Layout& L = net->L;
@@ -752,7 +831,8 @@ int forward(sx_ctx ctx, sx_gnn net, const Graph& g) {
     if (n > 0) {
       if (l == 0) k_gemm_bf16<kK0, 2 * kH><<<gb, 128, 0, ctx->stream>>>(A.h[0], net->wc[0], A.S, n);
       else k_gemm_bf16<kH, 2 * kH><<<gb, 128, 0, ctx->stream>>>(A.h[l], net->wc[l], A.S, n);
-      k_aggregate<<<wb, 256, 0, ctx->stream>>>(A.S, g.op, g.oi, g.ov, net->params + L.b[l], n, A.pre[l], A.h[l + 1]);
+      k_aggregate<<<wb, 256, 0, ctx->stream>>>(A.S, g.op, g.oi, g.ov, net->params + L.b[l], n,
+                                               keep_pre ? A.pre[l] : nullptr, A.h[l + 1]);
       ctx->launches += 2;
     }
   }
@@ -991,7 +1071,7 @@ int sx_gnn_loss_grad(sx_ctx ctx, sx_gnn net, sx_op a, const float* probes, uint6
   Graph* g = nullptr;
   SX_CHECK(prep_graph(ctx, net, a, &g));
   SX_CHECK(acts_ensure(net, g->n, g->ng, kWarpGrid * 8));
-  SX_CHECK(forward(ctx, net, *g));
+  SX_CHECK(forward(ctx, net, *g, true));
   if (probes) SX_CUDA(cudaMemcpyAsync(net->acts.Z, probes, g->n * kP * 4, cudaMemcpyHostToDevice, ctx->stream));
   else {
     k_probes<<<vec_grid(ctx, g->n * kP), kBlock, 0, ctx->stream>>>(net->acts.Z, g->n * kP, seed);
@@ -1030,7 +1110,7 @@ int sx_gnn_edge_values(sx_ctx ctx, sx_gnn net, sx_op a, float* g_out, uint64_t* 
   Graph* g = nullptr;
   SX_CHECK(prep_graph(ctx, net, a, &g));
   SX_CHECK(acts_ensure(net, g->n, g->ng, kWarpGrid * 8));
-  SX_CHECK(forward(ctx, net, *g));
+  SX_CHECK(forward(ctx, net, *g, false));
   if (ng_out) *ng_out = (uint64_t)g->ng;
   if (g_out) SX_CUDA(cudaMemcpyAsync(g_out, net->acts.g, g->ng * 4, cudaMemcpyDeviceToHost, ctx->stream));
   SX_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1056,7 +1136,7 @@ int sx_precond_learned(sx_ctx ctx, sx_op a, sx_gnn net, sx_op* out) {
     }
   };
   int frc = acts_ensure(net, g->n, g->ng, kWarpGrid * 8);
-  if (frc == SX_OK) frc = forward(ctx, net, *g);
+  if (frc == SX_OK) frc = forward(ctx, net, *g, false);
   if (frc != SX_OK) { drop_fresh(); return frc; }
   const int64_t n = g->n;
   const size_t w = elt_size(a->dtype);

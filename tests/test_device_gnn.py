@@ -105,13 +105,23 @@ def test_learned_preconditioner_is_spd_apply(S, ctx):
         assert x @ mx > 0
 
 
-@pytest.mark.parametrize("dtype", [np.float64, np.float32])
-def test_learned_factor_matches_dense_g(S, ctx, dtype):
+@pytest.mark.parametrize("dtype,symmetric", [(np.float64, True), (np.float32, True), (np.float64, False)])
+def test_learned_factor_matches_dense_g(S, ctx, dtype, symmetric):
     # M^-1 x = G (G^T x) with G = D^-1/2 G^ on the network's pattern (each
     # row's strict-lower columns, then the diagonal): G^T comes from the
-    # graph's transposed pattern, so a wrong entry permutation would break
-    # the product (and its symmetry), not just round it differently
+    # graph's transposed pattern (read off A's upper triangle when A's
+    # pattern is symmetric, a sort otherwise), so a wrong entry permutation
+    # would break the product (and its symmetry), not just round it
     ip, ix, v, a = _aniso(S, ctx, 20, 17, 30.0, 0.6, dtype)
+    if not symmetric:
+        # drop some upper entries: a pattern without (j, i) for some (i, j)
+        n = a.shape[0]
+        a.close()
+        rows = np.repeat(np.arange(n), np.diff(ip))
+        keep = ~((ix > rows) & ((rows + ix) % 5 == 0))
+        ix, v = ix[keep], v[keep]
+        ip = np.concatenate([[0], np.cumsum(np.bincount(rows[keep], minlength=n))]).astype(ip.dtype)
+        a = S.csr_from_arrays(ctx, ip, ix, v.astype(dtype), (n, n))
     net = S.LearnedSAI(ctx, seed=2)
     m = net.preconditioner(a)
     g = net.edge_values(a).astype(np.float64)
