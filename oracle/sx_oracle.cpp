@@ -779,6 +779,7 @@ struct SolveOut {
   F residual_norm = F(0);
   bool converged = false;
   int message = M_MAX_ITER;
+  int stalled = 0;  // gmres: a cycle that cannot advance (the reference loops forever)
 };
 
 template <class F>
@@ -914,7 +915,10 @@ SolveOut<F> bicgstab(const or_op* a, const std::vector<F>& b, uint64_t max_iter,
 // gmres, iterative.rs:641-816: left-preconditioned restarted GMRES with
 // modified Gram-Schmidt and Givens rotations.  On a happy breakdown the
 // column being built is dropped (the loop breaks before the rotation and
-// before inner_iter is advanced).
+// before inner_iter is advanced).  A cycle that ends with inner_iter = 0
+// (restart = 0, or a breakdown at the first step: A r0 parallel to r0, as
+// for A = c I) leaves x, r and the iteration count as they were, so the
+// reference's loop repeats it forever; here the solve stops (stalled).
 template <class F>
 SolveOut<F> gmres(const or_op* a, const std::vector<F>& b, uint64_t max_iter, uint64_t restart_opt,
                   F rtol, F atol, const F* x0, const or_op* m) {
@@ -979,6 +983,10 @@ SolveOut<F> gmres(const or_op* a, const std::vector<F>& b, uint64_t max_iter, ui
     rnorm = norm2(r);
     outer += j;
     if (rnorm <= tol) break;
+    if (j == 0) {
+      o.stalled = 1;
+      break;
+    }
   }
   o.x = x;
   o.iterations = outer;
@@ -1670,15 +1678,24 @@ int or_gmres(const or_op* a, const void* b, uint64_t max_iter, uint64_t restart,
              or_err* err) {
   if (int rc = check_square_and_len<double>(a, "GMRES", err)) return rc;
   const uint64_t n = a->nrows;
+  int stalled = 0;
   if (a->f64) {
     std::vector<double> bv((const double*)b, (const double*)b + n);
     auto s = gmres<double>(a, bv, max_iter, restart, rtol, atol, (const double*)x0, m);
     fill_result(s, x_out, res);
+    stalled = s.stalled;
   } else {
     std::vector<float> bv((const float*)b, (const float*)b + n);
     auto s = gmres<float>(a, bv, max_iter, restart, (float)rtol, (float)atol, (const float*)x0, m);
     fill_result(s, x_out, res);
+    stalled = s.stalled;
   }
+  if (stalled)
+    return restart == 0
+               ? set_err(err, E_VALUE, value_msg("restart = 0 makes no progress (the reference loops forever)"))
+               : set_err(err, E_COMPUTATION,
+                         "Computation error: gmres cannot advance: breakdown at the first Arnoldi step "
+                         "(the reference loops forever)");
   return ok(err);
 }
 

@@ -1332,7 +1332,7 @@ struct GmState {
   LoopCtl c;
   T rnorm, tol, rtol, atol, hnorm;
   int restart, j, active;  // j: inner_iter of the current cycle; active: cycle running
-  int pad3;
+  int stalled;             // a cycle ended with j = 0: the next would repeat it
   unsigned long long outer;
 };
 
@@ -1525,6 +1525,12 @@ struct GmEnd {
       st->c.status = ST_DONE;
       st->c.converged = rnorm <= st->tol ? 1 : 0;
       st->c.message = st->c.converged ? MSG_CONVERGED : MSG_MAX_ITER;
+    } else if (st->j == 0) {
+      // a breakdown at the first Arnoldi step (A r0 parallel to r0) left x,
+      // r and the count unchanged: the reference's loop would repeat this
+      // cycle forever (iterative.rs:697-808)
+      st->c.status = ST_DONE;
+      st->stalled = 1;
     }
     if (st->c.budget > 0) st->c.budget -= 1;
     set_cond(st->c.use_cond, st->c.cond,
@@ -1645,6 +1651,10 @@ static int gmres_run(sx_ctx ctx, sx_op a, const void* b, const sx_gmres_options*
   SX_CHECK(run_loop(ctx, st, key, op_graphable(a) && op_graphable(m), body));
   SX_CHECK(ic0_health(ctx, m));
   SX_CHECK(read_ctl(ctx, st, &h, sizeof(h)));
+  if (h.stalled)
+    return set_error(SX_ERR_COMPUTATION,
+                     "Computation error: gmres cannot advance: breakdown at the first Arnoldi step "
+                     "(the reference loops forever)");
   SX_CHECK(vec_out(ctx, x_out, X, n * w, mem));
   SX_CUDA(cudaStreamSynchronize(ctx->stream));
   if (res) {
