@@ -417,7 +417,10 @@ int sx_cg(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_cg_option
 /* bicgstab (iterative.rs:377-611). */
 int sx_bicgstab(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len,
                 const sx_bicgstab_options* opt, void* x_out, sx_mem mem, sx_iter_result* res);
-/* gmres (iterative.rs:641-816). */
+/* gmres (iterative.rs:641-816).  Where the reference's loop would repeat a
+ * cycle forever without progress, the call returns instead: restart = 0 with
+ * SX_ERR_VALUE, a breakdown at a cycle's first Arnoldi step (A r0 parallel
+ * to r0, e.g. A = 2 I) with SX_ERR_COMPUTATION; x_out is then not written. */
 int sx_gmres(sx_ctx ctx, sx_op a, const void* b, uint64_t b_len, const sx_gmres_options* opt,
              void* x_out, sx_mem mem, sx_iter_result* res);
 
