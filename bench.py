@@ -223,6 +223,18 @@ def cpu_reference_solve(ip, ix, v, n, b, max_iter, threads):
     return r, dt
 
 
+def max_over_ranks(value, dist, device):
+    """The slowest rank's time: with replicas every rank times the same step,
+    and the job's step ends when the last replica's does."""
+    if not dist:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     """The reference's method -- cg with a Jacobi preconditioner in FP64
     (iterative.rs:40-162, preconditioners.rs:14-92) -- as the oracle restates
@@ -569,11 +581,7 @@ def run_ours(args):
                          f"threads (bit-identical to one thread), reductions serial as in the reference"}
         cpu_rows = run_cpu_rows(threads, workloads or {})
 
-    value = statistics.mean(t_dev)
-    if dist:
-        tt = torch.tensor([value], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        value = float(tt.item())
+    value = max_over_ranks(statistics.mean(t_dev), dist, dev)
     jac = statistics.mean(t_jac)
     jacf = statistics.mean(t_jacf)
     jacf_iter_s = jacf / max(int(r_jacf.iterations), 1)
