@@ -62,6 +62,28 @@ def test_cycle_minimises_over_the_krylov_space(k):
     assert r["residual_norm"] == pytest.approx(np.linalg.norm(b - a @ r["x"]), rel=1e-12)
 
 
+def test_initial_guess_shifts_the_krylov_space():
+    a, b = _matrix()
+    x0 = np.linspace(-1.0, 1.0, 6)
+    r = O.gmres(_op(a), b, max_iter=3, restart=30, rtol=1e-14, atol=0.0, x0=x0)
+    ref = _krylov_min(a, np.eye(6), b, x0, 3)
+    assert r["iterations"] == 3
+    assert np.linalg.norm(r["x"] - ref) <= 1e-11 * np.linalg.norm(ref)
+
+
+def test_single_precision_follows_the_same_minimisation():
+    a, b = _matrix()
+    a32, b32 = a.astype(np.float32), b.astype(np.float32)
+    n = 6
+    ip = np.arange(0, n * n + 1, n, dtype=np.int64)
+    ix = np.tile(np.arange(n, dtype=np.int32), n)
+    op = O.op_csr_i32(ip, ix, a32.ravel().copy(), (n, n), f64=False)
+    r = O.gmres(op, b32, max_iter=3, restart=30, rtol=1e-7, atol=0.0)
+    ref = _krylov_min(a32.astype(np.float64), np.eye(6), b32.astype(np.float64), np.zeros(6), 3)
+    assert r["x"].dtype == np.float32 and r["iterations"] == 3
+    assert np.linalg.norm(r["x"] - ref) <= 1e-5 * np.linalg.norm(ref)
+
+
 def test_restarted_cycles_chain_minimisations():
     a, b = _matrix()
     r = O.gmres(_op(a), b, max_iter=5, restart=2, rtol=1e-14, atol=0.0)
